@@ -1,0 +1,410 @@
+#!/usr/bin/env python
+"""LETKF analysis benchmark on GB300: grid columns per second.
+
+Workload (default): 1 deg grid 360x180x32, state ps,u,v,T (97 rows), k = 64
+members, 200,000 clustered observations (4x density in 0-60E x 10S-30N),
+Gaspari-Cohn cut-off 800 km (c = 400 km), inflation 1.08; seeded synthetic
+inputs (see dida-thhpca-sc23_gb300/synthetic.py).  One step is one full
+analysis: H on all members, the bucket grid, the local observation search and
+the fused core + update over every column.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun each rank analyses its own instance (replicas; the analysis
+of one instance has no cross-GPU exchange).  Rank 0 prints one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import importlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+PKG = "dida-thhpca-sc23_gb300"
+METRIC = "LETKF columns/s: mixed-prec vs FP64 on one GB300 at ≤1e-4 err vs FP64"
+
+
+def pkg(name):
+    return importlib.import_module(f"{PKG}.{name}")
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--config", type=int, default=1)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0,
+                    help="target CPU time of the bounded CPU-baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi samples of SM clock and throttle reasons during a region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_id: str):
+        self.gpu_id = gpu_id
+        self.lines: list[str] = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", self.gpu_id, f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, parts[3:7]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def algorithmic_work(w, sum_p):
+    """FLOPs and bytes of one analysis: sum_c[2k^2 p_c + 2k p_c + 2k^2 n] +
+    N_col 13 k^3; state in and out in FP64 plus the observation arrays."""
+    k, n, ncol, nobs = w.k, w.n, w.ncol, w.obs["lat"].size
+    flops = 2.0 * k * k * sum_p + 2.0 * k * sum_p + ncol * (2.0 * k * k * n + 13.0 * k ** 3)
+    nbytes = ncol * n * (k + 1) * 8.0 * 2 + nobs * (k + 4) * 8.0
+    return flops, nbytes
+
+
+def fp64_peak_tflops(torch, dev):
+    """Measured FP64 matrix throughput (cuBLAS DGEMM, best of 5)."""
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device=dev)
+    b = torch.randn(n, n, dtype=torch.float64, device=dev)
+    torch.matmul(a, b)
+    torch.cuda.synchronize()
+    best = 1e30
+    for _ in range(5):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1))
+    return 2.0 * n ** 3 / (best * 1e-3) / 1e12
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except OSError:
+        return {}
+
+
+def cpu_baseline(w, seconds_target, label):
+    """The CPU oracle on a bounded sample of the workload's columns."""
+    from oracle import oracle as O
+    orc = O.Oracle(w)
+    t0 = time.perf_counter()
+    yb, dep = orc.obs_operator()
+    t_h = time.perf_counter() - t0
+    rng = np.random.default_rng(12345)
+    nc = orc.ncubes
+    probe = np.sort(rng.choice(nc, min(nc, 256), replace=False))
+    xa = np.full_like(orc.xb, np.nan)
+    axa = np.full_like(orc.axb, np.nan)
+    t0 = time.perf_counter()
+    orc.run_cubes(probe, yb, dep, xa, axa)
+    t_probe = time.perf_counter() - t0
+    per = t_probe / probe.size
+    ns = int(min(nc, max(probe.size, seconds_target / max(per, 1e-9))))
+    sample = np.sort(rng.choice(nc, ns, replace=False))
+    t0 = time.perf_counter()
+    orc.run_cubes(sample, yb, dep, xa, axa)
+    t_s = time.perf_counter() - t0
+    # H over all obs is charged pro rata to the sampled columns
+    t_total = t_s + t_h * ns / nc
+    cols = ns * w.ncol / nc
+    return {"value": cols / t_total, "unit": "columns/s", "cores": O.num_threads(), "kind": "port",
+            "sample": (f"{ns} of {nc} columns of {label} ({100.0 * ns / nc:.1f}%), C oracle "
+                       f"with OpenMP; H over all {w.obs['lat'].size} obs charged pro rata "
+                       f"({t_h:.2f} s full)"),
+            "seconds": t_total}
+
+
+def cpu_model():
+    try:
+        with open("/proc/cpuinfo") as f:
+            for ln in f:
+                if ln.lower().startswith(("model name", "cpu part")):
+                    return ln.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return "unknown"
+
+
+# ---------------------------------------------------------------------------
+def run_reference(args, rank, world):
+    """--impl reference: the CPU oracle (the reference's algorithm restated in
+    C; the Fortran reference cannot be built here) on the host cores."""
+    if rank != 0:
+        return
+    synthetic = pkg("synthetic")
+    w = synthetic.config(args.config)
+    from oracle import oracle as O
+    orc = O.Oracle(w)
+    rng = np.random.default_rng(777)
+    yb, dep = orc.obs_operator()
+    t0 = time.perf_counter()
+    orc.obs_operator()
+    t_h = time.perf_counter() - t0
+    nc = orc.ncubes
+    probe = np.sort(rng.choice(nc, 128, replace=False))
+    xa = np.full_like(orc.xb, np.nan)
+    axa = np.full_like(orc.axb, np.nan)
+    t0 = time.perf_counter()
+    orc.run_cubes(probe, yb, dep, xa, axa)
+    per = (time.perf_counter() - t0) / probe.size
+    ns = int(min(nc, max(128, 6.0 / max(per, 1e-9))))       # ~6 s per step
+    sample = np.sort(rng.choice(nc, ns, replace=False))
+    for _ in range(args.warmup):
+        orc.run_cubes(sample[: max(1, ns // 8)], yb, dep, xa, axa)
+    times = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        orc.run_cubes(sample, yb, dep, xa, axa)
+        times.append(time.perf_counter() - t0 + t_h * ns / nc)
+    t = sum(times) / len(times)
+    value = ns / t
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "columns/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * t, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": f"config{args.config}: 1deg 360x180x32, k=64, 200k clustered obs, "
+                               f"c=400 km, rho=1.08 (sample of {ns} columns per step)"},
+        "cpu_baseline": {"value": value, "unit": "columns/s", "cores": O.num_threads(),
+                         "kind": "port",
+                         "sample": f"{ns} of {nc} columns per step; H over all obs pro rata; "
+                                   f"{cpu_model()}"},
+        "e2e": {"value": value, "unit": "columns/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+def run_ours(args, rank, world, local_rank):
+    import torch
+    dev = torch.device("cuda", local_rank)
+    torch.cuda.set_device(dev)
+    synthetic = pkg("synthetic")
+    letkf = pkg("letkf")
+    pkg("build").build()
+    letkf.load_library()
+    dist = world > 1
+    if dist:
+        import torch.distributed as tdist
+
+    t_gen = time.perf_counter()
+    w = synthetic.config(args.config)
+    t_gen = time.perf_counter() - t_gen
+    ctx = letkf.LetkfGPU.from_workload(w, device=local_rank)
+    stream = torch.cuda.current_stream(dev)
+    ctx.set_stream(stream.cuda_stream)
+
+    # device-resident inputs
+    xb_d = torch.from_numpy(w.xb).to(dev)
+    axb_d = torch.from_numpy(w.axb).to(dev)
+    xa_d = torch.empty_like(xb_d)
+    axa_d = torch.empty_like(axb_d)
+    o = w.obs
+    obs_d = {key: torch.from_numpy(np.ascontiguousarray(o[key])).to(dev)
+             for key in ("lat", "lon", "ph", "lev", "var", "yo", "rinv")}
+    obs_dev = letkf.ObsArrays(obs_d, device=True)
+    torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        ctx.run_device(xb_d, axb_d, obs_dev, xa_d, axa_d)
+    torch.cuda.synchronize()
+    if dist:
+        tdist.barrier()
+    gpu_uuid = torch.cuda.get_device_properties(dev).uuid
+    clocks = ClockSampler(f"GPU-{gpu_uuid}" if not str(gpu_uuid).startswith("GPU-") else str(gpu_uuid))
+    clocks.start()
+    time.sleep(0.3)
+    n0 = letkf.launch_count()
+    core_ms, stages = [], []
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        ctx.run_device(xb_d, axb_d, obs_dev, xa_d, axa_d)
+        st = ctx.stats()
+        core_ms.append(st["ms_core"])
+        stages.append((st["ms_obs"], st["ms_search"], st["ms_core"]))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    launches = letkf.launch_count() - n0
+    ms = e0.elapsed_time(e1) / args.steps
+    if dist:
+        t = torch.tensor([ms], device=dev)
+        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+        ms = float(t.item())
+        tdist.barrier()
+    st = ctx.stats()
+    value = world * w.ncol / (ms * 1e-3)
+
+    # end to end through the C-ABI with pinned host buffers
+    xb_h = torch.empty(w.xb.shape, dtype=torch.float64, pin_memory=True)
+    xb_h.numpy()[...] = w.xb
+    axb_h = torch.empty(w.axb.shape, dtype=torch.float64, pin_memory=True)
+    axb_h.numpy()[...] = w.axb
+    xa_h = torch.empty(w.xb.shape, dtype=torch.float64, pin_memory=True)
+    axa_h = torch.empty(w.axb.shape, dtype=torch.float64, pin_memory=True)
+    obs_h = {}
+    for key in ("lat", "lon", "ph", "lev", "var", "yo", "rinv"):
+        a = np.ascontiguousarray(o[key])
+        t_ = torch.empty(a.shape, dtype=torch.from_numpy(a[:1]).dtype, pin_memory=True)
+        t_.numpy()[...] = a
+        obs_h[key] = t_.numpy()
+    obs_host = letkf.ObsArrays(obs_h)
+    xbn, axbn, xan, axan = xb_h.numpy(), axb_h.numpy(), xa_h.numpy(), axa_h.numpy()
+    ctx.run(xbn, axbn, obs_host, xan, axan)
+    if dist:
+        tdist.barrier()
+    torch.cuda.synchronize()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    e2e_steps = max(1, min(args.steps, 3))
+    for _ in range(e2e_steps):
+        ctx.run(xbn, axbn, obs_host, xan, axan)
+    f1.record(stream)
+    torch.cuda.synchronize()
+    ms_e2e = f0.elapsed_time(f1) / e2e_steps
+    if dist:
+        t = torch.tensor([ms_e2e], device=dev)
+        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+        ms_e2e = float(t.item())
+    h2d = sum(a.nbytes for a in (xbn, axbn)) + sum(a.nbytes for a in obs_h.values())
+    d2h = xan.nbytes + axan.nbytes
+    err_h = float(np.abs(xan - xa_d.cpu().numpy()).max())   # e2e and device runs agree
+
+    if rank != 0:
+        return
+    peaks = measured_peaks()
+    fp64_peak = fp64_peak_tflops(torch, dev)
+    flops, nbytes = algorithmic_work(w, st["sum_p"])
+    core = statistics.mean(core_ms)
+    achieved = flops / (core * 1e-3) / 1e12
+    traffic = None
+    tfile = os.path.join(REPO, "profiles", "core_fp64_traffic.json")
+    if os.path.exists(tfile):
+        with open(tfile) as f:
+            tr = json.load(f)
+        traffic = tr.get("bytes_per_full_launch")
+    line = {
+        "metric": METRIC, "value": value, "unit": "columns/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded; no public dataset for this path)",
+        "config": {"workload": "config1: 1deg 360x180x32, k=64, 200k obs (4x box 0-60E 10S-30N), "
+                               "GC c=400 km (cut-off 800 km), rho=1.08, level-select H",
+                   "form": "plain FP64 (precision 0)", "columns": w.ncol, "ensemble": w.k,
+                   "obs": int(w.obs["lat"].size), "sum_p": st["sum_p"], "max_p": st["max_p"],
+                   "l2": "inputs larger than L2 (xb 3.2 GB)",
+                   "parallelism": f"replicas x{world}"},
+        "e2e": {"value": world * w.ncol / (ms_e2e * 1e-3), "unit": "columns/s",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "max_abs_diff_vs_device_run": err_h},
+        "gpu_launches": launches,
+        "roofline": {"bound": "fp64", "kernel": "k_core_fp64<64>", "achieved": achieved,
+                     "peak": fp64_peak, "unit": "TFLOP/s", "frac": achieved / fp64_peak,
+                     "traffic": traffic,
+                     "peak_source": "measured here: cuBLAS FP64 GEMM 4096^3, best of 5 "
+                                    "(MEASURED_PEAKS.json has no FP64 entry)",
+                     "algorithmic_flops_per_launch": flops, "kernel_ms": core},
+        "roofline_hbm_step": {"achieved": nbytes / (ms * 1e-3) / 1e9,
+                              "peak": peaks.get("hbm_gbs", 6800.0), "unit": "GB/s",
+                              "frac": nbytes / (ms * 1e-3) / 1e9 / peaks.get("hbm_gbs", 6800.0),
+                              "algorithmic_bytes": nbytes},
+        "stages_ms": {"obs_H_buckets": statistics.mean(s[0] for s in stages),
+                      "search": statistics.mean(s[1] for s in stages),
+                      "core_update": statistics.mean(s[2] for s in stages)},
+        "clocks": clk,
+        "workload_generation_s": t_gen,
+    }
+    if world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(w, args.cpu_seconds, "config1")
+        line["cpu_baseline"]["cpu"] = cpu_model()
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    if world > 1:
+        import torch
+        import torch.distributed as tdist
+        torch.cuda.set_device(local_rank)
+        tdist.init_process_group("nccl")
+    try:
+        run_ours(args, rank, world, local_rank)
+    finally:
+        if world > 1:
+            import torch.distributed as tdist
+            tdist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,724 @@
+// letkf_api.cu -- C-ABI host side of the GB300 LETKF analysis.
+//
+// The reference runs letkf_run (code/x86/TradDA/DA/LETKF/src/letkf.F90:157-257)
+// once per DA cycle: gen_obs_struct, the MPI obs halo exchange, then the column
+// loop.  Here one call does H, the bucket grid, the local search and the fused
+// core + update on one GPU; the halo exchange has no counterpart because all
+// observations live in one device array.
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "letkf_internal.cuh"
+
+bool lg_core_supports(int k);
+int lg_search_cap(int max_obs);
+
+namespace {
+
+std::atomic<int64_t> g_launches{0};
+
+int set_err(letkf_ctx *ctx, int code, const std::string &msg)
+{
+    if (ctx) ctx->last_error = msg;
+    return code;
+}
+
+#define LG_CUDA(call)                                                                          \
+    do {                                                                                       \
+        cudaError_t e_ = (call);                                                               \
+        if (e_ != cudaSuccess)                                                                 \
+            return set_err(ctx, e_ == cudaErrorMemoryAllocation ? LETKF_ERR_ALLOC : LETKF_ERR_CUDA, \
+                           std::string(#call) + ": " + cudaGetErrorString(e_));                \
+    } while (0)
+
+template <typename T>
+cudaError_t h2d(DevBuf<T> &buf, const T *src, size_t count, cudaStream_t s)
+{
+    cudaError_t e = buf.reserve(count);
+    if (e != cudaSuccess || count == 0) return e;
+    return cudaMemcpyAsync(buf.p, src, sizeof(T) * count, cudaMemcpyHostToDevice, s);
+}
+
+float elapsed(cudaEvent_t a, cudaEvent_t b)
+{
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, a, b) != cudaSuccess) return 0.f;
+    return ms;
+}
+
+int check_obs(letkf_ctx *ctx, const letkf_obs *obs)
+{
+    if (!obs) return set_err(ctx, LETKF_ERR_INVALID, "obs is NULL");
+    if (obs->nobs < 0 || obs->nobs >= (int64_t)INT32_MAX)
+        return set_err(ctx, LETKF_ERR_INVALID, "nobs out of range");
+    if (obs->nobs == 0) return LETKF_OK;
+    if (!obs->lat || !obs->lon || !obs->var || !obs->yo || !obs->rinv)
+        return set_err(ctx, LETKF_ERR_INVALID, "obs lat/lon/var/yo/rinv must be set");
+    const bool need_ph = ctx->params.h_mode == 0 || ctx->params.vert_dist > 0.0;
+    if (need_ph && !obs->ph) return set_err(ctx, LETKF_ERR_INVALID, "obs ph required");
+    if (ctx->params.h_mode == 1 && ctx->nvar3d > 0 && !obs->lev)
+        return set_err(ctx, LETKF_ERR_INVALID, "obs lev required for level select");
+    return LETKF_OK;
+}
+
+// Stage observation arrays on the device (copies for host pointers).
+struct ObsDev {
+    const double *lat, *lon, *ph, *yo, *rinv;
+    const int32_t *lev, *var;
+};
+
+int stage_obs(letkf_ctx *ctx, const letkf_obs *obs, bool host, ObsDev &d)
+{
+    const int64_t no = obs->nobs;
+    if (host) {
+        LG_CUDA(h2d(ctx->d_olat, obs->lat, no, ctx->stream));
+        LG_CUDA(h2d(ctx->d_olon, obs->lon, no, ctx->stream));
+        LG_CUDA(h2d(ctx->d_oyo, obs->yo, no, ctx->stream));
+        LG_CUDA(h2d(ctx->d_orinv, obs->rinv, no, ctx->stream));
+        LG_CUDA(h2d(ctx->d_ovar, obs->var, no, ctx->stream));
+        if (obs->ph) LG_CUDA(h2d(ctx->d_oph, obs->ph, no, ctx->stream));
+        else LG_CUDA(ctx->d_oph.reserve(1));
+        if (obs->lev) LG_CUDA(h2d(ctx->d_olev, obs->lev, no, ctx->stream));
+        else LG_CUDA(ctx->d_olev.reserve(1));
+        d = {ctx->d_olat.p, ctx->d_olon.p, ctx->d_oph.p, ctx->d_oyo.p, ctx->d_orinv.p,
+             ctx->d_olev.p, ctx->d_ovar.p};
+    } else {
+        LG_CUDA(ctx->d_oph.reserve(1));
+        LG_CUDA(ctx->d_olev.reserve(1));
+        d = {obs->lat, obs->lon, obs->ph ? obs->ph : ctx->d_oph.p, obs->yo, obs->rinv,
+             obs->lev ? obs->lev : ctx->d_olev.p, obs->var};
+    }
+    return LETKF_OK;
+}
+
+int reserve_obs_work(letkf_ctx *ctx, int64_t no)
+{
+    const size_t n = (size_t)std::max<int64_t>(no, 1);
+    LG_CUDA(ctx->d_yb.reserve(n * ctx->k));
+    LG_CUDA(ctx->d_dep.reserve(n));
+    LG_CUDA(ctx->d_rinvf.reserve(n));
+    LG_CUDA(ctx->d_os.reserve(n));
+    LG_CUDA(ctx->d_oc.reserve(n));
+    LG_CUDA(ctx->d_oyr.reserve(n));
+    LG_CUDA(ctx->d_oxyz.reserve(n));
+    LG_CUDA(ctx->d_obucket.reserve(n));
+    LG_CUDA(ctx->d_bidx.reserve(n));
+    LG_CUDA(ctx->d_bxyz.reserve(n));
+    return LETKF_OK;
+}
+
+int read_status(letkf_ctx *ctx, unsigned &status, unsigned long long *cnt)
+{
+    LG_CUDA(cudaMemcpyAsync(&status, ctx->d_status.p, sizeof(unsigned), cudaMemcpyDeviceToHost,
+                            ctx->stream));
+    LG_CUDA(cudaMemcpyAsync(cnt, ctx->d_counters.p, sizeof(unsigned long long) * LG_CNT_N,
+                            cudaMemcpyDeviceToHost, ctx->stream));
+    LG_CUDA(cudaStreamSynchronize(ctx->stream));
+    return LETKF_OK;
+}
+
+int reset_status(letkf_ctx *ctx)
+{
+    LG_CUDA(cudaMemsetAsync(ctx->d_status.p, 0, sizeof(unsigned), ctx->stream));
+    LG_CUDA(cudaMemsetAsync(ctx->d_counters.p, 0, sizeof(unsigned long long) * LG_CNT_N, ctx->stream));
+    return LETKF_OK;
+}
+
+// H, buckets and local lists for the staged observations; grows the list
+// storage and repeats the search if it was too small.
+int obs_and_search(letkf_ctx *ctx, const double *xb, const double *axb, const letkf_obs *obs,
+                   const ObsDev &od, unsigned long long *cnt)
+{
+    const int64_t no = obs->nobs;
+    const LgGrid g = lg_grid(ctx);
+    int rc = reserve_obs_work(ctx, no);
+    if (rc) return rc;
+    LG_CUDA(lg_launch_obs_prepare(ctx, g, xb, axb, no, od.lat, od.lon, od.ph, od.lev, od.var, od.yo,
+                                  od.rinv));
+    LG_CUDA(lg_launch_buckets(ctx, no));
+    LG_CUDA(cudaEventRecord(ctx->ev[2], ctx->stream));
+    if (ctx->list_cap == 0) {
+        const int64_t guess = ctx->ncubes * (int64_t)std::min(ctx->params.max_obs, 512);
+        LG_CUDA(ctx->d_lidx.reserve((size_t)std::max<int64_t>(guess, 1)));
+        LG_CUDA(ctx->d_lrloc.reserve((size_t)std::max<int64_t>(guess, 1)));
+        ctx->list_cap = std::max<int64_t>(guess, 1);
+    }
+    for (int attempt = 0; attempt < 3; attempt++) {
+        LG_CUDA(lg_launch_search(ctx, g, no));
+        unsigned st = 0;
+        rc = read_status(ctx, st, cnt);
+        if (rc) return rc;
+        if (st & LG_ST_SEGMENTS)
+            return set_err(ctx, LETKF_ERR_UNSUPPORTED, "localization cap spans too many buckets");
+        if (!(st & LG_ST_LIST_FULL)) {
+            if (st & LG_ST_BAD_OBS)
+                return set_err(ctx, LETKF_ERR_INVALID,
+                               "observation outside the grid or with a bad variable/level/pressure");
+            return LETKF_OK;
+        }
+        const int64_t need = (int64_t)cnt[LG_CNT_CURSOR];
+        const int64_t cap = need + need / 16 + 1024;
+        ctx->d_lidx.release();
+        ctx->d_lrloc.release();
+        LG_CUDA(ctx->d_lidx.reserve((size_t)cap));
+        LG_CUDA(ctx->d_lrloc.reserve((size_t)cap));
+        ctx->list_cap = cap;
+        // the search counters start again; status keeps any obs error
+        LG_CUDA(cudaMemsetAsync(ctx->d_counters.p, 0, sizeof(unsigned long long) * LG_CNT_N,
+                                ctx->stream));
+        unsigned keep = st & LG_ST_BAD_OBS;
+        LG_CUDA(cudaMemcpyAsync(ctx->d_status.p, &keep, sizeof(unsigned), cudaMemcpyHostToDevice,
+                                ctx->stream));
+        LG_CUDA(cudaStreamSynchronize(ctx->stream));
+    }
+    return set_err(ctx, LETKF_ERR_ALLOC, "local observation lists did not fit");
+}
+
+void fill_stats(letkf_ctx *ctx, const unsigned long long *cnt)
+{
+    letkf_stats &s = ctx->stats;
+    s.ncubes = ctx->ncubes;
+    s.sum_p = (int64_t)cnt[LG_CNT_SUMP];
+    s.max_p = (int64_t)cnt[LG_CNT_MAXP];
+    s.n_truncated = (int64_t)cnt[LG_CNT_TRUNC];
+    s.n_borderline = (int64_t)cnt[LG_CNT_BORDER];
+    s.n_not_converged = (int64_t)cnt[LG_CNT_NOTCONV];
+    s.max_sweeps = (int32_t)cnt[LG_CNT_MAXSWEEP];
+    s.precision = ctx->params.precision;
+}
+
+}  // namespace
+
+void lg_count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+LgGrid lg_grid(letkf_ctx *ctx)
+{
+    LgGrid g;
+    g.nlat = ctx->nlat;
+    g.nlon = ctx->nlon;
+    g.nz = ctx->nz;
+    g.nvar2d = ctx->nvar2d;
+    g.nvar3d = ctx->nvar3d;
+    g.k = ctx->k;
+    g.n = ctx->n;
+    g.ps_row = ctx->ps_row;
+    g.p0 = ctx->p0;
+    g.ptop = ctx->ptop;
+    g.glat = ctx->d_glat.p;
+    g.glon = ctx->d_glon.p;
+    g.hyai = ctx->d_hyai.p;
+    g.hybi = ctx->d_hybi.p;
+    return g;
+}
+
+LgParams lg_params(letkf_ctx *ctx)
+{
+    LgParams p;
+    const letkf_params &q = ctx->params;
+    p.local_dist = q.loc_dist_km;
+    p.vert_dist = q.vert_dist;
+    p.inflation = q.inflation;
+    p.obs_polar = q.obs_polar_deg;
+    p.gc_filter = q.gc_filter;
+    p.gc_filter_vertical = q.gc_filter_vertical;
+    p.max_obs = q.max_obs;
+    p.cube_n = q.cube_n;
+    p.cube_nz = q.cube_nz;
+    p.overlap = q.overlap;
+    p.h_mode = q.h_mode;
+    p.precision = q.precision;
+    p.nbj = ctx->nbj;
+    p.nbi = ctx->nbi;
+    return p;
+}
+
+extern "C" {
+
+int64_t letkf_gpu_launch_count(void) { return g_launches.load(); }
+
+int letkf_gpu_create(letkf_ctx **out, const letkf_grid *grid, const letkf_params *params, int device)
+{
+    letkf_ctx *ctx = nullptr;
+    if (!out || !grid || !params) return LETKF_ERR_INVALID;
+    *out = nullptr;
+    const letkf_grid &G = *grid;
+    const letkf_params &P = *params;
+    if (G.nlat < 2 || G.nlon < 2 || G.nz < 1 || G.nvar2d < 0 || G.nvar3d < 0 ||
+        G.nvar2d + G.nvar3d < 1 || !G.lat || !G.lon)
+        return LETKF_ERR_INVALID;
+    if (!lg_core_supports(G.ens)) return LETKF_ERR_UNSUPPORTED;
+    for (int i = 0; i < G.nlat; i++)
+        if (!(G.lat[i] > -90.0f && G.lat[i] < 90.0f) || (i > 0 && !(G.lat[i] > G.lat[i - 1])))
+            return LETKF_ERR_INVALID;
+    for (int i = 0; i < G.nlon; i++)
+        if (!(G.lon[i] >= 0.0f && G.lon[i] < 360.0f) || (i > 0 && !(G.lon[i] > G.lon[i - 1])))
+            return LETKF_ERR_INVALID;
+    const int n = G.nvar2d + G.nvar3d * G.nz;
+    if (!(P.loc_dist_km > 0.0 && P.loc_dist_km <= 4000.0) || !(P.inflation > 0.0) ||
+        P.max_obs < 1 || P.cube_n < 1 || P.cube_nz < 1 || P.overlap < 0 ||
+        P.overlap >= P.cube_n || (P.h_mode != 0 && P.h_mode != 1) ||
+        (P.precision != LETKF_PREC_FP64 && P.precision != LETKF_PREC_MIXED) ||
+        !(P.obs_polar_deg >= 0.0))
+        return LETKF_ERR_INVALID;
+    const bool need_hybrid = P.h_mode == 0 || P.vert_dist > 0.0;
+    if (need_hybrid && (!G.hyai || !G.hybi || G.ps_row < 0 || G.ps_row >= n))
+        return LETKF_ERR_INVALID;
+    if (P.overlap != 0 || P.vert_dist > 0.0) return LETKF_ERR_UNSUPPORTED;
+    if (P.precision != LETKF_PREC_FP64) return LETKF_ERR_UNSUPPORTED;
+
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return LETKF_ERR_CUDA;
+    if (device >= ndev) return LETKF_ERR_INVALID;
+    if (device >= 0 && cudaSetDevice(device) != cudaSuccess) return LETKF_ERR_CUDA;
+
+    ctx = new letkf_ctx();
+    cudaGetDevice(&ctx->device);
+    ctx->params = P;
+    ctx->nlat = G.nlat;
+    ctx->nlon = G.nlon;
+    ctx->nz = G.nz;
+    ctx->nvar2d = G.nvar2d;
+    ctx->nvar3d = G.nvar3d;
+    ctx->k = G.ens;
+    ctx->n = n;
+    ctx->ps_row = G.ps_row;
+    ctx->p0 = G.p0;
+    ctx->ptop = G.ptop;
+    ctx->ncol = (int64_t)G.nlat * G.nlon;
+    ctx->nbj = (G.nlat + P.cube_n - 1) / P.cube_n;
+    ctx->nbi = (G.nlon + P.cube_n - 1) / P.cube_n;
+    ctx->ncubes = (int64_t)ctx->nbj * ctx->nbi;
+    ctx->have_hybrid = G.hyai && G.hybi;
+
+    int rc = LETKF_OK;
+    auto setup = [&]() -> int {
+        LG_CUDA(cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking));
+        ctx->stream = ctx->own_stream;
+        for (int i = 0; i < 8; i++) LG_CUDA(cudaEventCreate(&ctx->ev[i]));
+        std::vector<float> glat(G.lat, G.lat + G.nlat), glon(G.lon, G.lon + G.nlon);
+        glat.push_back(90.0f);      // grid_lat(nx+1) = 90 (pro_info.F90:77,82)
+        glon.push_back(360.0f);     // grid_lon(ny+1) = 360 (pro_info.F90:78,83)
+        LG_CUDA(h2d(ctx->d_glat, glat.data(), glat.size(), ctx->stream));
+        LG_CUDA(h2d(ctx->d_glon, glon.data(), glon.size(), ctx->stream));
+        std::vector<double> zero(G.nz + 1, 0.0);
+        LG_CUDA(h2d(ctx->d_hyai, G.hyai ? G.hyai : zero.data(), (size_t)G.nz + 1, ctx->stream));
+        LG_CUDA(h2d(ctx->d_hybi, G.hybi ? G.hybi : zero.data(), (size_t)G.nz + 1, ctx->stream));
+        // bucket cells about a third of the cut-off radius 2c
+        const double radius_deg = 2.0 * P.loc_dist_km / LG_EARTH_A * 180.0 / M_PI;
+        ctx->cell_deg = std::min(10.0, std::max(0.25, radius_deg / 3.0));
+        ctx->nblat = (int)std::ceil(180.0 / ctx->cell_deg);
+        ctx->nblon = (int)std::ceil(360.0 / ctx->cell_deg);
+        const size_t nb = (size_t)ctx->nblat * ctx->nblon;
+        LG_CUDA(ctx->d_bcount.reserve(nb));
+        LG_CUDA(ctx->d_bstart.reserve(nb + 1));
+        LG_CUDA(ctx->d_loff.reserve((size_t)ctx->ncubes));
+        LG_CUDA(ctx->d_lcnt.reserve((size_t)ctx->ncubes));
+        LG_CUDA(ctx->d_status.reserve(1));
+        LG_CUDA(ctx->d_counters.reserve(LG_CNT_N));
+        LG_CUDA(cudaStreamSynchronize(ctx->stream));
+        return LETKF_OK;
+    };
+    rc = setup();
+    if (rc != LETKF_OK) {
+        letkf_gpu_destroy(ctx);
+        return rc;
+    }
+    *out = ctx;
+    return LETKF_OK;
+}
+
+int letkf_gpu_set_stream(letkf_ctx *ctx, void *stream)
+{
+    if (!ctx) return LETKF_ERR_INVALID;
+    ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
+    return LETKF_OK;
+}
+
+int letkf_gpu_set_keep_trans(letkf_ctx *ctx, int keep)
+{
+    if (!ctx) return LETKF_ERR_INVALID;
+    if (keep) {
+        LG_CUDA(ctx->d_trans.reserve((size_t)ctx->ncubes * ctx->k * ctx->k));
+        LG_CUDA(ctx->d_w.reserve((size_t)ctx->ncubes * ctx->k));
+    } else {
+        ctx->d_trans.release();
+        ctx->d_w.release();
+    }
+    return LETKF_OK;
+}
+
+int letkf_gpu_run(letkf_ctx *ctx, const double *xb, const double *axb, const letkf_obs *obs,
+                  double *xa, double *axa, int flags)
+{
+    if (!ctx) return LETKF_ERR_INVALID;
+    if (!xb || !axb || !xa || !axa) return set_err(ctx, LETKF_ERR_INVALID, "NULL state pointer");
+    if (flags != LETKF_HOST_PTRS && flags != LETKF_DEVICE_PTRS)
+        return set_err(ctx, LETKF_ERR_INVALID, "bad flags");
+    int rc = check_obs(ctx, obs);
+    if (rc) return rc;
+    LG_CUDA(cudaSetDevice(ctx->device));
+    const bool host = flags == LETKF_HOST_PTRS;
+    const size_t nstate = (size_t)ctx->ncol * ctx->n * ctx->k, nmean = (size_t)ctx->ncol * ctx->n;
+    LG_CUDA(cudaEventRecord(ctx->ev[0], ctx->stream));
+    rc = reset_status(ctx);
+    if (rc) return rc;
+    const double *dxb = xb, *daxb = axb;
+    double *dxa = xa, *daxa = axa;
+    if (host) {
+        LG_CUDA(h2d(ctx->d_xb, xb, nstate, ctx->stream));
+        LG_CUDA(h2d(ctx->d_axb, axb, nmean, ctx->stream));
+        LG_CUDA(ctx->d_xa.reserve(nstate));
+        LG_CUDA(ctx->d_axa.reserve(nmean));
+        dxb = ctx->d_xb.p;
+        daxb = ctx->d_axb.p;
+        dxa = ctx->d_xa.p;
+        daxa = ctx->d_axa.p;
+    }
+    ObsDev od;
+    rc = stage_obs(ctx, obs, host, od);
+    if (rc) return rc;
+    LG_CUDA(cudaEventRecord(ctx->ev[1], ctx->stream));
+    unsigned long long cnt[LG_CNT_N] = {};
+    rc = obs_and_search(ctx, dxb, daxb, obs, od, cnt);
+    if (rc) return rc;
+    LG_CUDA(cudaEventRecord(ctx->ev[3], ctx->stream));
+    const LgGrid g = lg_grid(ctx);
+    LG_CUDA(lg_launch_core_fp64(ctx, g, dxb, daxb, dxa, daxa, ctx->d_trans.p != nullptr));
+    LG_CUDA(cudaEventRecord(ctx->ev[4], ctx->stream));
+    if (host) {
+        LG_CUDA(cudaMemcpyAsync(xa, dxa, sizeof(double) * nstate, cudaMemcpyDeviceToHost, ctx->stream));
+        LG_CUDA(cudaMemcpyAsync(axa, daxa, sizeof(double) * nmean, cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    LG_CUDA(cudaEventRecord(ctx->ev[5], ctx->stream));
+    unsigned st = 0;
+    rc = read_status(ctx, st, cnt);
+    if (rc) return rc;
+    fill_stats(ctx, cnt);
+    ctx->stats.ms_h2d = elapsed(ctx->ev[0], ctx->ev[1]);
+    ctx->stats.ms_obs = elapsed(ctx->ev[1], ctx->ev[2]);
+    ctx->stats.ms_search = elapsed(ctx->ev[2], ctx->ev[3]);
+    ctx->stats.ms_core = elapsed(ctx->ev[3], ctx->ev[4]);
+    ctx->stats.ms_d2h = elapsed(ctx->ev[4], ctx->ev[5]);
+    ctx->stats.ms_total = elapsed(ctx->ev[0], ctx->ev[5]);
+    ctx->have_run = true;
+    ctx->last_nobs = obs->nobs;
+    if (st & LG_ST_NOT_CONV)
+        return set_err(ctx, LETKF_ERR_NOT_CONVERGED, "an eigensolve reached its sweep limit");
+    return LETKF_OK;
+}
+
+int letkf_gpu_synchronize(letkf_ctx *ctx)
+{
+    if (!ctx) return LETKF_ERR_INVALID;
+    LG_CUDA(cudaStreamSynchronize(ctx->stream));
+    return LETKF_OK;
+}
+
+int letkf_gpu_obs_operator(letkf_ctx *ctx, const double *xb, const double *axb,
+                           const letkf_obs *obs, double *yb, double *dep)
+{
+    if (!ctx) return LETKF_ERR_INVALID;
+    if (!xb || !axb || !yb || !dep) return set_err(ctx, LETKF_ERR_INVALID, "NULL pointer");
+    int rc = check_obs(ctx, obs);
+    if (rc) return rc;
+    LG_CUDA(cudaSetDevice(ctx->device));
+    const size_t nstate = (size_t)ctx->ncol * ctx->n * ctx->k, nmean = (size_t)ctx->ncol * ctx->n;
+    rc = reset_status(ctx);
+    if (rc) return rc;
+    LG_CUDA(h2d(ctx->d_xb, xb, nstate, ctx->stream));
+    LG_CUDA(h2d(ctx->d_axb, axb, nmean, ctx->stream));
+    ObsDev od;
+    rc = stage_obs(ctx, obs, true, od);
+    if (rc) return rc;
+    rc = reserve_obs_work(ctx, obs->nobs);
+    if (rc) return rc;
+    LG_CUDA(lg_launch_obs_prepare(ctx, lg_grid(ctx), ctx->d_xb.p, ctx->d_axb.p, obs->nobs, od.lat,
+                                  od.lon, od.ph, od.lev, od.var, od.yo, od.rinv));
+    if (obs->nobs > 0) {
+        LG_CUDA(cudaMemcpyAsync(yb, ctx->d_yb.p, sizeof(double) * obs->nobs * ctx->k,
+                                cudaMemcpyDeviceToHost, ctx->stream));
+        LG_CUDA(cudaMemcpyAsync(dep, ctx->d_dep.p, sizeof(double) * obs->nobs,
+                                cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    unsigned st = 0;
+    unsigned long long cnt[LG_CNT_N];
+    rc = read_status(ctx, st, cnt);
+    if (rc) return rc;
+    if (st & LG_ST_BAD_OBS)
+        return set_err(ctx, LETKF_ERR_INVALID,
+                       "observation outside the grid or with a bad variable/level/pressure");
+    return LETKF_OK;
+}
+
+int letkf_gpu_local_obs(letkf_ctx *ctx, int64_t *offsets, int32_t *idx, double *rloc)
+{
+    if (!ctx || !offsets) return LETKF_ERR_INVALID;
+    if (!ctx->have_run) return set_err(ctx, LETKF_ERR_STATE, "no run yet");
+    const int64_t nc = ctx->ncubes;
+    std::vector<int64_t> off(nc);
+    std::vector<int32_t> cnt(nc);
+    LG_CUDA(cudaMemcpy(off.data(), ctx->d_loff.p, sizeof(int64_t) * nc, cudaMemcpyDeviceToHost));
+    LG_CUDA(cudaMemcpy(cnt.data(), ctx->d_lcnt.p, sizeof(int32_t) * nc, cudaMemcpyDeviceToHost));
+    offsets[0] = 0;
+    for (int64_t c = 0; c < nc; c++) offsets[c + 1] = offsets[c] + cnt[c];
+    if (idx || rloc) {
+        const int64_t total = offsets[nc];
+        int64_t hi = 0;
+        for (int64_t c = 0; c < nc; c++) hi = std::max<int64_t>(hi, off[c] + cnt[c]);
+        std::vector<int32_t> li((size_t)std::max<int64_t>(hi, 1));
+        std::vector<double> lr((size_t)std::max<int64_t>(hi, 1));
+        if (hi > 0) {
+            LG_CUDA(cudaMemcpy(li.data(), ctx->d_lidx.p, sizeof(int32_t) * hi, cudaMemcpyDeviceToHost));
+            LG_CUDA(cudaMemcpy(lr.data(), ctx->d_lrloc.p, sizeof(double) * hi, cudaMemcpyDeviceToHost));
+        }
+        for (int64_t c = 0; c < nc; c++) {
+            if (idx) std::memcpy(idx + offsets[c], li.data() + off[c], sizeof(int32_t) * cnt[c]);
+            if (rloc) std::memcpy(rloc + offsets[c], lr.data() + off[c], sizeof(double) * cnt[c]);
+        }
+        (void)total;
+    }
+    return LETKF_OK;
+}
+
+int letkf_gpu_last_trans(letkf_ctx *ctx, const int64_t *cubes, int64_t ncubes, double *trans, double *w)
+{
+    if (!ctx || (!cubes && ncubes > 0)) return LETKF_ERR_INVALID;
+    if (!ctx->have_run || !ctx->d_trans.p)
+        return set_err(ctx, LETKF_ERR_STATE, "no run with kept transforms (letkf_gpu_set_keep_trans)");
+    const int k = ctx->k;
+    for (int64_t i = 0; i < ncubes; i++) {
+        if (cubes[i] < 0 || cubes[i] >= ctx->ncubes) return set_err(ctx, LETKF_ERR_INVALID, "cube index");
+        if (trans)
+            LG_CUDA(cudaMemcpy(trans + i * k * k, ctx->d_trans.p + cubes[i] * k * k,
+                               sizeof(double) * k * k, cudaMemcpyDeviceToHost));
+        if (w)
+            LG_CUDA(cudaMemcpy(w + i * k, ctx->d_w.p + cubes[i] * k, sizeof(double) * k,
+                               cudaMemcpyDeviceToHost));
+    }
+    return LETKF_OK;
+}
+
+int letkf_gpu_core_batch(letkf_ctx *ctx, int64_t nb, const int64_t *offsets, const double *hxens,
+                         const float *rdiaginv, const double *dep, const double *rloc,
+                         double *trans, double *w)
+{
+    if (!ctx || nb < 0 || !offsets || !trans || !w) return LETKF_ERR_INVALID;
+    if (nb == 0) return LETKF_OK;
+    const int k = ctx->k;
+    const int64_t total = offsets[nb];
+    if (offsets[0] != 0 || total < 0) return set_err(ctx, LETKF_ERR_INVALID, "offsets");
+    std::vector<int32_t> cnt(nb);
+    for (int64_t b = 0; b < nb; b++) {
+        const int64_t c = offsets[b + 1] - offsets[b];
+        if (c < 0 || c > INT32_MAX) return set_err(ctx, LETKF_ERR_INVALID, "offsets not ascending");
+        cnt[b] = (int32_t)c;
+    }
+    if (total > 0 && (!hxens || !rdiaginv || !dep || !rloc))
+        return set_err(ctx, LETKF_ERR_INVALID, "NULL obs arrays");
+    LG_CUDA(cudaSetDevice(ctx->device));
+    int rc = reset_status(ctx);
+    if (rc) return rc;
+    LG_CUDA(h2d(ctx->d_boff, offsets, (size_t)nb, ctx->stream));
+    LG_CUDA(ctx->d_lcnt.reserve((size_t)std::max<int64_t>(nb, ctx->ncubes)));
+    LG_CUDA(cudaMemcpyAsync(ctx->d_lcnt.p, cnt.data(), sizeof(int32_t) * nb, cudaMemcpyHostToDevice,
+                            ctx->stream));
+    LG_CUDA(h2d(ctx->d_bhx, hxens, (size_t)std::max<int64_t>(total, 1) * k * (total > 0), ctx->stream));
+    LG_CUDA(h2d(ctx->d_brdi, rdiaginv, (size_t)total, ctx->stream));
+    LG_CUDA(h2d(ctx->d_bdep, dep, (size_t)total, ctx->stream));
+    LG_CUDA(h2d(ctx->d_brloc, rloc, (size_t)total, ctx->stream));
+    DevBuf<double> dt, dw;
+    LG_CUDA(dt.reserve((size_t)nb * k * k));
+    LG_CUDA(dw.reserve((size_t)nb * k));
+    cudaError_t e = lg_launch_core_batch_fp64(ctx, nb, ctx->d_boff.p, ctx->d_bhx.p, ctx->d_brdi.p,
+                                              ctx->d_bdep.p, ctx->d_brloc.p, dt.p, dw.p);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(trans, dt.p, sizeof(double) * nb * k * k, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(w, dw.p, sizeof(double) * nb * k, cudaMemcpyDeviceToHost, ctx->stream);
+    unsigned st = 0;
+    unsigned long long cnt2[LG_CNT_N];
+    rc = (e == cudaSuccess) ? read_status(ctx, st, cnt2) : LETKF_ERR_CUDA;
+    cudaStreamSynchronize(ctx->stream);
+    dt.release();
+    dw.release();
+    // the per-cube counts of the last run were overwritten
+    ctx->have_run = false;
+    if (e != cudaSuccess) return set_err(ctx, LETKF_ERR_CUDA, cudaGetErrorString(e));
+    if (rc) return rc;
+    if (st & LG_ST_NOT_CONV)
+        return set_err(ctx, LETKF_ERR_NOT_CONVERGED, "an eigensolve reached its sweep limit");
+    return LETKF_OK;
+}
+
+int letkf_gpu_get_stats(letkf_ctx *ctx, letkf_stats *stats)
+{
+    if (!ctx || !stats) return LETKF_ERR_INVALID;
+    *stats = ctx->stats;
+    return LETKF_OK;
+}
+
+const char *letkf_gpu_last_error(letkf_ctx *ctx)
+{
+    return ctx ? ctx->last_error.c_str() : "no context";
+}
+
+int letkf_gpu_destroy(letkf_ctx *ctx)
+{
+    if (!ctx) return LETKF_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->own_stream) cudaStreamSynchronize(ctx->own_stream);
+    DevBuf<float> *fb[] = {&ctx->d_glat, &ctx->d_glon, &ctx->d_rinvf, &ctx->d_brdi};
+    for (auto *b : fb) b->release();
+    DevBuf<double> *db[] = {&ctx->d_hyai, &ctx->d_hybi, &ctx->d_xb, &ctx->d_axb, &ctx->d_xa,
+                            &ctx->d_axa, &ctx->d_olat, &ctx->d_olon, &ctx->d_oph, &ctx->d_oyo,
+                            &ctx->d_orinv, &ctx->d_yb, &ctx->d_dep, &ctx->d_os, &ctx->d_oc,
+                            &ctx->d_oyr, &ctx->d_lrloc, &ctx->d_trans, &ctx->d_w, &ctx->d_bhx,
+                            &ctx->d_bdep, &ctx->d_brloc};
+    for (auto *b : db) b->release();
+    ctx->d_olev.release();
+    ctx->d_ovar.release();
+    ctx->d_lcnt.release();
+    ctx->d_lidx.release();
+    ctx->d_loff.release();
+    ctx->d_boff.release();
+    ctx->d_oxyz.release();
+    ctx->d_bxyz.release();
+    ctx->d_obucket.release();
+    ctx->d_bcount.release();
+    ctx->d_bstart.release();
+    ctx->d_bidx.release();
+    ctx->d_status.release();
+    ctx->d_counters.release();
+    for (int i = 0; i < 8; i++)
+        if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
+    if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+    delete ctx;
+    return LETKF_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Fortran-callable shims (one context per process).
+
+static letkf_ctx *g_fctx = nullptr;
+static std::vector<double> g_olat, g_olon, g_oph, g_oyo, g_orinv;
+static std::vector<int32_t> g_olev, g_ovar;
+static std::vector<double> g_xb, g_axb, g_xa, g_axa;
+
+void letkf_init_gpu_(const int *nlat, const int *nlon, const int *nz, const int *nvar2d,
+                     const int *nvar3d, const int *ens, const float *lat, const float *lon,
+                     const double *hyai, const double *hybi, const double *p0,
+                     const double *ptop, const int *ps_row, const double *loc_dist_km,
+                     const double *vert_dist, const double *inflation,
+                     const double *obs_polar_deg, const int *gc_filter,
+                     const int *gc_filter_vertical, const int *cube_n, const int *cube_nz,
+                     const int *overlap, const int *h_mode, const int *precision, int *ierr)
+{
+    if (g_fctx) {
+        letkf_gpu_destroy(g_fctx);
+        g_fctx = nullptr;
+    }
+    letkf_grid g{};
+    g.nlat = *nlat;
+    g.nlon = *nlon;
+    g.nz = *nz;
+    g.nvar2d = *nvar2d;
+    g.nvar3d = *nvar3d;
+    g.ens = *ens;
+    g.lat = lat;
+    g.lon = lon;
+    g.hyai = hyai;
+    g.hybi = hybi;
+    g.p0 = *p0;
+    g.ptop = *ptop;
+    g.ps_row = *ps_row - 1;   // Fortran ps_indx is 1-based
+    letkf_params p{};
+    p.loc_dist_km = *loc_dist_km;
+    p.vert_dist = *vert_dist;
+    p.inflation = *inflation;
+    p.obs_polar_deg = *obs_polar_deg;
+    p.gc_filter = *gc_filter;
+    p.gc_filter_vertical = *gc_filter_vertical;
+    p.max_obs = 10000;
+    p.cube_n = *cube_n;
+    p.cube_nz = *cube_nz;
+    p.overlap = *overlap;
+    p.h_mode = *h_mode;
+    p.precision = *precision;
+    *ierr = letkf_gpu_create(&g_fctx, &g, &p, -1);
+}
+
+void letkf_set_obs_gpu_(const int64_t *nobs, const double *lat, const double *lon, const double *ph,
+                        const int *lev, const int *var, const double *yo, const double *rinv,
+                        int *ierr)
+{
+    const int64_t n = *nobs;
+    if (n < 0) {
+        *ierr = LETKF_ERR_INVALID;
+        return;
+    }
+    g_olat.assign(lat, lat + n);
+    g_olon.assign(lon, lon + n);
+    g_oph.assign(ph, ph + n);
+    g_oyo.assign(yo, yo + n);
+    g_orinv.assign(rinv, rinv + n);
+    g_olev.assign(lev, lev + n);
+    g_ovar.resize(n);
+    for (int64_t i = 0; i < n; i++) g_ovar[i] = var[i] - 1;
+    *ierr = LETKF_OK;
+}
+
+void letkf_run_gpu_(const int *ntimes, const int *halo, const double *xb, const double *axb,
+                    double *xa, double *axa, int *ierr)
+{
+    (void)ntimes;
+    if (!g_fctx) {
+        *ierr = LETKF_ERR_STATE;
+        return;
+    }
+    const int h = *halo, nlat = g_fctx->nlat, nlon = g_fctx->nlon, n = g_fctx->n, k = g_fctx->k;
+    const int64_t lath = nlat + 2 * h;
+    const size_t ncol = (size_t)nlat * nlon;
+    g_xb.resize(ncol * n * k);
+    g_axb.resize(ncol * n);
+    g_xa.resize(ncol * n * k);
+    g_axa.resize(ncol * n);
+    // strip the halo: xb(ens, n, 1-h:nlat+h, 1-h:nlon+h)
+    for (int i = 0; i < nlon; i++)
+        for (int j = 0; j < nlat; j++) {
+            const int64_t src = (int64_t)(j + h) + lath * (i + h);
+            const size_t dst = (size_t)j + (size_t)nlat * i;
+            std::memcpy(&g_xb[dst * n * k], xb + src * n * k, sizeof(double) * n * k);
+            std::memcpy(&g_axb[dst * n], axb + src * n, sizeof(double) * n);
+        }
+    letkf_obs o{};
+    o.nobs = (int64_t)g_olat.size();
+    o.lat = g_olat.data();
+    o.lon = g_olon.data();
+    o.ph = g_oph.data();
+    o.lev = g_olev.data();
+    o.var = g_ovar.data();
+    o.yo = g_oyo.data();
+    o.rinv = g_orinv.data();
+    *ierr = letkf_gpu_run(g_fctx, g_xb.data(), g_axb.data(), &o, g_xa.data(), g_axa.data(),
+                          LETKF_HOST_PTRS);
+    if (*ierr != LETKF_OK && *ierr != LETKF_ERR_NOT_CONVERGED) return;
+    for (int i = 0; i < nlon; i++)
+        for (int j = 0; j < nlat; j++) {
+            const int64_t dst = (int64_t)(j + h) + lath * (i + h);
+            const size_t src = (size_t)j + (size_t)nlat * i;
+            std::memcpy(xa + dst * n * k, &g_xa[src * n * k], sizeof(double) * n * k);
+            std::memcpy(axa + dst * n, &g_axa[src * n], sizeof(double) * n);
+        }
+}
+
+void letkf_final_gpu_(int *ierr)
+{
+    *ierr = letkf_gpu_destroy(g_fctx);
+    g_fctx = nullptr;
+}
+
+}  // extern "C"

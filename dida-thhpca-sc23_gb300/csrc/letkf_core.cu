@@ -1,0 +1,428 @@
+// letkf_core.cu -- FP64 per-cube LETKF core fused with the ensemble update.
+//
+// Reference: letkf_core (code/x86/TradDA/DA/LETKF/src/letkf_core.F90:14-233) and
+// xb_2_xa (letkf_compute.F90:231-301), called per cube by
+// letkf_compute_nooverlap (letkf_compute.F90:12-126).  One CTA per cube:
+//
+//   A' = (k-1)/rho I + Yhat Yhat^T,  Yhat = Y diag(sqrt(rdiaginv*rloc))
+//        (lower-triangle 4x4 register tiles, obs rows staged in shared memory)
+//   g  = Yhat (sqrt(rdiaginv*rloc) .* dep)
+//   eigendecomposition of the SPD A' by one-sided (Hestenes) Jacobi on its
+//        columns with a parallel round-robin pair ordering; for an SPD matrix
+//        the converged columns are w_j = lambda_j v_j, so no separate
+//        eigenvector matrix is kept
+//   T  = sqrt(k-1) A'^(-1/2)   = sum_j sqrt((k-1)/lambda_j)/lambda_j^2 w_j w_j^T
+//   wb = A'^(-1) g             = sum_j (w_j.g)/lambda_j^3 w_j
+//   trans = T + wb 1^T         (letkf_core.F90:221-225)
+//   xa = trans^T xb + axb, then the mean is recomputed and removed.
+//
+// The reference forms Pa and the k x p matrix Pa*Yhat^T (:129-195); the
+// products here are the same quantities in O(k p + k^3) instead of O(k^2 p).
+#include "letkf_internal.cuh"
+
+namespace {
+
+constexpr int kT = LG_THREADS;
+
+template <int K>
+struct Cfg {
+    static constexpr int KB = K / 4;
+    static constexpr int NBLK = KB * (KB + 1) / 2;            // lower 4x4 blocks
+    static constexpr int MB = (NBLK + kT - 1) / kT;            // blocks per thread
+    static constexpr int NPAIR = K / 2;
+    static constexpr int G = (NPAIR * 16 <= kT) ? 16 : (NPAIR * 8 <= kT) ? 8 : 4;  // threads per pair
+    static constexpr int CH = (K <= 64) ? 64 : (K <= 96 ? 48 : 32);                // staged rows
+    static constexpr int NO = (CH * K + kT - 1) / kT;          // update outputs per thread
+    static constexpr size_t SMEM = sizeof(double) * (size_t)(K * K + CH * K + 5 * K + 2 * CH);
+};
+
+// Where the rows of a cube's local problem come from.
+struct RowSrc {
+    bool batch;
+    // analysis run: global obs arrays + local lists
+    const double *yb, *dep;
+    const float *rinvf;
+    const int32_t *lidx;
+    const double *lrloc;
+    // batched core: packed per-problem rows
+    const double *hx, *bdep, *brloc;
+    const float *brdi;
+};
+
+__device__ __forceinline__ void decode_block(int b, int &bi, int &bj)
+{
+    int i = (int)((sqrtf(8.0f * (float)b + 1.0f) - 1.0f) * 0.5f);
+    while ((i + 1) * (i + 2) / 2 <= b) i++;
+    while (i * (i + 1) / 2 > b) i--;
+    bi = i;
+    bj = b - i * (i + 1) / 2;
+}
+
+// One-sided Jacobi on the columns of W (column j at W[j*K ..]).  Returns the
+// sweeps used, or max_sweeps+1 if not converged.
+template <int K>
+__device__ int jacobi_fp64(double *W, double *nrm, int *s_rot, double tol, int max_sweeps)
+{
+    constexpr int NP = Cfg<K>::NPAIR, G = Cfg<K>::G;
+    const int tid = threadIdx.x;
+    const int pair = tid / G, lane = tid % G;
+    const bool act = pair < NP;
+    int sweep;
+    for (sweep = 1; sweep <= max_sweeps; sweep++) {
+        if (tid < K) {
+            double s = 0.0;
+            for (int r = 0; r < K; r++) s += W[tid * K + r] * W[tid * K + r];
+            nrm[tid] = s;
+        }
+        if (tid == 0) *s_rot = 0;
+        __syncthreads();
+        for (int r = 0; r < K - 1; r++) {
+            if (act) {
+                int p, q;
+                if (pair == 0) {
+                    p = K - 1;
+                    q = r;
+                } else {
+                    p = (r + pair) % (K - 1);
+                    q = (r - pair + (K - 1)) % (K - 1);
+                }
+                double *wp = W + p * K, *wq = W + q * K;
+                double gam = 0.0;
+#pragma unroll
+                for (int rr = lane; rr < K; rr += G) gam += wp[rr] * wq[rr];
+#pragma unroll
+                for (int o = G / 2; o > 0; o >>= 1) gam += __shfl_xor_sync(0xffffffffu, gam, o);
+                const double al = nrm[p], be = nrm[q];
+                if (fabs(gam) > tol * sqrt(al * be)) {
+                    const double zeta = (be - al) / (2.0 * gam);
+                    const double t = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+                    const double c = 1.0 / sqrt(1.0 + t * t);
+                    const double s = c * t;
+#pragma unroll
+                    for (int rr = lane; rr < K; rr += G) {
+                        const double a = wp[rr], b = wq[rr];
+                        wp[rr] = c * a - s * b;
+                        wq[rr] = s * a + c * b;
+                    }
+                    if (lane == 0) {
+                        nrm[p] = al - t * gam;
+                        nrm[q] = be + t * gam;
+                        *s_rot = 1;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+        const int rot = *s_rot;
+        __syncthreads();
+        if (!rot) break;
+    }
+    return sweep;
+}
+
+template <int K>
+__global__ void __launch_bounds__(kT)
+k_core_fp64(LgGrid g, LgParams prm, RowSrc src, const int64_t *__restrict__ loff,
+            const int32_t *__restrict__ lcnt, int64_t ncubes, const double *__restrict__ xb,
+            const double *__restrict__ axb, double *__restrict__ xa, double *__restrict__ axa,
+            double *__restrict__ trans_out, double *__restrict__ w_out,
+            unsigned long long *__restrict__ counters, unsigned *__restrict__ status)
+{
+    using C = Cfg<K>;
+    constexpr int MB = C::MB, CH = C::CH;
+    extern __shared__ double sm[];
+    double *W = sm;                    // K*K: A', Jacobi columns, then trans (row-major [i][e])
+    double *S = W + K * K;             // CH*K staging
+    double *gv = S + CH * K;           // K
+    double *nrm = gv + K;              // K
+    double *fco = nrm + K;             // K
+    double *hco = fco + K;             // K
+    double *wbar = hco + K;            // K
+    double *sd = wbar + K;             // CH
+    double *scl = sd + CH;             // CH
+    __shared__ int s_rot;
+
+    const int tid = threadIdx.x;
+    int bi[MB], bj[MB];
+    bool bok[MB];
+#pragma unroll
+    for (int m = 0; m < MB; m++) {
+        const int b = tid + m * kT;
+        bok[m] = b < C::NBLK;
+        decode_block(bok[m] ? b : 0, bi[m], bj[m]);
+    }
+
+    for (int64_t cube = blockIdx.x; cube < ncubes; cube += gridDim.x) {
+        const int64_t off = loff[cube];
+        const int p = lcnt[cube];
+
+        // ---- A = Yhat Yhat^T (lower blocks), g = Yhat (s .* dep)
+        double acc[MB][16];
+#pragma unroll
+        for (int m = 0; m < MB; m++)
+#pragma unroll
+            for (int i = 0; i < 16; i++) acc[m][i] = 0.0;
+        double gacc = 0.0;
+        for (int s0 = 0; s0 < p; s0 += CH) {
+            const int cnt = min(CH, p - s0);
+            if (tid < cnt) {
+                const int64_t li = off + s0 + tid;
+                double rdi, rl, d;
+                if (src.batch) {
+                    rdi = (double)src.brdi[li];
+                    rl = src.brloc[li];
+                    d = src.bdep[li];
+                } else {
+                    const int gi = src.lidx[li];
+                    rdi = (double)src.rinvf[gi];
+                    rl = src.lrloc[li];
+                    d = src.dep[gi];
+                }
+                const double sc = sqrt(rdi * rl);     // rrloc (letkf_core.F90:64-66)
+                scl[tid] = sc;
+                sd[tid] = sc * d;
+            }
+            __syncthreads();
+            for (int idx = tid; idx < cnt * K; idx += kT) {
+                const int o = idx / K, e = idx - o * K;
+                const int64_t li = off + s0 + o;
+                const double *row = src.batch ? src.hx + li * K : src.yb + (int64_t)src.lidx[li] * K;
+                S[o * K + e] = row[e] * scl[o];
+            }
+            __syncthreads();
+            if (tid < K)
+                for (int o = 0; o < cnt; o++) gacc += S[o * K + tid] * sd[o];
+            for (int o = 0; o < cnt; o++) {
+                const double *ro = S + o * K;
+#pragma unroll
+                for (int m = 0; m < MB; m++) {
+                    if (!bok[m]) continue;
+                    const double2 a01 = *reinterpret_cast<const double2 *>(ro + 4 * bi[m]);
+                    const double2 a23 = *reinterpret_cast<const double2 *>(ro + 4 * bi[m] + 2);
+                    const double2 b01 = *reinterpret_cast<const double2 *>(ro + 4 * bj[m]);
+                    const double2 b23 = *reinterpret_cast<const double2 *>(ro + 4 * bj[m] + 2);
+                    const double a[4] = {a01.x, a01.y, a23.x, a23.y};
+                    const double b[4] = {b01.x, b01.y, b23.x, b23.y};
+#pragma unroll
+                    for (int i = 0; i < 4; i++)
+#pragma unroll
+                        for (int j = 0; j < 4; j++) acc[m][i * 4 + j] += a[i] * b[j];
+                }
+            }
+            __syncthreads();
+        }
+#pragma unroll
+        for (int m = 0; m < MB; m++) {
+            if (!bok[m]) continue;
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const int r = 4 * bi[m] + i, c = 4 * bj[m] + j;
+                    W[c * K + r] = acc[m][i * 4 + j];
+                    W[r * K + c] = acc[m][i * 4 + j];
+                }
+        }
+        if (tid < K) gv[tid] = gacc;
+        __syncthreads();
+        if (tid < K) W[tid * K + tid] += (double)(K - 1) / prm.inflation;
+        __syncthreads();
+
+        // ---- eigendecomposition of A'
+        const int sweeps = jacobi_fp64<K>(W, nrm, &s_rot, 1e-15, 40);
+        if (tid == 0) {
+            atomicMax(&counters[LG_CNT_MAXSWEEP], (unsigned long long)sweeps);
+            if (sweeps > 40) {
+                atomicAdd(&counters[LG_CNT_NOTCONV], 1ull);
+                atomicOr(status, LG_ST_NOT_CONV);
+            }
+        }
+        if (tid < K) {
+            double s = 0.0, dot = 0.0;
+            for (int r = 0; r < K; r++) {
+                const double wv = W[tid * K + r];
+                s += wv * wv;
+                dot += wv * gv[r];
+            }
+            const double lam = sqrt(s);
+            fco[tid] = sqrt((double)(K - 1) / lam) / (lam * lam);
+            hco[tid] = dot / (lam * lam * lam);
+        }
+        __syncthreads();
+        if (tid < K) {
+            double s = 0.0;
+            for (int j = 0; j < K; j++) s += hco[j] * W[j * K + tid];
+            wbar[tid] = s;
+        }
+        // ---- T = sum_j f_j w_j w_j^T (lower blocks)
+#pragma unroll
+        for (int m = 0; m < MB; m++)
+#pragma unroll
+            for (int i = 0; i < 16; i++) acc[m][i] = 0.0;
+        for (int j = 0; j < K; j++) {
+            const double *wj = W + j * K;
+            const double f = fco[j];
+#pragma unroll
+            for (int m = 0; m < MB; m++) {
+                if (!bok[m]) continue;
+                const double2 a01 = *reinterpret_cast<const double2 *>(wj + 4 * bi[m]);
+                const double2 a23 = *reinterpret_cast<const double2 *>(wj + 4 * bi[m] + 2);
+                const double2 b01 = *reinterpret_cast<const double2 *>(wj + 4 * bj[m]);
+                const double2 b23 = *reinterpret_cast<const double2 *>(wj + 4 * bj[m] + 2);
+                const double a[4] = {a01.x, a01.y, a23.x, a23.y};
+                const double b[4] = {b01.x * f, b01.y * f, b23.x * f, b23.y * f};
+#pragma unroll
+                for (int i = 0; i < 4; i++)
+#pragma unroll
+                    for (int jj = 0; jj < 4; jj++) acc[m][i * 4 + jj] += a[i] * b[jj];
+            }
+        }
+        __syncthreads();
+        // trans(i, e) = T(i, e) + wbar(i), stored row-major Tr[i*K + e]
+#pragma unroll
+        for (int m = 0; m < MB; m++) {
+            if (!bok[m]) continue;
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+#pragma unroll
+                for (int j = 0; j < 4; j++) {
+                    const int r = 4 * bi[m] + i, c = 4 * bj[m] + j;
+                    const double v = acc[m][i * 4 + j];
+                    W[r * K + c] = v + wbar[r];
+                    W[c * K + r] = v + wbar[c];
+                }
+        }
+        __syncthreads();
+        if (trans_out) {
+            for (int idx = tid; idx < K * K; idx += kT) {
+                const int i = idx % K, j = idx / K;       // column-major (i, j)
+                trans_out[cube * K * K + idx] = W[i * K + j];
+            }
+            if (tid < K) w_out[cube * K + tid] = wbar[tid];
+        }
+        if (xb == nullptr) {
+            __syncthreads();
+            continue;
+        }
+
+        // ---- xa = trans^T xb + axb for every column of the cube, then mean removal
+        const int n = g.n;
+        const int bjc = (int)(cube % prm.nbj), bic = (int)(cube / prm.nbj);
+        const int sj = bjc * prm.cube_n, ej = min(sj + prm.cube_n - 1, g.nlat - 1);
+        const int si = bic * prm.cube_n, ei = min(si + prm.cube_n - 1, g.nlon - 1);
+        for (int ii = si; ii <= ei; ii++)
+            for (int jj = sj; jj <= ej; jj++) {
+                const int64_t c = jj + (int64_t)g.nlat * ii;
+                const double *xbc = xb + c * n * K;
+                double *xac = xa + c * n * K;
+                for (int r0 = 0; r0 < n; r0 += CH) {
+                    const int R = min(CH, n - r0);
+                    for (int idx = tid; idx < R * K; idx += kT) S[idx] = xbc[(int64_t)r0 * K + idx];
+                    __syncthreads();
+                    double out[C::NO];
+#pragma unroll
+                    for (int q = 0; q < C::NO; q++) {
+                        const int idx = tid + q * kT;
+                        out[q] = 0.0;
+                        if (idx < R * K) {
+                            const int rl = idx / K, e = idx - rl * K;
+                            const double *xr = S + rl * K;
+                            double a = 0.0;
+#pragma unroll 8
+                            for (int i = 0; i < K; i++) a += W[i * K + e] * xr[i];
+                            out[q] = a + axb[c * n + r0 + rl];
+                        }
+                    }
+                    __syncthreads();
+#pragma unroll
+                    for (int q = 0; q < C::NO; q++) {
+                        const int idx = tid + q * kT;
+                        if (idx < R * K) S[idx] = out[q];
+                    }
+                    __syncthreads();
+                    if (tid < R) {
+                        double m = 0.0;
+                        for (int e = 0; e < K; e++) m += S[tid * K + e];
+                        m = m / K;
+                        sd[tid] = m;
+                        axa[c * n + r0 + tid] = m;
+                    }
+                    __syncthreads();
+                    for (int idx = tid; idx < R * K; idx += kT)
+                        xac[(int64_t)r0 * K + idx] = S[idx] - sd[idx / K];
+                    __syncthreads();
+                }
+            }
+    }
+}
+
+template <int K>
+cudaError_t launch_k(letkf_ctx *ctx, const LgGrid &g, const RowSrc &src, const int64_t *loff,
+                     const int32_t *lcnt, int64_t ncubes, const double *xb, const double *axb,
+                     double *xa, double *axa, double *trans_out, double *w_out)
+{
+    const size_t smem = Cfg<K>::SMEM;
+    cudaError_t e = cudaFuncSetAttribute(k_core_fp64<K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    if (ncubes <= 0) return cudaSuccess;
+    const unsigned blocks = (unsigned)(ncubes < (1 << 30) ? ncubes : (1 << 30));
+    lg_count_launch();
+    k_core_fp64<K><<<blocks, kT, smem, ctx->stream>>>(g, lg_params(ctx), src, loff, lcnt, ncubes, xb,
+                                                      axb, xa, axa, trans_out, w_out,
+                                                      ctx->d_counters.p, ctx->d_status.p);
+    return cudaGetLastError();
+}
+
+cudaError_t dispatch(letkf_ctx *ctx, const LgGrid &g, const RowSrc &src, const int64_t *loff,
+                     const int32_t *lcnt, int64_t ncubes, const double *xb, const double *axb,
+                     double *xa, double *axa, double *trans_out, double *w_out)
+{
+    switch (g.k) {
+    case 32: return launch_k<32>(ctx, g, src, loff, lcnt, ncubes, xb, axb, xa, axa, trans_out, w_out);
+    case 48: return launch_k<48>(ctx, g, src, loff, lcnt, ncubes, xb, axb, xa, axa, trans_out, w_out);
+    case 64: return launch_k<64>(ctx, g, src, loff, lcnt, ncubes, xb, axb, xa, axa, trans_out, w_out);
+    case 96: return launch_k<96>(ctx, g, src, loff, lcnt, ncubes, xb, axb, xa, axa, trans_out, w_out);
+    case 128: return launch_k<128>(ctx, g, src, loff, lcnt, ncubes, xb, axb, xa, axa, trans_out, w_out);
+    case 8: return launch_k<8>(ctx, g, src, loff, lcnt, ncubes, xb, axb, xa, axa, trans_out, w_out);
+    case 16: return launch_k<16>(ctx, g, src, loff, lcnt, ncubes, xb, axb, xa, axa, trans_out, w_out);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+}  // namespace
+
+bool lg_core_supports(int k)
+{
+    return k == 8 || k == 16 || k == 32 || k == 48 || k == 64 || k == 96 || k == 128;
+}
+
+cudaError_t lg_launch_core_fp64(letkf_ctx *ctx, const LgGrid &g, const double *xb,
+                                const double *axb, double *xa, double *axa, bool keep_trans)
+{
+    RowSrc src{};
+    src.batch = false;
+    src.yb = ctx->d_yb.p;
+    src.dep = ctx->d_dep.p;
+    src.rinvf = ctx->d_rinvf.p;
+    src.lidx = ctx->d_lidx.p;
+    src.lrloc = ctx->d_lrloc.p;
+    return dispatch(ctx, g, src, ctx->d_loff.p, ctx->d_lcnt.p, ctx->ncubes, xb, axb, xa, axa,
+                    keep_trans ? ctx->d_trans.p : nullptr, keep_trans ? ctx->d_w.p : nullptr);
+}
+
+cudaError_t lg_launch_core_batch_fp64(letkf_ctx *ctx, int64_t nb, const int64_t *d_off,
+                                      const double *d_hx, const float *d_rdi,
+                                      const double *d_dep, const double *d_rloc,
+                                      double *d_trans, double *d_w)
+{
+    RowSrc src{};
+    src.batch = true;
+    src.hx = d_hx;
+    src.brdi = d_rdi;
+    src.bdep = d_dep;
+    src.brloc = d_rloc;
+    LgGrid g = lg_grid(ctx);
+    return dispatch(ctx, g, src, d_off, ctx->d_lcnt.p, nb, nullptr, nullptr, nullptr, nullptr,
+                    d_trans, d_w);
+}

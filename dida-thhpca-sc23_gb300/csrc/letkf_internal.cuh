@@ -1,0 +1,216 @@
+// letkf_internal.cuh -- shared definitions of the GB300 LETKF kernels and host code.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "letkf_gpu.h"
+
+// ---------------------------------------------------------------------------
+// Constants of the reference's distance and localization functions.
+// pi = atan(1.0)*4 in single precision (code/x86/TradDA/DA/utils/pro_info.F90:156),
+// a = 6371.393 as a default-real literal (pro_info.F90:148), and the
+// default-real literals of schr2 (DA/LETKF/src/letkf_yb.F90:256-261), all
+// promoted to double exactly as the Fortran promotes them.
+#define LG_PI_F32 3.1415927410125732421875
+#define LG_EARTH_A 6371.39306640625
+#define LG_GC_C1 1.66666698455810546875
+#define LG_GC_C2 0.666666686534881591796875
+
+#define LG_THREADS 256          // threads of the per-cube kernels
+#define LG_MAX_ENS 128          // largest ensemble the kernels are built for
+
+// Status bits written by kernels into ctx->d_status.
+#define LG_ST_BAD_OBS      1u   // obs outside the grid / bad variable or level
+#define LG_ST_LIST_FULL    2u   // local-list storage too small
+#define LG_ST_NOT_CONV     4u   // an eigensolve hit its sweep limit
+#define LG_ST_SEGMENTS     8u   // a cap needed more bucket segments than the search holds
+
+// Counters in ctx->d_counters.
+enum {
+    LG_CNT_CURSOR = 0,    // list allocation cursor
+    LG_CNT_SUMP,
+    LG_CNT_MAXP,
+    LG_CNT_TRUNC,
+    LG_CNT_BORDER,
+    LG_CNT_NOTCONV,
+    LG_CNT_MAXSWEEP,
+    LG_CNT_N
+};
+
+// ---------------------------------------------------------------------------
+// Exact-arithmetic helpers: every operation rounded separately (no fused
+// multiply-add), matching the left-to-right evaluation of the Fortran source.
+__device__ __forceinline__ double lg_rad(double deg)
+{
+    return __dmul_rn(__ddiv_rn(deg, 180.0), LG_PI_F32);
+}
+
+// schr2, DA/LETKF/src/letkf_yb.F90:245-269.  NaN fails every test -> 1.0.
+__device__ __forceinline__ double lg_schr2(double ri)
+{
+    if (ri > 2.0) return 0.0;
+    if (ri > 1.0) {
+        double rj = __dsub_rn(__ddiv_rn(ri, 12.0), 0.5);
+        rj = __dadd_rn(__dmul_rn(rj, ri), 0.625);
+        rj = __dadd_rn(__dmul_rn(rj, ri), LG_GC_C1);
+        return __dsub_rn(__dadd_rn(__dmul_rn(__dsub_rn(__dmul_rn(rj, ri), 5.0), ri), 4.0),
+                         __ddiv_rn(LG_GC_C2, ri));
+    }
+    if (ri > 0.0) {
+        double rk = __dmul_rn(ri, ri);
+        double rj = __dadd_rn(__dmul_rn(__dadd_rn(__dmul_rn(-0.25, ri), 0.5), ri), 0.625);
+        return __dadd_rn(__dmul_rn(__dsub_rn(__dmul_rn(rj, ri), LG_GC_C1), rk), 1.0);
+    }
+    return 1.0;
+}
+
+// schr (box-car), letkf_yb.F90:270-285.
+__device__ __forceinline__ double lg_schr(double ri) { return (ri > 2.0) ? 0.0 : 1.0; }
+
+// latlon_dist_r8 (pro_info.F90:149-161) with sin/cos of both latitudes and
+// the longitudes in radians precomputed: a*acos(min(c1*c2*cos(y1-y2)+s1*s2, 1)).
+__device__ __forceinline__ double lg_dist(double s1, double c1, double y1r,
+                                          double s2, double c2, double y2r)
+{
+    double v = __dadd_rn(__dmul_rn(__dmul_rn(c1, c2), cos(__dsub_rn(y1r, y2r))),
+                         __dmul_rn(s1, s2));
+    if (v > 1.0) v = 1.0;
+    return __dmul_rn(LG_EARTH_A, acos(v));
+}
+
+// ri = obs_dist * 1d0 / local_dist (letkf_yb.F90:89)
+__device__ __forceinline__ double lg_ri(double dist, double local_dist)
+{
+    return __ddiv_rn(__dmul_rn(dist, 1.0), local_dist);
+}
+
+// ---------------------------------------------------------------------------
+// Device-side parameter blocks passed by value to kernels.
+struct LgGrid {
+    int nlat, nlon, nz, nvar2d, nvar3d, k, n;
+    int ps_row;
+    double p0, ptop;
+    const float *glat;    // nlat+1 (last = 90)
+    const float *glon;    // nlon+1 (last = 360)
+    const double *hyai, *hybi;
+};
+
+struct LgParams {
+    double local_dist, vert_dist, inflation, obs_polar;
+    int gc_filter, gc_filter_vertical, max_obs, cube_n, cube_nz, overlap, h_mode, precision;
+    int nbj, nbi;         // cube counts along lat and lon
+};
+
+// Lat-lon bucket grid of the observations.
+struct LgBuckets {
+    int nblat, nblon;
+    double cell_deg;
+    const int *start;     // nblat*nblon+1
+    const int *idx;       // obs index, bucket order
+    const float4 *xyz;    // unit vector (x, y, z) and obs index bits, bucket order
+};
+
+// Per-obs precomputed search data (original order).
+struct LgObsGeo {
+    const double *s, *c, *yr;   // sin, cos of latitude, longitude in radians
+};
+
+// ---------------------------------------------------------------------------
+// Grow-only device buffer.
+template <typename T>
+struct DevBuf {
+    T *p = nullptr;
+    size_t n = 0;
+    cudaError_t reserve(size_t count)
+    {
+        if (count <= n && p) return cudaSuccess;
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+        size_t bytes = (count ? count : 1) * sizeof(T);
+        cudaError_t e = cudaMalloc((void **)&p, bytes);
+        if (e == cudaSuccess) n = count ? count : 1;
+        return e;
+    }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+};
+
+struct letkf_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaStream_t own_stream = nullptr;
+    letkf_params params{};
+    int nlat = 0, nlon = 0, nz = 0, nvar2d = 0, nvar3d = 0, k = 0, n = 0, ps_row = 0;
+    double p0 = 0, ptop = 0;
+    int64_t ncol = 0, ncubes = 0;
+    int nbj = 0, nbi = 0;
+    bool have_hybrid = false;
+
+    DevBuf<float> d_glat, d_glon;
+    DevBuf<double> d_hyai, d_hybi;
+    DevBuf<double> d_xb, d_axb, d_xa, d_axa;          // host-pointer runs
+    // observations
+    DevBuf<double> d_olat, d_olon, d_oph, d_oyo, d_orinv;
+    DevBuf<int32_t> d_olev, d_ovar;
+    DevBuf<double> d_yb, d_dep;
+    DevBuf<float> d_rinvf;
+    DevBuf<double> d_os, d_oc, d_oyr;
+    DevBuf<float4> d_oxyz;
+    DevBuf<int> d_obucket;
+    // bucket grid
+    int nblat = 0, nblon = 0;
+    double cell_deg = 1.0;
+    DevBuf<int> d_bcount, d_bstart, d_bidx;
+    DevBuf<float4> d_bxyz;
+    // local lists
+    DevBuf<int64_t> d_loff;
+    DevBuf<int32_t> d_lcnt;
+    DevBuf<int32_t> d_lidx;
+    DevBuf<double> d_lrloc;
+    int64_t list_cap = 0;
+    // per-cube results
+    DevBuf<double> d_trans, d_w;
+    // core_batch staging
+    DevBuf<double> d_bhx, d_bdep, d_brloc;
+    DevBuf<float> d_brdi;
+    DevBuf<int64_t> d_boff;
+    // status
+    DevBuf<unsigned int> d_status;
+    DevBuf<unsigned long long> d_counters;
+    int64_t last_nobs = -1;
+    bool have_run = false;
+
+    cudaEvent_t ev[8] = {};
+    letkf_stats stats{};
+    std::string last_error;
+};
+
+// ---------------------------------------------------------------------------
+// Launch counting (every kernel launch of this library goes through it).
+void lg_count_launch();
+
+// Kernel launchers (letkf_prep.cu, letkf_search.cu, letkf_core.cu).
+cudaError_t lg_launch_obs_prepare(letkf_ctx *ctx, const LgGrid &g, const double *xb,
+                                  const double *axb, int64_t nobs, const double *olat,
+                                  const double *olon, const double *oph, const int32_t *olev,
+                                  const int32_t *ovar, const double *oyo, const double *orinv);
+cudaError_t lg_launch_buckets(letkf_ctx *ctx, int64_t nobs);
+cudaError_t lg_launch_search(letkf_ctx *ctx, const LgGrid &g, int64_t nobs);
+cudaError_t lg_launch_core_fp64(letkf_ctx *ctx, const LgGrid &g, const double *xb,
+                                const double *axb, double *xa, double *axa, bool keep_trans);
+cudaError_t lg_launch_core_batch_fp64(letkf_ctx *ctx, int64_t nb, const int64_t *d_off,
+                                      const double *d_hx, const float *d_rdi,
+                                      const double *d_dep, const double *d_rloc,
+                                      double *d_trans, double *d_w);
+
+LgGrid lg_grid(letkf_ctx *ctx);
+LgParams lg_params(letkf_ctx *ctx);

@@ -1,0 +1,275 @@
+// letkf_prep.cu -- observation operator H on all members, mean removal, and
+// the lat-lon bucket grid of the observations.
+//
+// Reference: gen_obs_struct (code/x86/TradDA/DA/LETKF/src/letkf_obs.F90:16-182)
+// with find_obs_grid (:187-243), ps2ph_3d_interp and obs_interpolation_3d_2
+// (obs_make.F90:233-381).  One warp per observation; lanes stride over the
+// members, so every state read is a contiguous run of the member-fastest
+// state (coalesced), and the ensemble mean is a warp-shuffle reduction.
+#include "letkf_internal.cuh"
+
+namespace {
+
+// First 1-based index i (1..m) with (double)g[i-1] >= x, 0 if none.  g is
+// ascending, so the binary search returns the linear scan's answer.
+__device__ __forceinline__ int first_ge(const float *g, int m, double x)
+{
+    int lo = 0, hi = m;
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if ((double)g[mid] >= x) hi = mid; else lo = mid + 1;
+    }
+    return (lo < m) ? lo + 1 : 0;
+}
+
+struct Corners {
+    int64_t c11, c21, c12, c22;   // (lat tx-1, lon ty-1), (tx, ty-1), (tx-1, ty), (tx, ty)
+    double t1, t2;
+};
+
+// Bilinear value of (xb + axb) for member e at row r (obs_make.F90:285-294).
+__device__ __forceinline__ double bilin(const double *__restrict__ xb, const double *__restrict__ axb,
+                                        int n, int k, const Corners &q, int r, int e)
+{
+    const double v11 = xb[(q.c11 * n + r) * k + e] + axb[q.c11 * n + r];
+    const double v21 = xb[(q.c21 * n + r) * k + e] + axb[q.c21 * n + r];
+    const double v12 = xb[(q.c12 * n + r) * k + e] + axb[q.c12 * n + r];
+    const double v22 = xb[(q.c22 * n + r) * k + e] + axb[q.c22 * n + r];
+    const double r1 = v11 * q.t1 + v21 * (1.0 - q.t1);
+    const double r2 = v12 * q.t1 + v22 * (1.0 - q.t1);
+    return r1 * q.t2 + r2 * (1.0 - q.t2);
+}
+
+__device__ __forceinline__ double ph_interface(const LgGrid &g, int i, double ps)
+{
+    return g.hyai[i] * (g.p0 - g.ptop) + g.hybi[i] * (ps - g.ptop) + g.ptop;
+}
+
+__device__ __forceinline__ double ph_mid(const LgGrid &g, int i /* 0-based level */, double ps)
+{
+    return 0.5 * (ph_interface(g, i, ps) + ph_interface(g, i + 1, ps));
+}
+
+__global__ void __launch_bounds__(256)
+k_obs_prepare(LgGrid g, LgParams prm, const double *__restrict__ xb, const double *__restrict__ axb,
+              int64_t nobs, const double *__restrict__ olat, const double *__restrict__ olon,
+              const double *__restrict__ oph, const int32_t *__restrict__ olev,
+              const int32_t *__restrict__ ovar, const double *__restrict__ oyo,
+              const double *__restrict__ orinv, double *__restrict__ yb, double *__restrict__ dep,
+              float *__restrict__ rinvf, double *__restrict__ os, double *__restrict__ oc,
+              double *__restrict__ oyr, float4 *__restrict__ oxyz, int *__restrict__ obucket,
+              int nblat, int nblon, double cell_deg, unsigned *status)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int k = g.k, n = g.n;
+
+    for (int64_t o = warp; o < nobs; o += nwarps) {
+        const double lat = olat[o], lon = olon[o];
+        const int v = ovar[o];
+        const bool is3d = v >= g.nvar2d;
+        int lev = 1;
+        bool ok = (lat >= -90.0 && lat <= 90.0 && lon >= 0.0 && lon <= 360.0 &&
+                   v >= 0 && v < g.nvar2d + g.nvar3d);
+        if (ok && is3d && prm.h_mode == 1) {
+            lev = olev[o];
+            ok = lev >= 1 && lev <= g.nz;
+        }
+        if (ok && is3d && prm.h_mode == 0) ok = oph[o] > 0.0;
+        if (!ok) {
+            for (int e = lane; e < k; e += 32) yb[o * k + e] = 0.0;
+            if (lane == 0) {
+                dep[o] = 0.0;
+                rinvf[o] = 0.0f;
+                obucket[o] = -1;
+                atomicOr(status, LG_ST_BAD_OBS);
+            }
+            continue;
+        }
+        // find_obs_grid (letkf_obs.F90:199-241); the spacing is a float difference
+        const int tx = first_ge(g.glat, g.nlat + 1, lat);
+        const int ty = first_ge(g.glon, g.nlon + 1, lon);
+        double ax = 0.0, ay = 0.0;
+        if (tx > 1) {
+            const double dlat = (double)(g.glat[tx - 1] - g.glat[tx - 2]);
+            ax = (dlat - lat + (double)g.glat[tx - 2]) / dlat;
+        }
+        if (ty > 1) {
+            const double dlon = (double)(g.glon[ty - 1] - g.glon[ty - 2]);
+            ay = (dlon - lon + (double)g.glon[ty - 2]) / dlon;
+        }
+        Corners q;
+        {
+            // rows beyond the poles clamp, columns wrap around the circle
+            const int la0 = min(max(tx - 2, 0), g.nlat - 1), la1 = min(max(tx - 1, 0), g.nlat - 1);
+            const int lo0 = ((ty - 2) % g.nlon + g.nlon) % g.nlon, lo1 = (ty - 1) % g.nlon;
+            q.c11 = la0 + (int64_t)g.nlat * lo0;
+            q.c21 = la1 + (int64_t)g.nlat * lo0;
+            q.c12 = la0 + (int64_t)g.nlat * lo1;
+            q.c22 = la1 + (int64_t)g.nlat * lo1;
+            q.t1 = ax;
+            q.t2 = ay;
+        }
+        const int start = is3d ? g.nvar2d + (v - g.nvar2d) * g.nz : v;
+        double sum = 0.0;
+        double yv[LG_MAX_ENS / 32];
+#pragma unroll
+        for (int j = 0; j < LG_MAX_ENS / 32; j++) {
+            const int e = lane + 32 * j;
+            double y = 0.0;
+            if (e < k) {
+                if (!is3d) {
+                    y = bilin(xb, axb, n, k, q, start, e);
+                } else if (prm.h_mode == 1) {
+                    y = bilin(xb, axb, n, k, q, start + lev - 1, e);
+                } else {
+                    // member's pressure profile, level search, log-p interpolation
+                    const double ps = bilin(xb, axb, n, k, q, g.ps_row, e);
+                    const double p_obs = oph[o];
+                    int jl = 1;
+                    while (jl <= g.nz && p_obs > ph_mid(g, jl - 1, ps)) jl++;
+                    const int pos = jl - 1;
+                    if (pos >= 1 && pos < g.nz) {
+                        const int tl = start + pos - 1;
+                        const double pa = ph_mid(g, pos, ps), pb = ph_mid(g, pos - 1, ps);
+                        const double t3 = (log(pa) - log(p_obs)) / (log(pa) - log(pb));
+                        const double r1 = bilin(xb, axb, n, k, q, tl, e);
+                        const double r3 = bilin(xb, axb, n, k, q, tl + 1, e);
+                        y = r1 * t3 + r3 * (1.0 - t3);
+                    } else {
+                        const int tl = (pos == 0) ? start : start + g.nz - 1;
+                        y = bilin(xb, axb, n, k, q, tl, e);
+                    }
+                }
+                sum += y;
+            }
+            yv[j] = y;
+        }
+#pragma unroll
+        for (int s = 16; s > 0; s >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, s);
+        const double mean = sum / (double)k;
+#pragma unroll
+        for (int j = 0; j < LG_MAX_ENS / 32; j++) {
+            const int e = lane + 32 * j;
+            if (e < k) yb[o * k + e] = yv[j] - mean;
+        }
+        if (lane == 0) {
+            dep[o] = oyo[o] - mean;
+            rinvf[o] = (float)orinv[o];
+            const double xr = lg_rad(lat), yr = lg_rad(lon);
+            const double s = sin(xr), c = cos(xr);
+            os[o] = s;
+            oc[o] = c;
+            oyr[o] = yr;
+            oxyz[o] = make_float4((float)(c * cos(yr)), (float)(c * sin(yr)), (float)s,
+                                  __int_as_float((int)o));
+            int b = -1;
+            if (fabs(lat) <= prm.obs_polar) {
+                int bl = (int)floor((lat + 90.0) / cell_deg);
+                int bn = (int)floor(lon / cell_deg);
+                bl = min(max(bl, 0), nblat - 1);
+                bn = min(max(bn, 0), nblon - 1);
+                b = bl * nblon + bn;
+            }
+            obucket[o] = b;
+        }
+    }
+}
+
+__global__ void k_bucket_count(int64_t nobs, const int *__restrict__ obucket, int *__restrict__ count)
+{
+    for (int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; o < nobs;
+         o += (int64_t)gridDim.x * blockDim.x) {
+        const int b = obucket[o];
+        if (b >= 0) atomicAdd(&count[b], 1);
+    }
+}
+
+// Exclusive scan of n counts into out[0..n] with one block of 1024 threads.
+__global__ void __launch_bounds__(1024) k_scan_exclusive(const int *__restrict__ in, int *__restrict__ out, int n)
+{
+    __shared__ int part[1024];
+    const int t = threadIdx.x;
+    const int per = (n + 1023) / 1024;
+    const int b = min(n, t * per), e = min(n, b + per);
+    int s = 0;
+    for (int i = b; i < e; i++) s += in[i];
+    part[t] = s;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {
+        int v = (t >= off) ? part[t - off] : 0;
+        __syncthreads();
+        part[t] += v;
+        __syncthreads();
+    }
+    int run = part[t] - s;
+    for (int i = b; i < e; i++) {
+        out[i] = run;
+        run += in[i];
+    }
+    if (t == 1023) out[n] = part[1023];
+}
+
+__global__ void k_bucket_fill(int64_t nobs, const int *__restrict__ obucket, const int *__restrict__ start,
+                              int *__restrict__ cursor, const float4 *__restrict__ oxyz,
+                              int *__restrict__ bidx, float4 *__restrict__ bxyz)
+{
+    for (int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; o < nobs;
+         o += (int64_t)gridDim.x * blockDim.x) {
+        const int b = obucket[o];
+        if (b < 0) continue;
+        const int pos = start[b] + atomicAdd(&cursor[b], 1);
+        bidx[pos] = (int)o;
+        bxyz[pos] = oxyz[o];
+    }
+}
+
+int grid_for(int64_t work, int threads, int cap)
+{
+    int64_t b = (work + threads - 1) / threads;
+    if (b < 1) b = 1;
+    if (b > cap) b = cap;
+    return (int)b;
+}
+
+}  // namespace
+
+cudaError_t lg_launch_obs_prepare(letkf_ctx *ctx, const LgGrid &g, const double *xb,
+                                  const double *axb, int64_t nobs, const double *olat,
+                                  const double *olon, const double *oph, const int32_t *olev,
+                                  const int32_t *ovar, const double *oyo, const double *orinv)
+{
+    if (nobs == 0) return cudaSuccess;
+    const LgParams prm = lg_params(ctx);
+    const int blocks = grid_for(nobs * 32, 256, 152 * 64);
+    lg_count_launch();
+    k_obs_prepare<<<blocks, 256, 0, ctx->stream>>>(
+        g, prm, xb, axb, nobs, olat, olon, oph, olev, ovar, oyo, orinv, ctx->d_yb.p, ctx->d_dep.p,
+        ctx->d_rinvf.p, ctx->d_os.p, ctx->d_oc.p, ctx->d_oyr.p, ctx->d_oxyz.p, ctx->d_obucket.p,
+        ctx->nblat, ctx->nblon, ctx->cell_deg, ctx->d_status.p);
+    return cudaGetLastError();
+}
+
+cudaError_t lg_launch_buckets(letkf_ctx *ctx, int64_t nobs)
+{
+    const int nb = ctx->nblat * ctx->nblon;
+    cudaError_t e = cudaMemsetAsync(ctx->d_bcount.p, 0, sizeof(int) * nb, ctx->stream);
+    if (e != cudaSuccess) return e;
+    if (nobs > 0) {
+        lg_count_launch();
+        k_bucket_count<<<grid_for(nobs, 256, 152 * 16), 256, 0, ctx->stream>>>(nobs, ctx->d_obucket.p,
+                                                                          ctx->d_bcount.p);
+    }
+    lg_count_launch();
+    k_scan_exclusive<<<1, 1024, 0, ctx->stream>>>(ctx->d_bcount.p, ctx->d_bstart.p, nb);
+    e = cudaMemsetAsync(ctx->d_bcount.p, 0, sizeof(int) * nb, ctx->stream);
+    if (e != cudaSuccess) return e;
+    if (nobs > 0) {
+        lg_count_launch();
+        k_bucket_fill<<<grid_for(nobs, 256, 152 * 16), 256, 0, ctx->stream>>>(
+            nobs, ctx->d_obucket.p, ctx->d_bstart.p, ctx->d_bcount.p, ctx->d_oxyz.p, ctx->d_bidx.p,
+            ctx->d_bxyz.p);
+    }
+    return cudaGetLastError();
+}

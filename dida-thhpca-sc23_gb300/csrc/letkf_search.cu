@@ -1,0 +1,292 @@
+// letkf_search.cu -- localized observation search over the bucket grid.
+//
+// Reference: gen_yb_dis (code/x86/TradDA/DA/LETKF/src/letkf_yb.F90:3-133).  For
+// every cube centre the reference scans all candidate obs in canonical order,
+// keeps an obs iff |lat| <= obs_polar and gc = schr2(dist/c) > 0, and stops at
+// MAX_OBS.  Here one CTA handles one cube:
+//   1. it visits only the buckets that intersect the cap of radius 2c (plus
+//      the few buckets at the antipode, where rounding can make acos return
+//      NaN and schr2(NaN) = 1 keeps the obs, as in the reference);
+//   2. a float chord-length test classifies candidates that are clearly
+//      inside or outside (a 1e-3 relative margin around 2c); only candidates
+//      in the margin get the reference's double-precision formula;
+//   3. kept obs indices are sorted in shared memory (bitonic), which restores
+//      canonical order, and cut at max_obs (if more are kept than shared
+//      memory holds, a threshold search finds the max_obs-th smallest index);
+//   4. the localization weight of every kept obs is computed with the
+//      reference's double formula and the list is written at a slot reserved
+//      with one atomic add.
+#include <climits>
+
+#include "letkf_internal.cuh"
+
+namespace {
+
+constexpr int kMaxSeg = 128;
+constexpr int kThreads = 256;
+
+struct Seg {
+    int b, e, exact;   // [b, e) in bucket order; exact: skip the float prefilter
+};
+
+struct CubeGeo {
+    double s2, c2, y2r;      // centre sin/cos latitude, longitude (rad)
+    float cx, cy, cz;        // centre unit vector
+    float lo2, hi2;          // chord^2 thresholds: below lo2 keep, above hi2 drop
+};
+
+__device__ __forceinline__ void add_lon_range(Seg *seg, int &ns, const LgBuckets &bk, int band,
+                                              double lon0, double lon1, int exact)
+{
+    const int nbl = bk.nblon;
+    const int base = band * nbl;
+    int j0 = (int)floor(lon0 / bk.cell_deg), j1 = (int)floor(lon1 / bk.cell_deg);
+    if (j1 - j0 + 1 >= nbl) {
+        if (ns < kMaxSeg) seg[ns++] = {bk.start[base], bk.start[base + nbl], exact};
+        return;
+    }
+    auto add = [&](int a, int b) {
+        if (a > b) return;
+        if (ns < kMaxSeg) seg[ns++] = {bk.start[base + a], bk.start[base + b + 1], exact};
+    };
+    if (j0 < 0) {
+        add(j0 + nbl, nbl - 1);
+        add(0, j1);
+    } else if (j1 >= nbl) {
+        add(j0, nbl - 1);
+        add(0, j1 - nbl);
+    } else {
+        add(j0, j1);
+    }
+}
+
+// Classify one candidate; returns true if kept.  Counts borderline pairs.
+__device__ __forceinline__ bool keep_candidate(const float4 &p, int exact, const CubeGeo &cg,
+                                               const LgObsGeo &geo, const LgParams &prm,
+                                               unsigned long long *border)
+{
+    if (!exact) {
+        const float dx = p.x - cg.cx, dy = p.y - cg.cy, dz = p.z - cg.cz;
+        const float d2 = dx * dx + dy * dy + dz * dz;
+        if (d2 > cg.hi2) return false;
+        if (d2 < cg.lo2) return true;
+    }
+    const int o = __float_as_int(p.w);
+    const double dist = lg_dist(geo.s[o], geo.c[o], geo.yr[o], cg.s2, cg.c2, cg.y2r);
+    const double ri = lg_ri(dist, prm.local_dist);
+    if (fabs(ri - 2.0) < 1e-12) atomicAdd(border, 1ull);
+    const double gc = prm.gc_filter ? lg_schr2(ri) : lg_schr(ri);
+    return gc > 0.0;
+}
+
+// One pass over all candidate segments.
+//   mode 0: append every kept index (up to cap) and count them
+//   mode 1: count kept indices below `thr`
+//   mode 2: append kept indices below `thr`
+__device__ int scan_pass(int mode, int thr, const Seg *seg, int ns, const LgBuckets &bk,
+                         const CubeGeo &cg, const LgObsGeo &geo, const LgParams &prm,
+                         int32_t *keys, int cap, int *s_count, unsigned long long *border)
+{
+    if (threadIdx.x == 0) *s_count = 0;
+    __syncthreads();
+    for (int si = 0; si < ns; si++) {
+        const Seg s = seg[si];
+        for (int i = s.b + threadIdx.x; i < s.e; i += kThreads) {
+            const float4 p = bk.xyz[i];
+            const int o = __float_as_int(p.w);
+            if (mode != 0 && o >= thr) continue;
+            if (!keep_candidate(p, s.exact, cg, geo, prm, mode == 0 ? border : nullptr)) continue;
+            const int pos = atomicAdd(s_count, 1);
+            if (mode != 1 && pos < cap) keys[pos] = o;
+        }
+    }
+    __syncthreads();
+    const int c = *s_count;
+    __syncthreads();
+    return c;
+}
+
+__device__ void bitonic_sort(int32_t *keys, int n_pow2)
+{
+    for (int k2 = 2; k2 <= n_pow2; k2 <<= 1) {
+        for (int j = k2 >> 1; j > 0; j >>= 1) {
+            for (int i = threadIdx.x; i < n_pow2; i += kThreads) {
+                const int ixj = i ^ j;
+                if (ixj > i) {
+                    const int32_t a = keys[i], b = keys[ixj];
+                    const bool up = (i & k2) == 0;
+                    if ((a > b) == up) {
+                        keys[i] = b;
+                        keys[ixj] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kThreads)
+k_search(LgGrid g, LgParams prm, LgBuckets bk, LgObsGeo geo, int64_t nobs, int cap_sort,
+         int32_t *__restrict__ lidx, double *__restrict__ lrloc, int64_t list_cap,
+         int64_t *__restrict__ loff, int32_t *__restrict__ lcnt,
+         unsigned long long *__restrict__ counters, unsigned *__restrict__ status, int64_t ncubes)
+{
+    extern __shared__ int32_t keys[];
+    __shared__ Seg seg[kMaxSeg];
+    __shared__ int s_ns, s_count;
+    __shared__ CubeGeo s_cg;
+    __shared__ long long s_off;
+
+    for (int64_t cube = blockIdx.x; cube < ncubes; cube += gridDim.x) {
+        if (threadIdx.x == 0) {
+            const int bj = (int)(cube % prm.nbj), bi = (int)(cube / prm.nbj);
+            const int sj = bj * prm.cube_n, ej = min(sj + prm.cube_n - 1, g.nlat - 1);
+            const int si = bi * prm.cube_n, ei = min(si + prm.cube_n - 1, g.nlon - 1);
+            const int cj = ((sj + 1) + (ej + 1)) / 2 - 1, ci = ((si + 1) + (ei + 1)) / 2 - 1;
+            const double clat = (double)g.glat[cj], clon = (double)g.glon[ci];
+            CubeGeo cg;
+            const double xr = lg_rad(clat);
+            cg.s2 = sin(xr);
+            cg.c2 = cos(xr);
+            cg.y2r = lg_rad(clon);
+            cg.cx = (float)(cg.c2 * cos(cg.y2r));
+            cg.cy = (float)(cg.c2 * sin(cg.y2r));
+            cg.cz = (float)cg.s2;
+            const double theta = 2.0 * prm.local_dist / LG_EARTH_A;
+            if (theta > 0.01) {
+                const double a = 2.0 * sin(0.5 * theta * (1.0 - 1e-3));
+                const double b = 2.0 * sin(0.5 * theta * (1.0 + 1e-3));
+                cg.lo2 = (float)(a * a);
+                cg.hi2 = (float)(b * b);
+            } else {
+                cg.lo2 = -1.0f;           // every candidate takes the double test
+                cg.hi2 = 1.0e30f;
+            }
+            s_cg = cg;
+            // buckets of the cap
+            int ns = 0;
+            const double deg = 180.0 / M_PI;
+            const double band = (theta + 1e-6) * deg;
+            const int b0 = max(0, (int)floor((clat - band + 90.0) / bk.cell_deg));
+            const int b1 = min(bk.nblat - 1, (int)floor((clat + band + 90.0) / bk.cell_deg));
+            const double clat_r = clat / deg;
+            bool full = true;
+            double dlon = 360.0;
+            if (fabs(clat_r) + theta + 1e-6 < M_PI / 2 - 1e-6) {
+                const double sv = sin(theta) / cos(clat_r);
+                if (sv < 1.0) {
+                    full = false;
+                    dlon = (asin(sv) + 1e-6) * deg + 1e-9;
+                }
+            }
+            for (int b = b0; b <= b1; b++) {
+                if (full) add_lon_range(seg, ns, bk, b, 0.0, 720.0, 0);
+                else add_lon_range(seg, ns, bk, b, clon - dlon, clon + dlon, 0);
+            }
+            // buckets within 1e-6 rad of the antipode
+            {
+                const double alat = -clat, alon = fmod(clon + 180.0, 360.0);
+                const double ad = 1e-6 * deg + 1e-9;
+                const int a0 = max(0, (int)floor((alat - ad + 90.0) / bk.cell_deg));
+                const int a1 = min(bk.nblat - 1, (int)floor((alat + ad + 90.0) / bk.cell_deg));
+                const double ca = cos(alat / deg);
+                for (int b = a0; b <= a1; b++) {
+                    if (ca < 1e-3) add_lon_range(seg, ns, bk, b, 0.0, 720.0, 1);
+                    else add_lon_range(seg, ns, bk, b, alon - ad / ca, alon + ad / ca, 1);
+                }
+            }
+            if (ns >= kMaxSeg) atomicOr(status, LG_ST_SEGMENTS);
+            s_ns = ns;
+        }
+        __syncthreads();
+        const int ns = s_ns;
+        const CubeGeo cg = s_cg;
+
+        int nk = scan_pass(0, 0, seg, ns, bk, cg, geo, prm, keys, cap_sort, &s_count,
+                           &counters[LG_CNT_BORDER]);
+        int nout;
+        if (nk <= cap_sort) {
+            int np2 = 1;
+            while (np2 < nk) np2 <<= 1;
+            for (int i = nk + threadIdx.x; i < np2; i += kThreads) keys[i] = INT_MAX;
+            __syncthreads();
+            bitonic_sort(keys, np2);
+            nout = min(nk, prm.max_obs);
+        } else {
+            // smallest threshold T with max_obs kept indices below it
+            int lo = 1, hi = (int)nobs;
+            while (lo < hi) {
+                const int mid = lo + (hi - lo) / 2;
+                const int c = scan_pass(1, mid, seg, ns, bk, cg, geo, prm, keys, cap_sort, &s_count,
+                                        nullptr);
+                if (c >= prm.max_obs) hi = mid; else lo = mid + 1;
+            }
+            const int c = scan_pass(2, lo, seg, ns, bk, cg, geo, prm, keys, cap_sort, &s_count,
+                                    nullptr);
+            int np2 = 1;
+            while (np2 < c) np2 <<= 1;
+            for (int i = c + threadIdx.x; i < np2; i += kThreads) keys[i] = INT_MAX;
+            __syncthreads();
+            bitonic_sort(keys, np2);
+            nout = min(c, prm.max_obs);
+        }
+        if (threadIdx.x == 0) {
+            long long off = (long long)atomicAdd(&counters[LG_CNT_CURSOR], (unsigned long long)nout);
+            if (off + nout > list_cap) {
+                atomicOr(status, LG_ST_LIST_FULL);
+                off = -1;
+            }
+            s_off = off;
+            loff[cube] = off < 0 ? 0 : off;
+            lcnt[cube] = off < 0 ? 0 : nout;
+            atomicAdd(&counters[LG_CNT_SUMP], (unsigned long long)nout);
+            atomicMax(&counters[LG_CNT_MAXP], (unsigned long long)nout);
+            if (nk > prm.max_obs) atomicAdd(&counters[LG_CNT_TRUNC], 1ull);
+        }
+        __syncthreads();
+        const long long off = s_off;
+        if (off >= 0) {
+            for (int i = threadIdx.x; i < nout; i += kThreads) {
+                const int o = keys[i];
+                const double dist = lg_dist(geo.s[o], geo.c[o], geo.yr[o], cg.s2, cg.c2, cg.y2r);
+                const double ri = lg_ri(dist, prm.local_dist);
+                lidx[off + i] = o;
+                lrloc[off + i] = prm.gc_filter ? lg_schr2(ri) : lg_schr(ri);
+            }
+        }
+        __syncthreads();
+    }
+}
+
+}  // namespace
+
+int lg_search_cap(int max_obs)
+{
+    int c = 1024;
+    while (c < max_obs) c <<= 1;
+    return c;
+}
+
+cudaError_t lg_launch_search(letkf_ctx *ctx, const LgGrid &g, int64_t nobs)
+{
+    const LgParams prm = lg_params(ctx);
+    LgBuckets bk;
+    bk.nblat = ctx->nblat;
+    bk.nblon = ctx->nblon;
+    bk.cell_deg = ctx->cell_deg;
+    bk.start = ctx->d_bstart.p;
+    bk.idx = ctx->d_bidx.p;
+    bk.xyz = ctx->d_bxyz.p;
+    LgObsGeo geo{ctx->d_os.p, ctx->d_oc.p, ctx->d_oyr.p};
+    const int cap = lg_search_cap(prm.max_obs);
+    const size_t smem = sizeof(int32_t) * cap;
+    cudaError_t e = cudaFuncSetAttribute(k_search, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const int64_t blocks = ctx->ncubes < (1 << 30) ? ctx->ncubes : (1 << 30);
+    lg_count_launch();
+    k_search<<<(unsigned)(blocks > 0 ? blocks : 1), kThreads, smem, ctx->stream>>>(
+        g, prm, bk, geo, nobs, cap, ctx->d_lidx.p, ctx->d_lrloc.p, ctx->list_cap, ctx->d_loff.p,
+        ctx->d_lcnt.p, ctx->d_counters.p, ctx->d_status.p, ctx->ncubes);
+    return cudaGetLastError();
+}

@@ -1,0 +1,326 @@
+"""Python binding of the GB300 LETKF C-ABI (include/letkf_gpu.h).
+
+Mirrors the reference's module interface (code/x86/TradDA/DA/LETKF/src/):
+``letkf_init`` (letkf_init.F90:2-98), ``letkf_run`` (letkf.F90:157-257) and
+``letkf_final`` (letkf_final.F90:1-13), with the observations passed as arrays
+instead of being read from Redis.  Every call goes to the CUDA library
+``_build/libletkf_gpu.so``; there is no CPU fallback, and loading fails with
+an error when the library or a CUDA device is missing.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_build", "libletkf_gpu.so")
+
+LETKF_OK = 0
+LETKF_ERR_INVALID = -1
+LETKF_ERR_CUDA = -2
+LETKF_ERR_ALLOC = -3
+LETKF_ERR_TIMEOUT = -4
+LETKF_ERR_NOT_CONVERGED = -5
+LETKF_ERR_UNSUPPORTED = -6
+LETKF_ERR_STATE = -7
+LETKF_HOST_PTRS = 0
+LETKF_DEVICE_PTRS = 1
+LETKF_PREC_FP64 = 0
+LETKF_PREC_MIXED = 1
+
+ERROR_NAMES = {
+    LETKF_ERR_INVALID: "LETKF_ERR_INVALID", LETKF_ERR_CUDA: "LETKF_ERR_CUDA",
+    LETKF_ERR_ALLOC: "LETKF_ERR_ALLOC", LETKF_ERR_TIMEOUT: "LETKF_ERR_TIMEOUT",
+    LETKF_ERR_NOT_CONVERGED: "LETKF_ERR_NOT_CONVERGED",
+    LETKF_ERR_UNSUPPORTED: "LETKF_ERR_UNSUPPORTED", LETKF_ERR_STATE: "LETKF_ERR_STATE",
+}
+
+EXPORTED = [
+    "letkf_gpu_create", "letkf_gpu_set_stream", "letkf_gpu_set_keep_trans", "letkf_gpu_run",
+    "letkf_gpu_synchronize", "letkf_gpu_obs_operator", "letkf_gpu_local_obs",
+    "letkf_gpu_last_trans", "letkf_gpu_core_batch", "letkf_gpu_get_stats",
+    "letkf_gpu_last_error", "letkf_gpu_destroy", "letkf_gpu_launch_count",
+    "letkf_init_gpu_", "letkf_set_obs_gpu_", "letkf_run_gpu_", "letkf_final_gpu_",
+]
+
+
+class LetkfError(RuntimeError):
+    def __init__(self, code, msg=""):
+        super().__init__(f"{ERROR_NAMES.get(code, code)}: {msg}")
+        self.code = code
+
+
+class Grid(C.Structure):
+    _fields_ = [
+        ("nlat", C.c_int), ("nlon", C.c_int), ("nz", C.c_int), ("nvar2d", C.c_int),
+        ("nvar3d", C.c_int), ("ens", C.c_int),
+        ("lat", C.POINTER(C.c_float)), ("lon", C.POINTER(C.c_float)),
+        ("hyai", C.POINTER(C.c_double)), ("hybi", C.POINTER(C.c_double)),
+        ("p0", C.c_double), ("ptop", C.c_double), ("ps_row", C.c_int),
+    ]
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("loc_dist_km", C.c_double), ("vert_dist", C.c_double), ("inflation", C.c_double),
+        ("obs_polar_deg", C.c_double), ("gc_filter", C.c_int), ("gc_filter_vertical", C.c_int),
+        ("max_obs", C.c_int), ("cube_n", C.c_int), ("cube_nz", C.c_int), ("overlap", C.c_int),
+        ("h_mode", C.c_int), ("precision", C.c_int),
+    ]
+
+
+class Obs(C.Structure):
+    _fields_ = [
+        ("nobs", C.c_int64), ("lat", C.c_void_p), ("lon", C.c_void_p), ("ph", C.c_void_p),
+        ("lev", C.c_void_p), ("var", C.c_void_p), ("yo", C.c_void_p), ("rinv", C.c_void_p),
+    ]
+
+
+class Stats(C.Structure):
+    _fields_ = [
+        ("ncubes", C.c_int64), ("sum_p", C.c_int64), ("max_p", C.c_int64),
+        ("n_truncated", C.c_int64), ("n_borderline", C.c_int64),
+        ("n_not_converged", C.c_int64), ("max_sweeps", C.c_int32), ("precision", C.c_int32),
+        ("ms_h2d", C.c_double), ("ms_obs", C.c_double), ("ms_search", C.c_double),
+        ("ms_core", C.c_double), ("ms_d2h", C.c_double), ("ms_total", C.c_double),
+    ]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH):
+    """Load the CUDA library; raises if it is missing (no fallback path)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ImportError(f"GB300 LETKF library not built: {path} (run build())")
+    L = C.CDLL(path)
+    vp, i64, i32 = C.c_void_p, C.c_int64, C.c_int
+    L.letkf_gpu_create.argtypes = [C.POINTER(vp), C.POINTER(Grid), C.POINTER(Params), i32]
+    L.letkf_gpu_set_stream.argtypes = [vp, vp]
+    L.letkf_gpu_set_keep_trans.argtypes = [vp, i32]
+    L.letkf_gpu_run.argtypes = [vp, vp, vp, C.POINTER(Obs), vp, vp, i32]
+    L.letkf_gpu_synchronize.argtypes = [vp]
+    L.letkf_gpu_obs_operator.argtypes = [vp, vp, vp, C.POINTER(Obs), vp, vp]
+    L.letkf_gpu_local_obs.argtypes = [vp, vp, vp, vp]
+    L.letkf_gpu_last_trans.argtypes = [vp, vp, i64, vp, vp]
+    L.letkf_gpu_core_batch.argtypes = [vp, i64, vp, vp, vp, vp, vp, vp, vp]
+    L.letkf_gpu_get_stats.argtypes = [vp, C.POINTER(Stats)]
+    L.letkf_gpu_last_error.argtypes = [vp]
+    L.letkf_gpu_last_error.restype = C.c_char_p
+    L.letkf_gpu_destroy.argtypes = [vp]
+    L.letkf_gpu_launch_count.restype = i64
+    _lib = L
+    return L
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+class ObsArrays:
+    """Observation arrays kept alive for one call (host numpy or device torch)."""
+
+    def __init__(self, obs: dict, device: bool = False):
+        self.device = device
+        if device:
+            import torch
+            t = {k: v.contiguous() for k, v in obs.items()}
+            self._keep = t
+            p = lambda k: (t[k].data_ptr() if k in t and t[k] is not None else None)
+            n = int(t["lat"].numel())
+        else:
+            t = {
+                "lat": _f64(obs["lat"]), "lon": _f64(obs["lon"]),
+                "ph": _f64(obs["ph"]) if obs.get("ph") is not None else None,
+                "lev": (np.ascontiguousarray(obs["lev"], dtype=np.int32)
+                        if obs.get("lev") is not None else None),
+                "var": np.ascontiguousarray(obs["var"], dtype=np.int32),
+                "yo": _f64(obs["yo"]), "rinv": _f64(obs["rinv"]),
+            }
+            self._keep = t
+            p = lambda k: _ptr(t[k])
+            n = int(t["lat"].size)
+        self.c = Obs(nobs=n, lat=p("lat"), lon=p("lon"), ph=p("ph"), lev=p("lev"),
+                     var=p("var"), yo=p("yo"), rinv=p("rinv"))
+
+
+class LetkfGPU:
+    """One analysis context (grid + namelist parameters) on one GPU."""
+
+    def __init__(self, glat, glon, nz, ens, *, nvar2d=1, nvar3d=3, hyai=None, hybi=None,
+                 p0=1.0e5, ptop=219.4, ps_row=0, loc_dist_km, inflation, vert_dist=-999.0,
+                 obs_polar_deg=91.0, gc_filter=1, gc_filter_vertical=1, max_obs=10000,
+                 cube_n=1, cube_nz=1, overlap=0, h_mode=1, precision=LETKF_PREC_FP64, device=0):
+        L = load_library()
+        self._glat = np.ascontiguousarray(glat, dtype=np.float32)
+        self._glon = np.ascontiguousarray(glon, dtype=np.float32)
+        self._hyai = None if hyai is None else _f64(hyai)
+        self._hybi = None if hybi is None else _f64(hybi)
+        g = Grid(nlat=self._glat.size, nlon=self._glon.size, nz=nz, nvar2d=nvar2d, nvar3d=nvar3d,
+                 ens=ens, lat=self._glat.ctypes.data_as(C.POINTER(C.c_float)),
+                 lon=self._glon.ctypes.data_as(C.POINTER(C.c_float)),
+                 hyai=(None if self._hyai is None else self._hyai.ctypes.data_as(C.POINTER(C.c_double))),
+                 hybi=(None if self._hybi is None else self._hybi.ctypes.data_as(C.POINTER(C.c_double))),
+                 p0=p0, ptop=ptop, ps_row=ps_row)
+        prm = Params(loc_dist_km=loc_dist_km, vert_dist=vert_dist, inflation=inflation,
+                     obs_polar_deg=obs_polar_deg, gc_filter=gc_filter,
+                     gc_filter_vertical=gc_filter_vertical, max_obs=max_obs, cube_n=cube_n,
+                     cube_nz=cube_nz, overlap=overlap, h_mode=h_mode, precision=precision)
+        h = C.c_void_p()
+        rc = L.letkf_gpu_create(C.byref(h), C.byref(g), C.byref(prm), device)
+        if rc != LETKF_OK:
+            raise LetkfError(rc, "letkf_gpu_create")
+        self.h = h
+        self.L = L
+        self.nlat, self.nlon, self.nz, self.k = self._glat.size, self._glon.size, nz, ens
+        self.n = nvar2d + nvar3d * nz
+        self.cube_n = cube_n
+        self.ncubes = (-(-self.nlat // cube_n)) * (-(-self.nlon // cube_n))
+
+    @classmethod
+    def from_workload(cls, w, **kw):
+        args = dict(nvar2d=w.nvar2d, nvar3d=w.nvar3d, hyai=w.hyai, hybi=w.hybi, p0=w.p0,
+                    ptop=w.ptop, ps_row=w.ps_row, loc_dist_km=w.loc_dist_km,
+                    inflation=w.inflation, obs_polar_deg=w.obs_polar, gc_filter=w.gc_filter,
+                    max_obs=w.max_obs, h_mode=w.h_mode)
+        args.update(kw)
+        return cls(w.glat, w.glon, w.nz, w.k, **args)
+
+    def _check(self, rc, what):
+        if rc != LETKF_OK:
+            msg = self.L.letkf_gpu_last_error(self.h)
+            raise LetkfError(rc, f"{what}: {msg.decode() if msg else ''}")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.letkf_gpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_stream(self, stream_handle: int | None):
+        self._check(self.L.letkf_gpu_set_stream(self.h, stream_handle), "set_stream")
+
+    def keep_trans(self, keep: bool = True):
+        self._check(self.L.letkf_gpu_set_keep_trans(self.h, int(keep)), "set_keep_trans")
+
+    def run(self, xb, axb, obs, xa=None, axa=None, allow_not_converged=False):
+        """Host arrays in, host arrays out (letkf_run)."""
+        xb = _f64(xb)
+        axb = _f64(axb)
+        xa = np.empty_like(xb) if xa is None else xa
+        axa = np.empty_like(axb) if axa is None else axa
+        o = obs if isinstance(obs, ObsArrays) else ObsArrays(obs)
+        rc = self.L.letkf_gpu_run(self.h, _ptr(xb), _ptr(axb), C.byref(o.c), _ptr(xa), _ptr(axa),
+                                  LETKF_HOST_PTRS)
+        if not (allow_not_converged and rc == LETKF_ERR_NOT_CONVERGED):
+            self._check(rc, "letkf_gpu_run")
+        return xa, axa
+
+    def run_device(self, xb, axb, obs: ObsArrays, xa, axa):
+        """Device tensors (torch, this GPU) in and out."""
+        rc = self.L.letkf_gpu_run(self.h, xb.data_ptr(), axb.data_ptr(), C.byref(obs.c),
+                                  xa.data_ptr(), axa.data_ptr(), LETKF_DEVICE_PTRS)
+        self._check(rc, "letkf_gpu_run")
+
+    def obs_operator(self, xb, axb, obs):
+        xb = _f64(xb)
+        axb = _f64(axb)
+        o = obs if isinstance(obs, ObsArrays) else ObsArrays(obs)
+        yb = np.empty((o.c.nobs, self.k))
+        dep = np.empty(o.c.nobs)
+        self._check(self.L.letkf_gpu_obs_operator(self.h, _ptr(xb), _ptr(axb), C.byref(o.c),
+                                                  _ptr(yb), _ptr(dep)), "obs_operator")
+        return yb, dep
+
+    def local_obs(self):
+        off = np.zeros(self.ncubes + 1, dtype=np.int64)
+        self._check(self.L.letkf_gpu_local_obs(self.h, _ptr(off), None, None), "local_obs")
+        idx = np.empty(max(int(off[-1]), 1), dtype=np.int32)
+        rloc = np.empty(max(int(off[-1]), 1))
+        self._check(self.L.letkf_gpu_local_obs(self.h, _ptr(off), _ptr(idx), _ptr(rloc)), "local_obs")
+        return off, idx[:off[-1]], rloc[:off[-1]]
+
+    def last_trans(self, cubes):
+        cubes = np.ascontiguousarray(cubes, dtype=np.int64)
+        tr = np.empty((cubes.size, self.k, self.k))
+        w = np.empty((cubes.size, self.k))
+        self._check(self.L.letkf_gpu_last_trans(self.h, _ptr(cubes), cubes.size, _ptr(tr), _ptr(w)),
+                    "last_trans")
+        # stored column-major: tr[b].T[i, j] = trans(i+1, j+1)
+        return np.ascontiguousarray(np.transpose(tr, (0, 2, 1))), w
+
+    def core_batch(self, offsets, hxens, rdiaginv, dep, rloc):
+        offsets = np.ascontiguousarray(offsets, dtype=np.int64)
+        nb = offsets.size - 1
+        hx = _f64(hxens)
+        rd = np.ascontiguousarray(rdiaginv, dtype=np.float32)
+        dp = _f64(dep)
+        rl = _f64(rloc)
+        tr = np.empty((nb, self.k, self.k))
+        w = np.empty((nb, self.k))
+        self._check(self.L.letkf_gpu_core_batch(self.h, nb, _ptr(offsets), _ptr(hx), _ptr(rd),
+                                                _ptr(dp), _ptr(rl), _ptr(tr), _ptr(w)), "core_batch")
+        return np.ascontiguousarray(np.transpose(tr, (0, 2, 1))), w
+
+    def stats(self) -> dict:
+        s = Stats()
+        self._check(self.L.letkf_gpu_get_stats(self.h, C.byref(s)), "get_stats")
+        return s.as_dict()
+
+
+def launch_count() -> int:
+    return int(load_library().letkf_gpu_launch_count())
+
+
+# ---- module interface of the reference (letkf_init / letkf_run / letkf_final)
+
+_module_ctx: LetkfGPU | None = None
+_module_obs = None
+
+
+def letkf_init(glat, glon, nz, ens, **kw):
+    """letkf_init: build the analysis context (grid, namelist knobs)."""
+    global _module_ctx
+    letkf_final()
+    _module_ctx = LetkfGPU(glat, glon, nz, ens, **kw)
+    return _module_ctx
+
+
+def letkf_set_obs(obs: dict):
+    """Stage the observations of the next letkf_run (replaces the Redis read)."""
+    global _module_obs
+    _module_obs = ObsArrays(obs)
+
+
+def letkf_run(ntimes, xb, axb):
+    """letkf_run(ntimes, xb, axb) -> (xa, axa); ntimes selects the obs time in
+    the reference and is accepted for interface parity."""
+    del ntimes
+    if _module_ctx is None or _module_obs is None:
+        raise LetkfError(LETKF_ERR_STATE, "letkf_init and letkf_set_obs come first")
+    return _module_ctx.run(xb, axb, _module_obs)
+
+
+def letkf_final():
+    global _module_ctx, _module_obs
+    if _module_ctx is not None:
+        _module_ctx.close()
+    _module_ctx = None
+    _module_obs = None

@@ -1,0 +1,200 @@
+/*
+ * letkf_gpu.h -- C-ABI of the GB300 LETKF analysis.
+ *
+ * Drop-in for the reference's analysis call
+ *     letkf_init(...)                   code/x86/TradDA/DA/LETKF/src/letkf_init.F90:2-4
+ *     letkf_run(ntimes, xb, axb, xa, axa)   code/x86/TradDA/DA/LETKF/src/letkf.F90:157
+ * and, for callers that drive the steps themselves, for the reference's own
+ * C entry points of the Sunway build
+ *     letkf_core_half_c_(...)   code/sw/TradDA/DA/LETKF/src/letkf_half/letkf_core_half_master.c:24-26
+ *     letkf_yb_fast_(...)       code/sw/TradDA/DA/LETKF/src/letkf_yb/letkf_yb_master.c:9-13
+ *
+ * All arrays are plain pointers with the reference's memory order (Fortran
+ * column-major, member fastest):
+ *     column index      c = ilat + nlat * ilon
+ *     xb, xa            [c][row][member]     = xb(ens, n, lat, lon)
+ *     axb, axa          [c][row]             = axb(n, lat, lon)
+ *     state rows        2-D variables first, then each 3-D variable x nz levels
+ *                       (letkf_init.F90:63-73)
+ *     trans             column-major ens x ens per cube, trans[i + ens*j] = trans(i+1, j+1)
+ * Observations are one flat list of scalar observations in canonical order
+ * (the order in which the reference scans obs types and obs; a profile's
+ * levels and variables are consecutive entries, level-major).
+ *
+ * Every entry point returns LETKF_OK (0) or a negative LETKF_ERR_* code and
+ * never exits or prints; letkf_gpu_last_error() gives a message.  A context
+ * belongs to one host thread at a time.  There is no CPU fallback: without a
+ * usable CUDA device letkf_gpu_create fails with LETKF_ERR_CUDA.
+ */
+#ifndef LETKF_GPU_H
+#define LETKF_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define LETKF_OK                 0
+#define LETKF_ERR_INVALID       -1   /* bad argument or input value              */
+#define LETKF_ERR_CUDA          -2   /* CUDA runtime error / no device           */
+#define LETKF_ERR_ALLOC         -3   /* device or pinned allocation failed       */
+#define LETKF_ERR_TIMEOUT       -4   /* a bounded device wait ran out            */
+#define LETKF_ERR_NOT_CONVERGED -5   /* an eigensolve hit its sweep limit        */
+#define LETKF_ERR_UNSUPPORTED   -6   /* configuration not supported              */
+#define LETKF_ERR_STATE         -7   /* call order (e.g. no run yet)             */
+
+/* letkf_gpu_run flags */
+#define LETKF_HOST_PTRS    0   /* xb/axb/obs/xa/axa are host memory                */
+#define LETKF_DEVICE_PTRS  1   /* xb/axb/obs/xa/axa are device memory of this GPU */
+
+/* letkf_params.precision (the reference's computing_precision knob,
+ * da_namelist_mod.F90:49, selects the core's arithmetic the same way)       */
+#define LETKF_PREC_FP64    0   /* FP64 throughout                                  */
+#define LETKF_PREC_MIXED   1   /* BF16 hi/lo tensor-core products, FP64 eigensolve */
+
+typedef struct letkf_ctx letkf_ctx;
+
+/* Grid and state layout: the values letkf_init takes from coupler_config and
+ * pro_info (letkf_init.F90:27-73, pro_info.F90:11).                          */
+typedef struct letkf_grid {
+    int nlat, nlon;            /* global grid (one logical block)                   */
+    int nz;                    /* num_lev                                           */
+    int nvar2d, nvar3d;        /* n = nvar2d + nvar3d * nz state rows               */
+    int ens;                   /* atm_ensemble_total (k)                            */
+    const float *lat;          /* nlat cell-centre latitudes (deg, ascending)       */
+    const float *lon;          /* nlon cell-centre longitudes (deg, ascending, [0,360)) */
+    const double *hyai, *hybi; /* nz+1 hybrid coefficients; NULL allowed when h_mode
+                                  is level select and vertical localization is off  */
+    double p0, ptop;           /* hybrid reference / top pressure (Pa)              */
+    int ps_row;                /* state row of surface pressure (ps_indx)           */
+} letkf_grid;
+
+/* Namelist knobs of &namelist_da (da_namelist_mod.F90:27-49). */
+typedef struct letkf_params {
+    double loc_dist_km;        /* da_loc_distance: GC half-width c; obs kept to 2c  */
+    double vert_dist;          /* da_vert_distance; <= 0 turns vertical loc. off    */
+    double inflation;          /* da_inflation_factor                               */
+    double obs_polar_deg;      /* da_polar_letkf_lat with polar_discard, else 91    */
+    int gc_filter;             /* da_gc_enable: 1 Gaspari-Cohn, 0 box-car           */
+    int gc_filter_vertical;    /* da_gc_enable_vertical                             */
+    int max_obs;               /* MAX_OBS (letkf.F90:155): 10000                    */
+    int cube_n;                /* da_block_interval                                 */
+    int cube_nz;               /* da_vertical_interval                              */
+    int overlap;               /* da_block_overlap                                  */
+    int h_mode;                /* 0: hybrid log-p interpolation (obs_make.F90:233-381),
+                                  1: level select (obs carries a model level)       */
+    int precision;             /* LETKF_PREC_*                                      */
+} letkf_params;
+
+/* Observations (the obs_list fields, read_obs_mod.F90:15-27, flattened). */
+typedef struct letkf_obs {
+    int64_t nobs;
+    const double *lat, *lon;   /* degrees, lat in [-90,90], lon in [0,360]          */
+    const double *ph;          /* pressure (Pa): h_mode 0 and vertical loc.; may be NULL otherwise */
+    const int32_t *lev;        /* model level 1..nz for h_mode 1 (3-D variables)    */
+    const int32_t *var;        /* variable index 0..nvar2d+nvar3d-1                 */
+    const double *yo;          /* observed values                                   */
+    const double *rinv;        /* 1/sigma^2; used narrowed to float as the reference */
+} letkf_obs;
+
+/* Per-run diagnostics. */
+typedef struct letkf_stats {
+    int64_t ncubes;            /* analysis units (cubes) of the last run            */
+    int64_t sum_p;             /* total local observations over all cubes           */
+    int64_t max_p;             /* largest local observation count                   */
+    int64_t n_truncated;       /* cubes whose list stopped at max_obs               */
+    int64_t n_borderline;      /* obs-cube pairs with |dist/c - 2| < 1e-12          */
+    int64_t n_not_converged;   /* eigensolves that hit the sweep limit              */
+    int32_t max_sweeps;        /* most Jacobi sweeps any cube needed                */
+    int32_t precision;
+    double ms_h2d, ms_obs, ms_search, ms_core, ms_d2h, ms_total;  /* device-event times */
+} letkf_stats;
+
+/* Create a context on CUDA device `device` (the current device if < 0).
+ * Copies the grid; replaces letkf_init.                                      */
+int letkf_gpu_create(letkf_ctx **ctx, const letkf_grid *grid, const letkf_params *params,
+                     int device);
+
+/* Use this CUDA stream (a cudaStream_t) for all following work; NULL = the
+ * context's own stream.                                                     */
+int letkf_gpu_set_stream(letkf_ctx *ctx, void *stream);
+
+/* The analysis: letkf_run(ntimes, xb, axb, xa, axa) with the observations
+ * passed in instead of read from Redis.  xb holds perturbations and axb the
+ * mean, as run_da_parallel hands them over (module_da_parallel.F90:184-211);
+ * xa/axa receive the analysis perturbations and mean.  With
+ * LETKF_HOST_PTRS the call copies in and out and returns when xa/axa are
+ * written; with LETKF_DEVICE_PTRS it returns with the work queued on the
+ * stream (call letkf_gpu_synchronize before reading the outputs).           */
+int letkf_gpu_run(letkf_ctx *ctx, const double *xb, const double *axb, const letkf_obs *obs,
+                  double *xa, double *axa, int flags);
+
+/* Keep (1) or drop (0) every cube's trans and w of the following runs in
+ * device memory (ncubes * ens * (ens+1) doubles) for letkf_gpu_last_trans. */
+int letkf_gpu_set_keep_trans(letkf_ctx *ctx, int keep);
+
+/* Wait for the context's stream and report any deferred device error. */
+int letkf_gpu_synchronize(letkf_ctx *ctx);
+
+/* Observation operator H and mean removal only (gen_obs_struct,
+ * letkf_obs.F90:16-182): yb[obs][ens] perturbations and dep = yo - mean(H xb).
+ * Host pointers.                                                             */
+int letkf_gpu_obs_operator(letkf_ctx *ctx, const double *xb, const double *axb,
+                           const letkf_obs *obs, double *yb, double *dep);
+
+/* Local observation lists of the last run (gen_yb_dis selection,
+ * letkf_yb.F90:3-133): counts[cube] and, if idx != NULL, the obs indices in
+ * canonical order and their localization weights, packed by cube
+ * (offsets[cube] = start; ncubes+1 entries).  Host pointers.                */
+int letkf_gpu_local_obs(letkf_ctx *ctx, int64_t *offsets, int32_t *idx, double *rloc);
+
+/* Transform matrices of the last run for the listed cubes: trans (ens x ens,
+ * column-major, trans(i,j) + w(i) as letkf_core returns it) and w.          */
+int letkf_gpu_last_trans(letkf_ctx *ctx, const int64_t *cubes, int64_t ncubes,
+                         double *trans, double *w);
+
+/* Batched letkf_core (letkf_core.F90:14-233; Sunway letkf_core_batch,
+ * code/sw/TradDA/DA/LETKF/src/letkf_core.F90:16-379): for nb independent
+ * problems, problem b uses rows offsets[b]..offsets[b+1]-1 of hxens[obs][ens],
+ * rdiaginv (float, as the reference), dep and rloc.  Writes trans
+ * (nb x ens x ens, column-major each) and w (nb x ens).  Host pointers.      */
+int letkf_gpu_core_batch(letkf_ctx *ctx, int64_t nb, const int64_t *offsets,
+                         const double *hxens, const float *rdiaginv, const double *dep,
+                         const double *rloc, double *trans, double *w);
+
+int letkf_gpu_get_stats(letkf_ctx *ctx, letkf_stats *stats);
+const char *letkf_gpu_last_error(letkf_ctx *ctx);
+int letkf_gpu_destroy(letkf_ctx *ctx);
+
+/* Number of kernel launches this library made on the calling thread so far. */
+int64_t letkf_gpu_launch_count(void);
+
+/* Fortran-callable shims, by reference with a trailing underscore as the
+ * reference's own C interop (letkf_core_half_c_).  They keep one context per
+ * process.  letkf_init_gpu_ takes the grid of the whole globe; ierr receives
+ * the status code.                                                           */
+void letkf_init_gpu_(const int *nlat, const int *nlon, const int *nz, const int *nvar2d,
+                     const int *nvar3d, const int *ens, const float *lat, const float *lon,
+                     const double *hyai, const double *hybi, const double *p0,
+                     const double *ptop, const int *ps_row, const double *loc_dist_km,
+                     const double *vert_dist, const double *inflation,
+                     const double *obs_polar_deg, const int *gc_filter,
+                     const int *gc_filter_vertical, const int *cube_n, const int *cube_nz,
+                     const int *overlap, const int *h_mode, const int *precision, int *ierr);
+/* Stage the observations of the next letkf_run_gpu_ call (replaces the
+ * Redis read of gen_obs_struct).  var is 1-based as Fortran indices are.    */
+void letkf_set_obs_gpu_(const int64_t *nobs, const double *lat, const double *lon,
+                        const double *ph, const int *lev, const int *var, const double *yo,
+                        const double *rinv, int *ierr);
+/* letkf_run with the reference's halo layout: xb(ens, n, 1-halo:nlat+halo,
+ * 1-halo:nlon+halo); only the interior is read and written.                */
+void letkf_run_gpu_(const int *ntimes, const int *halo, const double *xb, const double *axb,
+                    double *xa, double *axa, int *ierr);
+void letkf_final_gpu_(int *ierr);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LETKF_GPU_H */
