@@ -307,11 +307,15 @@ int letkf_gpu_create(letkf_ctx **out, const letkf_grid *grid, const letkf_params
         std::vector<double> zero(G.nz + 1, 0.0);
         LG_CUDA(h2d(ctx->d_hyai, G.hyai ? G.hyai : zero.data(), (size_t)G.nz + 1, ctx->stream));
         LG_CUDA(h2d(ctx->d_hybi, G.hybi ? G.hybi : zero.data(), (size_t)G.nz + 1, ctx->stream));
-        // bucket cells about a third of the cut-off radius 2c
+        // bucket cells about a third of the cut-off radius 2c; the cell sizes
+        // divide 180 and 360 degrees exactly so that cell index j + nblon is
+        // longitude + 360 (the longitude ranges of a cap wrap around)
         const double radius_deg = 2.0 * P.loc_dist_km / LG_EARTH_A * 180.0 / M_PI;
-        ctx->cell_deg = std::min(10.0, std::max(0.25, radius_deg / 3.0));
-        ctx->nblat = (int)std::ceil(180.0 / ctx->cell_deg);
-        ctx->nblon = (int)std::ceil(360.0 / ctx->cell_deg);
+        const double cell = std::min(10.0, std::max(0.25, radius_deg / 3.0));
+        ctx->nblat = (int)std::ceil(180.0 / cell);
+        ctx->nblon = (int)std::ceil(360.0 / cell);
+        ctx->cell_lat = 180.0 / ctx->nblat;
+        ctx->cell_lon = 360.0 / ctx->nblon;
         const size_t nb = (size_t)ctx->nblat * ctx->nblon;
         LG_CUDA(ctx->d_bcount.reserve(nb));
         LG_CUDA(ctx->d_bstart.reserve(nb + 1));

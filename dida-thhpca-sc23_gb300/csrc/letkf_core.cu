@@ -384,6 +384,7 @@ cudaError_t dispatch(letkf_ctx *ctx, const LgGrid &g, const RowSrc &src, const i
     case 64: return launch_k<64>(ctx, g, src, loff, lcnt, ncubes, xb, axb, xa, axa, trans_out, w_out);
     case 96: return launch_k<96>(ctx, g, src, loff, lcnt, ncubes, xb, axb, xa, axa, trans_out, w_out);
     case 128: return launch_k<128>(ctx, g, src, loff, lcnt, ncubes, xb, axb, xa, axa, trans_out, w_out);
+    case 4: return launch_k<4>(ctx, g, src, loff, lcnt, ncubes, xb, axb, xa, axa, trans_out, w_out);
     case 8: return launch_k<8>(ctx, g, src, loff, lcnt, ncubes, xb, axb, xa, axa, trans_out, w_out);
     case 16: return launch_k<16>(ctx, g, src, loff, lcnt, ncubes, xb, axb, xa, axa, trans_out, w_out);
     default: return cudaErrorInvalidValue;
@@ -394,7 +395,7 @@ cudaError_t dispatch(letkf_ctx *ctx, const LgGrid &g, const RowSrc &src, const i
 
 bool lg_core_supports(int k)
 {
-    return k == 8 || k == 16 || k == 32 || k == 48 || k == 64 || k == 96 || k == 128;
+    return k == 4 || k == 8 || k == 16 || k == 32 || k == 48 || k == 64 || k == 96 || k == 128;
 }
 
 cudaError_t lg_launch_core_fp64(letkf_ctx *ctx, const LgGrid &g, const double *xb,

@@ -108,7 +108,7 @@ struct LgParams {
 // Lat-lon bucket grid of the observations.
 struct LgBuckets {
     int nblat, nblon;
-    double cell_deg;
+    double cell_lat, cell_lon;   // 180/nblat and 360/nblon degrees
     const int *start;     // nblat*nblon+1
     const int *idx;       // obs index, bucket order
     const float4 *xyz;    // unit vector (x, y, z) and obs index bits, bucket order
@@ -168,7 +168,7 @@ struct letkf_ctx {
     DevBuf<int> d_obucket;
     // bucket grid
     int nblat = 0, nblon = 0;
-    double cell_deg = 1.0;
+    double cell_lat = 1.0, cell_lon = 1.0;
     DevBuf<int> d_bcount, d_bstart, d_bidx;
     DevBuf<float4> d_bxyz;
     // local lists

@@ -58,7 +58,7 @@ k_obs_prepare(LgGrid g, LgParams prm, const double *__restrict__ xb, const doubl
               const double *__restrict__ orinv, double *__restrict__ yb, double *__restrict__ dep,
               float *__restrict__ rinvf, double *__restrict__ os, double *__restrict__ oc,
               double *__restrict__ oyr, float4 *__restrict__ oxyz, int *__restrict__ obucket,
-              int nblat, int nblon, double cell_deg, unsigned *status)
+              int nblat, int nblon, double cell_lat, double cell_lon, unsigned *status)
 {
     const int lane = threadIdx.x & 31;
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -166,8 +166,8 @@ k_obs_prepare(LgGrid g, LgParams prm, const double *__restrict__ xb, const doubl
                                   __int_as_float((int)o));
             int b = -1;
             if (fabs(lat) <= prm.obs_polar) {
-                int bl = (int)floor((lat + 90.0) / cell_deg);
-                int bn = (int)floor(lon / cell_deg);
+                int bl = (int)floor((lat + 90.0) / cell_lat);
+                int bn = (int)floor(lon / cell_lon);
                 bl = min(max(bl, 0), nblat - 1);
                 bn = min(max(bn, 0), nblon - 1);
                 b = bl * nblon + bn;
@@ -247,7 +247,7 @@ cudaError_t lg_launch_obs_prepare(letkf_ctx *ctx, const LgGrid &g, const double 
     k_obs_prepare<<<blocks, 256, 0, ctx->stream>>>(
         g, prm, xb, axb, nobs, olat, olon, oph, olev, ovar, oyo, orinv, ctx->d_yb.p, ctx->d_dep.p,
         ctx->d_rinvf.p, ctx->d_os.p, ctx->d_oc.p, ctx->d_oyr.p, ctx->d_oxyz.p, ctx->d_obucket.p,
-        ctx->nblat, ctx->nblon, ctx->cell_deg, ctx->d_status.p);
+        ctx->nblat, ctx->nblon, ctx->cell_lat, ctx->cell_lon, ctx->d_status.p);
     return cudaGetLastError();
 }
 

@@ -40,7 +40,7 @@ __device__ __forceinline__ void add_lon_range(Seg *seg, int &ns, const LgBuckets
 {
     const int nbl = bk.nblon;
     const int base = band * nbl;
-    int j0 = (int)floor(lon0 / bk.cell_deg), j1 = (int)floor(lon1 / bk.cell_deg);
+    int j0 = (int)floor(lon0 / bk.cell_lon), j1 = (int)floor(lon1 / bk.cell_lon);
     if (j1 - j0 + 1 >= nbl) {
         if (ns < kMaxSeg) seg[ns++] = {bk.start[base], bk.start[base + nbl], exact};
         return;
@@ -168,8 +168,8 @@ k_search(LgGrid g, LgParams prm, LgBuckets bk, LgObsGeo geo, int64_t nobs, int c
             int ns = 0;
             const double deg = 180.0 / M_PI;
             const double band = (theta + 1e-6) * deg;
-            const int b0 = max(0, (int)floor((clat - band + 90.0) / bk.cell_deg));
-            const int b1 = min(bk.nblat - 1, (int)floor((clat + band + 90.0) / bk.cell_deg));
+            const int b0 = max(0, (int)floor((clat - band + 90.0) / bk.cell_lat));
+            const int b1 = min(bk.nblat - 1, (int)floor((clat + band + 90.0) / bk.cell_lat));
             const double clat_r = clat / deg;
             bool full = true;
             double dlon = 360.0;
@@ -188,8 +188,8 @@ k_search(LgGrid g, LgParams prm, LgBuckets bk, LgObsGeo geo, int64_t nobs, int c
             {
                 const double alat = -clat, alon = fmod(clon + 180.0, 360.0);
                 const double ad = 1e-6 * deg + 1e-9;
-                const int a0 = max(0, (int)floor((alat - ad + 90.0) / bk.cell_deg));
-                const int a1 = min(bk.nblat - 1, (int)floor((alat + ad + 90.0) / bk.cell_deg));
+                const int a0 = max(0, (int)floor((alat - ad + 90.0) / bk.cell_lat));
+                const int a1 = min(bk.nblat - 1, (int)floor((alat + ad + 90.0) / bk.cell_lat));
                 const double ca = cos(alat / deg);
                 for (int b = a0; b <= a1; b++) {
                     if (ca < 1e-3) add_lon_range(seg, ns, bk, b, 0.0, 720.0, 1);
@@ -274,7 +274,8 @@ cudaError_t lg_launch_search(letkf_ctx *ctx, const LgGrid &g, int64_t nobs)
     LgBuckets bk;
     bk.nblat = ctx->nblat;
     bk.nblon = ctx->nblon;
-    bk.cell_deg = ctx->cell_deg;
+    bk.cell_lat = ctx->cell_lat;
+    bk.cell_lon = ctx->cell_lon;
     bk.start = ctx->d_bstart.p;
     bk.idx = ctx->d_bidx.p;
     bk.xyz = ctx->d_bxyz.p;

@@ -42,7 +42,9 @@ def compare_lists(ctx, orc):
     assert np.array_equal(off_g, off_o)
     assert np.array_equal(idx_g, idx_o)
     if rloc_o.size:
-        assert np.max(np.abs(rloc_g - rloc_o)) <= 1e-13
+        # CUDA's and glibc's cos/acos differ by ulps; acos amplifies them near
+        # zero distance (the weights themselves are <= 1)
+        assert np.max(np.abs(rloc_g - rloc_o)) <= 1e-12
     return off_o
 
 
