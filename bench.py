@@ -47,6 +47,8 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=15.0,
                     help="target CPU time of the bounded CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--grid-res", type=float, default=None,
+                    help="grid spacing override (same obs density; profiling cases)")
     return ap.parse_args()
 
 
@@ -251,7 +253,7 @@ def run_ours(args, rank, world, local_rank):
         import torch.distributed as tdist
 
     t_gen = time.perf_counter()
-    w = synthetic.config(args.config)
+    w = synthetic.config(args.config, res_deg=args.grid_res)
     t_gen = time.perf_counter() - t_gen
     ctx = letkf.LetkfGPU.from_workload(w, device=local_rank)
     stream = torch.cuda.current_stream(dev)

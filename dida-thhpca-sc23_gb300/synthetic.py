@@ -320,16 +320,17 @@ INSTANCES_3 = [  # (res_deg, k, nobs, radius_km, inflation)
 ]
 
 
-def config(cfg: int, instance: int = 0, nobs: int | None = None):
+def config(cfg: int, instance: int = 0, nobs: int | None = None, res_deg: float | None = None):
     """Workload of a benchmark configuration (0, 1, 2 and the instances of 3).
-    nobs overrides the observation count (smaller test cases)."""
+    nobs overrides the observation count and res_deg the grid spacing (smaller
+    cases with the same observation density, e.g. for profiling)."""
     seed = 1000 * cfg + instance
     if cfg == 0:
-        return generate("cfg0", 2.0, 32, 32, nobs or 20_000, 500.0, 1.1, seed)
+        return generate("cfg0", res_deg or 2.0, 32, 32, nobs or 20_000, 500.0, 1.1, seed)
     if cfg in (1, 2):
         # configuration 2 runs on configuration 1's inputs
-        return generate("cfg1", 1.0, 32, 64, nobs or 200_000, 400.0, 1.08, 1000 + instance,
-                        boxes=CLUSTER_BOX_1, box_factor=4.0)
+        return generate("cfg1", res_deg or 1.0, 32, 64, nobs or 200_000, 400.0, 1.08,
+                        1000 + instance, boxes=CLUSTER_BOX_1, box_factor=4.0)
     if cfg == 3:
         res, k, no, radius, infl = INSTANCES_3[instance]
         return generate(f"cfg3.{instance}", res, 32, k, nobs or no, radius / 2, infl, seed)
