@@ -345,11 +345,11 @@ def run_ours(args, rank, world, local_rank):
     core = statistics.mean(core_ms)
     achieved = flops / (core * 1e-3) / 1e12
     traffic = None
-    tfile = os.path.join(REPO, "profiles", "core_fp64_traffic.json")
+    tfile = os.path.join(REPO, "profiles", "core_fp64_cfg1_2deg.md")
     if os.path.exists(tfile):
-        with open(tfile) as f:
-            tr = json.load(f)
-        traffic = tr.get("bytes_per_full_launch")
+        import re
+        m = re.search(r"bytes_per_full_launch:\s*([0-9.eE+]+)", open(tfile).read())
+        traffic = float(m.group(1)) if m else None
     line = {
         "metric": METRIC, "value": value, "unit": "columns/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,

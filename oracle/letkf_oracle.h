@@ -14,6 +14,11 @@
  * Its eigensolver is a self-written cyclic Jacobi method (Golub & Van Loan,
  * Matrix Computations, 4th ed., section 8.5), standing in for MKL dsyevd.
  *
+ * Parity unpinned against the reference's own binaries: the Fortran LETKF
+ * (MKL, MPI) cannot be built here and ships no golden vectors.  The oracle is
+ * checked against closed-form known answers and against an independent
+ * numpy/LAPACK restatement (tests/golden/make_golden.py and its fixtures).
+ *
  * Data layout (identical to the reference's Fortran arrays):
  *   column index   c = ilat + nlat * ilon            (lat fastest)
  *   xb, xa         [c][row][member]  = xb(ens, n, lat, lon)
