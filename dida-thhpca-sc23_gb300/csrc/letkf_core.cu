@@ -427,3 +427,54 @@ cudaError_t lg_launch_core_batch_fp64(letkf_ctx *ctx, int64_t nb, const int64_t 
     return dispatch(ctx, g, src, d_off, ctx->d_lcnt.p, nb, nullptr, nullptr, nullptr, nullptr,
                     d_trans, d_w);
 }
+
+// Launch of the batched core with every buffer supplied by the caller
+// (letkf_noalloc.cu): problem b uses rows d_off[b] .. d_off[b] + d_cnt[b] - 1.
+namespace {
+template <int K>
+cudaError_t launch_raw(double inflation, int64_t nb, const int64_t *d_off, const int32_t *d_cnt,
+                       const RowSrc &src, double *d_trans, double *d_w,
+                       unsigned long long *counters, unsigned *status, cudaStream_t stream)
+{
+    const size_t smem = Cfg<K>::SMEM;
+    cudaError_t e = cudaFuncSetAttribute(k_core_fp64<K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    LgGrid g{};
+    g.k = K;
+    LgParams prm{};
+    prm.inflation = inflation;
+    prm.nbj = 1;
+    prm.cube_n = 1;
+    const unsigned blocks = (unsigned)(nb < (1 << 30) ? nb : (1 << 30));
+    lg_count_launch();
+    k_core_fp64<K><<<blocks, kT, smem, stream>>>(g, prm, src, d_off, d_cnt, nb, nullptr, nullptr,
+                                                 nullptr, nullptr, d_trans, d_w, counters, status);
+    return cudaGetLastError();
+}
+}  // namespace
+
+cudaError_t lg_launch_core_batch_raw(int k, double inflation, int64_t nb, const int64_t *d_off,
+                                     const int32_t *d_cnt, const double *d_hx, const float *d_rdi,
+                                     const double *d_dep, const double *d_rloc, double *d_trans,
+                                     double *d_w, unsigned long long *counters, unsigned *status,
+                                     cudaStream_t stream)
+{
+    RowSrc src{};
+    src.batch = true;
+    src.hx = d_hx;
+    src.brdi = d_rdi;
+    src.bdep = d_dep;
+    src.brloc = d_rloc;
+    switch (k) {
+    case 4: return launch_raw<4>(inflation, nb, d_off, d_cnt, src, d_trans, d_w, counters, status, stream);
+    case 8: return launch_raw<8>(inflation, nb, d_off, d_cnt, src, d_trans, d_w, counters, status, stream);
+    case 16: return launch_raw<16>(inflation, nb, d_off, d_cnt, src, d_trans, d_w, counters, status, stream);
+    case 32: return launch_raw<32>(inflation, nb, d_off, d_cnt, src, d_trans, d_w, counters, status, stream);
+    case 48: return launch_raw<48>(inflation, nb, d_off, d_cnt, src, d_trans, d_w, counters, status, stream);
+    case 64: return launch_raw<64>(inflation, nb, d_off, d_cnt, src, d_trans, d_w, counters, status, stream);
+    case 96: return launch_raw<96>(inflation, nb, d_off, d_cnt, src, d_trans, d_w, counters, status, stream);
+    case 128: return launch_raw<128>(inflation, nb, d_off, d_cnt, src, d_trans, d_w, counters, status, stream);
+    default: return cudaErrorInvalidValue;
+    }
+}

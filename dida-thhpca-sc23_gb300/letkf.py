@@ -42,6 +42,7 @@ EXPORTED = [
     "letkf_gpu_synchronize", "letkf_gpu_obs_operator", "letkf_gpu_local_obs",
     "letkf_gpu_last_trans", "letkf_gpu_core_batch", "letkf_gpu_get_stats",
     "letkf_gpu_last_error", "letkf_gpu_destroy", "letkf_gpu_launch_count",
+    "letkf_gpu_core_batch_noalloc",
     "letkf_init_gpu_", "letkf_set_obs_gpu_", "letkf_run_gpu_", "letkf_final_gpu_",
 ]
 
@@ -117,6 +118,7 @@ def load_library(path: str = LIB_PATH):
     L.letkf_gpu_last_error.restype = C.c_char_p
     L.letkf_gpu_destroy.argtypes = [vp]
     L.letkf_gpu_launch_count.restype = i64
+    L.letkf_gpu_core_batch_noalloc.argtypes = [i32, C.c_double, i64, vp, vp, vp, vp, vp, vp, vp, vp]
     _lib = L
     return L
 

@@ -163,6 +163,27 @@ int letkf_gpu_core_batch(letkf_ctx *ctx, int64_t nb, const int64_t *offsets,
                          const double *hxens, const float *rdiaginv, const double *dep,
                          const double *rloc, double *trans, double *w);
 
+/* The batched letkf_core above for callers that cannot allocate device
+ * memory (a model that owns all of the GPU's memory through its own pool, or
+ * a caller that must not add the device-wide synchronization of cudaMalloc and
+ * cudaFree).  No counterpart in the reference: it is an addition of this
+ * library.  Every pointer is device memory of the current device, owned by the
+ * caller; offsets has nb+1 entries.  No context is needed and nothing is
+ * allocated: the scratch (per-problem counts, a status word, counters) is a
+ * fixed array inside the library that every GPU which loads the library holds
+ * until the process exits, sized for at most LETKF_NOALLOC_MAX_PROBLEMS
+ * problems; larger nb returns LETKF_ERR_INVALID.  The first call on a device
+ * looks up that array's device address (make it before any stream capture).
+ * All calls share the one array, so calls that overlap on the GPU (different
+ * streams or host threads at once) race; issue them one after another.  The
+ * call waits for `stream` (a cudaStream_t, NULL = the default stream) before it
+ * returns, to report LETKF_ERR_INVALID for bad offsets and
+ * LETKF_ERR_NOT_CONVERGED from the eigensolves.                              */
+#define LETKF_NOALLOC_MAX_PROBLEMS 65536
+int letkf_gpu_core_batch_noalloc(int ens, double inflation, int64_t nb, const int64_t *offsets,
+                                 const double *hxens, const float *rdiaginv, const double *dep,
+                                 const double *rloc, double *trans, double *w, void *stream);
+
 int letkf_gpu_get_stats(letkf_ctx *ctx, letkf_stats *stats);
 const char *letkf_gpu_last_error(letkf_ctx *ctx);
 int letkf_gpu_destroy(letkf_ctx *ctx);
