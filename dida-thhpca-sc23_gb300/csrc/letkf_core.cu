@@ -33,7 +33,7 @@ struct Cfg {
     static constexpr int G = (NPAIR * 16 <= kT) ? 16 : (NPAIR * 8 <= kT) ? 8 : 4;  // threads per pair
     static constexpr int CH = (K <= 64) ? 64 : (K <= 96 ? 48 : 32);                // staged rows
     static constexpr int NO = (CH * K + kT - 1) / kT;          // update outputs per thread
-    static constexpr size_t SMEM = sizeof(double) * (size_t)(K * K + CH * K + 5 * K + 2 * CH);
+    static constexpr size_t SMEM = sizeof(double) * (size_t)(K * K + CH * K + 5 * K + 2 * CH + K);
 };
 
 // Where the rows of a cube's local problem come from.
@@ -58,15 +58,21 @@ __device__ __forceinline__ void decode_block(int b, int &bi, int &bj)
     bj = b - i * (i + 1) / 2;
 }
 
-// One-sided Jacobi on the columns of W (column j at W[j*K ..]).  Returns the
-// sweeps used, or max_sweeps+1 if not converged.
+// One-sided Jacobi on the columns of W (column j at W[j*K ..]).  Each step of
+// a sweep rotates k/2 disjoint column pairs (round-robin ordering): a group of
+// G threads forms each pair's inner product, one thread per pair turns
+// (alpha, beta, gamma) into the rotation (so the divisions and square roots
+// are done once per pair, not once per thread), and the groups rotate the
+// columns.  Returns the sweeps used, or max_sweeps+1 if not converged.
 template <int K>
-__device__ int jacobi_fp64(double *W, double *nrm, int *s_rot, double tol, int max_sweeps)
+__device__ int jacobi_fp64(double *W, double *nrm, double2 *rot, int *s_rot, double tol,
+                           int max_sweeps)
 {
     constexpr int NP = Cfg<K>::NPAIR, G = Cfg<K>::G;
     const int tid = threadIdx.x;
     const int pair = tid / G, lane = tid % G;
     const bool act = pair < NP;
+    const double tol2 = tol * tol;
     int sweep;
     for (sweep = 1; sweep <= max_sweeps; sweep++) {
         if (tid < K) {
@@ -77,8 +83,8 @@ __device__ int jacobi_fp64(double *W, double *nrm, int *s_rot, double tol, int m
         if (tid == 0) *s_rot = 0;
         __syncthreads();
         for (int r = 0; r < K - 1; r++) {
+            int p = 0, q = 0;
             if (act) {
-                int p, q;
                 if (pair == 0) {
                     p = K - 1;
                     q = r;
@@ -86,36 +92,56 @@ __device__ int jacobi_fp64(double *W, double *nrm, int *s_rot, double tol, int m
                     p = (r + pair) % (K - 1);
                     q = (r - pair + (K - 1)) % (K - 1);
                 }
-                double *wp = W + p * K, *wq = W + q * K;
+                const double *wp = W + p * K, *wq = W + q * K;
                 double gam = 0.0;
 #pragma unroll
                 for (int rr = lane; rr < K; rr += G) gam += wp[rr] * wq[rr];
 #pragma unroll
                 for (int o = G / 2; o > 0; o >>= 1) gam += __shfl_xor_sync(0xffffffffu, gam, o);
-                const double al = nrm[p], be = nrm[q];
-                if (fabs(gam) > tol * sqrt(al * be)) {
+                if (lane == 0) rot[pair].x = gam;
+            }
+            __syncthreads();
+            if (tid < NP) {
+                int pp, qq;
+                if (tid == 0) {
+                    pp = K - 1;
+                    qq = r;
+                } else {
+                    pp = (r + tid) % (K - 1);
+                    qq = (r - tid + (K - 1)) % (K - 1);
+                }
+                const double gam = rot[tid].x;
+                const double al = nrm[pp], be = nrm[qq];
+                double c = 1.0, s = 0.0;
+                if (gam * gam > tol2 * (al * be)) {
                     const double zeta = (be - al) / (2.0 * gam);
                     const double t = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-                    const double c = 1.0 / sqrt(1.0 + t * t);
-                    const double s = c * t;
+                    c = 1.0 / sqrt(1.0 + t * t);
+                    s = c * t;
+                    nrm[pp] = al - t * gam;
+                    nrm[qq] = be + t * gam;
+                    *s_rot = 1;
+                }
+                rot[tid] = make_double2(c, s);
+            }
+            __syncthreads();
+            if (act) {
+                const double2 cs = rot[pair];
+                if (cs.y != 0.0) {
+                    double *wp = W + p * K, *wq = W + q * K;
 #pragma unroll
                     for (int rr = lane; rr < K; rr += G) {
                         const double a = wp[rr], b = wq[rr];
-                        wp[rr] = c * a - s * b;
-                        wq[rr] = s * a + c * b;
-                    }
-                    if (lane == 0) {
-                        nrm[p] = al - t * gam;
-                        nrm[q] = be + t * gam;
-                        *s_rot = 1;
+                        wp[rr] = cs.x * a - cs.y * b;
+                        wq[rr] = cs.y * a + cs.x * b;
                     }
                 }
             }
             __syncthreads();
         }
-        const int rot = *s_rot;
+        const int rotated = *s_rot;
         __syncthreads();
-        if (!rot) break;
+        if (!rotated) break;
     }
     return sweep;
 }
@@ -140,6 +166,7 @@ k_core_fp64(LgGrid g, LgParams prm, RowSrc src, const int64_t *__restrict__ loff
     double *wbar = hco + K;            // K
     double *sd = wbar + K;             // CH
     double *scl = sd + CH;             // CH
+    double2 *rot = reinterpret_cast<double2 *>(scl + CH);   // K/2 rotations
     __shared__ int s_rot;
 
     const int tid = threadIdx.x;
@@ -229,7 +256,7 @@ k_core_fp64(LgGrid g, LgParams prm, RowSrc src, const int64_t *__restrict__ loff
         __syncthreads();
 
         // ---- eigendecomposition of A'
-        const int sweeps = jacobi_fp64<K>(W, nrm, &s_rot, 1e-15, 40);
+        const int sweeps = jacobi_fp64<K>(W, nrm, rot, &s_rot, 1e-15, 40);
         if (tid == 0) {
             atomicMax(&counters[LG_CNT_MAXSWEEP], (unsigned long long)sweeps);
             if (sweeps > 40) {
