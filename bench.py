@@ -47,6 +47,8 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=15.0,
                     help="target CPU time of the bounded CPU-baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--precision", choices=["both", "mixed", "fp64"], default="both",
+                    help="forms to time; the mixed form is the headline when timed")
     ap.add_argument("--grid-res", type=float, default=None,
                     help="grid spacing override (same obs density; profiling cases)")
     return ap.parse_args()
@@ -240,6 +242,56 @@ def run_reference(args, rank, world):
 
 
 # ---------------------------------------------------------------------------
+def _time_form(torch, letkf, ctx, bufs, stream, steps, warmup):
+    """Warm up, then time `steps` device-resident analyses with CUDA events."""
+    xb_d, axb_d, obs_dev, xa_d, axa_d = bufs
+    for _ in range(warmup):
+        ctx.run_device(xb_d, axb_d, obs_dev, xa_d, axa_d)
+    torch.cuda.synchronize()
+    n0 = letkf.launch_count()
+    core_ms, stages = [], []
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        ctx.run_device(xb_d, axb_d, obs_dev, xa_d, axa_d)
+        st = ctx.stats()
+        core_ms.append(st["ms_core"])
+        stages.append((st["ms_obs"], st["ms_search"], st["ms_core"]))
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return (e0.elapsed_time(e1) / steps, core_ms, stages, letkf.launch_count() - n0, ctx.stats())
+
+
+def _max_over_ranks(torch, tdist, dev, ms):
+    t = torch.tensor([ms], device=dev)
+    tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _field_errors(w, xa, axa, xa_ref, axa_ref):
+    """Relative error per state variable of the analysis mean and spread."""
+    rows = {"ps": slice(0, w.nvar2d)}
+    for i, nm in enumerate(["u", "v", "T"][: w.nvar3d]):
+        s0 = w.nvar2d + i * w.nz
+        rows[nm] = slice(s0, s0 + w.nz)
+    sp = np.sqrt(np.mean(xa * xa, axis=2))
+    sp_ref = np.sqrt(np.mean(xa_ref * xa_ref, axis=2))
+    out = {"mean": {}, "spread": {}}
+    for nm, sl in rows.items():
+        out["mean"][nm] = float(np.abs(axa[:, sl] - axa_ref[:, sl]).max() / np.abs(axa_ref[:, sl]).max())
+        out["spread"][nm] = float(np.abs(sp[:, sl] - sp_ref[:, sl]).max() / np.abs(sp_ref[:, sl]).max())
+    return out
+
+
+def mixed_fp64_flops(w, sum_p):
+    """FP64 work the mixed form does by design per analysis: g (k p), the
+    refinement (A'Xhat, Xhat E: k^3 each; S, R: k^2(k+1)/2 each), T
+    (k^2(k+1)/2), wbar (2k^2) and the mean increment (n k) multiply-adds."""
+    k, n, ncol = w.k, w.n, w.ncol
+    fma = k * sum_p + ncol * (2 * k ** 3 + 1.5 * k * k * (k + 1) + 2 * k * k + n * k)
+    return 2.0 * fma
+
+
 def run_ours(args, rank, world, local_rank):
     import torch
     dev = torch.device("cuda", local_rank)
@@ -249,60 +301,59 @@ def run_ours(args, rank, world, local_rank):
     pkg("build").build()
     letkf.load_library()
     dist = world > 1
+    tdist = None
     if dist:
         import torch.distributed as tdist
 
     t_gen = time.perf_counter()
     w = synthetic.config(args.config, res_deg=args.grid_res)
     t_gen = time.perf_counter() - t_gen
-    ctx = letkf.LetkfGPU.from_workload(w, device=local_rank)
     stream = torch.cuda.current_stream(dev)
-    ctx.set_stream(stream.cuda_stream)
+    forms = {}
+    if args.precision in ("both", "mixed"):
+        forms["mixed"] = letkf.LetkfGPU.from_workload(w, device=local_rank,
+                                                      precision=letkf.LETKF_PREC_MIXED)
+    if args.precision in ("both", "fp64"):
+        forms["fp64"] = letkf.LetkfGPU.from_workload(w, device=local_rank)
+    for ctx in forms.values():
+        ctx.set_stream(stream.cuda_stream)
+    head = "mixed" if "mixed" in forms else "fp64"
 
     # device-resident inputs
     xb_d = torch.from_numpy(w.xb).to(dev)
     axb_d = torch.from_numpy(w.axb).to(dev)
-    xa_d = torch.empty_like(xb_d)
-    axa_d = torch.empty_like(axb_d)
     o = w.obs
     obs_d = {key: torch.from_numpy(np.ascontiguousarray(o[key])).to(dev)
              for key in ("lat", "lon", "ph", "lev", "var", "yo", "rinv")}
     obs_dev = letkf.ObsArrays(obs_d, device=True)
+    outs = {nm: (torch.empty_like(xb_d), torch.empty_like(axb_d)) for nm in forms}
     torch.cuda.synchronize()
 
-    for _ in range(args.warmup):
-        ctx.run_device(xb_d, axb_d, obs_dev, xa_d, axa_d)
-    torch.cuda.synchronize()
+    gpu_uuid = str(torch.cuda.get_device_properties(dev).uuid)
+    clocks = ClockSampler(gpu_uuid if gpu_uuid.startswith("GPU-") else f"GPU-{gpu_uuid}")
+    res = {}
+    order = [nm for nm in ("fp64", "mixed") if nm in forms]
+    for nm in order:
+        if dist:
+            tdist.barrier()
+        if nm == head:
+            clocks.start()
+            time.sleep(0.3)
+        bufs = (xb_d, axb_d, obs_dev, outs[nm][0], outs[nm][1])
+        res[nm] = _time_form(torch, letkf, forms[nm], bufs, stream, args.steps, args.warmup)
+        if nm == head:
+            clk = clocks.stop()
     if dist:
+        for nm in order:
+            r = res[nm]
+            res[nm] = (_max_over_ranks(torch, tdist, dev, r[0]),) + r[1:]
         tdist.barrier()
-    gpu_uuid = torch.cuda.get_device_properties(dev).uuid
-    clocks = ClockSampler(f"GPU-{gpu_uuid}" if not str(gpu_uuid).startswith("GPU-") else str(gpu_uuid))
-    clocks.start()
-    time.sleep(0.3)
-    n0 = letkf.launch_count()
-    core_ms, stages = [], []
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    e0.record(stream)
-    for _ in range(args.steps):
-        ctx.run_device(xb_d, axb_d, obs_dev, xa_d, axa_d)
-        st = ctx.stats()
-        core_ms.append(st["ms_core"])
-        stages.append((st["ms_obs"], st["ms_search"], st["ms_core"]))
-    e1.record(stream)
-    torch.cuda.synchronize()
-    clk = clocks.stop()
-    launches = letkf.launch_count() - n0
-    ms = e0.elapsed_time(e1) / args.steps
-    if dist:
-        t = torch.tensor([ms], device=dev)
-        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-        ms = float(t.item())
-        tdist.barrier()
-    st = ctx.stats()
+    ms = res[head][0]
+    st = res[head][4]
     value = world * w.ncol / (ms * 1e-3)
 
-    # end to end through the C-ABI with pinned host buffers
+    # end to end through the C-ABI with pinned host buffers (headline form)
+    ctx = forms[head]
     xb_h = torch.empty(w.xb.shape, dtype=torch.float64, pin_memory=True)
     xb_h.numpy()[...] = w.xb
     axb_h = torch.empty(w.axb.shape, dtype=torch.float64, pin_memory=True)
@@ -322,55 +373,66 @@ def run_ours(args, rank, world, local_rank):
         tdist.barrier()
     torch.cuda.synchronize()
     f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    f0.record(stream)
     e2e_steps = max(1, min(args.steps, 3))
+    f0.record(stream)
     for _ in range(e2e_steps):
         ctx.run(xbn, axbn, obs_host, xan, axan)
     f1.record(stream)
     torch.cuda.synchronize()
     ms_e2e = f0.elapsed_time(f1) / e2e_steps
     if dist:
-        t = torch.tensor([ms_e2e], device=dev)
-        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-        ms_e2e = float(t.item())
+        ms_e2e = _max_over_ranks(torch, tdist, dev, ms_e2e)
     h2d = sum(a.nbytes for a in (xbn, axbn)) + sum(a.nbytes for a in obs_h.values())
     d2h = xan.nbytes + axan.nbytes
-    err_h = float(np.abs(xan - xa_d.cpu().numpy()).max())   # e2e and device runs agree
+    e2e_vs_device = float(np.abs(xan - outs[head][0].cpu().numpy()).max())
 
     if rank != 0:
         return
     peaks = measured_peaks()
     fp64_peak = fp64_peak_tflops(torch, dev)
     flops, nbytes = algorithmic_work(w, st["sum_p"])
-    core = statistics.mean(core_ms)
-    achieved = flops / (core * 1e-3) / 1e12
+    core = statistics.mean(res[head][1])
     traffic = None
     tfile = os.path.join(REPO, "profiles", "core_fp64_cfg1_2deg.md")
-    if os.path.exists(tfile):
+    if head == "fp64" and os.path.exists(tfile):
         import re
         m = re.search(r"bytes_per_full_launch:\s*([0-9.eE+]+)", open(tfile).read())
         traffic = float(m.group(1)) if m else None
+    if head == "mixed":
+        f64 = mixed_fp64_flops(w, st["sum_p"])
+        roof = {"bound": "fp64", "kernel": f"k_core_mixed<{w.k}>",
+                "achieved": f64 / (core * 1e-3) / 1e12, "peak": fp64_peak, "unit": "TFLOP/s",
+                "frac": f64 / (core * 1e-3) / 1e12 / fp64_peak, "traffic": traffic,
+                "work": "FP64 multiply-adds the mixed core does by design (mean increment g, "
+                        "eigen refinement, T, wbar, xb^T wbar)",
+                "fp64_flops_per_launch": f64,
+                "algorithmic_flops_per_launch": flops,
+                "algorithmic_tflops": flops / (core * 1e-3) / 1e12, "kernel_ms": core}
+    else:
+        roof = {"bound": "fp64", "kernel": f"k_core_fp64<{w.k}>",
+                "achieved": flops / (core * 1e-3) / 1e12, "peak": fp64_peak, "unit": "TFLOP/s",
+                "frac": flops / (core * 1e-3) / 1e12 / fp64_peak, "traffic": traffic,
+                "algorithmic_flops_per_launch": flops, "kernel_ms": core}
+    roof["peak_source"] = ("measured here: cuBLAS FP64 GEMM 4096^3, best of 5 "
+                           "(MEASURED_PEAKS.json has no FP64 entry)")
+    stages = res[head][2]
     line = {
         "metric": METRIC, "value": value, "unit": "columns/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "bf16 hi/lo tensor products + f64 eigen/mean" if head == "mixed" else "f64",
         "data": "synthetic (seeded; no public dataset for this path)",
-        "config": {"workload": "config1: 1deg 360x180x32, k=64, 200k obs (4x box 0-60E 10S-30N), "
+        "config": {"workload": "config1/2: 1deg 360x180x32, k=64, 200k obs (4x box 0-60E 10S-30N), "
                                "GC c=400 km (cut-off 800 km), rho=1.08, level-select H",
-                   "form": "plain FP64 (precision 0)", "columns": w.ncol, "ensemble": w.k,
-                   "obs": int(w.obs["lat"].size), "sum_p": st["sum_p"], "max_p": st["max_p"],
-                   "l2": "inputs larger than L2 (xb 3.2 GB)",
-                   "parallelism": f"replicas x{world}"},
+                   "form": "mixed precision (precision 1)" if head == "mixed" else "plain FP64",
+                   "columns": w.ncol, "ensemble": w.k, "obs": int(w.obs["lat"].size),
+                   "sum_p": st["sum_p"], "max_p": st["max_p"],
+                   "l2": "inputs larger than L2 (xb 3.2 GB)", "parallelism": f"replicas x{world}"},
         "e2e": {"value": world * w.ncol / (ms_e2e * 1e-3), "unit": "columns/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "max_abs_diff_vs_device_run": err_h},
-        "gpu_launches": launches,
-        "roofline": {"bound": "fp64", "kernel": "k_core_fp64<64>", "achieved": achieved,
-                     "peak": fp64_peak, "unit": "TFLOP/s", "frac": achieved / fp64_peak,
-                     "traffic": traffic,
-                     "peak_source": "measured here: cuBLAS FP64 GEMM 4096^3, best of 5 "
-                                    "(MEASURED_PEAKS.json has no FP64 entry)",
-                     "algorithmic_flops_per_launch": flops, "kernel_ms": core},
+                "max_abs_diff_vs_device_run": e2e_vs_device},
+        "gpu_launches": res[head][3],
+        "roofline": roof,
         "roofline_hbm_step": {"achieved": nbytes / (ms * 1e-3) / 1e9,
                               "peak": peaks.get("hbm_gbs", 6800.0), "unit": "GB/s",
                               "frac": nbytes / (ms * 1e-3) / 1e9 / peaks.get("hbm_gbs", 6800.0),
@@ -381,6 +443,16 @@ def run_ours(args, rank, world, local_rank):
         "clocks": clk,
         "workload_generation_s": t_gen,
     }
+    if "fp64" in res and head == "mixed":
+        ms64 = res["fp64"][0]
+        line["fp64_form"] = {"value": world * w.ncol / (ms64 * 1e-3), "unit": "columns/s",
+                             "ms_per_step": ms64, "core_ms": statistics.mean(res["fp64"][1])}
+        line["speedup_mixed_vs_fp64"] = ms64 / ms
+        xa16, axa16 = (t.cpu().numpy() for t in outs["mixed"])
+        xa64, axa64 = (t.cpu().numpy() for t in outs["fp64"])
+        errs = _field_errors(w, xa16, axa16, xa64, axa64)
+        line["mixed_error_vs_fp64"] = errs
+        line["mixed_error_max"] = max(max(v.values()) for v in errs.values())
     if world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(w, args.cpu_seconds, "config1")
         line["cpu_baseline"]["cpu"] = cpu_model()

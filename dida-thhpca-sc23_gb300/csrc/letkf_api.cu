@@ -15,6 +15,7 @@
 #include "letkf_internal.cuh"
 
 bool lg_core_supports(int k);
+bool lg_mixed_supports(int k);
 int lg_search_cap(int max_obs);
 
 namespace {
@@ -99,6 +100,7 @@ int reserve_obs_work(letkf_ctx *ctx, int64_t no)
 {
     const size_t n = (size_t)std::max<int64_t>(no, 1);
     LG_CUDA(ctx->d_yb.reserve(n * ctx->k));
+    if (ctx->params.precision == LETKF_PREC_MIXED) LG_CUDA(ctx->d_ys32.reserve(n * ctx->k));
     LG_CUDA(ctx->d_dep.reserve(n));
     LG_CUDA(ctx->d_rinvf.reserve(n));
     LG_CUDA(ctx->d_os.reserve(n));
@@ -268,7 +270,7 @@ int letkf_gpu_create(letkf_ctx **out, const letkf_grid *grid, const letkf_params
     if (need_hybrid && (!G.hyai || !G.hybi || G.ps_row < 0 || G.ps_row >= n))
         return LETKF_ERR_INVALID;
     if (P.overlap != 0 || P.vert_dist > 0.0) return LETKF_ERR_UNSUPPORTED;
-    if (P.precision != LETKF_PREC_FP64) return LETKF_ERR_UNSUPPORTED;
+    if (P.precision == LETKF_PREC_MIXED && !lg_mixed_supports(G.ens)) return LETKF_ERR_UNSUPPORTED;
 
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return LETKF_ERR_CUDA;
@@ -391,7 +393,10 @@ int letkf_gpu_run(letkf_ctx *ctx, const double *xb, const double *axb, const let
     if (rc) return rc;
     LG_CUDA(cudaEventRecord(ctx->ev[3], ctx->stream));
     const LgGrid g = lg_grid(ctx);
-    LG_CUDA(lg_launch_core_fp64(ctx, g, dxb, daxb, dxa, daxa, ctx->d_trans.p != nullptr));
+    if (ctx->params.precision == LETKF_PREC_MIXED)
+        LG_CUDA(lg_launch_core_mixed(ctx, g, dxb, daxb, dxa, daxa, ctx->d_trans.p != nullptr));
+    else
+        LG_CUDA(lg_launch_core_fp64(ctx, g, dxb, daxb, dxa, daxa, ctx->d_trans.p != nullptr));
     LG_CUDA(cudaEventRecord(ctx->ev[4], ctx->stream));
     if (host) {
         LG_CUDA(cudaMemcpyAsync(xa, dxa, sizeof(double) * nstate, cudaMemcpyDeviceToHost, ctx->stream));
@@ -410,6 +415,8 @@ int letkf_gpu_run(letkf_ctx *ctx, const double *xb, const double *axb, const let
     ctx->stats.ms_total = elapsed(ctx->ev[0], ctx->ev[5]);
     ctx->have_run = true;
     ctx->last_nobs = obs->nobs;
+    if (st & LG_ST_TIMEOUT)
+        return set_err(ctx, LETKF_ERR_TIMEOUT, "a bounded wait on the tensor cores ran out");
     if (st & LG_ST_NOT_CONV)
         return set_err(ctx, LETKF_ERR_NOT_CONVERGED, "an eigensolve reached its sweep limit");
     return LETKF_OK;

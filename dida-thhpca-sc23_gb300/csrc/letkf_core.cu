@@ -19,6 +19,7 @@
 // The reference forms Pa and the k x p matrix Pa*Yhat^T (:129-195); the
 // products here are the same quantities in O(k p + k^3) instead of O(k^2 p).
 #include "letkf_internal.cuh"
+#include "letkf_jacobi.cuh"
 
 namespace {
 
@@ -48,103 +49,6 @@ struct RowSrc {
     const double *hx, *bdep, *brloc;
     const float *brdi;
 };
-
-__device__ __forceinline__ void decode_block(int b, int &bi, int &bj)
-{
-    int i = (int)((sqrtf(8.0f * (float)b + 1.0f) - 1.0f) * 0.5f);
-    while ((i + 1) * (i + 2) / 2 <= b) i++;
-    while (i * (i + 1) / 2 > b) i--;
-    bi = i;
-    bj = b - i * (i + 1) / 2;
-}
-
-// One-sided Jacobi on the columns of W (column j at W[j*K ..]).  Each step of
-// a sweep rotates k/2 disjoint column pairs (round-robin ordering): a group of
-// G threads forms each pair's inner product, one thread per pair turns
-// (alpha, beta, gamma) into the rotation (so the divisions and square roots
-// are done once per pair, not once per thread), and the groups rotate the
-// columns.  Returns the sweeps used, or max_sweeps+1 if not converged.
-template <int K>
-__device__ int jacobi_fp64(double *W, double *nrm, double2 *rot, int *s_rot, double tol,
-                           int max_sweeps)
-{
-    constexpr int NP = Cfg<K>::NPAIR, G = Cfg<K>::G;
-    const int tid = threadIdx.x;
-    const int pair = tid / G, lane = tid % G;
-    const bool act = pair < NP;
-    const double tol2 = tol * tol;
-    int sweep;
-    for (sweep = 1; sweep <= max_sweeps; sweep++) {
-        if (tid < K) {
-            double s = 0.0;
-            for (int r = 0; r < K; r++) s += W[tid * K + r] * W[tid * K + r];
-            nrm[tid] = s;
-        }
-        if (tid == 0) *s_rot = 0;
-        __syncthreads();
-        for (int r = 0; r < K - 1; r++) {
-            int p = 0, q = 0;
-            if (act) {
-                if (pair == 0) {
-                    p = K - 1;
-                    q = r;
-                } else {
-                    p = (r + pair) % (K - 1);
-                    q = (r - pair + (K - 1)) % (K - 1);
-                }
-                const double *wp = W + p * K, *wq = W + q * K;
-                double gam = 0.0;
-#pragma unroll
-                for (int rr = lane; rr < K; rr += G) gam += wp[rr] * wq[rr];
-#pragma unroll
-                for (int o = G / 2; o > 0; o >>= 1) gam += __shfl_xor_sync(0xffffffffu, gam, o);
-                if (lane == 0) rot[pair].x = gam;
-            }
-            __syncthreads();
-            if (tid < NP) {
-                int pp, qq;
-                if (tid == 0) {
-                    pp = K - 1;
-                    qq = r;
-                } else {
-                    pp = (r + tid) % (K - 1);
-                    qq = (r - tid + (K - 1)) % (K - 1);
-                }
-                const double gam = rot[tid].x;
-                const double al = nrm[pp], be = nrm[qq];
-                double c = 1.0, s = 0.0;
-                if (gam * gam > tol2 * (al * be)) {
-                    const double zeta = (be - al) / (2.0 * gam);
-                    const double t = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-                    c = 1.0 / sqrt(1.0 + t * t);
-                    s = c * t;
-                    nrm[pp] = al - t * gam;
-                    nrm[qq] = be + t * gam;
-                    *s_rot = 1;
-                }
-                rot[tid] = make_double2(c, s);
-            }
-            __syncthreads();
-            if (act) {
-                const double2 cs = rot[pair];
-                if (cs.y != 0.0) {
-                    double *wp = W + p * K, *wq = W + q * K;
-#pragma unroll
-                    for (int rr = lane; rr < K; rr += G) {
-                        const double a = wp[rr], b = wq[rr];
-                        wp[rr] = cs.x * a - cs.y * b;
-                        wq[rr] = cs.y * a + cs.x * b;
-                    }
-                }
-            }
-            __syncthreads();
-        }
-        const int rotated = *s_rot;
-        __syncthreads();
-        if (!rotated) break;
-    }
-    return sweep;
-}
 
 template <int K>
 __global__ void __launch_bounds__(kT)
@@ -176,7 +80,7 @@ k_core_fp64(LgGrid g, LgParams prm, RowSrc src, const int64_t *__restrict__ loff
     for (int m = 0; m < MB; m++) {
         const int b = tid + m * kT;
         bok[m] = b < C::NBLK;
-        decode_block(bok[m] ? b : 0, bi[m], bj[m]);
+        lg_decode_block(bok[m] ? b : 0, bi[m], bj[m]);
     }
 
     for (int64_t cube = blockIdx.x; cube < ncubes; cube += gridDim.x) {
@@ -256,7 +160,7 @@ k_core_fp64(LgGrid g, LgParams prm, RowSrc src, const int64_t *__restrict__ loff
         __syncthreads();
 
         // ---- eigendecomposition of A'
-        const int sweeps = jacobi_fp64<K>(W, nrm, rot, &s_rot, 1e-15, 40);
+        const int sweeps = lg_jacobi<double, K, Cfg<K>::G>(W, nrm, rot, &s_rot, 1e-15, 40);
         if (tid == 0) {
             atomicMax(&counters[LG_CNT_MAXSWEEP], (unsigned long long)sweeps);
             if (sweeps > 40) {

@@ -28,6 +28,7 @@
 #define LG_ST_LIST_FULL    2u   // local-list storage too small
 #define LG_ST_NOT_CONV     4u   // an eigensolve hit its sweep limit
 #define LG_ST_SEGMENTS     8u   // a cap needed more bucket segments than the search holds
+#define LG_ST_TIMEOUT     16u   // a bounded wait on the tensor cores ran out
 
 // Counters in ctx->d_counters.
 enum {
@@ -162,6 +163,7 @@ struct letkf_ctx {
     DevBuf<double> d_olat, d_olon, d_oph, d_oyo, d_orinv;
     DevBuf<int32_t> d_olev, d_ovar;
     DevBuf<double> d_yb, d_dep;
+    DevBuf<float> d_ys32;         // yb * sqrt(rinv) in FP32 (mixed precision)
     DevBuf<float> d_rinvf;
     DevBuf<double> d_os, d_oc, d_oyr;
     DevBuf<float4> d_oxyz;
@@ -207,6 +209,8 @@ cudaError_t lg_launch_buckets(letkf_ctx *ctx, int64_t nobs);
 cudaError_t lg_launch_search(letkf_ctx *ctx, const LgGrid &g, int64_t nobs);
 cudaError_t lg_launch_core_fp64(letkf_ctx *ctx, const LgGrid &g, const double *xb,
                                 const double *axb, double *xa, double *axa, bool keep_trans);
+cudaError_t lg_launch_core_mixed(letkf_ctx *ctx, const LgGrid &g, const double *xb,
+                                 const double *axb, double *xa, double *axa, bool keep_trans);
 cudaError_t lg_launch_core_batch_fp64(letkf_ctx *ctx, int64_t nb, const int64_t *d_off,
                                       const double *d_hx, const float *d_rdi,
                                       const double *d_dep, const double *d_rloc,

@@ -1,0 +1,664 @@
+// letkf_mixed.cu -- mixed-precision per-cube LETKF core (precision 1).
+//
+// Same analysis as letkf_core.cu (letkf_core, code/x86/TradDA/DA/LETKF/src/
+// letkf_core.F90:14-233, and xb_2_xa, letkf_compute.F90:231-301), with the two
+// dense products on the Blackwell tensor cores and the conditioning-sensitive
+// steps in FP64:
+//
+//   1. A = Yhat Yhat^T on tcgen05 (BF16 operands, FP32 accumulation in TMEM).
+//      Yhat = Y sqrt(rdiaginv rloc) is split per element into hi + lo BF16
+//      parts; one MMA stream multiplies the stacked [Yhat_hi; Yhat_lo]
+//      (M = 128 rows) by Yhat_hi (N = k), so A = HH + LH + LH^T recovers the
+//      hi*lo cross terms.  The observation rows are gathered, scaled and split
+//      into 128-byte-swizzled K-major tiles by all threads while the previous
+//      tile's MMAs run (two tiles, mbarrier-tracked).
+//      g = Yhat (sqrt(rdiaginv rloc) dep) is accumulated in FP64 alongside.
+//   2. A' = A + (k-1)/rho I in FP64.
+//   3. FP32 one-sided Jacobi gives approximate eigenvectors Xhat.
+//   4. One FP64 refinement step of the eigendecomposition (Ogita & Aishima,
+//      "Iterative refinement for symmetric eigenvalue decomposition", Japan J.
+//      Indust. Appl. Math. 35 (2018), Algorithm 1): R = I - Xhat^T Xhat,
+//      S = Xhat^T A' Xhat, lambda_i = s_ii/(1-r_ii), E from S, R and the gaps,
+//      X = Xhat + Xhat E; the eigenpairs come out FP64-accurate.
+//   5. T = X diag(sqrt((k-1)/lambda)) X^T and wbar = X diag(1/lambda) X^T g in FP64.
+//   6. xa = xb^T T on tcgen05 (hi/lo BF16 of both operands, three products in
+//      one accumulator); the mean increment xb^T wbar is FP64.
+#include <cuda_bf16.h>
+
+#include "letkf_internal.cuh"
+#include "letkf_jacobi.cuh"
+#include "letkf_umma.cuh"
+
+namespace {
+
+constexpr int kT = 256;
+
+template <int K>
+struct MCfg {
+    static constexpr int KB = K / 4;
+    static constexpr int NLOW = KB * (KB + 1) / 2;     // lower 4x4 blocks
+    static constexpr int ML = (NLOW + kT - 1) / kT;
+    static constexpr int NFULL = KB * KB;              // all 4x4 blocks
+    static constexpr int MF = (NFULL + kT - 1) / kT;
+    static constexpr int G = (K / 2 * 16 <= kT) ? 16 : (K / 2 * 8 <= kT) ? 8 : 4;
+    static constexpr int CH = 64;                      // observations per MMA tile (K of the MMA)
+    static constexpr uint32_t TMEM_COLS = 64;
+    static constexpr size_t AREA = 48 * 1024;          // tiles / FP32 scratch / Xhat, P, X
+    static constexpr size_t B1 = sizeof(double) * K * K;
+    static constexpr size_t VEC = sizeof(double) * (7 * K + 128 + CH) +
+                                  sizeof(float) * (2 * K + CH) + sizeof(int) * CH;
+    static constexpr size_t SMEM = 1024 + AREA + B1 + VEC + 256;
+    static_assert(2 * K <= 128, "stacked hi/lo rows must fit M = 128");
+    static_assert(K % 16 == 0, "N must be a multiple of 16");
+};
+
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b)
+{
+    __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<uint32_t *>(&h);
+}
+
+// hi/lo BF16 split of 8 floats into two 16-byte chunks.
+__device__ __forceinline__ void split8(const float *v, uint4 &hi, uint4 &lo)
+{
+    uint32_t h[4], l[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        const __nv_bfloat16 h0 = __float2bfloat16_rn(v[2 * j]), h1 = __float2bfloat16_rn(v[2 * j + 1]);
+        const float r0 = v[2 * j] - __bfloat162float(h0), r1 = v[2 * j + 1] - __bfloat162float(h1);
+        __nv_bfloat162 hh;
+        hh.x = h0;
+        hh.y = h1;
+        h[j] = *reinterpret_cast<uint32_t *>(&hh);
+        l[j] = pack_bf16(r0, r1);
+    }
+    hi = make_uint4(h[0], h[1], h[2], h[3]);
+    lo = make_uint4(l[0], l[1], l[2], l[3]);
+}
+
+__device__ __forceinline__ double block_sum(double v, double *red)
+{
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1) v += __shfl_xor_sync(0xffffffffu, v, s);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double t = 0.0;
+#pragma unroll
+    for (int w = 0; w < kT / 32; w++) t += red[w];
+    __syncthreads();
+    return t;
+}
+
+template <int K>
+__global__ void __launch_bounds__(kT, 2)
+k_core_mixed(LgGrid g, LgParams prm, const double *__restrict__ yb, const float *__restrict__ ys32,
+             const double *__restrict__ dep, const float *__restrict__ rinvf,
+             const int32_t *__restrict__ lidx, const double *__restrict__ lrloc,
+             const int64_t *__restrict__ loff, const int32_t *__restrict__ lcnt, int64_t ncubes,
+             const double *__restrict__ xb, const double *__restrict__ axb, double *__restrict__ xa,
+             double *__restrict__ axa, double *__restrict__ trans_out, double *__restrict__ w_out,
+             unsigned long long *__restrict__ counters, unsigned *__restrict__ status)
+{
+    using C = MCfg<K>;
+    constexpr int CH = C::CH;
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char *area = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    double *B1 = reinterpret_cast<double *>(area + C::AREA);
+    double *gv = B1 + K * K;
+    double *lam = gv + K;
+    double *fco = lam + K;
+    double *hco = fco + K;
+    double *wbar = hco + K;
+    double *misc = wbar + K;       // 2K
+    double *inc = misc + 2 * K;    // 128
+    double *cd = inc + 128;        // CH
+    float *nrm32 = reinterpret_cast<float *>(cd + CH);             // K
+    float2 *rot32 = reinterpret_cast<float2 *>(nrm32 + K);          // K/2
+    float *sq32 = reinterpret_cast<float *>(rot32 + K / 2);         // CH
+    int *gidx = reinterpret_cast<int *>(sq32 + CH);                 // CH
+    __shared__ uint64_t mbar[3];
+    __shared__ uint32_t s_tmem;
+    __shared__ int s_rot, s_ok;
+    __shared__ double red[kT / 32];
+
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    if (warp == 0) lg_tmem_alloc(lg_smem_u32(&s_tmem), C::TMEM_COLS);
+    if (tid == 0) {
+        lg_mbar_init(&mbar[0], 1);
+        lg_mbar_init(&mbar[1], 1);
+        lg_mbar_init(&mbar[2], 1);
+    }
+    lg_tc_fence_before();
+    __syncthreads();
+    lg_tc_fence_after();
+    const uint32_t tmem = s_tmem;
+    const uint32_t idesc = lg_idesc_bf16(128, K);
+    uint32_t ncommit[3] = {0u, 0u, 0u};
+    bool pending[3] = {false, false, false};
+    bool failed = false;
+
+    // Wait (thread 0 polls, bounded) for the last commit on barrier b.
+    auto wait_bar = [&](int b) -> bool {
+        if (!pending[b]) return true;
+        if (tid == 0) s_ok = lg_mbar_wait(&mbar[b], (ncommit[b] - 1u) & 1u) ? 1 : 0;
+        __syncthreads();
+        const int ok = s_ok;
+        __syncthreads();
+        pending[b] = false;
+        return ok != 0;
+    };
+
+    // 4x4 block ownership
+    int lbi[C::ML], lbj[C::ML];
+    bool lok[C::ML];
+#pragma unroll
+    for (int m = 0; m < C::ML; m++) {
+        const int b = tid + m * kT;
+        lok[m] = b < C::NLOW;
+        lg_decode_block(lok[m] ? b : 0, lbi[m], lbj[m]);
+    }
+    int fbi[C::MF], fbj[C::MF];
+    bool fok[C::MF];
+#pragma unroll
+    for (int m = 0; m < C::MF; m++) {
+        const int b = tid + m * kT;
+        fok[m] = b < C::NFULL;
+        fbi[m] = (fok[m] ? b : 0) / C::KB;
+        fbj[m] = (fok[m] ? b : 0) % C::KB;
+    }
+
+    for (int64_t cube = blockIdx.x; cube < ncubes; cube += gridDim.x) {
+        const int64_t off = loff[cube];
+        const int p = lcnt[cube];
+
+        // ---------------- phase 1: A on the tensor cores, g in FP64 ----------------
+        if (2 * K < 128) {
+            // rows 2K..127 of both tiles stay zero
+            for (int t = tid; t < 2 * (128 - 2 * K) * 8; t += kT) {
+                const int b = t / ((128 - 2 * K) * 8), rest = t % ((128 - 2 * K) * 8);
+                const int r = 2 * K + rest / 8, c = rest % 8;
+                *reinterpret_cast<uint4 *>(area + b * 16384 + lg_sw128_offset(r, c)) = make_uint4(0, 0, 0, 0);
+            }
+        }
+        double gacc = 0.0;
+        const int nch = (p + CH - 1) / CH;
+        for (int ch = 0; ch < nch; ch++) {
+            const int b = ch & 1;
+            unsigned char *tile = area + b * 16384;
+            if (!wait_bar(b)) {
+                failed = true;
+                break;
+            }
+            const int cnt = min(CH, p - ch * CH);
+            if (tid < CH) {
+                if (tid < cnt) {
+                    const int64_t li = off + (int64_t)ch * CH + tid;
+                    const int gi = lidx[li];
+                    const double rl = lrloc[li];
+                    gidx[tid] = gi;
+                    sq32[tid] = sqrtf((float)rl);
+                    cd[tid] = ((double)rinvf[gi] * rl) * dep[gi];
+                } else {
+                    gidx[tid] = 0;
+                    sq32[tid] = 0.0f;
+                    cd[tid] = 0.0;
+                }
+            }
+            __syncthreads();
+            if (tid < K)
+                for (int o = 0; o < cnt; o++) gacc += yb[(int64_t)gidx[o] * K + tid] * cd[o];
+            for (int t = tid; t < K * 8; t += kT) {
+                const int m = t % K, c = t / K;
+                float v[8];
+#pragma unroll
+                for (int j = 0; j < 8; j++) {
+                    const int o = 8 * c + j;
+                    v[j] = (o < cnt) ? ys32[(int64_t)gidx[o] * K + m] * sq32[o] : 0.0f;
+                }
+                uint4 hi, lo;
+                split8(v, hi, lo);
+                *reinterpret_cast<uint4 *>(tile + lg_sw128_offset(m, c)) = hi;
+                *reinterpret_cast<uint4 *>(tile + lg_sw128_offset(K + m, c)) = lo;
+            }
+            lg_fence_async_smem();
+            __syncthreads();
+            if (tid == 0) {
+                lg_tc_fence_after();
+                const uint64_t d = lg_desc_sw128(lg_smem_u32(tile));
+#pragma unroll
+                for (int kk = 0; kk < 4; kk++)
+                    lg_umma_bf16(tmem, d + 2 * kk, d + 2 * kk, idesc, (ch > 0 || kk > 0) ? 1u : 0u);
+                lg_umma_commit(&mbar[b]);
+            }
+            ncommit[b]++;
+            pending[b] = true;
+        }
+        if (failed) break;
+        if (!wait_bar(0) || !wait_bar(1)) {
+            failed = true;
+            break;
+        }
+        if (tid < K) gv[tid] = gacc;
+        lg_tc_fence_after();
+
+        // ---------------- phase 2: A' = HH + LH + LH^T + (k-1)/rho I -------------------
+        float *Dhh = reinterpret_cast<float *>(area);
+        float *Dlh = Dhh + K * K;
+        float *W32 = reinterpret_cast<float *>(area + 32768);
+        if (warp < 4) {
+            const int row = warp * 32 + lane;
+#pragma unroll
+            for (int c0 = 0; c0 < K; c0 += 16) {
+                float v[16];
+                if (p > 0) {
+                    lg_tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 16; j++) v[j] = 0.0f;
+                }
+                if (row < K) {
+#pragma unroll
+                    for (int j = 0; j < 16; j++) Dhh[row * K + c0 + j] = v[j];
+                } else if (row < 2 * K) {
+#pragma unroll
+                    for (int j = 0; j < 16; j++) Dlh[(row - K) * K + c0 + j] = v[j];
+                }
+            }
+        }
+        lg_tc_fence_before();
+        __syncthreads();
+        const double cdiag = (double)(K - 1) / prm.inflation;
+        double fro = 0.0;
+        for (int idx = tid; idx < K * K; idx += kT) {
+            const int i = idx / K, j = idx % K;
+            double a = 0.5 * ((double)Dhh[i * K + j] + (double)Dhh[j * K + i]) + (double)Dlh[i * K + j] +
+                       (double)Dlh[j * K + i];
+            if (i == j) a += cdiag;
+            B1[idx] = a;
+            fro += a * a;
+        }
+        __syncthreads();
+        for (int idx = tid; idx < K * K; idx += kT) W32[idx] = (float)B1[idx];
+        const double normA = sqrt(block_sum(fro, red));
+
+        // ---------------- phase 3: FP32 Jacobi -> Xhat (columns of W32) ----------------
+        const int sw = lg_jacobi<float, K, C::G>(W32, nrm32, rot32, &s_rot, 2e-6f, 24);
+        if (tid == 0) {
+            atomicMax(&counters[LG_CNT_MAXSWEEP], (unsigned long long)sw);
+            if (sw > 24) atomicAdd(&counters[LG_CNT_NOTCONV], 1ull);
+        }
+        if (tid < K) {
+            float s = 0.0f;
+            for (int r = 0; r < K; r++) s += W32[tid * K + r] * W32[tid * K + r];
+            nrm32[tid] = 1.0f / sqrtf(s);
+        }
+        __syncthreads();
+        for (int idx = tid; idx < K * K; idx += kT) W32[idx] *= nrm32[idx / K];
+        __syncthreads();
+        const float *Xh = W32;                       // column j at Xh[j*K]
+
+        // ---------------- phase 4: FP64 refinement (Ogita-Aishima) ---------------------
+        double *P = reinterpret_cast<double *>(area);   // column j = A' xhat_j
+#pragma unroll
+        for (int m = 0; m < C::MF; m++) {
+            if (!fok[m]) continue;
+            double acc[16];
+#pragma unroll
+            for (int i = 0; i < 16; i++) acc[i] = 0.0;
+            for (int l = 0; l < K; l++) {
+                const double2 a01 = *reinterpret_cast<const double2 *>(B1 + l * K + 4 * fbi[m]);
+                const double2 a23 = *reinterpret_cast<const double2 *>(B1 + l * K + 4 * fbi[m] + 2);
+                const double a[4] = {a01.x, a01.y, a23.x, a23.y};
+#pragma unroll
+                for (int jj = 0; jj < 4; jj++) {
+                    const double x = (double)Xh[(4 * fbj[m] + jj) * K + l];
+#pragma unroll
+                    for (int i = 0; i < 4; i++) acc[i * 4 + jj] += a[i] * x;
+                }
+            }
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+#pragma unroll
+                for (int jj = 0; jj < 4; jj++) P[(4 * fbj[m] + jj) * K + 4 * fbi[m] + i] = acc[i * 4 + jj];
+        }
+        __syncthreads();
+        // S = Xhat^T A' Xhat (lower blocks, mirrored) into B1
+        {
+            double sacc[C::ML][16];
+#pragma unroll
+            for (int m = 0; m < C::ML; m++) {
+#pragma unroll
+                for (int i = 0; i < 16; i++) sacc[m][i] = 0.0;
+                if (!lok[m]) continue;
+                for (int l = 0; l < K; l++) {
+                    double x[4], q[4];
+#pragma unroll
+                    for (int i = 0; i < 4; i++) {
+                        x[i] = (double)Xh[(4 * lbi[m] + i) * K + l];
+                        q[i] = P[(4 * lbj[m] + i) * K + l];
+                    }
+#pragma unroll
+                    for (int i = 0; i < 4; i++)
+#pragma unroll
+                        for (int jj = 0; jj < 4; jj++) sacc[m][i * 4 + jj] += x[i] * q[jj];
+                }
+            }
+            __syncthreads();
+#pragma unroll
+            for (int m = 0; m < C::ML; m++) {
+                if (!lok[m]) continue;
+#pragma unroll
+                for (int i = 0; i < 4; i++)
+#pragma unroll
+                    for (int jj = 0; jj < 4; jj++) {
+                        const int r = 4 * lbi[m] + i, c = 4 * lbj[m] + jj;
+                        B1[r * K + c] = sacc[m][i * 4 + jj];
+                        B1[c * K + r] = sacc[m][i * 4 + jj];
+                    }
+            }
+        }
+        __syncthreads();
+        // R = I - Xhat^T Xhat (lower blocks, mirrored) into the area (P is dead)
+        double *Rm = reinterpret_cast<double *>(area);
+        {
+            double racc[C::ML][16];
+#pragma unroll
+            for (int m = 0; m < C::ML; m++) {
+#pragma unroll
+                for (int i = 0; i < 16; i++) racc[m][i] = 0.0;
+                if (!lok[m]) continue;
+                for (int l = 0; l < K; l++) {
+                    double x[4], y[4];
+#pragma unroll
+                    for (int i = 0; i < 4; i++) {
+                        x[i] = (double)Xh[(4 * lbi[m] + i) * K + l];
+                        y[i] = (double)Xh[(4 * lbj[m] + i) * K + l];
+                    }
+#pragma unroll
+                    for (int i = 0; i < 4; i++)
+#pragma unroll
+                        for (int jj = 0; jj < 4; jj++) racc[m][i * 4 + jj] += x[i] * y[jj];
+                }
+            }
+#pragma unroll
+            for (int m = 0; m < C::ML; m++) {
+                if (!lok[m]) continue;
+#pragma unroll
+                for (int i = 0; i < 4; i++)
+#pragma unroll
+                    for (int jj = 0; jj < 4; jj++) {
+                        const int r = 4 * lbi[m] + i, c = 4 * lbj[m] + jj;
+                        const double v = (r == c ? 1.0 : 0.0) - racc[m][i * 4 + jj];
+                        Rm[r * K + c] = v;
+                        Rm[c * K + r] = v;
+                    }
+            }
+        }
+        __syncthreads();
+        if (tid < K) lam[tid] = B1[tid * K + tid] / (1.0 - Rm[tid * K + tid]);
+        __syncthreads();
+        double offs = 0.0, rr2 = 0.0;
+        for (int idx = tid; idx < K * K; idx += kT) {
+            const int i = idx / K, j = idx % K;
+            const double d = (i == j) ? B1[idx] - lam[i] : B1[idx];
+            offs += d * d;
+            rr2 += Rm[idx] * Rm[idx];
+        }
+        offs = block_sum(offs, red);
+        rr2 = block_sum(rr2, red);
+        const double delta = 2.0 * (sqrt(offs) + normA * sqrt(rr2));
+        // E (in place of S): gaps above delta get the Newton correction
+        for (int idx = tid; idx < K * K; idx += kT) {
+            const int i = idx / K, j = idx % K;
+            const double r = Rm[idx];
+            double e;
+            if (i == j) {
+                e = 0.5 * r;
+            } else {
+                const double gap = lam[j] - lam[i];
+                e = (fabs(gap) > delta) ? (B1[idx] + lam[j] * r) / gap : 0.5 * r;
+            }
+            B1[idx] = e;
+        }
+        __syncthreads();
+        // X = Xhat + Xhat E (columns) into the area (R is dead)
+        double *Xp = reinterpret_cast<double *>(area);
+#pragma unroll
+        for (int m = 0; m < C::MF; m++) {
+            if (!fok[m]) continue;
+            double acc[16];
+#pragma unroll
+            for (int i = 0; i < 16; i++) acc[i] = 0.0;
+            for (int l = 0; l < K; l++) {
+                // rows 4*fbi.. of column l of Xhat, row l of E at columns 4*fbj..
+                double x[4], e[4];
+#pragma unroll
+                for (int i = 0; i < 4; i++) x[i] = (double)Xh[l * K + 4 * fbi[m] + i];
+                const double2 e01 = *reinterpret_cast<const double2 *>(B1 + l * K + 4 * fbj[m]);
+                const double2 e23 = *reinterpret_cast<const double2 *>(B1 + l * K + 4 * fbj[m] + 2);
+                e[0] = e01.x; e[1] = e01.y; e[2] = e23.x; e[3] = e23.y;
+#pragma unroll
+                for (int i = 0; i < 4; i++)
+#pragma unroll
+                    for (int jj = 0; jj < 4; jj++) acc[i * 4 + jj] += x[i] * e[jj];
+            }
+            // write after every thread has read Rm? Rm is not read here; Xp aliases
+            // Rm but Rm was last read before the previous barrier.
+#pragma unroll
+            for (int i = 0; i < 4; i++)
+#pragma unroll
+                for (int jj = 0; jj < 4; jj++) {
+                    const int row = 4 * fbi[m] + i, col = 4 * fbj[m] + jj;
+                    Xp[col * K + row] = (double)Xh[col * K + row] + acc[i * 4 + jj];
+                }
+        }
+        __syncthreads();
+
+        // ---------------- phase 5: T and wbar in FP64 -----------------------------------
+        if (tid < K) {
+            double dot = 0.0;
+            for (int l = 0; l < K; l++) dot += Xp[tid * K + l] * gv[l];
+            hco[tid] = dot / lam[tid];
+            fco[tid] = sqrt((double)(K - 1) / lam[tid]);
+        }
+        __syncthreads();
+        if (tid < K) {
+            double s = 0.0;
+            for (int j = 0; j < K; j++) s += Xp[j * K + tid] * hco[j];
+            wbar[tid] = s;
+        }
+        {
+            double tacc[C::ML][16];
+#pragma unroll
+            for (int m = 0; m < C::ML; m++) {
+#pragma unroll
+                for (int i = 0; i < 16; i++) tacc[m][i] = 0.0;
+                if (!lok[m]) continue;
+                for (int j = 0; j < K; j++) {
+                    const double f = fco[j];
+                    double a[4], bq[4];
+#pragma unroll
+                    for (int i = 0; i < 4; i++) {
+                        a[i] = Xp[j * K + 4 * lbi[m] + i];
+                        bq[i] = Xp[j * K + 4 * lbj[m] + i] * f;
+                    }
+#pragma unroll
+                    for (int i = 0; i < 4; i++)
+#pragma unroll
+                        for (int jj = 0; jj < 4; jj++) tacc[m][i * 4 + jj] += a[i] * bq[jj];
+                }
+            }
+            // B1 (E) is no longer read: write T (symmetric, row-major)
+#pragma unroll
+            for (int m = 0; m < C::ML; m++) {
+                if (!lok[m]) continue;
+#pragma unroll
+                for (int i = 0; i < 4; i++)
+#pragma unroll
+                    for (int jj = 0; jj < 4; jj++) {
+                        const int r = 4 * lbi[m] + i, c = 4 * lbj[m] + jj;
+                        B1[r * K + c] = tacc[m][i * 4 + jj];
+                        B1[c * K + r] = tacc[m][i * 4 + jj];
+                    }
+            }
+        }
+        __syncthreads();
+        if (trans_out) {
+            for (int idx = tid; idx < K * K; idx += kT) {
+                const int i = idx % K, j = idx / K;
+                trans_out[cube * K * K + idx] = B1[i * K + j] + wbar[i];
+            }
+            if (tid < K) w_out[cube * K + tid] = wbar[tid];
+        }
+
+        // ---------------- phase 6: xa = xb^T (T + wbar 1^T) -------------------------------
+        unsigned char *xa_hi = area, *xa_lo = area + 16384;
+        unsigned char *tb_hi = area + 32768, *tb_lo = area + 40960;
+        // B operand rows e = T row e (T symmetric), K dimension = source member
+        for (int t = tid; t < K * (K / 8); t += kT) {
+            const int e = t / (K / 8), c = t % (K / 8);
+            float v[8];
+#pragma unroll
+            for (int j = 0; j < 8; j++) v[j] = (float)B1[e * K + 8 * c + j];
+            uint4 hi, lo;
+            split8(v, hi, lo);
+            *reinterpret_cast<uint4 *>(tb_hi + lg_sw128_offset(e, c)) = hi;
+            *reinterpret_cast<uint4 *>(tb_lo + lg_sw128_offset(e, c)) = lo;
+        }
+        const int n = g.n;
+        const int bjc = (int)(cube % prm.nbj), bic = (int)(cube / prm.nbj);
+        const int sj = bjc * prm.cube_n, ej = min(sj + prm.cube_n - 1, g.nlat - 1);
+        const int si = bic * prm.cube_n, ei = min(si + prm.cube_n - 1, g.nlon - 1);
+        for (int ii = si; ii <= ei && !failed; ii++)
+            for (int jj = sj; jj <= ej && !failed; jj++) {
+                const int64_t col = jj + (int64_t)g.nlat * ii;
+                const double *xbc = xb + col * n * K;
+                double *xac = xa + col * n * K;
+                for (int r0 = 0; r0 < n; r0 += 128) {
+                    const int R = min(128, n - r0);
+                    for (int t = tid; t < 128 * (K / 8); t += kT) {
+                        const int r = t / (K / 8), c = t % (K / 8);
+                        float v[8];
+                        if (r < R) {
+                            const double2 *src =
+                                reinterpret_cast<const double2 *>(xbc + (int64_t)(r0 + r) * K + 8 * c);
+#pragma unroll
+                            for (int j = 0; j < 4; j++) {
+                                const double2 q = src[j];
+                                v[2 * j] = (float)q.x;
+                                v[2 * j + 1] = (float)q.y;
+                            }
+                        } else {
+#pragma unroll
+                            for (int j = 0; j < 8; j++) v[j] = 0.0f;
+                        }
+                        uint4 hi, lo;
+                        split8(v, hi, lo);
+                        *reinterpret_cast<uint4 *>(xa_hi + lg_sw128_offset(r, c)) = hi;
+                        *reinterpret_cast<uint4 *>(xa_lo + lg_sw128_offset(r, c)) = lo;
+                    }
+                    // FP64 mean increment xb^T wbar, one row per thread
+                    if (tid < R) {
+                        const double *src = xbc + (int64_t)(r0 + tid) * K;
+                        double s = 0.0;
+                        for (int i = 0; i < K; i++) s += src[i] * wbar[i];
+                        inc[tid] = s;
+                    }
+                    lg_fence_async_smem();
+                    __syncthreads();
+                    if (tid == 0) {
+                        lg_tc_fence_after();
+                        const uint64_t dh = lg_desc_sw128(lg_smem_u32(xa_hi)), dl = lg_desc_sw128(lg_smem_u32(xa_lo));
+                        const uint64_t th = lg_desc_sw128(lg_smem_u32(tb_hi)), tl = lg_desc_sw128(lg_smem_u32(tb_lo));
+#pragma unroll
+                        for (int kk = 0; kk < K / 16; kk++) {
+                            lg_umma_bf16(tmem, dh + 2 * kk, th + 2 * kk, idesc, kk > 0 ? 1u : 0u);
+                            lg_umma_bf16(tmem, dh + 2 * kk, tl + 2 * kk, idesc, 1u);
+                            lg_umma_bf16(tmem, dl + 2 * kk, th + 2 * kk, idesc, 1u);
+                        }
+                        lg_umma_commit(&mbar[2]);
+                    }
+                    ncommit[2]++;
+                    pending[2] = true;
+                    if (!wait_bar(2)) {
+                        failed = true;
+                        break;
+                    }
+                    lg_tc_fence_after();
+                    if (warp < 4) {
+                        const int r = warp * 32 + lane;
+                        float v[K];
+#pragma unroll
+                        for (int c0 = 0; c0 < K; c0 += 16)
+                            lg_tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v + c0);
+                        if (r < R) {
+                            double mean = 0.0;
+#pragma unroll
+                            for (int e = 0; e < K; e++) mean += (double)v[e];
+                            mean = mean / K;
+                            const int64_t row = col * n + r0 + r;
+                            axa[row] = axb[row] + inc[r] + mean;
+                            double *dst = xac + (int64_t)(r0 + r) * K;
+#pragma unroll
+                            for (int e = 0; e < K; e += 2)
+                                *reinterpret_cast<double2 *>(dst + e) =
+                                    make_double2((double)v[e] - mean, (double)v[e + 1] - mean);
+                        }
+                    }
+                    lg_tc_fence_before();
+                    __syncthreads();
+                }
+            }
+        if (failed) break;
+    }
+    if (failed && tid == 0) atomicOr(status, LG_ST_TIMEOUT);
+    // let any MMA still in flight finish before the TMEM is freed
+    for (int b = 0; b < 3; b++) wait_bar(b);
+    lg_tc_fence_before();
+    __syncthreads();
+    lg_tc_fence_after();
+    if (warp == 0) lg_tmem_dealloc(tmem, C::TMEM_COLS);
+}
+
+template <int K>
+cudaError_t launch_mixed(letkf_ctx *ctx, const LgGrid &g, const double *xb, const double *axb,
+                         double *xa, double *axa, double *trans_out, double *w_out)
+{
+    const size_t smem = MCfg<K>::SMEM;
+    cudaError_t e = cudaFuncSetAttribute(k_core_mixed<K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    if (ctx->ncubes <= 0) return cudaSuccess;
+    int dev = 0, nsm = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_core_mixed<K>, kT, smem);
+    if (per_sm < 1) per_sm = 1;
+    // persistent grid: each CTA allocates its tensor memory once
+    const int64_t want = (int64_t)nsm * per_sm;
+    const unsigned blocks = (unsigned)(ctx->ncubes < want ? ctx->ncubes : want);
+    lg_count_launch();
+    k_core_mixed<K><<<blocks, kT, smem, ctx->stream>>>(
+        g, lg_params(ctx), ctx->d_yb.p, ctx->d_ys32.p, ctx->d_dep.p, ctx->d_rinvf.p, ctx->d_lidx.p,
+        ctx->d_lrloc.p, ctx->d_loff.p, ctx->d_lcnt.p, ctx->ncubes, xb, axb, xa, axa, trans_out, w_out,
+        ctx->d_counters.p, ctx->d_status.p);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+bool lg_mixed_supports(int k) { return k == 32 || k == 48 || k == 64; }
+
+cudaError_t lg_launch_core_mixed(letkf_ctx *ctx, const LgGrid &g, const double *xb, const double *axb,
+                                 double *xa, double *axa, bool keep_trans)
+{
+    double *tr = keep_trans ? ctx->d_trans.p : nullptr;
+    double *w = keep_trans ? ctx->d_w.p : nullptr;
+    switch (g.k) {
+    case 32: return launch_mixed<32>(ctx, g, xb, axb, xa, axa, tr, w);
+    case 48: return launch_mixed<48>(ctx, g, xb, axb, xa, axa, tr, w);
+    case 64: return launch_mixed<64>(ctx, g, xb, axb, xa, axa, tr, w);
+    default: return cudaErrorInvalidValue;
+    }
+}

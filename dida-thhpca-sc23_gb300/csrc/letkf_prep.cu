@@ -58,6 +58,7 @@ k_obs_prepare(LgGrid g, LgParams prm, const double *__restrict__ xb, const doubl
               const double *__restrict__ orinv, double *__restrict__ yb, double *__restrict__ dep,
               float *__restrict__ rinvf, double *__restrict__ os, double *__restrict__ oc,
               double *__restrict__ oyr, float4 *__restrict__ oxyz, int *__restrict__ obucket,
+              float *__restrict__ ys32,
               int nblat, int nblon, double cell_lat, double cell_lon, unsigned *status)
 {
     const int lane = threadIdx.x & 31;
@@ -78,7 +79,10 @@ k_obs_prepare(LgGrid g, LgParams prm, const double *__restrict__ xb, const doubl
         }
         if (ok && is3d && prm.h_mode == 0) ok = oph[o] > 0.0;
         if (!ok) {
-            for (int e = lane; e < k; e += 32) yb[o * k + e] = 0.0;
+            for (int e = lane; e < k; e += 32) {
+                yb[o * k + e] = 0.0;
+                if (ys32) ys32[o * k + e] = 0.0f;
+            }
             if (lane == 0) {
                 dep[o] = 0.0;
                 rinvf[o] = 0.0f;
@@ -153,6 +157,15 @@ k_obs_prepare(LgGrid g, LgParams prm, const double *__restrict__ xb, const doubl
         for (int j = 0; j < LG_MAX_ENS / 32; j++) {
             const int e = lane + 32 * j;
             if (e < k) yb[o * k + e] = yv[j] - mean;
+        }
+        if (ys32) {
+            // scaled perturbations for the tensor-core products: y sqrt(rdiaginv)
+            const double sr = sqrt((double)(float)orinv[o]);
+#pragma unroll
+            for (int j = 0; j < LG_MAX_ENS / 32; j++) {
+                const int e = lane + 32 * j;
+                if (e < k) ys32[o * k + e] = (float)((yv[j] - mean) * sr);
+            }
         }
         if (lane == 0) {
             dep[o] = oyo[o] - mean;
@@ -247,6 +260,7 @@ cudaError_t lg_launch_obs_prepare(letkf_ctx *ctx, const LgGrid &g, const double 
     k_obs_prepare<<<blocks, 256, 0, ctx->stream>>>(
         g, prm, xb, axb, nobs, olat, olon, oph, olev, ovar, oyo, orinv, ctx->d_yb.p, ctx->d_dep.p,
         ctx->d_rinvf.p, ctx->d_os.p, ctx->d_oc.p, ctx->d_oyr.p, ctx->d_oxyz.p, ctx->d_obucket.p,
+        ctx->params.precision == LETKF_PREC_MIXED ? ctx->d_ys32.p : nullptr,
         ctx->nblat, ctx->nblon, ctx->cell_lat, ctx->cell_lon, ctx->d_status.p);
     return cudaGetLastError();
 }

@@ -14,7 +14,7 @@
 
 #include <stdint.h>
 
-#define LG_MBAR_SPIN_LIMIT (1u << 26)
+#define LG_MBAR_SPIN_LIMIT (1u << 22)
 
 __device__ __forceinline__ uint32_t lg_smem_u32(const void *p)
 {

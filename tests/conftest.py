@@ -56,3 +56,15 @@ def field_rel_err(a, b, w):
         s = np.abs(b[:, sl]).max()
         out[nm] = float(d / s) if s > 0 else float(d)
     return out
+
+
+def spread(xa):
+    """Ensemble spread per column and row: sqrt(mean over members of xa^2)."""
+    return np.sqrt(np.mean(xa * xa, axis=-1))
+
+
+def mean_spread_errors(xa, axa, xa_ref, axa_ref, w):
+    """Per-variable relative errors of the analysis mean and spread (max abs
+    difference over the variable's rows and columns / max abs reference)."""
+    return {"mean": field_rel_err(axa, axa_ref, w),
+            "spread": field_rel_err(spread(xa), spread(xa_ref), w)}

@@ -1,0 +1,93 @@
+"""Mixed-precision form (BF16 hi/lo tensor-core products, FP64 eigensolve
+refinement and mean increment) against the FP64 oracle and the FP64 GPU form.
+
+Bar: relative error of the analysis mean and of the analysis spread of every
+state variable (ps, u, v, T) within 1e-4 of the FP64 result; local observation
+sets identical (the search is shared with the FP64 form).
+"""
+import numpy as np
+import pytest
+
+from conftest import mean_spread_errors, pkg
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+TOL_MIXED = 1e-4
+
+
+@pytest.fixture(scope="module")
+def letkf():
+    pkg("build").build()
+    m = pkg("letkf")
+    m.load_library()
+    return m
+
+
+@pytest.fixture(scope="module")
+def synthetic():
+    return pkg("synthetic")
+
+
+def assert_mixed(xa, axa, xa_ref, axa_ref, w):
+    errs = mean_spread_errors(xa, axa, xa_ref, axa_ref, w)
+    worst = max(max(v.values()) for v in errs.values())
+    assert worst <= TOL_MIXED, errs
+    return errs
+
+
+@pytest.mark.parametrize("k", [32, 48, 64])
+def test_mixed_small_cases_vs_oracle(letkf, synthetic, k):
+    w = synthetic.small_case(nlat=12, nlon=24, nz=4, k=k, nobs=900, loc_dist_km=900.0, seed=100 + k)
+    ctx = letkf.LetkfGPU.from_workload(w, precision=letkf.LETKF_PREC_MIXED)
+    xa, axa = ctx.run(w.xb, w.axb, w.obs)
+    orc = O.Oracle(w)
+    off_g, idx_g, _ = ctx.local_obs()
+    off_o, idx_o, _ = orc.local_obs()
+    assert np.array_equal(off_g, off_o) and np.array_equal(idx_g, idx_o)
+    xa_o, axa_o = orc.run()
+    assert_mixed(xa, axa, xa_o, axa_o, w)
+    assert np.isfinite(xa).all()
+
+
+def test_mixed_no_observations(letkf, synthetic):
+    w = synthetic.small_case(nlat=8, nlon=16, nz=2, k=32, nobs=10, seed=2)
+    w.obs = {key: v[:0] for key, v in w.obs.items()}
+    ctx = letkf.LetkfGPU.from_workload(w, precision=letkf.LETKF_PREC_MIXED)
+    xa, axa = ctx.run(w.xb, w.axb, w.obs)
+    assert np.max(np.abs(axa - w.axb)) <= 1e-6 * np.abs(w.axb).max()
+    assert np.max(np.abs(xa - np.sqrt(w.inflation) * w.xb)) <= 1e-4 * np.abs(w.xb).max()
+
+
+def test_mixed_transforms_close_to_fp64(letkf, synthetic):
+    w = synthetic.small_case(nlat=10, nlon=20, nz=3, k=64, nobs=1500, loc_dist_km=1000.0, seed=31)
+    fp = letkf.LetkfGPU.from_workload(w)
+    mx = letkf.LetkfGPU.from_workload(w, precision=letkf.LETKF_PREC_MIXED)
+    fp.keep_trans(True)
+    mx.keep_trans(True)
+    fp.run(w.xb, w.axb, w.obs)
+    mx.run(w.xb, w.axb, w.obs)
+    cubes = np.arange(fp.ncubes)
+    t64, w64 = fp.last_trans(cubes)
+    t16, w16 = mx.last_trans(cubes)
+    assert np.max(np.abs(t16 - t64)) <= 1e-4 * np.abs(t64).max()
+    assert np.max(np.abs(w16 - w64)) <= 1e-3 * np.abs(w64).max()
+
+
+def test_mixed_config0_vs_oracle(letkf, synthetic):
+    w = synthetic.config(0)
+    ctx = letkf.LetkfGPU.from_workload(w, precision=letkf.LETKF_PREC_MIXED)
+    xa, axa = ctx.run(w.xb, w.axb, w.obs)
+    xa_o, axa_o = O.Oracle(w).run()
+    assert_mixed(xa, axa, xa_o, axa_o, w)
+
+
+def test_mixed_config1_vs_fp64(letkf, synthetic):
+    w = synthetic.config(1)
+    fp = letkf.LetkfGPU.from_workload(w)
+    mx = letkf.LetkfGPU.from_workload(w, precision=letkf.LETKF_PREC_MIXED)
+    xa64, axa64 = fp.run(w.xb, w.axb, w.obs)
+    xa16, axa16 = mx.run(w.xb, w.axb, w.obs)
+    errs = assert_mixed(xa16, axa16, xa64, axa64, w)
+    st = mx.stats()
+    assert st["n_borderline"] == 0
+    print("config1 mixed vs fp64:", errs)
