@@ -285,10 +285,11 @@ def _field_errors(w, xa, axa, xa_ref, axa_ref):
 
 def mixed_fp64_flops(w, sum_p):
     """FP64 work the mixed form does by design per analysis: g (k p), the
-    refinement (A'Xhat, Xhat E: k^3 each; S, R: k^2(k+1)/2 each), T
-    (k^2(k+1)/2), wbar (2k^2) and the mean increment (n k) multiply-adds."""
+    refinement (A'Xhat: k^3; S, R: k^2(k+1)/2 each; the small correction
+    Xhat E is FP32), T (k^2(k+1)/2), wbar (2k^2) and the mean increment (n k)
+    multiply-adds."""
     k, n, ncol = w.k, w.n, w.ncol
-    fma = k * sum_p + ncol * (2 * k ** 3 + 1.5 * k * k * (k + 1) + 2 * k * k + n * k)
+    fma = k * sum_p + ncol * (k ** 3 + 1.5 * k * k * (k + 1) + 2 * k * k + n * k)
     return 2.0 * fma
 
 
@@ -427,6 +428,7 @@ def run_ours(args, rank, world, local_rank):
                    "form": "mixed precision (precision 1)" if head == "mixed" else "plain FP64",
                    "columns": w.ncol, "ensemble": w.k, "obs": int(w.obs["lat"].size),
                    "sum_p": st["sum_p"], "max_p": st["max_p"],
+                   "jacobi_max_sweeps": st["max_sweeps"], "jacobi_sweep_cap_hits": st["n_not_converged"],
                    "l2": "inputs larger than L2 (xb 3.2 GB)", "parallelism": f"replicas x{world}"},
         "e2e": {"value": world * w.ncol / (ms_e2e * 1e-3), "unit": "columns/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,

@@ -19,7 +19,9 @@
 //      "Iterative refinement for symmetric eigenvalue decomposition", Japan J.
 //      Indust. Appl. Math. 35 (2018), Algorithm 1): R = I - Xhat^T Xhat,
 //      S = Xhat^T A' Xhat, lambda_i = s_ii/(1-r_ii), E from S, R and the gaps,
-//      X = Xhat + Xhat E; the eigenpairs come out FP64-accurate.
+//      X = Xhat + Xhat E; the eigenpairs come out FP64-accurate.  R, S and the
+//      products they need are FP64; the correction Xhat E, whose size is that
+//      of Xhat's error, is formed in FP32 and added in FP64.
 //   5. T = X diag(sqrt((k-1)/lambda)) X^T and wbar = X diag(1/lambda) X^T g in FP64.
 //   6. xa = xb^T T on tcgen05 (hi/lo BF16 of both operands, three products in
 //      one accumulator); the mean increment xb^T wbar is FP64.
@@ -43,7 +45,8 @@ struct MCfg {
     static constexpr int G = (K / 2 * 16 <= kT) ? 16 : (K / 2 * 8 <= kT) ? 8 : 4;
     static constexpr int CH = 64;                      // observations per MMA tile (K of the MMA)
     static constexpr uint32_t TMEM_COLS = 64;
-    static constexpr size_t AREA = 48 * 1024;          // tiles / FP32 scratch / Xhat, P, X
+    static constexpr int LDW = K + 1;                  // padded column stride of the FP32 Jacobi
+    static constexpr size_t AREA = 64 * 1024;          // tiles / FP32 scratch / P, R, Xhat
     static constexpr size_t B1 = sizeof(double) * K * K;
     static constexpr size_t VEC = sizeof(double) * (7 * K + 128 + CH) +
                                   sizeof(float) * (2 * K + CH) + sizeof(int) * CH;
@@ -181,7 +184,8 @@ k_core_mixed(LgGrid g, LgParams prm, const double *__restrict__ yb, const float 
                 *reinterpret_cast<uint4 *>(area + b * 16384 + lg_sw128_offset(r, c)) = make_uint4(0, 0, 0, 0);
             }
         }
-        double gacc = 0.0;
+        double gacc = 0.0;                       // member tid % K, obs parts tid / K
+        const int gpart = tid / K, nparts = kT / K;
         const int nch = (p + CH - 1) / CH;
         for (int ch = 0; ch < nch; ch++) {
             const int b = ch & 1;
@@ -206,8 +210,11 @@ k_core_mixed(LgGrid g, LgParams prm, const double *__restrict__ yb, const float 
                 }
             }
             __syncthreads();
-            if (tid < K)
-                for (int o = 0; o < cnt; o++) gacc += yb[(int64_t)gidx[o] * K + tid] * cd[o];
+            if (gpart < nparts) {
+                const int m = tid % K;
+#pragma unroll 4
+                for (int o = gpart; o < cnt; o += nparts) gacc += yb[(int64_t)gidx[o] * K + m] * cd[o];
+            }
             for (int t = tid; t < K * 8; t += kT) {
                 const int m = t % K, c = t / K;
                 float v[8];
@@ -239,13 +246,25 @@ k_core_mixed(LgGrid g, LgParams prm, const double *__restrict__ yb, const float 
             failed = true;
             break;
         }
-        if (tid < K) gv[tid] = gacc;
+        // reduce the partial g sums of the obs parts in a fixed order (the MMAs
+        // are done, so the tile area is free)
+        double *gpart_sum = reinterpret_cast<double *>(area + 32768);
+        if (gpart < nparts) gpart_sum[gpart * K + tid % K] = gacc;
+        __syncthreads();
+        if (tid < K) {
+            double s = 0.0;
+            for (int q = 0; q < nparts; q++) s += gpart_sum[q * K + tid];
+            gv[tid] = s;
+        }
+        __syncthreads();
         lg_tc_fence_after();
 
         // ---------------- phase 2: A' = HH + LH + LH^T + (k-1)/rho I -------------------
+        constexpr int LDD = K + 1;                             // padded rows: conflict-free both ways
         float *Dhh = reinterpret_cast<float *>(area);
-        float *Dlh = Dhh + K * K;
-        float *W32 = reinterpret_cast<float *>(area + 32768);
+        float *Dlh = Dhh + K * LDD;
+        float *W32 = reinterpret_cast<float *>(area + 34816);  // FP32 Jacobi columns (stride LDW), past Dlh
+        double *Xr = reinterpret_cast<double *>(area + 32768);  // Xhat by rows, Xr[row*K + j], after the Jacobi
         if (warp < 4) {
             const int row = warp * 32 + lane;
 #pragma unroll
@@ -259,47 +278,62 @@ k_core_mixed(LgGrid g, LgParams prm, const double *__restrict__ yb, const float 
                 }
                 if (row < K) {
 #pragma unroll
-                    for (int j = 0; j < 16; j++) Dhh[row * K + c0 + j] = v[j];
+                    for (int j = 0; j < 16; j++) Dhh[row * LDD + c0 + j] = v[j];
                 } else if (row < 2 * K) {
 #pragma unroll
-                    for (int j = 0; j < 16; j++) Dlh[(row - K) * K + c0 + j] = v[j];
+                    for (int j = 0; j < 16; j++) Dlh[(row - K) * LDD + c0 + j] = v[j];
                 }
             }
         }
         lg_tc_fence_before();
         __syncthreads();
+        // A = HH + LH + LH^T is formed in FP32 (the accumulators are FP32), then
+        // A' = A + (k-1)/rho I in FP64 and in FP32 for the Jacobi
         const double cdiag = (double)(K - 1) / prm.inflation;
         double fro = 0.0;
         for (int idx = tid; idx < K * K; idx += kT) {
             const int i = idx / K, j = idx % K;
-            double a = 0.5 * ((double)Dhh[i * K + j] + (double)Dhh[j * K + i]) + (double)Dlh[i * K + j] +
-                       (double)Dlh[j * K + i];
-            if (i == j) a += cdiag;
+            const float a32 = 0.5f * (Dhh[i * LDD + j] + Dhh[j * LDD + i]) + (Dlh[i * LDD + j] + Dlh[j * LDD + i]);
+            const double a = (double)a32 + (i == j ? cdiag : 0.0);
             B1[idx] = a;
+            W32[(idx / K) * C::LDW + idx % K] = (float)a;
             fro += a * a;
         }
-        __syncthreads();
-        for (int idx = tid; idx < K * K; idx += kT) W32[idx] = (float)B1[idx];
         const double normA = sqrt(block_sum(fro, red));
 
         // ---------------- phase 3: FP32 Jacobi -> Xhat (columns of W32) ----------------
-        const int sw = lg_jacobi<float, K, C::G>(W32, nrm32, rot32, &s_rot, 2e-6f, 24);
+        const int sw = lg_jacobi<float, K, C::G, C::LDW, false>(W32, nrm32, rot32, &s_rot, 2e-6f, 24);
         if (tid == 0) {
             atomicMax(&counters[LG_CNT_MAXSWEEP], (unsigned long long)sw);
             if (sw > 24) atomicAdd(&counters[LG_CNT_NOTCONV], 1ull);
         }
         if (tid < K) {
             float s = 0.0f;
-            for (int r = 0; r < K; r++) s += W32[tid * K + r] * W32[tid * K + r];
+            for (int r = 0; r < K; r++) s += W32[tid * C::LDW + r] * W32[tid * C::LDW + r];
             nrm32[tid] = 1.0f / sqrtf(s);
         }
         __syncthreads();
-        for (int idx = tid; idx < K * K; idx += kT) W32[idx] *= nrm32[idx / K];
+        // Xhat (FP32 values) by rows in FP64: converted once.  W32 and Xr share
+        // memory, so the values pass through registers first.
+        {
+            constexpr int PER = (K * K + kT - 1) / kT;
+            float xv[PER];
+#pragma unroll
+            for (int q = 0; q < PER; q++) {
+                const int idx = tid + q * kT;
+                xv[q] = (idx < K * K) ? W32[(idx % K) * C::LDW + idx / K] * nrm32[idx % K] : 0.0f;
+            }
+            __syncthreads();
+#pragma unroll
+            for (int q = 0; q < PER; q++) {
+                const int idx = tid + q * kT;
+                if (idx < K * K) Xr[idx] = (double)xv[q];
+            }
+        }
         __syncthreads();
-        const float *Xh = W32;                       // column j at Xh[j*K]
 
         // ---------------- phase 4: FP64 refinement (Ogita-Aishima) ---------------------
-        double *P = reinterpret_cast<double *>(area);   // column j = A' xhat_j
+        double *P = reinterpret_cast<double *>(area);   // A' Xhat, row-major
 #pragma unroll
         for (int m = 0; m < C::MF; m++) {
             if (!fok[m]) continue;
@@ -310,17 +344,19 @@ k_core_mixed(LgGrid g, LgParams prm, const double *__restrict__ yb, const float 
                 const double2 a01 = *reinterpret_cast<const double2 *>(B1 + l * K + 4 * fbi[m]);
                 const double2 a23 = *reinterpret_cast<const double2 *>(B1 + l * K + 4 * fbi[m] + 2);
                 const double a[4] = {a01.x, a01.y, a23.x, a23.y};
+                const double2 x01 = *reinterpret_cast<const double2 *>(Xr + l * K + 4 * fbj[m]);
+                const double2 x23 = *reinterpret_cast<const double2 *>(Xr + l * K + 4 * fbj[m] + 2);
+                const double x[4] = {x01.x, x01.y, x23.x, x23.y};
 #pragma unroll
-                for (int jj = 0; jj < 4; jj++) {
-                    const double x = (double)Xh[(4 * fbj[m] + jj) * K + l];
+                for (int i = 0; i < 4; i++)
 #pragma unroll
-                    for (int i = 0; i < 4; i++) acc[i * 4 + jj] += a[i] * x;
-                }
+                    for (int jj = 0; jj < 4; jj++) acc[i * 4 + jj] += a[i] * x[jj];
             }
+            // P row-major: P[row*K + col] = (A' Xhat)[row][col]
 #pragma unroll
             for (int i = 0; i < 4; i++)
 #pragma unroll
-                for (int jj = 0; jj < 4; jj++) P[(4 * fbj[m] + jj) * K + 4 * fbi[m] + i] = acc[i * 4 + jj];
+                for (int jj = 0; jj < 4; jj++) P[(4 * fbi[m] + i) * K + 4 * fbj[m] + jj] = acc[i * 4 + jj];
         }
         __syncthreads();
         // S = Xhat^T A' Xhat (lower blocks, mirrored) into B1
@@ -332,12 +368,12 @@ k_core_mixed(LgGrid g, LgParams prm, const double *__restrict__ yb, const float 
                 for (int i = 0; i < 16; i++) sacc[m][i] = 0.0;
                 if (!lok[m]) continue;
                 for (int l = 0; l < K; l++) {
-                    double x[4], q[4];
-#pragma unroll
-                    for (int i = 0; i < 4; i++) {
-                        x[i] = (double)Xh[(4 * lbi[m] + i) * K + l];
-                        q[i] = P[(4 * lbj[m] + i) * K + l];
-                    }
+                    const double2 x01 = *reinterpret_cast<const double2 *>(Xr + l * K + 4 * lbi[m]);
+                    const double2 x23 = *reinterpret_cast<const double2 *>(Xr + l * K + 4 * lbi[m] + 2);
+                    const double2 q01 = *reinterpret_cast<const double2 *>(P + l * K + 4 * lbj[m]);
+                    const double2 q23 = *reinterpret_cast<const double2 *>(P + l * K + 4 * lbj[m] + 2);
+                    const double x[4] = {x01.x, x01.y, x23.x, x23.y};
+                    const double q[4] = {q01.x, q01.y, q23.x, q23.y};
 #pragma unroll
                     for (int i = 0; i < 4; i++)
 #pragma unroll
@@ -369,12 +405,12 @@ k_core_mixed(LgGrid g, LgParams prm, const double *__restrict__ yb, const float 
                 for (int i = 0; i < 16; i++) racc[m][i] = 0.0;
                 if (!lok[m]) continue;
                 for (int l = 0; l < K; l++) {
-                    double x[4], y[4];
-#pragma unroll
-                    for (int i = 0; i < 4; i++) {
-                        x[i] = (double)Xh[(4 * lbi[m] + i) * K + l];
-                        y[i] = (double)Xh[(4 * lbj[m] + i) * K + l];
-                    }
+                    const double2 x01 = *reinterpret_cast<const double2 *>(Xr + l * K + 4 * lbi[m]);
+                    const double2 x23 = *reinterpret_cast<const double2 *>(Xr + l * K + 4 * lbi[m] + 2);
+                    const double2 y01 = *reinterpret_cast<const double2 *>(Xr + l * K + 4 * lbj[m]);
+                    const double2 y23 = *reinterpret_cast<const double2 *>(Xr + l * K + 4 * lbj[m] + 2);
+                    const double x[4] = {x01.x, x01.y, x23.x, x23.y};
+                    const double y[4] = {y01.x, y01.y, y23.x, y23.y};
 #pragma unroll
                     for (int i = 0; i < 4; i++)
 #pragma unroll
@@ -422,45 +458,60 @@ k_core_mixed(LgGrid g, LgParams prm, const double *__restrict__ yb, const float 
             B1[idx] = e;
         }
         __syncthreads();
-        // X = Xhat + Xhat E (columns) into the area (R is dead)
-        double *Xp = reinterpret_cast<double *>(area);
+        // X = Xhat + Xhat E into B1 (by columns).  E is of the size of Xhat's
+        // error (~1e-6), so the correction product Xhat E is formed in FP32
+        // (rounding ~1e-13 absolute) and added to Xhat in FP64.
+        {
+            float *X32c = reinterpret_cast<float *>(area);           // Xhat by columns, FP32
+            float *E32 = reinterpret_cast<float *>(area + 16384);    // E by rows, FP32
+            for (int idx = tid; idx < K * K; idx += kT) {
+                const int l = idx / K, r = idx % K;
+                X32c[idx] = (float)Xr[r * K + l];
+                E32[idx] = (float)B1[idx];
+            }
+            __syncthreads();
+            float acc[C::MF][16];
 #pragma unroll
-        for (int m = 0; m < C::MF; m++) {
-            if (!fok[m]) continue;
-            double acc[16];
+            for (int m = 0; m < C::MF; m++) {
 #pragma unroll
-            for (int i = 0; i < 16; i++) acc[i] = 0.0;
-            for (int l = 0; l < K; l++) {
-                // rows 4*fbi.. of column l of Xhat, row l of E at columns 4*fbj..
-                double x[4], e[4];
+                for (int i = 0; i < 16; i++) acc[m][i] = 0.0f;
+                if (!fok[m]) continue;
+                for (int l = 0; l < K; l++) {
+                    const float4 xv = *reinterpret_cast<const float4 *>(X32c + l * K + 4 * fbi[m]);
+                    const float4 ev = *reinterpret_cast<const float4 *>(E32 + l * K + 4 * fbj[m]);
+                    const float x[4] = {xv.x, xv.y, xv.z, xv.w};
+                    const float e[4] = {ev.x, ev.y, ev.z, ev.w};
 #pragma unroll
-                for (int i = 0; i < 4; i++) x[i] = (double)Xh[l * K + 4 * fbi[m] + i];
-                const double2 e01 = *reinterpret_cast<const double2 *>(B1 + l * K + 4 * fbj[m]);
-                const double2 e23 = *reinterpret_cast<const double2 *>(B1 + l * K + 4 * fbj[m] + 2);
-                e[0] = e01.x; e[1] = e01.y; e[2] = e23.x; e[3] = e23.y;
+                    for (int i = 0; i < 4; i++)
+#pragma unroll
+                        for (int jj = 0; jj < 4; jj++) acc[m][i * 4 + jj] += x[i] * e[jj];
+                }
+            }
+#pragma unroll
+            for (int m = 0; m < C::MF; m++) {
+                if (!fok[m]) continue;
 #pragma unroll
                 for (int i = 0; i < 4; i++)
 #pragma unroll
-                    for (int jj = 0; jj < 4; jj++) acc[i * 4 + jj] += x[i] * e[jj];
+                    for (int jj = 0; jj < 4; jj++) {
+                        const int row = 4 * fbi[m] + i, col = 4 * fbj[m] + jj;
+                        B1[col * K + row] = Xr[row * K + col] + (double)acc[m][i * 4 + jj];
+                    }
             }
-            // write after every thread has read Rm? Rm is not read here; Xp aliases
-            // Rm but Rm was last read before the previous barrier.
-#pragma unroll
-            for (int i = 0; i < 4; i++)
-#pragma unroll
-                for (int jj = 0; jj < 4; jj++) {
-                    const int row = 4 * fbi[m] + i, col = 4 * fbj[m] + jj;
-                    Xp[col * K + row] = (double)Xh[col * K + row] + acc[i * 4 + jj];
-                }
         }
         __syncthreads();
+        const double *Xp = B1;                         // X by columns
 
         // ---------------- phase 5: T and wbar in FP64 -----------------------------------
-        if (tid < K) {
+        for (int j = warp; j < K; j += kT / 32) {          // one warp per eigenvector
             double dot = 0.0;
-            for (int l = 0; l < K; l++) dot += Xp[tid * K + l] * gv[l];
-            hco[tid] = dot / lam[tid];
-            fco[tid] = sqrt((double)(K - 1) / lam[tid]);
+            for (int l = lane; l < K; l += 32) dot += Xp[j * K + l] * gv[l];
+#pragma unroll
+            for (int s = 16; s > 0; s >>= 1) dot += __shfl_xor_sync(0xffffffffu, dot, s);
+            if (lane == 0) {
+                hco[j] = dot / lam[j];
+                fco[j] = sqrt((double)(K - 1) / lam[j]);
+            }
         }
         __syncthreads();
         if (tid < K) {
@@ -477,19 +528,19 @@ k_core_mixed(LgGrid g, LgParams prm, const double *__restrict__ yb, const float 
                 if (!lok[m]) continue;
                 for (int j = 0; j < K; j++) {
                     const double f = fco[j];
-                    double a[4], bq[4];
-#pragma unroll
-                    for (int i = 0; i < 4; i++) {
-                        a[i] = Xp[j * K + 4 * lbi[m] + i];
-                        bq[i] = Xp[j * K + 4 * lbj[m] + i] * f;
-                    }
+                    const double2 a01 = *reinterpret_cast<const double2 *>(Xp + j * K + 4 * lbi[m]);
+                    const double2 a23 = *reinterpret_cast<const double2 *>(Xp + j * K + 4 * lbi[m] + 2);
+                    const double2 b01 = *reinterpret_cast<const double2 *>(Xp + j * K + 4 * lbj[m]);
+                    const double2 b23 = *reinterpret_cast<const double2 *>(Xp + j * K + 4 * lbj[m] + 2);
+                    const double a[4] = {a01.x, a01.y, a23.x, a23.y};
+                    const double bq[4] = {b01.x * f, b01.y * f, b23.x * f, b23.y * f};
 #pragma unroll
                     for (int i = 0; i < 4; i++)
 #pragma unroll
                         for (int jj = 0; jj < 4; jj++) tacc[m][i * 4 + jj] += a[i] * bq[jj];
                 }
             }
-            // B1 (E) is no longer read: write T (symmetric, row-major)
+            __syncthreads();                  // X (in B1) is read by every thread above
 #pragma unroll
             for (int m = 0; m < C::ML; m++) {
                 if (!lok[m]) continue;
@@ -559,11 +610,13 @@ k_core_mixed(LgGrid g, LgParams prm, const double *__restrict__ yb, const float 
                         *reinterpret_cast<uint4 *>(xa_lo + lg_sw128_offset(r, c)) = lo;
                     }
                     // FP64 mean increment xb^T wbar, one row per thread
-                    if (tid < R) {
-                        const double *src = xbc + (int64_t)(r0 + tid) * K;
+                    for (int r = warp; r < R; r += kT / 32) {    // one warp per state row
+                        const double *src = xbc + (int64_t)(r0 + r) * K;
                         double s = 0.0;
-                        for (int i = 0; i < K; i++) s += src[i] * wbar[i];
-                        inc[tid] = s;
+                        for (int i = lane; i < K; i += 32) s += src[i] * wbar[i];
+#pragma unroll
+                        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+                        if (lane == 0) inc[r] = s;
                     }
                     lg_fence_async_smem();
                     __syncthreads();
@@ -630,11 +683,15 @@ cudaError_t launch_mixed(letkf_ctx *ctx, const LgGrid &g, const double *xb, cons
                                          (int)smem);
     if (e != cudaSuccess) return e;
     if (ctx->ncubes <= 0) return cudaSuccess;
-    int dev = 0, nsm = 0, per_sm = 0;
+    e = cudaFuncSetAttribute(k_core_mixed<K>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    if (e != cudaSuccess) return e;
+    int dev = 0, nsm = 0, smem_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_core_mixed<K>, kT, smem);
-    if (per_sm < 1) per_sm = 1;
+    cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
+    // two CTAs per SM when their shared memory fits (registers are capped at
+    // 128 per thread by the launch bounds, so two 256-thread CTAs fit)
+    const int per_sm = (2 * (smem + 1024) <= (size_t)smem_sm) ? 2 : 1;
     // persistent grid: each CTA allocates its tensor memory once
     const int64_t want = (int64_t)nsm * per_sm;
     const unsigned blocks = (unsigned)(ctx->ncubes < want ? ctx->ncubes : want);
