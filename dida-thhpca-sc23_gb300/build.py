@@ -29,8 +29,8 @@ def sources():
     return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
 
 
-def _compile(src: str, extra: list[str]) -> str:
-    obj = os.path.join(OUT, os.path.basename(src)[:-3] + ".o")
+def _compile(src: str, extra: list[str], out: str = OUT) -> str:
+    obj = os.path.join(out, os.path.basename(src)[:-3] + ".o")
     deps = [src] + [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".cuh", ".h"))]
     deps.append(os.path.join(REPO, "include", "letkf_gpu.h"))
     if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(d) for d in deps):
@@ -43,22 +43,25 @@ def _compile(src: str, extra: list[str]) -> str:
     return obj
 
 
-def build(verbose: bool = False, extra: list[str] | None = None) -> str:
-    """Compile and link the library; returns its path."""
-    os.makedirs(OUT, exist_ok=True)
+def build(verbose: bool = False, extra: list[str] | None = None, out_dir: str | None = None) -> str:
+    """Compile and link the library; returns its path.  `extra` adds nvcc flags
+    (e.g. -DLG_PHASE_CLOCKS) and `out_dir` builds into another directory."""
+    out = out_dir or OUT
+    lib = os.path.join(out, "libletkf_gpu.so")
+    os.makedirs(out, exist_ok=True)
     extra = list(extra or [])
     srcs = sources()
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
-        objs = list(ex.map(lambda s: _compile(s, extra), srcs))
-    if not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(o) for o in objs):
-        cmd = [nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-cudart", "shared",
+        objs = list(ex.map(lambda s: _compile(s, extra, out), srcs))
+    if not os.path.exists(lib) or os.path.getmtime(lib) < max(os.path.getmtime(o) for o in objs):
+        cmd = [nvcc(), *ARCH, "-shared", "-o", lib, *objs, "-cudart", "shared",
                "-Xlinker", f"-rpath,{os.path.join(CUDA_HOME, 'lib64')}"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     if verbose:
-        print(LIB)
-    return LIB
+        print(lib)
+    return lib
 
 
 if __name__ == "__main__":

@@ -69,6 +69,27 @@ __device__ __forceinline__ double lg_schr2(double ri)
     return 1.0;
 }
 
+// schr2 evaluated in FP32 with the same (default-real) literals, for
+// localization weights of the mixed-precision form; clamped at zero.
+__device__ __forceinline__ float lg_schr2f(float ri)
+{
+    if (ri > 2.0f) return 0.0f;
+    float r;
+    if (ri > 1.0f) {
+        float rj = ri / 12.0f - 0.5f;
+        rj = rj * ri + 0.625f;
+        rj = rj * ri + 1.666667f;
+        r = (rj * ri - 5.0f) * ri + 4.0f - 0.6666667f / ri;
+    } else if (ri > 0.0f) {
+        const float rk = ri * ri;
+        const float rj = (-0.25f * ri + 0.5f) * ri + 0.625f;
+        r = (rj * ri - 1.666667f) * rk + 1.0f;
+    } else {
+        r = 1.0f;
+    }
+    return r > 0.0f ? r : 0.0f;
+}
+
 // schr (box-car), letkf_yb.F90:270-285.
 __device__ __forceinline__ double lg_schr(double ri) { return (ri > 2.0) ? 0.0 : 1.0; }
 
@@ -118,6 +139,7 @@ struct LgBuckets {
 // Per-obs precomputed search data (original order).
 struct LgObsGeo {
     const double *s, *c, *yr;   // sin, cos of latitude, longitude in radians
+    const float4 *xyz;          // unit vector (x, y, z) and index bits, obs order
 };
 
 // ---------------------------------------------------------------------------

@@ -7,6 +7,28 @@ template <typename T> struct LgVec2;
 template <> struct LgVec2<double> { using type = double2; };
 template <> struct LgVec2<float> { using type = float2; };
 
+// Rotation (c, s, t) that zeroes the inner product gam of two columns with
+// squared norms al, be.  The FP32 variant uses the fast reciprocal and
+// reciprocal square root: it only feeds approximate eigenvectors that are
+// refined in FP64 afterwards.
+__device__ __forceinline__ void lg_rotation(double al, double be, double gam, double &c, double &s,
+                                            double &t)
+{
+    const double zeta = (be - al) / (2.0 * gam);
+    t = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
+    c = 1.0 / sqrt(1.0 + t * t);
+    s = c * t;
+}
+__device__ __forceinline__ void lg_rotation(float al, float be, float gam, float &c, float &s, float &t)
+{
+    const float zeta = (be - al) * __frcp_rn(2.0f * gam);
+    const float az = fabsf(zeta);
+    const float root = az < 1e18f ? az + sqrtf(fmaf(zeta, zeta, 1.0f)) : 2.0f * az;
+    t = copysignf(__frcp_rn(root), zeta);
+    c = rsqrtf(fmaf(t, t, 1.0f));
+    s = c * t;
+}
+
 __device__ __forceinline__ void lg_decode_block(int b, int &bi, int &bj)
 {
     int i = (int)((sqrtf(8.0f * (float)b + 1.0f) - 1.0f) * 0.5f);
@@ -43,6 +65,9 @@ __device__ int lg_jacobi(T *W, T *nrm, typename LgVec2<T>::type *rot, int *s_rot
         }
         if (tid == 0) *s_rot = 0;
         __syncthreads();
+        // round-robin pairs: pair 0 is (K-1, r); pair m > 0 is
+        // ((r + m) mod (K-1), (r - m) mod (K-1)), advanced incrementally
+        int pr = pair % (K - 1), qr = (K - 1 - pair) % (K - 1);
         for (int r = 0; r < K - 1; r++) {
             int p = 0, q = 0;
             T gam = 0;
@@ -51,9 +76,11 @@ __device__ int lg_jacobi(T *W, T *nrm, typename LgVec2<T>::type *rot, int *s_rot
                     p = K - 1;
                     q = r;
                 } else {
-                    p = (r + pair) % (K - 1);
-                    q = (r - pair + (K - 1)) % (K - 1);
+                    p = pr;
+                    q = qr;
                 }
+                if (++pr == K - 1) pr = 0;
+                if (++qr == K - 1) qr = 0;
                 const T *wp = W + p * LD, *wq = W + q * LD;
 #pragma unroll
                 for (int rr = lane; rr < K; rr += G) gam += wp[rr] * wq[rr];
@@ -76,10 +103,8 @@ __device__ int lg_jacobi(T *W, T *nrm, typename LgVec2<T>::type *rot, int *s_rot
                     const T al = nrm[pp], be = nrm[qq];
                     T c = 1, s = 0;
                     if (g2 * g2 > tol2 * (al * be)) {
-                        const T zeta = (be - al) / (T(2) * g2);
-                        const T t = (zeta >= T(0) ? T(1) : T(-1)) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
-                        c = T(1) / sqrt(T(1) + t * t);
-                        s = c * t;
+                        T t;
+                        lg_rotation(al, be, g2, c, s, t);
                         nrm[pp] = al - t * g2;
                         nrm[qq] = be + t * g2;
                         *s_rot = 1;
@@ -104,16 +129,111 @@ __device__ int lg_jacobi(T *W, T *nrm, typename LgVec2<T>::type *rot, int *s_rot
                 const T al = nrm[p], be = nrm[q];
                 __syncwarp();
                 if (gam * gam > tol2 * (al * be)) {
-                    const T zeta = (be - al) / (T(2) * gam);
-                    const T t = (zeta >= T(0) ? T(1) : T(-1)) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
-                    const T c = T(1) / sqrt(T(1) + t * t);
-                    const T s = c * t;
+                    T c, s, t;
+                    lg_rotation(al, be, gam, c, s, t);
                     T *wp = W + p * LD, *wq = W + q * LD;
 #pragma unroll
                     for (int rr = lane; rr < K; rr += G) {
                         const T a = wp[rr], b = wq[rr];
                         wp[rr] = c * a - s * b;
                         wq[rr] = s * a + c * b;
+                    }
+                    if (lane == 0) {
+                        nrm[p] = al - t * gam;
+                        nrm[q] = be + t * gam;
+                        *s_rot = 1;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+        const int rotated = *s_rot;
+        __syncthreads();
+        if (!rotated) break;
+    }
+    return sweep;
+}
+
+// FP32 one-sided Jacobi for the mixed-precision form.  Same round-robin
+// scheme as lg_jacobi, but each lane of a pair group owns a contiguous run of
+// K/G rows, keeps the pair's rows in registers between the inner product and
+// the rotation, and moves them with vector shared-memory accesses; every lane
+// computes the rotation (FP32, cheap) so a step needs one barrier.  LD (the
+// column stride) must keep the rows of a lane aligned for the vector width.
+template <int K, int G, int LD>
+__device__ int lg_jacobi32(float *W, float *nrm, int *s_rot, float tol, int max_sweeps)
+{
+    constexpr int NP = K / 2, RPL = K / G;
+    constexpr int VW = (RPL % 4 == 0) ? 4 : ((RPL % 2 == 0) ? 2 : 1);
+    static_assert(K % G == 0, "rows per lane");
+    static_assert(LD % VW == 0, "vector alignment of columns");
+    const int tid = threadIdx.x;
+    const int pair = tid / G, lane = tid % G;
+    const bool act = pair < NP;
+    const float tol2 = tol * tol;
+    int sweep;
+    for (sweep = 1; sweep <= max_sweeps; sweep++) {
+        if (tid < K) {
+            float s = 0.0f;
+            for (int r = 0; r < K; r++) s += W[tid * LD + r] * W[tid * LD + r];
+            nrm[tid] = s;
+        }
+        if (tid == 0) *s_rot = 0;
+        __syncthreads();
+        int pr = pair % (K - 1), qr = (K - 1 - pair) % (K - 1);
+        for (int r = 0; r < K - 1; r++) {
+            if (act) {
+                const int p = (pair == 0) ? K - 1 : pr;
+                const int q = (pair == 0) ? r : qr;
+                if (++pr == K - 1) pr = 0;
+                if (++qr == K - 1) qr = 0;
+                float *wp = W + p * LD + lane * RPL, *wq = W + q * LD + lane * RPL;
+                float a[RPL], b[RPL];
+#pragma unroll
+                for (int i = 0; i < RPL; i += VW) {
+                    if (VW == 4) {
+                        const float4 x = *reinterpret_cast<const float4 *>(wp + i);
+                        const float4 y = *reinterpret_cast<const float4 *>(wq + i);
+                        a[i] = x.x; a[i + 1] = x.y; a[i + 2] = x.z; a[i + 3] = x.w;
+                        b[i] = y.x; b[i + 1] = y.y; b[i + 2] = y.z; b[i + 3] = y.w;
+                    } else if (VW == 2) {
+                        const float2 x = *reinterpret_cast<const float2 *>(wp + i);
+                        const float2 y = *reinterpret_cast<const float2 *>(wq + i);
+                        a[i] = x.x; a[i + 1] = x.y;
+                        b[i] = y.x; b[i + 1] = y.y;
+                    } else {
+                        a[i] = wp[i];
+                        b[i] = wq[i];
+                    }
+                }
+                float gam = 0.0f;
+#pragma unroll
+                for (int i = 0; i < RPL; i++) gam = fmaf(a[i], b[i], gam);
+#pragma unroll
+                for (int o = G / 2; o > 0; o >>= 1) gam += __shfl_xor_sync(0xffffffffu, gam, o);
+                const float al = nrm[p], be = nrm[q];
+                __syncwarp();
+                if (gam * gam > tol2 * (al * be)) {
+                    float c, s, t;
+                    lg_rotation(al, be, gam, c, s, t);
+#pragma unroll
+                    for (int i = 0; i < RPL; i++) {
+                        const float x = a[i], y = b[i];
+                        a[i] = c * x - s * y;
+                        b[i] = s * x + c * y;
+                    }
+#pragma unroll
+                    for (int i = 0; i < RPL; i += VW) {
+                        if (VW == 4) {
+                            *reinterpret_cast<float4 *>(wp + i) = make_float4(a[i], a[i + 1], a[i + 2], a[i + 3]);
+                            *reinterpret_cast<float4 *>(wq + i) = make_float4(b[i], b[i + 1], b[i + 2], b[i + 3]);
+                        } else if (VW == 2) {
+                            *reinterpret_cast<float2 *>(wp + i) = make_float2(a[i], a[i + 1]);
+                            *reinterpret_cast<float2 *>(wq + i) = make_float2(b[i], b[i + 1]);
+                        } else {
+                            wp[i] = a[i];
+                            wq[i] = b[i];
+                        }
                     }
                     if (lane == 0) {
                         nrm[p] = al - t * gam;

@@ -35,6 +35,22 @@ namespace {
 
 constexpr int kT = 256;
 
+// Optional per-phase cycle counts of CTA 0 (built with -DLG_PHASE_CLOCKS).
+#ifdef LG_PHASE_CLOCKS
+#define LG_PHASE(i)                                                  \
+    do {                                                             \
+        if (tid == 0) {                                              \
+            const long long now_ = clock64();                        \
+            ph_cyc[i] += now_ - ph_last;                             \
+            ph_last = now_;                                          \
+        }                                                            \
+    } while (0)
+#else
+#define LG_PHASE(i) \
+    do {            \
+    } while (0)
+#endif
+
 template <int K>
 struct MCfg {
     static constexpr int KB = K / 4;
@@ -45,7 +61,7 @@ struct MCfg {
     static constexpr int G = (K / 2 * 16 <= kT) ? 16 : (K / 2 * 8 <= kT) ? 8 : 4;
     static constexpr int CH = 64;                      // observations per MMA tile (K of the MMA)
     static constexpr uint32_t TMEM_COLS = 64;
-    static constexpr int LDW = K + 1;                  // padded column stride of the FP32 Jacobi
+    static constexpr int LDW = K + 4;                  // padded column stride of the FP32 Jacobi
     static constexpr size_t AREA = 64 * 1024;          // tiles / FP32 scratch / P, R, Xhat
     static constexpr size_t B1 = sizeof(double) * K * K;
     static constexpr size_t VEC = sizeof(double) * (7 * K + 128 + CH) +
@@ -171,9 +187,20 @@ k_core_mixed(LgGrid g, LgParams prm, const double *__restrict__ yb, const float 
         fbj[m] = (fok[m] ? b : 0) % C::KB;
     }
 
-    for (int64_t cube = blockIdx.x; cube < ncubes; cube += gridDim.x) {
+#ifdef LG_PHASE_CLOCKS
+    long long ph_cyc[7] = {0, 0, 0, 0, 0, 0, 0};
+    long long ph_last = clock64();
+#endif
+    // each CTA takes a contiguous run of cubes (neighbours along latitude), so
+    // a cube's eigenvectors are a good start for the next one
+    const int64_t per_cta = (ncubes + gridDim.x - 1) / gridDim.x;
+    const int64_t cube_begin = (int64_t)blockIdx.x * per_cta;
+    const int64_t cube_end = min(ncubes, cube_begin + per_cta);
+    bool have_prev = false;
+    for (int64_t cube = cube_begin; cube < cube_end; cube++) {
         const int64_t off = loff[cube];
         const int p = lcnt[cube];
+        LG_PHASE(6);
 
         // ---------------- phase 1: A on the tensor cores, g in FP64 ----------------
         if (2 * K < 128) {
@@ -259,11 +286,14 @@ k_core_mixed(LgGrid g, LgParams prm, const double *__restrict__ yb, const float 
         __syncthreads();
         lg_tc_fence_after();
 
+        LG_PHASE(0);
         // ---------------- phase 2: A' = HH + LH + LH^T + (k-1)/rho I -------------------
         constexpr int LDD = K + 1;                             // padded rows: conflict-free both ways
         float *Dhh = reinterpret_cast<float *>(area);
         float *Dlh = Dhh + K * LDD;
-        float *W32 = reinterpret_cast<float *>(area + 34816);  // FP32 Jacobi columns (stride LDW), past Dlh
+        float *W32 = reinterpret_cast<float *>(area);          // FP32 Jacobi columns (stride LDW)
+        float *A32 = W32 + K * C::LDW;                          // A' in FP32 (warm start)
+        float *Vprev = reinterpret_cast<float *>(area + 49152); // previous cube's X by rows, FP32
         double *Xr = reinterpret_cast<double *>(area + 32768);  // Xhat by rows, Xr[row*K + j], after the Jacobi
         if (warp < 4) {
             const int row = warp * 32 + lane;
@@ -296,13 +326,46 @@ k_core_mixed(LgGrid g, LgParams prm, const double *__restrict__ yb, const float 
             const float a32 = 0.5f * (Dhh[i * LDD + j] + Dhh[j * LDD + i]) + (Dlh[i * LDD + j] + Dlh[j * LDD + i]);
             const double a = (double)a32 + (i == j ? cdiag : 0.0);
             B1[idx] = a;
-            W32[(idx / K) * C::LDW + idx % K] = (float)a;
             fro += a * a;
         }
-        const double normA = sqrt(block_sum(fro, red));
+        const double normA = sqrt(block_sum(fro, red));   // its barriers retire Dhh/Dlh
+        if (!have_prev) {
+            // cold start: the Jacobi works on A' itself
+            for (int idx = tid; idx < K * K; idx += kT) W32[(idx / K) * C::LDW + idx % K] = (float)B1[idx];
+        } else {
+            // warm start from the previous (neighbouring) cube's eigenvectors:
+            // the Jacobi works on A' Vprev, whose columns are nearly orthogonal
+            for (int idx = tid; idx < K * K; idx += kT) A32[idx] = (float)B1[idx];
+            __syncthreads();
+#pragma unroll
+            for (int m = 0; m < C::MF; m++) {
+                if (!fok[m]) continue;
+                float acc[16];
+#pragma unroll
+                for (int i = 0; i < 16; i++) acc[i] = 0.0f;
+                for (int l = 0; l < K; l++) {
+                    // A' symmetric: rows 4*fbi.. of column l = row l at 4*fbi..
+                    const float4 av = *reinterpret_cast<const float4 *>(A32 + l * K + 4 * fbi[m]);
+                    const float4 vv = *reinterpret_cast<const float4 *>(Vprev + l * K + 4 * fbj[m]);
+                    const float x[4] = {av.x, av.y, av.z, av.w};
+                    const float y[4] = {vv.x, vv.y, vv.z, vv.w};
+#pragma unroll
+                    for (int i = 0; i < 4; i++)
+#pragma unroll
+                        for (int jj = 0; jj < 4; jj++) acc[i * 4 + jj] = fmaf(x[i], y[jj], acc[i * 4 + jj]);
+                }
+#pragma unroll
+                for (int i = 0; i < 4; i++)
+#pragma unroll
+                    for (int jj = 0; jj < 4; jj++)
+                        W32[(4 * fbj[m] + jj) * C::LDW + 4 * fbi[m] + i] = acc[i * 4 + jj];
+            }
+        }
+        __syncthreads();
 
+        LG_PHASE(1);
         // ---------------- phase 3: FP32 Jacobi -> Xhat (columns of W32) ----------------
-        const int sw = lg_jacobi<float, K, C::G, C::LDW, false>(W32, nrm32, rot32, &s_rot, 2e-6f, 24);
+        const int sw = lg_jacobi32<K, C::G, C::LDW>(W32, nrm32, &s_rot, 2e-6f, 24);
         if (tid == 0) {
             atomicMax(&counters[LG_CNT_MAXSWEEP], (unsigned long long)sw);
             if (sw > 24) atomicAdd(&counters[LG_CNT_NOTCONV], 1ull);
@@ -332,6 +395,7 @@ k_core_mixed(LgGrid g, LgParams prm, const double *__restrict__ yb, const float 
         }
         __syncthreads();
 
+        LG_PHASE(2);
         // ---------------- phase 4: FP64 refinement (Ogita-Aishima) ---------------------
         double *P = reinterpret_cast<double *>(area);   // A' Xhat, row-major
 #pragma unroll
@@ -501,6 +565,7 @@ k_core_mixed(LgGrid g, LgParams prm, const double *__restrict__ yb, const float 
         }
         __syncthreads();
         const double *Xp = B1;                         // X by columns
+        LG_PHASE(3);
 
         // ---------------- phase 5: T and wbar in FP64 -----------------------------------
         for (int j = warp; j < K; j += kT / 32) {          // one warp per eigenvector
@@ -540,6 +605,12 @@ k_core_mixed(LgGrid g, LgParams prm, const double *__restrict__ yb, const float 
                         for (int jj = 0; jj < 4; jj++) tacc[m][i * 4 + jj] += a[i] * bq[jj];
                 }
             }
+            // keep X by rows for the next cube's warm start (Xr, which shared this
+            // memory, was last read before the previous barrier)
+            for (int idx = tid; idx < K * K; idx += kT) {
+                const int r = idx / K, j = idx % K;
+                Vprev[idx] = (float)Xp[j * K + r];
+            }
             __syncthreads();                  // X (in B1) is read by every thread above
 #pragma unroll
             for (int m = 0; m < C::ML; m++) {
@@ -563,6 +634,7 @@ k_core_mixed(LgGrid g, LgParams prm, const double *__restrict__ yb, const float 
             if (tid < K) w_out[cube * K + tid] = wbar[tid];
         }
 
+        LG_PHASE(4);
         // ---------------- phase 6: xa = xb^T (T + wbar 1^T) -------------------------------
         unsigned char *xa_hi = area, *xa_lo = area + 16384;
         unsigned char *tb_hi = area + 32768, *tb_lo = area + 40960;
@@ -663,8 +735,16 @@ k_core_mixed(LgGrid g, LgParams prm, const double *__restrict__ yb, const float 
                     __syncthreads();
                 }
             }
+        LG_PHASE(5);
         if (failed) break;
+        have_prev = true;
     }
+#ifdef LG_PHASE_CLOCKS
+    if (blockIdx.x == 0 && tid == 0)
+        printf("phase cycles cta0: A-build %lld, A'-form %lld, jacobi32 %lld, refine %lld, T/wbar %lld, "
+               "update %lld, loop %lld\n",
+               ph_cyc[0], ph_cyc[1], ph_cyc[2], ph_cyc[3], ph_cyc[4], ph_cyc[5], ph_cyc[6]);
+#endif
     if (failed && tid == 0) atomicOr(status, LG_ST_TIMEOUT);
     // let any MMA still in flight finish before the TMEM is freed
     for (int b = 0; b < 3; b++) wait_bar(b);

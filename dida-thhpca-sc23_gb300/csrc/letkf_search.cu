@@ -247,12 +247,27 @@ k_search(LgGrid g, LgParams prm, LgBuckets bk, LgObsGeo geo, int64_t nobs, int c
         __syncthreads();
         const long long off = s_off;
         if (off >= 0) {
-            for (int i = threadIdx.x; i < nout; i += kThreads) {
-                const int o = keys[i];
-                const double dist = lg_dist(geo.s[o], geo.c[o], geo.yr[o], cg.s2, cg.c2, cg.y2r);
-                const double ri = lg_ri(dist, prm.local_dist);
-                lidx[off + i] = o;
-                lrloc[off + i] = prm.gc_filter ? lg_schr2(ri) : lg_schr(ri);
+            if (prm.precision == LETKF_PREC_MIXED) {
+                // FP32 weights from the chord of the unit vectors (the selection
+                // above used the reference's double formula where it mattered)
+                const float scale = (float)(LG_EARTH_A / prm.local_dist);
+                for (int i = threadIdx.x; i < nout; i += kThreads) {
+                    const int o = keys[i];
+                    const float4 q = geo.xyz[o];
+                    const float dx = q.x - cg.cx, dy = q.y - cg.cy, dz = q.z - cg.cz;
+                    const float half = fminf(1.0f, 0.5f * sqrtf(dx * dx + dy * dy + dz * dz));
+                    const float ri = 2.0f * asinf(half) * scale;
+                    lidx[off + i] = o;
+                    lrloc[off + i] = prm.gc_filter ? (double)lg_schr2f(ri) : (ri > 2.0f ? 0.0 : 1.0);
+                }
+            } else {
+                for (int i = threadIdx.x; i < nout; i += kThreads) {
+                    const int o = keys[i];
+                    const double dist = lg_dist(geo.s[o], geo.c[o], geo.yr[o], cg.s2, cg.c2, cg.y2r);
+                    const double ri = lg_ri(dist, prm.local_dist);
+                    lidx[off + i] = o;
+                    lrloc[off + i] = prm.gc_filter ? lg_schr2(ri) : lg_schr(ri);
+                }
             }
         }
         __syncthreads();
@@ -279,7 +294,7 @@ cudaError_t lg_launch_search(letkf_ctx *ctx, const LgGrid &g, int64_t nobs)
     bk.start = ctx->d_bstart.p;
     bk.idx = ctx->d_bidx.p;
     bk.xyz = ctx->d_bxyz.p;
-    LgObsGeo geo{ctx->d_os.p, ctx->d_oc.p, ctx->d_oyr.p};
+    LgObsGeo geo{ctx->d_os.p, ctx->d_oc.p, ctx->d_oyr.p, ctx->d_oxyz.p};
     const int cap = lg_search_cap(prm.max_obs);
     const size_t smem = sizeof(int32_t) * cap;
     cudaError_t e = cudaFuncSetAttribute(k_search, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
