@@ -229,7 +229,8 @@ k_core_mixed(LgGrid g, LgParams prm, const double *__restrict__ yb, const float 
                     const double rl = lrloc[li];
                     gidx[tid] = gi;
                     sq32[tid] = sqrtf((float)rl);
-                    cd[tid] = ((double)rinvf[gi] * rl) * dep[gi];
+                    // g = sum_o y r rloc dep = sum_o (y sqrt(r)) (sqrt(r) rloc dep)
+                    cd[tid] = (sqrt((double)rinvf[gi]) * rl) * dep[gi];
                 } else {
                     gidx[tid] = 0;
                     sq32[tid] = 0.0f;
@@ -240,7 +241,7 @@ k_core_mixed(LgGrid g, LgParams prm, const double *__restrict__ yb, const float 
             if (gpart < nparts) {
                 const int m = tid % K;
 #pragma unroll 4
-                for (int o = gpart; o < cnt; o += nparts) gacc += yb[(int64_t)gidx[o] * K + m] * cd[o];
+                for (int o = gpart; o < cnt; o += nparts) gacc += (double)ys32[(int64_t)gidx[o] * K + m] * cd[o];
             }
             for (int t = tid; t < K * 8; t += kT) {
                 const int m = t % K, c = t / K;
@@ -584,32 +585,37 @@ k_core_mixed(LgGrid g, LgParams prm, const double *__restrict__ yb, const float 
             for (int j = 0; j < K; j++) s += Xp[j * K + tid] * hco[j];
             wbar[tid] = s;
         }
+        // T = X diag(f) X^T only feeds the BF16 hi/lo tensor-core update (16
+        // significant bits), so the product is formed in FP32 from the FP64
+        // eigenvectors and f = sqrt((k-1)/lambda); wbar stays FP64.
+        float *X32 = reinterpret_cast<float *>(area);            // X by columns, FP32
+        float *T32 = reinterpret_cast<float *>(B1);               // T, FP32, row-major
+        for (int idx = tid; idx < K * K; idx += kT) X32[idx] = (float)Xp[idx];
+        __syncthreads();
         {
-            double tacc[C::ML][16];
+            float tacc[C::ML][16];
 #pragma unroll
             for (int m = 0; m < C::ML; m++) {
 #pragma unroll
-                for (int i = 0; i < 16; i++) tacc[m][i] = 0.0;
+                for (int i = 0; i < 16; i++) tacc[m][i] = 0.0f;
                 if (!lok[m]) continue;
                 for (int j = 0; j < K; j++) {
-                    const double f = fco[j];
-                    const double2 a01 = *reinterpret_cast<const double2 *>(Xp + j * K + 4 * lbi[m]);
-                    const double2 a23 = *reinterpret_cast<const double2 *>(Xp + j * K + 4 * lbi[m] + 2);
-                    const double2 b01 = *reinterpret_cast<const double2 *>(Xp + j * K + 4 * lbj[m]);
-                    const double2 b23 = *reinterpret_cast<const double2 *>(Xp + j * K + 4 * lbj[m] + 2);
-                    const double a[4] = {a01.x, a01.y, a23.x, a23.y};
-                    const double bq[4] = {b01.x * f, b01.y * f, b23.x * f, b23.y * f};
+                    const float f = (float)fco[j];
+                    const float4 av = *reinterpret_cast<const float4 *>(X32 + j * K + 4 * lbi[m]);
+                    const float4 bv = *reinterpret_cast<const float4 *>(X32 + j * K + 4 * lbj[m]);
+                    const float a[4] = {av.x, av.y, av.z, av.w};
+                    const float bq[4] = {bv.x * f, bv.y * f, bv.z * f, bv.w * f};
 #pragma unroll
                     for (int i = 0; i < 4; i++)
 #pragma unroll
-                        for (int jj = 0; jj < 4; jj++) tacc[m][i * 4 + jj] += a[i] * bq[jj];
+                        for (int jj = 0; jj < 4; jj++) tacc[m][i * 4 + jj] = fmaf(a[i], bq[jj], tacc[m][i * 4 + jj]);
                 }
             }
             // keep X by rows for the next cube's warm start (Xr, which shared this
             // memory, was last read before the previous barrier)
             for (int idx = tid; idx < K * K; idx += kT) {
                 const int r = idx / K, j = idx % K;
-                Vprev[idx] = (float)Xp[j * K + r];
+                Vprev[idx] = X32[j * K + r];
             }
             __syncthreads();                  // X (in B1) is read by every thread above
 #pragma unroll
@@ -620,8 +626,8 @@ k_core_mixed(LgGrid g, LgParams prm, const double *__restrict__ yb, const float 
 #pragma unroll
                     for (int jj = 0; jj < 4; jj++) {
                         const int r = 4 * lbi[m] + i, c = 4 * lbj[m] + jj;
-                        B1[r * K + c] = tacc[m][i * 4 + jj];
-                        B1[c * K + r] = tacc[m][i * 4 + jj];
+                        T32[r * K + c] = tacc[m][i * 4 + jj];
+                        T32[c * K + r] = tacc[m][i * 4 + jj];
                     }
             }
         }
@@ -629,7 +635,7 @@ k_core_mixed(LgGrid g, LgParams prm, const double *__restrict__ yb, const float 
         if (trans_out) {
             for (int idx = tid; idx < K * K; idx += kT) {
                 const int i = idx % K, j = idx / K;
-                trans_out[cube * K * K + idx] = B1[i * K + j] + wbar[i];
+                trans_out[cube * K * K + idx] = (double)T32[i * K + j] + wbar[i];
             }
             if (tid < K) w_out[cube * K + tid] = wbar[tid];
         }
@@ -643,7 +649,7 @@ k_core_mixed(LgGrid g, LgParams prm, const double *__restrict__ yb, const float 
             const int e = t / (K / 8), c = t % (K / 8);
             float v[8];
 #pragma unroll
-            for (int j = 0; j < 8; j++) v[j] = (float)B1[e * K + 8 * c + j];
+            for (int j = 0; j < 8; j++) v[j] = T32[e * K + 8 * c + j];
             uint4 hi, lo;
             split8(v, hi, lo);
             *reinterpret_cast<uint4 *>(tb_hi + lg_sw128_offset(e, c)) = hi;
