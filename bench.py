@@ -123,22 +123,52 @@ def algorithmic_work(w, sum_p):
     return flops, nbytes
 
 
+def matmul_peak_tflops(torch, dev, dtype):
+    """Measured dense matrix throughput of cuBLAS for `dtype` (4096^3, best of
+    5); FP32 with TF32 off, so it is the FP32 CUDA-core rate."""
+    n = 4096
+    prev = torch.backends.cuda.matmul.allow_tf32
+    torch.backends.cuda.matmul.allow_tf32 = False
+    try:
+        a = torch.randn(n, n, dtype=dtype, device=dev)
+        b = torch.randn(n, n, dtype=dtype, device=dev)
+        torch.matmul(a, b)
+        torch.cuda.synchronize()
+        best = 1e30
+        for _ in range(5):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            torch.matmul(a, b)
+            e1.record()
+            torch.cuda.synchronize()
+            best = min(best, e0.elapsed_time(e1))
+    finally:
+        torch.backends.cuda.matmul.allow_tf32 = prev
+    return 2.0 * n ** 3 / (best * 1e-3) / 1e12
+
+
 def fp64_peak_tflops(torch, dev):
     """Measured FP64 matrix throughput (cuBLAS DGEMM, best of 5)."""
-    n = 4096
-    a = torch.randn(n, n, dtype=torch.float64, device=dev)
-    b = torch.randn(n, n, dtype=torch.float64, device=dev)
-    torch.matmul(a, b)
-    torch.cuda.synchronize()
-    best = 1e30
-    for _ in range(5):
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        torch.matmul(a, b)
-        e1.record()
-        torch.cuda.synchronize()
-        best = min(best, e0.elapsed_time(e1))
-    return 2.0 * n ** 3 / (best * 1e-3) / 1e12
+    return matmul_peak_tflops(torch, dev, torch.float64)
+
+
+def mixed_pipe_bounds(w, sum_p, peaks_tflops, hbm_gbs):
+    """Per-pipe lower bounds (ms) of the mixed core on the algorithmic work:
+    the two dense products on the tensor cores (2k^2 p and 2k^2 n per column;
+    the hi/lo split's extra products are implementation cost), the 13k^3
+    eigensolve and transform work on the FP32 pipe, g (2k p) on the FP64 pipe,
+    and the state and observation bytes on HBM."""
+    k, n, ncol = w.k, w.n, w.ncol
+    flops, nbytes = algorithmic_work(w, sum_p)
+    work = {"tensor": 2.0 * k * k * sum_p + 2.0 * k * k * n * ncol,
+            "fp32": 13.0 * k ** 3 * ncol,
+            "fp64": 2.0 * k * sum_p,
+            "hbm": nbytes}
+    ms = {"tensor": work["tensor"] / (peaks_tflops["bf16"] * 1e12) * 1e3,
+          "fp32": work["fp32"] / (peaks_tflops["fp32"] * 1e12) * 1e3,
+          "fp64": work["fp64"] / (peaks_tflops["fp64"] * 1e12) * 1e3,
+          "hbm": work["hbm"] / (hbm_gbs * 1e9) * 1e3}
+    return work, ms
 
 
 def measured_peaks():
@@ -292,11 +322,12 @@ def _field_errors(w, xa, axa, xa_ref, axa_ref):
 
 def mixed_fp64_flops(w, sum_p):
     """FP64 work the mixed form does by design per analysis: g (k p), the
-    refinement (A'Xhat: k^3; S, R: k^2(k+1)/2 each; the small correction
-    Xhat E is FP32), T (k^2(k+1)/2), wbar (2k^2) and the mean increment (n k)
-    multiply-adds."""
+    FP64 copy of A' (k^2), wbar with one refinement step (five k x k
+    matrix-vector products: 5k^2) and the mean increment xb^T wbar (n k)
+    multiply-adds.  The eigensolve, T and the two large products are FP32 or
+    tensor-core work."""
     k, n, ncol = w.k, w.n, w.ncol
-    fma = k * sum_p + ncol * (k ** 3 + 1.5 * k * k * (k + 1) + 2 * k * k + n * k)
+    fma = k * sum_p + ncol * (k * k + 5 * k * k + n * k)
     return 2.0 * fma
 
 
@@ -407,22 +438,33 @@ def run_ours(args, rank, world, local_rank):
         m = re.search(r"bytes_per_full_launch:\s*([0-9.eE+]+)", open(tfile).read())
         traffic = float(m.group(1)) if m else None
     if head == "mixed":
-        f64 = mixed_fp64_flops(w, st["sum_p"])
-        roof = {"bound": "fp64", "kernel": f"k_core_mixed<{w.k}>",
-                "achieved": f64 / (core * 1e-3) / 1e12, "peak": fp64_peak, "unit": "TFLOP/s",
-                "frac": f64 / (core * 1e-3) / 1e12 / fp64_peak, "traffic": traffic,
-                "work": "FP64 multiply-adds the mixed core does by design (mean increment g, "
-                        "eigen refinement, T, wbar, xb^T wbar)",
-                "fp64_flops_per_launch": f64,
+        fp32_peak = matmul_peak_tflops(torch, dev, torch.float32)
+        pk = {"bf16": peaks.get("bf16_tflops", 1900.0), "fp32": fp32_peak, "fp64": fp64_peak}
+        work, bound_ms = mixed_pipe_bounds(w, st["sum_p"], pk, peaks.get("hbm_gbs", 6800.0))
+        pipe = max(bound_ms, key=bound_ms.get)
+        unit = "GB/s" if pipe == "hbm" else "TFLOP/s"
+        scale = 1e9 if pipe == "hbm" else 1e12
+        achieved = work[pipe] / (core * 1e-3) / scale
+        peak = peaks.get("hbm_gbs", 6800.0) if pipe == "hbm" else pk[pipe]
+        roof = {"bound": pipe, "kernel": f"k_core_mixed<{w.k}>",
+                "achieved": achieved, "peak": peak, "unit": unit, "frac": achieved / peak,
+                "traffic": traffic, "kernel_ms": core,
+                "work": "algorithmic work per pipe: tensor 2k^2(p+n), FP32 13k^3, FP64 2kp "
+                        "(g), HBM state + obs bytes; the bound is the pipe with the largest "
+                        "work/peak time",
+                "pipe_bound_ms": bound_ms, "pipe_work": work,
+                "peaks_tflops": {"bf16": pk["bf16"], "fp32_measured_sgemm": fp32_peak,
+                                 "fp64_measured_dgemm": fp64_peak},
+                "fp64_flops_by_design": mixed_fp64_flops(w, st["sum_p"]),
                 "algorithmic_flops_per_launch": flops,
-                "algorithmic_tflops": flops / (core * 1e-3) / 1e12, "kernel_ms": core}
+                "fp64_equivalent_tflops": flops / (core * 1e-3) / 1e12}
     else:
         roof = {"bound": "fp64", "kernel": f"k_core_fp64<{w.k}>",
                 "achieved": flops / (core * 1e-3) / 1e12, "peak": fp64_peak, "unit": "TFLOP/s",
                 "frac": flops / (core * 1e-3) / 1e12 / fp64_peak, "traffic": traffic,
                 "algorithmic_flops_per_launch": flops, "kernel_ms": core}
-    roof["peak_source"] = ("measured here: cuBLAS FP64 GEMM 4096^3, best of 5 "
-                           "(MEASURED_PEAKS.json has no FP64 entry)")
+    roof["peak_source"] = ("FP64/FP32: measured here, cuBLAS GEMM 4096^3 best of 5 (MEASURED_PEAKS.json "
+                           "has neither); bf16 and HBM: MEASURED_PEAKS.json burst figures")
     stages = res[head][2]
     line = {
         "metric": METRIC, "value": value, "unit": "columns/s", "n_gpus": world,

@@ -14,15 +14,14 @@
 //      tile's MMAs run (two tiles, mbarrier-tracked).
 //      g = Yhat (sqrt(rdiaginv rloc) dep) is accumulated in FP64 alongside.
 //   2. A' = A + (k-1)/rho I in FP64.
-//   3. FP32 one-sided Jacobi gives approximate eigenvectors Xhat.
-//   4. One FP64 refinement step of the eigendecomposition (Ogita & Aishima,
-//      "Iterative refinement for symmetric eigenvalue decomposition", Japan J.
-//      Indust. Appl. Math. 35 (2018), Algorithm 1): R = I - Xhat^T Xhat,
-//      S = Xhat^T A' Xhat, lambda_i = s_ii/(1-r_ii), E from S, R and the gaps,
-//      X = Xhat + Xhat E; the eigenpairs come out FP64-accurate.  R, S and the
-//      products they need are FP64; the correction Xhat E, whose size is that
-//      of Xhat's error, is formed in FP32 and added in FP64.
-//   5. T = X diag(sqrt((k-1)/lambda)) X^T and wbar = X diag(1/lambda) X^T g in FP64.
+//   3. FP32 one-sided Jacobi of A' (warm-started from the neighbouring
+//      cube's eigenvectors) gives the eigenpairs: lambda_j = |w_j|, x_j = w_j/lambda_j.
+//   4. wbar = X diag(1/lambda) X^T g in FP64, then one step of iterative
+//      refinement: wbar += X diag(1/lambda) X^T (g - A' wbar) with the
+//      residual against the FP64 A'.  A' has condition numbers below ~1e3 at
+//      these sizes, so one step takes wbar from ~1e-7 to ~1e-13 relative.
+//   5. T = X diag(sqrt((k-1)/lambda)) X^T in FP32: it only feeds the BF16
+//      hi/lo update, and FP32 eigenpairs give it to ~1e-7 relative.
 //   6. xa = xb^T T on tcgen05 (hi/lo BF16 of both operands, three products in
 //      one accumulator); the mean increment xb^T wbar is FP64.
 #include <cuda_bf16.h>
@@ -295,7 +294,6 @@ k_core_mixed(LgGrid g, LgParams prm, const double *__restrict__ yb, const float 
         float *W32 = reinterpret_cast<float *>(area);          // FP32 Jacobi columns (stride LDW)
         float *A32 = W32 + K * C::LDW;                          // A' in FP32 (warm start)
         float *Vprev = reinterpret_cast<float *>(area + 49152); // previous cube's X by rows, FP32
-        double *Xr = reinterpret_cast<double *>(area + 32768);  // Xhat by rows, Xr[row*K + j], after the Jacobi
         if (warp < 4) {
             const int row = warp * 32 + lane;
 #pragma unroll
@@ -321,15 +319,13 @@ k_core_mixed(LgGrid g, LgParams prm, const double *__restrict__ yb, const float 
         // A = HH + LH + LH^T is formed in FP32 (the accumulators are FP32), then
         // A' = A + (k-1)/rho I in FP64 and in FP32 for the Jacobi
         const double cdiag = (double)(K - 1) / prm.inflation;
-        double fro = 0.0;
         for (int idx = tid; idx < K * K; idx += kT) {
             const int i = idx / K, j = idx % K;
             const float a32 = 0.5f * (Dhh[i * LDD + j] + Dhh[j * LDD + i]) + (Dlh[i * LDD + j] + Dlh[j * LDD + i]);
             const double a = (double)a32 + (i == j ? cdiag : 0.0);
             B1[idx] = a;
-            fro += a * a;
         }
-        const double normA = sqrt(block_sum(fro, red));   // its barriers retire Dhh/Dlh
+        __syncthreads();                                   // Dhh/Dlh are dead
         if (!have_prev) {
             // cold start: the Jacobi works on A' itself
             for (int idx = tid; idx < K * K; idx += kT) W32[(idx / K) * C::LDW + idx % K] = (float)B1[idx];
@@ -371,227 +367,76 @@ k_core_mixed(LgGrid g, LgParams prm, const double *__restrict__ yb, const float 
             atomicMax(&counters[LG_CNT_MAXSWEEP], (unsigned long long)sw);
             if (sw > 24) atomicAdd(&counters[LG_CNT_NOTCONV], 1ull);
         }
+        // lambda_j = |w_j| (A' is SPD, so the converged columns are lambda_j x_j)
         if (tid < K) {
             float s = 0.0f;
-            for (int r = 0; r < K; r++) s += W32[tid * C::LDW + r] * W32[tid * C::LDW + r];
+            for (int r = 0; r < K; r++) s = fmaf(W32[tid * C::LDW + r], W32[tid * C::LDW + r], s);
             nrm32[tid] = 1.0f / sqrtf(s);
+            lam[tid] = sqrt((double)s);
+            fco[tid] = sqrt((double)(K - 1) / lam[tid]);
         }
         __syncthreads();
-        // Xhat (FP32 values) by rows in FP64: converted once.  W32 and Xr share
+        LG_PHASE(2);
+        // ---------------- phase 4: X, wbar with one FP64 refinement step ------------------
+        // X by columns in FP32 (T, warm start) and FP64 (wbar).  W32 shares this
         // memory, so the values pass through registers first.
+        float *X32 = reinterpret_cast<float *>(area);            // X32[j*K + r] = x_j[r]
+        double *Xd = reinterpret_cast<double *>(area + 16384);   // the same in FP64
         {
             constexpr int PER = (K * K + kT - 1) / kT;
             float xv[PER];
 #pragma unroll
             for (int q = 0; q < PER; q++) {
                 const int idx = tid + q * kT;
-                xv[q] = (idx < K * K) ? W32[(idx % K) * C::LDW + idx / K] * nrm32[idx % K] : 0.0f;
+                xv[q] = (idx < K * K) ? W32[(idx / K) * C::LDW + idx % K] * nrm32[idx / K] : 0.0f;
             }
             __syncthreads();
 #pragma unroll
             for (int q = 0; q < PER; q++) {
                 const int idx = tid + q * kT;
-                if (idx < K * K) Xr[idx] = (double)xv[q];
-            }
-        }
-        __syncthreads();
-
-        LG_PHASE(2);
-        // ---------------- phase 4: FP64 refinement (Ogita-Aishima) ---------------------
-        double *P = reinterpret_cast<double *>(area);   // A' Xhat, row-major
-#pragma unroll
-        for (int m = 0; m < C::MF; m++) {
-            if (!fok[m]) continue;
-            double acc[16];
-#pragma unroll
-            for (int i = 0; i < 16; i++) acc[i] = 0.0;
-            for (int l = 0; l < K; l++) {
-                const double2 a01 = *reinterpret_cast<const double2 *>(B1 + l * K + 4 * fbi[m]);
-                const double2 a23 = *reinterpret_cast<const double2 *>(B1 + l * K + 4 * fbi[m] + 2);
-                const double a[4] = {a01.x, a01.y, a23.x, a23.y};
-                const double2 x01 = *reinterpret_cast<const double2 *>(Xr + l * K + 4 * fbj[m]);
-                const double2 x23 = *reinterpret_cast<const double2 *>(Xr + l * K + 4 * fbj[m] + 2);
-                const double x[4] = {x01.x, x01.y, x23.x, x23.y};
-#pragma unroll
-                for (int i = 0; i < 4; i++)
-#pragma unroll
-                    for (int jj = 0; jj < 4; jj++) acc[i * 4 + jj] += a[i] * x[jj];
-            }
-            // P row-major: P[row*K + col] = (A' Xhat)[row][col]
-#pragma unroll
-            for (int i = 0; i < 4; i++)
-#pragma unroll
-                for (int jj = 0; jj < 4; jj++) P[(4 * fbi[m] + i) * K + 4 * fbj[m] + jj] = acc[i * 4 + jj];
-        }
-        __syncthreads();
-        // S = Xhat^T A' Xhat (lower blocks, mirrored) into B1
-        {
-            double sacc[C::ML][16];
-#pragma unroll
-            for (int m = 0; m < C::ML; m++) {
-#pragma unroll
-                for (int i = 0; i < 16; i++) sacc[m][i] = 0.0;
-                if (!lok[m]) continue;
-                for (int l = 0; l < K; l++) {
-                    const double2 x01 = *reinterpret_cast<const double2 *>(Xr + l * K + 4 * lbi[m]);
-                    const double2 x23 = *reinterpret_cast<const double2 *>(Xr + l * K + 4 * lbi[m] + 2);
-                    const double2 q01 = *reinterpret_cast<const double2 *>(P + l * K + 4 * lbj[m]);
-                    const double2 q23 = *reinterpret_cast<const double2 *>(P + l * K + 4 * lbj[m] + 2);
-                    const double x[4] = {x01.x, x01.y, x23.x, x23.y};
-                    const double q[4] = {q01.x, q01.y, q23.x, q23.y};
-#pragma unroll
-                    for (int i = 0; i < 4; i++)
-#pragma unroll
-                        for (int jj = 0; jj < 4; jj++) sacc[m][i * 4 + jj] += x[i] * q[jj];
+                if (idx < K * K) {
+                    X32[idx] = xv[q];
+                    Xd[idx] = (double)xv[q];
                 }
+            }
+            if (tid < K) nrm32[tid] = (float)fco[tid];       // f = sqrt((k-1)/lambda) for T
+        }
+        __syncthreads();
+        // wbar = X diag(1/lambda) X^T g, then wbar += X diag(1/lambda) X^T (g - A' wbar):
+        // the residual against the FP64 A' removes the FP32 eigenpairs' error from wbar
+        for (int it = 0; it < 2; it++) {
+            const double *rhs = it == 0 ? gv : misc;
+            for (int j = warp; j < K; j += kT / 32) {          // one warp per eigenvector
+                double dot = 0.0;
+                for (int l = lane; l < K; l += 32) dot += Xd[j * K + l] * rhs[l];
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) dot += __shfl_xor_sync(0xffffffffu, dot, o);
+                if (lane == 0) hco[j] = dot / lam[j];
             }
             __syncthreads();
-#pragma unroll
-            for (int m = 0; m < C::ML; m++) {
-                if (!lok[m]) continue;
-#pragma unroll
-                for (int i = 0; i < 4; i++)
-#pragma unroll
-                    for (int jj = 0; jj < 4; jj++) {
-                        const int r = 4 * lbi[m] + i, c = 4 * lbj[m] + jj;
-                        B1[r * K + c] = sacc[m][i * 4 + jj];
-                        B1[c * K + r] = sacc[m][i * 4 + jj];
-                    }
-            }
-        }
-        __syncthreads();
-        // R = I - Xhat^T Xhat (lower blocks, mirrored) into the area (P is dead)
-        double *Rm = reinterpret_cast<double *>(area);
-        {
-            double racc[C::ML][16];
-#pragma unroll
-            for (int m = 0; m < C::ML; m++) {
-#pragma unroll
-                for (int i = 0; i < 16; i++) racc[m][i] = 0.0;
-                if (!lok[m]) continue;
-                for (int l = 0; l < K; l++) {
-                    const double2 x01 = *reinterpret_cast<const double2 *>(Xr + l * K + 4 * lbi[m]);
-                    const double2 x23 = *reinterpret_cast<const double2 *>(Xr + l * K + 4 * lbi[m] + 2);
-                    const double2 y01 = *reinterpret_cast<const double2 *>(Xr + l * K + 4 * lbj[m]);
-                    const double2 y23 = *reinterpret_cast<const double2 *>(Xr + l * K + 4 * lbj[m] + 2);
-                    const double x[4] = {x01.x, x01.y, x23.x, x23.y};
-                    const double y[4] = {y01.x, y01.y, y23.x, y23.y};
-#pragma unroll
-                    for (int i = 0; i < 4; i++)
-#pragma unroll
-                        for (int jj = 0; jj < 4; jj++) racc[m][i * 4 + jj] += x[i] * y[jj];
-                }
-            }
-#pragma unroll
-            for (int m = 0; m < C::ML; m++) {
-                if (!lok[m]) continue;
-#pragma unroll
-                for (int i = 0; i < 4; i++)
-#pragma unroll
-                    for (int jj = 0; jj < 4; jj++) {
-                        const int r = 4 * lbi[m] + i, c = 4 * lbj[m] + jj;
-                        const double v = (r == c ? 1.0 : 0.0) - racc[m][i * 4 + jj];
-                        Rm[r * K + c] = v;
-                        Rm[c * K + r] = v;
-                    }
-            }
-        }
-        __syncthreads();
-        if (tid < K) lam[tid] = B1[tid * K + tid] / (1.0 - Rm[tid * K + tid]);
-        __syncthreads();
-        double offs = 0.0, rr2 = 0.0;
-        for (int idx = tid; idx < K * K; idx += kT) {
-            const int i = idx / K, j = idx % K;
-            const double d = (i == j) ? B1[idx] - lam[i] : B1[idx];
-            offs += d * d;
-            rr2 += Rm[idx] * Rm[idx];
-        }
-        offs = block_sum(offs, red);
-        rr2 = block_sum(rr2, red);
-        const double delta = 2.0 * (sqrt(offs) + normA * sqrt(rr2));
-        // E (in place of S): gaps above delta get the Newton correction
-        for (int idx = tid; idx < K * K; idx += kT) {
-            const int i = idx / K, j = idx % K;
-            const double r = Rm[idx];
-            double e;
-            if (i == j) {
-                e = 0.5 * r;
-            } else {
-                const double gap = lam[j] - lam[i];
-                e = (fabs(gap) > delta) ? (B1[idx] + lam[j] * r) / gap : 0.5 * r;
-            }
-            B1[idx] = e;
-        }
-        __syncthreads();
-        // X = Xhat + Xhat E into B1 (by columns).  E is of the size of Xhat's
-        // error (~1e-6), so the correction product Xhat E is formed in FP32
-        // (rounding ~1e-13 absolute) and added to Xhat in FP64.
-        {
-            float *X32c = reinterpret_cast<float *>(area);           // Xhat by columns, FP32
-            float *E32 = reinterpret_cast<float *>(area + 16384);    // E by rows, FP32
-            for (int idx = tid; idx < K * K; idx += kT) {
-                const int l = idx / K, r = idx % K;
-                X32c[idx] = (float)Xr[r * K + l];
-                E32[idx] = (float)B1[idx];
+            if (tid < K) {
+                double s = 0.0;
+                for (int j = 0; j < K; j++) s += Xd[j * K + tid] * hco[j];
+                wbar[tid] = (it == 0 ? 0.0 : wbar[tid]) + s;
             }
             __syncthreads();
-            float acc[C::MF][16];
+            if (it == 0) {
+                for (int i = warp; i < K; i += kT / 32) {      // one warp per row of A'
+                    double s = 0.0;
+                    for (int l = lane; l < K; l += 32) s += B1[i * K + l] * wbar[l];
 #pragma unroll
-            for (int m = 0; m < C::MF; m++) {
-#pragma unroll
-                for (int i = 0; i < 16; i++) acc[m][i] = 0.0f;
-                if (!fok[m]) continue;
-                for (int l = 0; l < K; l++) {
-                    const float4 xv = *reinterpret_cast<const float4 *>(X32c + l * K + 4 * fbi[m]);
-                    const float4 ev = *reinterpret_cast<const float4 *>(E32 + l * K + 4 * fbj[m]);
-                    const float x[4] = {xv.x, xv.y, xv.z, xv.w};
-                    const float e[4] = {ev.x, ev.y, ev.z, ev.w};
-#pragma unroll
-                    for (int i = 0; i < 4; i++)
-#pragma unroll
-                        for (int jj = 0; jj < 4; jj++) acc[m][i * 4 + jj] += x[i] * e[jj];
+                    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+                    if (lane == 0) misc[i] = gv[i] - s;
                 }
-            }
-#pragma unroll
-            for (int m = 0; m < C::MF; m++) {
-                if (!fok[m]) continue;
-#pragma unroll
-                for (int i = 0; i < 4; i++)
-#pragma unroll
-                    for (int jj = 0; jj < 4; jj++) {
-                        const int row = 4 * fbi[m] + i, col = 4 * fbj[m] + jj;
-                        B1[col * K + row] = Xr[row * K + col] + (double)acc[m][i * 4 + jj];
-                    }
+                __syncthreads();
             }
         }
-        __syncthreads();
-        const double *Xp = B1;                         // X by columns
         LG_PHASE(3);
 
-        // ---------------- phase 5: T and wbar in FP64 -----------------------------------
-        for (int j = warp; j < K; j += kT / 32) {          // one warp per eigenvector
-            double dot = 0.0;
-            for (int l = lane; l < K; l += 32) dot += Xp[j * K + l] * gv[l];
-#pragma unroll
-            for (int s = 16; s > 0; s >>= 1) dot += __shfl_xor_sync(0xffffffffu, dot, s);
-            if (lane == 0) {
-                hco[j] = dot / lam[j];
-                fco[j] = sqrt((double)(K - 1) / lam[j]);
-            }
-        }
-        __syncthreads();
-        if (tid < K) {
-            double s = 0.0;
-            for (int j = 0; j < K; j++) s += Xp[j * K + tid] * hco[j];
-            wbar[tid] = s;
-        }
+        // ---------------- phase 5: T in FP32 ------------------------------------------------
         // T = X diag(f) X^T only feeds the BF16 hi/lo tensor-core update (16
-        // significant bits), so the product is formed in FP32 from the FP64
-        // eigenvectors and f = sqrt((k-1)/lambda); wbar stays FP64.
-        float *X32 = reinterpret_cast<float *>(area);            // X by columns, FP32
+        // significant bits); FP32 eigenpairs give it to ~1e-7 relative.
         float *T32 = reinterpret_cast<float *>(B1);               // T, FP32, row-major
-        for (int idx = tid; idx < K * K; idx += kT) X32[idx] = (float)Xp[idx];
-        __syncthreads();
         {
             float tacc[C::ML][16];
 #pragma unroll
@@ -600,7 +445,7 @@ k_core_mixed(LgGrid g, LgParams prm, const double *__restrict__ yb, const float 
                 for (int i = 0; i < 16; i++) tacc[m][i] = 0.0f;
                 if (!lok[m]) continue;
                 for (int j = 0; j < K; j++) {
-                    const float f = (float)fco[j];
+                    const float f = nrm32[j];
                     const float4 av = *reinterpret_cast<const float4 *>(X32 + j * K + 4 * lbi[m]);
                     const float4 bv = *reinterpret_cast<const float4 *>(X32 + j * K + 4 * lbj[m]);
                     const float a[4] = {av.x, av.y, av.z, av.w};
@@ -611,13 +456,12 @@ k_core_mixed(LgGrid g, LgParams prm, const double *__restrict__ yb, const float 
                         for (int jj = 0; jj < 4; jj++) tacc[m][i * 4 + jj] = fmaf(a[i], bq[jj], tacc[m][i * 4 + jj]);
                 }
             }
-            // keep X by rows for the next cube's warm start (Xr, which shared this
-            // memory, was last read before the previous barrier)
+            // keep X by rows for the next cube's warm start
             for (int idx = tid; idx < K * K; idx += kT) {
                 const int r = idx / K, j = idx % K;
                 Vprev[idx] = X32[j * K + r];
             }
-            __syncthreads();                  // X (in B1) is read by every thread above
+            // B1 (A') was last read before the previous barrier
 #pragma unroll
             for (int m = 0; m < C::ML; m++) {
                 if (!lok[m]) continue;
@@ -747,7 +591,7 @@ k_core_mixed(LgGrid g, LgParams prm, const double *__restrict__ yb, const float 
     }
 #ifdef LG_PHASE_CLOCKS
     if (blockIdx.x == 0 && tid == 0)
-        printf("phase cycles cta0: A-build %lld, A'-form %lld, jacobi32 %lld, refine %lld, T/wbar %lld, "
+        printf("phase cycles cta0: A-build %lld, A'-form %lld, jacobi32 %lld, X/wbar %lld, T %lld, "
                "update %lld, loop %lld\n",
                ph_cyc[0], ph_cyc[1], ph_cyc[2], ph_cyc[3], ph_cyc[4], ph_cyc[5], ph_cyc[6]);
 #endif
