@@ -12,7 +12,8 @@
 //      hi*lo cross terms.  The observation rows are gathered, scaled and split
 //      into 128-byte-swizzled K-major tiles by all threads while the previous
 //      tile's MMAs run (two tiles, mbarrier-tracked).
-//      g = Yhat (sqrt(rdiaginv rloc) dep) is accumulated in FP64 alongside.
+//      g = Yhat e with e = sqrt(rdiaginv rloc) dep comes out of the same MMAs:
+//      e's hi and lo parts are two more rows of the B operand (N = k + 16).
 //   2. A' = A + (k-1)/rho I in FP64.
 //   3. FP32 one-sided Jacobi of A' (warm-started from the neighbouring
 //      cube's eigenvectors) gives the eigenpairs: lambda_j = |w_j|, x_j = w_j/lambda_j.
@@ -59,7 +60,11 @@ struct MCfg {
     static constexpr int MF = (NFULL + kT - 1) / kT;
     static constexpr int G = (K / 2 * 16 <= kT) ? 16 : (K / 2 * 8 <= kT) ? 8 : 4;
     static constexpr int CH = 64;                      // observations per MMA tile (K of the MMA)
-    static constexpr uint32_t TMEM_COLS = 64;
+    static constexpr uint32_t TMEM_COLS = 128;         // A build: N = K + 16 columns
+    // A-build tile rows: Yhat_lo (K), Yhat_hi (K), e_hi, e_lo, zeros (to K + 16
+    // B rows), and at least the M = 128 rows of the A operand
+    static constexpr int TROWS = (2 * K + 16 > 128) ? 2 * K + 16 : 128;
+    static constexpr int TILE = TROWS * 128;
     static constexpr int LDW = K + 4;                  // padded column stride of the FP32 Jacobi
     static constexpr size_t AREA = 64 * 1024;          // tiles / FP32 scratch / P, R, Xhat
     static constexpr size_t B1 = sizeof(double) * K * K;
@@ -68,6 +73,8 @@ struct MCfg {
     static constexpr size_t SMEM = 1024 + AREA + B1 + VEC + 256;
     static_assert(2 * K <= 128, "stacked hi/lo rows must fit M = 128");
     static_assert(K % 16 == 0, "N must be a multiple of 16");
+    static_assert(2 * TILE <= 49152, "A-build tiles must not reach the warm-start vectors");
+    static_assert(K + 16 <= (int)TMEM_COLS, "A-build accumulator must fit the TMEM allocation");
 };
 
 __device__ __forceinline__ uint32_t pack_bf16(float a, float b)
@@ -151,7 +158,8 @@ k_core_mixed(LgGrid g, LgParams prm, const double *__restrict__ yb, const float 
     __syncthreads();
     lg_tc_fence_after();
     const uint32_t tmem = s_tmem;
-    const uint32_t idesc = lg_idesc_bf16(128, K);
+    const uint32_t idesc = lg_idesc_bf16(128, K);           // update: xb (hi/lo) x T
+    const uint32_t idesc_a = lg_idesc_bf16(128, K + 16);    // A build: [Yhat; e] products
     uint32_t ncommit[3] = {0u, 0u, 0u};
     bool pending[3] = {false, false, false};
     bool failed = false;
@@ -201,21 +209,25 @@ k_core_mixed(LgGrid g, LgParams prm, const double *__restrict__ yb, const float 
         const int p = lcnt[cube];
         LG_PHASE(6);
 
-        // ---------------- phase 1: A on the tensor cores, g in FP64 ----------------
-        if (2 * K < 128) {
-            // rows 2K..127 of both tiles stay zero
-            for (int t = tid; t < 2 * (128 - 2 * K) * 8; t += kT) {
-                const int b = t / ((128 - 2 * K) * 8), rest = t % ((128 - 2 * K) * 8);
-                const int r = 2 * K + rest / 8, c = rest % 8;
-                *reinterpret_cast<uint4 *>(area + b * 16384 + lg_sw128_offset(r, c)) = make_uint4(0, 0, 0, 0);
+        // ---------------- phase 1: A and g on the tensor cores ----------------------
+        // Tile rows: Yhat_lo (0..K-1), Yhat_hi (K..2K-1), e_hi (2K), e_lo (2K+1),
+        // zeros to TROWS.  The A operand is rows 0..127, the B operand rows
+        // K..2K+15 (N = K + 16), so D[lo/hi m][n < K] = Yhat_lo/hi(m) . Yhat_hi(n)
+        // and D[.][K], D[.][K+1] = Yhat(m) . e_hi/e_lo with
+        // e_o = sqrt(rdiaginv rloc) dep: g = sum_o y r rloc dep = Yhat e.
+        {
+            constexpr int Z0 = 2 * K + 2, NZ = C::TROWS - Z0;   // rows that stay zero
+            for (int t = tid; t < 2 * NZ * 8; t += kT) {
+                const int b = t / (NZ * 8), rest = t % (NZ * 8);
+                const int r = Z0 + rest / 8, c = rest % 8;
+                *reinterpret_cast<uint4 *>(area + b * C::TILE + lg_sw128_offset(r, c)) = make_uint4(0, 0, 0, 0);
             }
         }
-        double gacc = 0.0;                       // member tid % K, obs parts tid / K
-        const int gpart = tid / K, nparts = kT / K;
+        float *e32 = reinterpret_cast<float *>(cd);
         const int nch = (p + CH - 1) / CH;
         for (int ch = 0; ch < nch; ch++) {
             const int b = ch & 1;
-            unsigned char *tile = area + b * 16384;
+            unsigned char *tile = area + b * C::TILE;
             if (!wait_bar(b)) {
                 failed = true;
                 break;
@@ -225,44 +237,52 @@ k_core_mixed(LgGrid g, LgParams prm, const double *__restrict__ yb, const float 
                 if (tid < cnt) {
                     const int64_t li = off + (int64_t)ch * CH + tid;
                     const int gi = lidx[li];
-                    const double rl = lrloc[li];
+                    const float rl = (float)lrloc[li];
                     gidx[tid] = gi;
-                    sq32[tid] = sqrtf((float)rl);
-                    // g = sum_o y r rloc dep = sum_o (y sqrt(r)) (sqrt(r) rloc dep)
-                    cd[tid] = (sqrt((double)rinvf[gi]) * rl) * dep[gi];
+                    sq32[tid] = sqrtf(rl);
+                    e32[tid] = sqrtf(rinvf[gi] * rl) * (float)dep[gi];
                 } else {
                     gidx[tid] = 0;
                     sq32[tid] = 0.0f;
-                    cd[tid] = 0.0;
+                    e32[tid] = 0.0f;
                 }
             }
             __syncthreads();
-            if (gpart < nparts) {
-                const int m = tid % K;
-#pragma unroll 4
-                for (int o = gpart; o < cnt; o += nparts) gacc += (double)ys32[(int64_t)gidx[o] * K + m] * cd[o];
-            }
-            for (int t = tid; t < K * 8; t += kT) {
-                const int m = t % K, c = t / K;
+            for (int t = tid; t < K * 8 + 8; t += kT) {
                 float v[8];
+                int rh, rl;
+                if (t < K * 8) {
+                    const int m = t % K, c = t / K;
 #pragma unroll
-                for (int j = 0; j < 8; j++) {
-                    const int o = 8 * c + j;
-                    v[j] = (o < cnt) ? ys32[(int64_t)gidx[o] * K + m] * sq32[o] : 0.0f;
+                    for (int j = 0; j < 8; j++) {
+                        const int o = 8 * c + j;
+                        v[j] = (o < cnt) ? ys32[(int64_t)gidx[o] * K + m] * sq32[o] : 0.0f;
+                    }
+                    rh = K + m;
+                    rl = m;
+                    uint4 hi, lo;
+                    split8(v, hi, lo);
+                    *reinterpret_cast<uint4 *>(tile + lg_sw128_offset(rh, c)) = hi;
+                    *reinterpret_cast<uint4 *>(tile + lg_sw128_offset(rl, c)) = lo;
+                } else {
+                    const int c = t - K * 8;
+#pragma unroll
+                    for (int j = 0; j < 8; j++) v[j] = e32[8 * c + j];
+                    uint4 hi, lo;
+                    split8(v, hi, lo);
+                    *reinterpret_cast<uint4 *>(tile + lg_sw128_offset(2 * K, c)) = hi;
+                    *reinterpret_cast<uint4 *>(tile + lg_sw128_offset(2 * K + 1, c)) = lo;
                 }
-                uint4 hi, lo;
-                split8(v, hi, lo);
-                *reinterpret_cast<uint4 *>(tile + lg_sw128_offset(m, c)) = hi;
-                *reinterpret_cast<uint4 *>(tile + lg_sw128_offset(K + m, c)) = lo;
             }
             lg_fence_async_smem();
             __syncthreads();
             if (tid == 0) {
                 lg_tc_fence_after();
-                const uint64_t d = lg_desc_sw128(lg_smem_u32(tile));
+                const uint64_t da = lg_desc_sw128(lg_smem_u32(tile));
+                const uint64_t db = lg_desc_sw128(lg_smem_u32(tile + K * 128));
 #pragma unroll
                 for (int kk = 0; kk < 4; kk++)
-                    lg_umma_bf16(tmem, d + 2 * kk, d + 2 * kk, idesc, (ch > 0 || kk > 0) ? 1u : 0u);
+                    lg_umma_bf16(tmem, da + 2 * kk, db + 2 * kk, idesc_a, (ch > 0 || kk > 0) ? 1u : 0u);
                 lg_umma_commit(&mbar[b]);
             }
             ncommit[b]++;
@@ -273,17 +293,6 @@ k_core_mixed(LgGrid g, LgParams prm, const double *__restrict__ yb, const float 
             failed = true;
             break;
         }
-        // reduce the partial g sums of the obs parts in a fixed order (the MMAs
-        // are done, so the tile area is free)
-        double *gpart_sum = reinterpret_cast<double *>(area + 32768);
-        if (gpart < nparts) gpart_sum[gpart * K + tid % K] = gacc;
-        __syncthreads();
-        if (tid < K) {
-            double s = 0.0;
-            for (int q = 0; q < nparts; q++) s += gpart_sum[q * K + tid];
-            gv[tid] = s;
-        }
-        __syncthreads();
         lg_tc_fence_after();
 
         LG_PHASE(0);
@@ -296,28 +305,39 @@ k_core_mixed(LgGrid g, LgParams prm, const double *__restrict__ yb, const float 
         float *Vprev = reinterpret_cast<float *>(area + 49152); // previous cube's X by rows, FP32
         if (warp < 4) {
             const int row = warp * 32 + lane;
+            const uint32_t tl = tmem + ((uint32_t)(warp * 32) << 16);
 #pragma unroll
             for (int c0 = 0; c0 < K; c0 += 16) {
                 float v[16];
                 if (p > 0) {
-                    lg_tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c0, v);
+                    lg_tmem_ld16(tl + (uint32_t)c0, v);
                 } else {
 #pragma unroll
                     for (int j = 0; j < 16; j++) v[j] = 0.0f;
                 }
                 if (row < K) {
 #pragma unroll
-                    for (int j = 0; j < 16; j++) Dhh[row * LDD + c0 + j] = v[j];
+                    for (int j = 0; j < 16; j++) Dlh[row * LDD + c0 + j] = v[j];
                 } else if (row < 2 * K) {
 #pragma unroll
-                    for (int j = 0; j < 16; j++) Dlh[(row - K) * LDD + c0 + j] = v[j];
+                    for (int j = 0; j < 16; j++) Dhh[(row - K) * LDD + c0 + j] = v[j];
                 }
             }
+            // g parts: Yhat_lo/hi(m) . (e_hi + e_lo)
+            float v[16];
+            if (p > 0) {
+                lg_tmem_ld16(tl + (uint32_t)K, v);
+            } else {
+#pragma unroll
+                for (int j = 0; j < 16; j++) v[j] = 0.0f;
+            }
+            if (row < 2 * K) misc[row] = (double)v[0] + (double)v[1];
         }
         lg_tc_fence_before();
         __syncthreads();
         // A = HH + LH + LH^T is formed in FP32 (the accumulators are FP32), then
         // A' = A + (k-1)/rho I in FP64 and in FP32 for the Jacobi
+        if (tid < K) gv[tid] = misc[K + tid] + misc[tid];
         const double cdiag = (double)(K - 1) / prm.inflation;
         for (int idx = tid; idx < K * K; idx += kT) {
             const int i = idx / K, j = idx % K;
