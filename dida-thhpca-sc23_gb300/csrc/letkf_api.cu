@@ -142,6 +142,7 @@ int obs_and_search(letkf_ctx *ctx, const double *xb, const double *axb, const le
     LG_CUDA(lg_launch_obs_prepare(ctx, g, xb, axb, no, od.lat, od.lon, od.ph, od.lev, od.var, od.yo,
                                   od.rinv));
     LG_CUDA(lg_launch_buckets(ctx, no));
+    if (ctx->dec_nx > 0) LG_CUDA(lg_launch_block_members(ctx, no, od.lat, od.lon));
     LG_CUDA(cudaEventRecord(ctx->ev[2], ctx->stream));
     if (ctx->list_cap == 0) {
         const int64_t guess = ctx->ncubes * (int64_t)std::min(ctx->params.max_obs, 512);
@@ -150,7 +151,10 @@ int obs_and_search(letkf_ctx *ctx, const double *xb, const double *axb, const le
         ctx->list_cap = std::max<int64_t>(guess, 1);
     }
     for (int attempt = 0; attempt < 3; attempt++) {
-        LG_CUDA(lg_launch_search(ctx, g, no));
+        if (ctx->dec_nx > 0)
+            LG_CUDA(lg_launch_search_dec(ctx, g, od.lat));
+        else
+            LG_CUDA(lg_launch_search(ctx, g, no));
         unsigned st = 0;
         rc = read_status(ctx, st, cnt);
         if (rc) return rc;
@@ -190,6 +194,7 @@ void fill_stats(letkf_ctx *ctx, const unsigned long long *cnt)
     s.n_borderline = (int64_t)cnt[LG_CNT_BORDER];
     s.n_not_converged = (int64_t)cnt[LG_CNT_NOTCONV];
     s.max_sweeps = (int32_t)cnt[LG_CNT_MAXSWEEP];
+    s.sum_sweeps = (int64_t)cnt[LG_CNT_SUMSWEEP];
     s.precision = ctx->params.precision;
 }
 
@@ -242,6 +247,16 @@ extern "C" {
 
 int64_t letkf_gpu_launch_count(void) { return g_launches.load(); }
 
+int letkf_decomp_dims(int nranks, int *lat_blocks, int *lon_blocks)
+{
+    if (!lat_blocks || !lon_blocks) return LETKF_ERR_INVALID;
+    int a = 0, b = 0;
+    if (lg_decomp_dims(nranks, a, b) != 0) return LETKF_ERR_INVALID;
+    *lat_blocks = a;
+    *lon_blocks = b;
+    return LETKF_OK;
+}
+
 int letkf_gpu_create(letkf_ctx **out, const letkf_grid *grid, const letkf_params *params, int device)
 {
     letkf_ctx *ctx = nullptr;
@@ -269,6 +284,12 @@ int letkf_gpu_create(letkf_ctx **out, const letkf_grid *grid, const letkf_params
     const bool need_hybrid = P.h_mode == 0 || P.vert_dist > 0.0;
     if (need_hybrid && (!G.hyai || !G.hybi || G.ps_row < 0 || G.ps_row >= n))
         return LETKF_ERR_INVALID;
+    const bool decomposed = P.decomp_lat_blocks != 0 || P.decomp_lon_blocks != 0;
+    if (decomposed && (P.decomp_lat_blocks < 1 || P.decomp_lon_blocks < 1 || P.decomp_lat_blocks > G.nlat ||
+                       P.decomp_lon_blocks > G.nlon ||
+                       (int64_t)P.decomp_lat_blocks * P.decomp_lon_blocks > 65535))
+        return LETKF_ERR_INVALID;
+    if (decomposed && P.cube_n != 1) return LETKF_ERR_UNSUPPORTED;
     if (P.overlap != 0 || P.vert_dist > 0.0) return LETKF_ERR_UNSUPPORTED;
     if (P.precision == LETKF_PREC_MIXED && !lg_mixed_supports(G.ens)) return LETKF_ERR_UNSUPPORTED;
 
@@ -306,6 +327,7 @@ int letkf_gpu_create(letkf_ctx **out, const letkf_grid *grid, const letkf_params
         glon.push_back(360.0f);     // grid_lon(ny+1) = 360 (pro_info.F90:78,83)
         LG_CUDA(h2d(ctx->d_glat, glat.data(), glat.size(), ctx->stream));
         LG_CUDA(h2d(ctx->d_glon, glon.data(), glon.size(), ctx->stream));
+        if (decomposed) LG_CUDA(lg_decomp_setup(ctx, glat, glon));
         std::vector<double> zero(G.nz + 1, 0.0);
         LG_CUDA(h2d(ctx->d_hyai, G.hyai ? G.hyai : zero.data(), (size_t)G.nz + 1, ctx->stream));
         LG_CUDA(h2d(ctx->d_hybi, G.hybi ? G.hybi : zero.data(), (size_t)G.nz + 1, ctx->stream));

@@ -163,6 +163,7 @@ k_core_fp64(LgGrid g, LgParams prm, RowSrc src, const int64_t *__restrict__ loff
         const int sweeps = lg_jacobi<double, K, Cfg<K>::G>(W, nrm, rot, &s_rot, 1e-15, 40);
         if (tid == 0) {
             atomicMax(&counters[LG_CNT_MAXSWEEP], (unsigned long long)sweeps);
+            atomicAdd(&counters[LG_CNT_SUMSWEEP], (unsigned long long)sweeps);
             if (sweeps > 40) {
                 atomicAdd(&counters[LG_CNT_NOTCONV], 1ull);
                 atomicOr(status, LG_ST_NOT_CONV);

@@ -39,6 +39,7 @@ enum {
     LG_CNT_BORDER,
     LG_CNT_NOTCONV,
     LG_CNT_MAXSWEEP,
+    LG_CNT_SUMSWEEP,
     LG_CNT_N
 };
 
@@ -201,6 +202,12 @@ struct letkf_ctx {
     DevBuf<int32_t> d_lidx;
     DevBuf<double> d_lrloc;
     int64_t list_cap = 0;
+    // decomposed observation sets (letkf_decomp.cu)
+    int dec_nx = 0, dec_ny = 0, dec_nchunk = 0;
+    DevBuf<double> d_dec_box;                    // lat0[nx], lat1[nx], lon0[ny], lon1[ny]
+    DevBuf<int> d_dec_row_blk, d_dec_col_blk;    // lat block of each row, lon block of each column
+    DevBuf<int> d_dec_slot_off, d_dec_slot_blk;  // neighbour blocks of each block, scan order
+    DevBuf<int> d_dec_cnt, d_dec_pos, d_dec_obs; // per (block, chunk) counts, offsets; obs of blocks
     // per-cube results
     DevBuf<double> d_trans, d_w;
     // core_batch staging
@@ -228,7 +235,14 @@ cudaError_t lg_launch_obs_prepare(letkf_ctx *ctx, const LgGrid &g, const double 
                                   const double *olon, const double *oph, const int32_t *olev,
                                   const int32_t *ovar, const double *oyo, const double *orinv);
 cudaError_t lg_launch_buckets(letkf_ctx *ctx, int64_t nobs);
+void lg_launch_scan_exclusive(const int *in, int *out, int n, cudaStream_t stream);
 cudaError_t lg_launch_search(letkf_ctx *ctx, const LgGrid &g, int64_t nobs);
+// decomposed observation sets (letkf_decomp.cu, letkf_search.cu)
+int lg_decomp_dims(int nranks, int &lat_blocks, int &lon_blocks);
+cudaError_t lg_decomp_setup(letkf_ctx *ctx, const std::vector<float> &glat_ext,
+                            const std::vector<float> &glon_ext);
+cudaError_t lg_launch_block_members(letkf_ctx *ctx, int64_t nobs, const double *olat, const double *olon);
+cudaError_t lg_launch_search_dec(letkf_ctx *ctx, const LgGrid &g, const double *olat);
 cudaError_t lg_launch_core_fp64(letkf_ctx *ctx, const LgGrid &g, const double *xb,
                                 const double *axb, double *xa, double *axa, bool keep_trans);
 cudaError_t lg_launch_core_mixed(letkf_ctx *ctx, const LgGrid &g, const double *xb,

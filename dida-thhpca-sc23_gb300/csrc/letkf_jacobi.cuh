@@ -8,9 +8,7 @@ template <> struct LgVec2<double> { using type = double2; };
 template <> struct LgVec2<float> { using type = float2; };
 
 // Rotation (c, s, t) that zeroes the inner product gam of two columns with
-// squared norms al, be.  The FP32 variant uses the fast reciprocal and
-// reciprocal square root: it only feeds approximate eigenvectors that are
-// refined in FP64 afterwards.
+// squared norms al, be (t = tan of the angle, c = cos, s = sin).
 __device__ __forceinline__ void lg_rotation(double al, double be, double gam, double &c, double &s,
                                             double &t)
 {
@@ -19,13 +17,32 @@ __device__ __forceinline__ void lg_rotation(double al, double be, double gam, do
     c = 1.0 / sqrt(1.0 + t * t);
     s = c * t;
 }
+
+// FP32 variant for the approximate eigenpairs of the mixed form, written for
+// a short dependency chain: with d = be - al, r = sqrt(d^2 + (2 gam)^2),
+//     t = sign(d) 2 gam / (|d| + r),   c = 1 / sqrt(1 + t^2),   s = c t
+// (the same t as above, multiplied through by |2 gam|), using the hardware
+// approximate reciprocal and reciprocal square root (relative error ~1e-7).
+// The caller only rotates when gam^2 > tol^2 al be > 0, so r > 0.
+__device__ __forceinline__ float lg_rcp_approx(float x)
+{
+    float y;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float lg_rsqrt_approx(float x)
+{
+    float y;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
 __device__ __forceinline__ void lg_rotation(float al, float be, float gam, float &c, float &s, float &t)
 {
-    const float zeta = (be - al) * __frcp_rn(2.0f * gam);
-    const float az = fabsf(zeta);
-    const float root = az < 1e18f ? az + sqrtf(fmaf(zeta, zeta, 1.0f)) : 2.0f * az;
-    t = copysignf(__frcp_rn(root), zeta);
-    c = rsqrtf(fmaf(t, t, 1.0f));
+    const float d = be - al, g2 = 2.0f * gam;
+    const float r2 = fmaf(d, d, g2 * g2);
+    const float r = r2 * lg_rsqrt_approx(r2);
+    t = (d >= 0.0f ? g2 : -g2) * lg_rcp_approx(fabsf(d) + r);
+    c = lg_rsqrt_approx(fmaf(t, t, 1.0f));
     s = c * t;
 }
 
@@ -154,14 +171,18 @@ __device__ int lg_jacobi(T *W, T *nrm, typename LgVec2<T>::type *rot, int *s_rot
     return sweep;
 }
 
-// FP32 one-sided Jacobi for the mixed-precision form.  Same round-robin
+// FP32 one-sided Jacobi for the mixed-precision form.  Pairs whose cosine
+// exceeds tol are rotated; the sweeps stop after one in which no cosine
+// exceeded tol_continue: cyclic Jacobi converges quadratically, so a sweep
+// whose largest cosine is below sqrt(tol) leaves the columns orthogonal to
+// about tol, and the extra sweep that would only confirm it is skipped.  Same round-robin
 // scheme as lg_jacobi, but each lane of a pair group owns a contiguous run of
 // K/G rows, keeps the pair's rows in registers between the inner product and
 // the rotation, and moves them with vector shared-memory accesses; every lane
 // computes the rotation (FP32, cheap) so a step needs one barrier.  LD (the
 // column stride) must keep the rows of a lane aligned for the vector width.
 template <int K, int G, int LD>
-__device__ int lg_jacobi32(float *W, float *nrm, int *s_rot, float tol, int max_sweeps)
+__device__ int lg_jacobi32(float *W, float *nrm, int *s_rot, float tol, float tol_continue, int max_sweeps)
 {
     constexpr int NP = K / 2, RPL = K / G;
     constexpr int VW = (RPL % 4 == 0) ? 4 : ((RPL % 2 == 0) ? 2 : 1);
@@ -170,7 +191,7 @@ __device__ int lg_jacobi32(float *W, float *nrm, int *s_rot, float tol, int max_
     const int tid = threadIdx.x;
     const int pair = tid / G, lane = tid % G;
     const bool act = pair < NP;
-    const float tol2 = tol * tol;
+    const float tol2 = tol * tol, cont2 = tol_continue * tol_continue;
     int sweep;
     for (sweep = 1; sweep <= max_sweeps; sweep++) {
         if (tid < K) {
@@ -206,9 +227,13 @@ __device__ int lg_jacobi32(float *W, float *nrm, int *s_rot, float tol, int max_
                         b[i] = wq[i];
                     }
                 }
-                float gam = 0.0f;
+                float g0 = 0.0f, g1 = 0.0f;
 #pragma unroll
-                for (int i = 0; i < RPL; i++) gam = fmaf(a[i], b[i], gam);
+                for (int i = 0; i < RPL; i += 2) {
+                    g0 = fmaf(a[i], b[i], g0);
+                    if (i + 1 < RPL) g1 = fmaf(a[i + 1], b[i + 1], g1);
+                }
+                float gam = g0 + g1;
 #pragma unroll
                 for (int o = G / 2; o > 0; o >>= 1) gam += __shfl_xor_sync(0xffffffffu, gam, o);
                 const float al = nrm[p], be = nrm[q];
@@ -238,7 +263,7 @@ __device__ int lg_jacobi32(float *W, float *nrm, int *s_rot, float tol, int max_
                     if (lane == 0) {
                         nrm[p] = al - t * gam;
                         nrm[q] = be + t * gam;
-                        *s_rot = 1;
+                        if (gam * gam > cont2 * (al * be)) *s_rot = 1;
                     }
                 }
             }

@@ -265,6 +265,12 @@ cudaError_t lg_launch_obs_prepare(letkf_ctx *ctx, const LgGrid &g, const double 
     return cudaGetLastError();
 }
 
+void lg_launch_scan_exclusive(const int *in, int *out, int n, cudaStream_t stream)
+{
+    lg_count_launch();
+    k_scan_exclusive<<<1, 1024, 0, stream>>>(in, out, n);
+}
+
 cudaError_t lg_launch_buckets(letkf_ctx *ctx, int64_t nobs)
 {
     const int nb = ctx->nblat * ctx->nblon;

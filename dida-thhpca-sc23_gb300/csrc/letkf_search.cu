@@ -126,6 +126,86 @@ __device__ void bitonic_sort(int32_t *keys, int n_pow2)
     }
 }
 
+// Reserve the cube's slot in the list pool with one atomic add and write its
+// kept obs (keys[0..nout), in list order) with their localization weights.
+__device__ void write_list(const int32_t *keys, int nout, bool truncated, int64_t cube, const CubeGeo &cg,
+                           const LgObsGeo &geo, const LgParams &prm, int32_t *__restrict__ lidx,
+                           double *__restrict__ lrloc, int64_t list_cap, int64_t *__restrict__ loff,
+                           int32_t *__restrict__ lcnt, unsigned long long *__restrict__ counters,
+                           unsigned *__restrict__ status, long long *s_off)
+{
+    if (threadIdx.x == 0) {
+        long long off = (long long)atomicAdd(&counters[LG_CNT_CURSOR], (unsigned long long)nout);
+        if (off + nout > list_cap) {
+            atomicOr(status, LG_ST_LIST_FULL);
+            off = -1;
+        }
+        *s_off = off;
+        loff[cube] = off < 0 ? 0 : off;
+        lcnt[cube] = off < 0 ? 0 : nout;
+        atomicAdd(&counters[LG_CNT_SUMP], (unsigned long long)nout);
+        atomicMax(&counters[LG_CNT_MAXP], (unsigned long long)nout);
+        if (truncated) atomicAdd(&counters[LG_CNT_TRUNC], 1ull);
+    }
+    __syncthreads();
+    const long long off = *s_off;
+    if (off >= 0) {
+        if (prm.precision == LETKF_PREC_MIXED) {
+            // FP32 weights from the chord of the unit vectors (the selection
+            // used the reference's double formula where it mattered)
+            const float scale = (float)(LG_EARTH_A / prm.local_dist);
+            for (int i = threadIdx.x; i < nout; i += kThreads) {
+                const int o = keys[i];
+                const float4 q = geo.xyz[o];
+                const float dx = q.x - cg.cx, dy = q.y - cg.cy, dz = q.z - cg.cz;
+                const float half = fminf(1.0f, 0.5f * sqrtf(dx * dx + dy * dy + dz * dz));
+                const float ri = 2.0f * asinf(half) * scale;
+                lidx[off + i] = o;
+                lrloc[off + i] = prm.gc_filter ? (double)lg_schr2f(ri) : (ri > 2.0f ? 0.0 : 1.0);
+            }
+        } else {
+            for (int i = threadIdx.x; i < nout; i += kThreads) {
+                const int o = keys[i];
+                const double dist = lg_dist(geo.s[o], geo.c[o], geo.yr[o], cg.s2, cg.c2, cg.y2r);
+                const double ri = lg_ri(dist, prm.local_dist);
+                lidx[off + i] = o;
+                lrloc[off + i] = prm.gc_filter ? lg_schr2(ri) : lg_schr(ri);
+            }
+        }
+    }
+}
+
+// Centre geometry of cube (as k_search's): unit vector, sin/cos, the chord
+// thresholds of the float prefilter.
+__device__ CubeGeo cube_geo(const LgGrid &g, const LgParams &prm, int64_t cube, double &clat, double &clon)
+{
+    const int bj = (int)(cube % prm.nbj), bi = (int)(cube / prm.nbj);
+    const int sj = bj * prm.cube_n, ej = min(sj + prm.cube_n - 1, g.nlat - 1);
+    const int si = bi * prm.cube_n, ei = min(si + prm.cube_n - 1, g.nlon - 1);
+    const int cj = ((sj + 1) + (ej + 1)) / 2 - 1, ci = ((si + 1) + (ei + 1)) / 2 - 1;
+    clat = (double)g.glat[cj];
+    clon = (double)g.glon[ci];
+    CubeGeo cg;
+    const double xr = lg_rad(clat);
+    cg.s2 = sin(xr);
+    cg.c2 = cos(xr);
+    cg.y2r = lg_rad(clon);
+    cg.cx = (float)(cg.c2 * cos(cg.y2r));
+    cg.cy = (float)(cg.c2 * sin(cg.y2r));
+    cg.cz = (float)cg.s2;
+    const double theta = 2.0 * prm.local_dist / LG_EARTH_A;
+    if (theta > 0.01) {
+        const double a = 2.0 * sin(0.5 * theta * (1.0 - 1e-3));
+        const double b = 2.0 * sin(0.5 * theta * (1.0 + 1e-3));
+        cg.lo2 = (float)(a * a);
+        cg.hi2 = (float)(b * b);
+    } else {
+        cg.lo2 = -1.0f;           // every candidate takes the double test
+        cg.hi2 = 1.0e30f;
+    }
+    return cg;
+}
+
 __global__ void __launch_bounds__(kThreads)
 k_search(LgGrid g, LgParams prm, LgBuckets bk, LgObsGeo geo, int64_t nobs, int cap_sort,
          int32_t *__restrict__ lidx, double *__restrict__ lrloc, int64_t list_cap,
@@ -140,29 +220,9 @@ k_search(LgGrid g, LgParams prm, LgBuckets bk, LgObsGeo geo, int64_t nobs, int c
 
     for (int64_t cube = blockIdx.x; cube < ncubes; cube += gridDim.x) {
         if (threadIdx.x == 0) {
-            const int bj = (int)(cube % prm.nbj), bi = (int)(cube / prm.nbj);
-            const int sj = bj * prm.cube_n, ej = min(sj + prm.cube_n - 1, g.nlat - 1);
-            const int si = bi * prm.cube_n, ei = min(si + prm.cube_n - 1, g.nlon - 1);
-            const int cj = ((sj + 1) + (ej + 1)) / 2 - 1, ci = ((si + 1) + (ei + 1)) / 2 - 1;
-            const double clat = (double)g.glat[cj], clon = (double)g.glon[ci];
-            CubeGeo cg;
-            const double xr = lg_rad(clat);
-            cg.s2 = sin(xr);
-            cg.c2 = cos(xr);
-            cg.y2r = lg_rad(clon);
-            cg.cx = (float)(cg.c2 * cos(cg.y2r));
-            cg.cy = (float)(cg.c2 * sin(cg.y2r));
-            cg.cz = (float)cg.s2;
+            double clat, clon;
+            const CubeGeo cg = cube_geo(g, prm, cube, clat, clon);
             const double theta = 2.0 * prm.local_dist / LG_EARTH_A;
-            if (theta > 0.01) {
-                const double a = 2.0 * sin(0.5 * theta * (1.0 - 1e-3));
-                const double b = 2.0 * sin(0.5 * theta * (1.0 + 1e-3));
-                cg.lo2 = (float)(a * a);
-                cg.hi2 = (float)(b * b);
-            } else {
-                cg.lo2 = -1.0f;           // every candidate takes the double test
-                cg.hi2 = 1.0e30f;
-            }
             s_cg = cg;
             // buckets of the cap
             int ns = 0;
@@ -231,45 +291,81 @@ k_search(LgGrid g, LgParams prm, LgBuckets bk, LgObsGeo geo, int64_t nobs, int c
             bitonic_sort(keys, np2);
             nout = min(c, prm.max_obs);
         }
+        write_list(keys, nout, nk > prm.max_obs, cube, cg, geo, prm, lidx, lrloc, list_cap, loff, lcnt,
+                   counters, status, &s_off);
+        __syncthreads();
+    }
+}
+
+// Decomposed observation sets: the cube's list is the scan of gen_yb_dis
+// (letkf_yb.F90:71-133) over the obs of its block's neighbour blocks, block
+// by block in the neighbour order and by index within a block, kept iff
+// |lat| <= obs_polar and gc > 0, stopped at max_obs.  An obs that two scanned
+// blocks hold is listed twice, as in the reference.  Each chunk of 256
+// candidates is tested in parallel and compacted in order (ballots and warp
+// totals); candidates whose float chord is near the antipode's take the
+// double test, where the reference keeps NaN distances.
+__global__ void __launch_bounds__(kThreads)
+k_search_dec(LgGrid g, LgParams prm, LgObsGeo geo, const double *__restrict__ olat, int NY, int nchunk,
+             const int *__restrict__ row_blk, const int *__restrict__ col_blk,
+             const int *__restrict__ slot_off, const int *__restrict__ slot_blk,
+             const int *__restrict__ blk_pos, const int *__restrict__ blk_obs, int32_t *__restrict__ lidx,
+             double *__restrict__ lrloc, int64_t list_cap, int64_t *__restrict__ loff,
+             int32_t *__restrict__ lcnt, unsigned long long *__restrict__ counters,
+             unsigned *__restrict__ status, int64_t ncubes)
+{
+    extern __shared__ int32_t keys[];
+    __shared__ CubeGeo s_cg;
+    __shared__ int s_blk;
+    __shared__ int s_warp[kThreads / 32];
+    __shared__ long long s_off;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int max_obs = prm.max_obs;
+
+    for (int64_t cube = blockIdx.x; cube < ncubes; cube += gridDim.x) {
         if (threadIdx.x == 0) {
-            long long off = (long long)atomicAdd(&counters[LG_CNT_CURSOR], (unsigned long long)nout);
-            if (off + nout > list_cap) {
-                atomicOr(status, LG_ST_LIST_FULL);
-                off = -1;
-            }
-            s_off = off;
-            loff[cube] = off < 0 ? 0 : off;
-            lcnt[cube] = off < 0 ? 0 : nout;
-            atomicAdd(&counters[LG_CNT_SUMP], (unsigned long long)nout);
-            atomicMax(&counters[LG_CNT_MAXP], (unsigned long long)nout);
-            if (nk > prm.max_obs) atomicAdd(&counters[LG_CNT_TRUNC], 1ull);
+            double clat, clon;
+            s_cg = cube_geo(g, prm, cube, clat, clon);
+            const int sj = (int)(cube % prm.nbj), si = (int)(cube / prm.nbj);   // cube_n is 1
+            s_blk = row_blk[sj] * NY + col_blk[si];
         }
         __syncthreads();
-        const long long off = s_off;
-        if (off >= 0) {
-            if (prm.precision == LETKF_PREC_MIXED) {
-                // FP32 weights from the chord of the unit vectors (the selection
-                // above used the reference's double formula where it mattered)
-                const float scale = (float)(LG_EARTH_A / prm.local_dist);
-                for (int i = threadIdx.x; i < nout; i += kThreads) {
-                    const int o = keys[i];
-                    const float4 q = geo.xyz[o];
-                    const float dx = q.x - cg.cx, dy = q.y - cg.cy, dz = q.z - cg.cz;
-                    const float half = fminf(1.0f, 0.5f * sqrtf(dx * dx + dy * dy + dz * dz));
-                    const float ri = 2.0f * asinf(half) * scale;
-                    lidx[off + i] = o;
-                    lrloc[off + i] = prm.gc_filter ? (double)lg_schr2f(ri) : (ri > 2.0f ? 0.0 : 1.0);
+        const CubeGeo cg = s_cg;
+        const int blk = s_blk;
+        int n = 0;
+        for (int sl = slot_off[blk]; sl < slot_off[blk + 1] && n < max_obs; sl++) {
+            const int B = slot_blk[sl];
+            const int beg = blk_pos[(int64_t)B * nchunk], end = blk_pos[(int64_t)(B + 1) * nchunk];
+            for (int base = beg; base < end && n < max_obs; base += kThreads) {
+                const int i = base + threadIdx.x;
+                bool keep = false;
+                int o = 0;
+                if (i < end) {
+                    o = blk_obs[i];
+                    if (fabs(olat[o]) <= prm.obs_polar) {
+                        const float4 p = geo.xyz[o];
+                        const float dx = p.x - cg.cx, dy = p.y - cg.cy, dz = p.z - cg.cz;
+                        const int exact = (dx * dx + dy * dy + dz * dz) > 3.9999f;
+                        keep = keep_candidate(p, exact, cg, geo, prm, &counters[LG_CNT_BORDER]);
+                    }
                 }
-            } else {
-                for (int i = threadIdx.x; i < nout; i += kThreads) {
-                    const int o = keys[i];
-                    const double dist = lg_dist(geo.s[o], geo.c[o], geo.yr[o], cg.s2, cg.c2, cg.y2r);
-                    const double ri = lg_ri(dist, prm.local_dist);
-                    lidx[off + i] = o;
-                    lrloc[off + i] = prm.gc_filter ? lg_schr2(ri) : lg_schr(ri);
+                const unsigned ball = __ballot_sync(0xffffffffu, keep);
+                if (lane == 0) s_warp[warp] = __popc(ball);
+                __syncthreads();
+                int before = 0, all = 0;
+#pragma unroll
+                for (int w = 0; w < kThreads / 32; w++) {
+                    before += (w < warp) ? s_warp[w] : 0;
+                    all += s_warp[w];
                 }
+                const int pos = n + before + __popc(ball & ((1u << lane) - 1u));
+                if (keep && pos < max_obs) keys[pos] = o;
+                n += all;
+                __syncthreads();
             }
         }
+        write_list(keys, min(n, max_obs), n >= max_obs, cube, cg, geo, prm, lidx, lrloc, list_cap, loff,
+                   lcnt, counters, status, &s_off);
         __syncthreads();
     }
 }
@@ -304,5 +400,23 @@ cudaError_t lg_launch_search(letkf_ctx *ctx, const LgGrid &g, int64_t nobs)
     k_search<<<(unsigned)(blocks > 0 ? blocks : 1), kThreads, smem, ctx->stream>>>(
         g, prm, bk, geo, nobs, cap, ctx->d_lidx.p, ctx->d_lrloc.p, ctx->list_cap, ctx->d_loff.p,
         ctx->d_lcnt.p, ctx->d_counters.p, ctx->d_status.p, ctx->ncubes);
+    return cudaGetLastError();
+}
+
+cudaError_t lg_launch_search_dec(letkf_ctx *ctx, const LgGrid &g, const double *olat)
+{
+    const LgParams prm = lg_params(ctx);
+    LgObsGeo geo{ctx->d_os.p, ctx->d_oc.p, ctx->d_oyr.p, ctx->d_oxyz.p};
+    const int cap = lg_search_cap(prm.max_obs);
+    const size_t smem = sizeof(int32_t) * cap;
+    cudaError_t e = cudaFuncSetAttribute(k_search_dec, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    const int64_t blocks = ctx->ncubes < (1 << 30) ? ctx->ncubes : (1 << 30);
+    lg_count_launch();
+    k_search_dec<<<(unsigned)(blocks > 0 ? blocks : 1), kThreads, smem, ctx->stream>>>(
+        g, prm, geo, olat, ctx->dec_ny, ctx->dec_nchunk, ctx->d_dec_row_blk.p, ctx->d_dec_col_blk.p,
+        ctx->d_dec_slot_off.p, ctx->d_dec_slot_blk.p, ctx->d_dec_pos.p, ctx->d_dec_obs.p, ctx->d_lidx.p,
+        ctx->d_lrloc.p, ctx->list_cap, ctx->d_loff.p, ctx->d_lcnt.p, ctx->d_counters.p, ctx->d_status.p,
+        ctx->ncubes);
     return cudaGetLastError();
 }

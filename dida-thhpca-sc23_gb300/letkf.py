@@ -42,7 +42,7 @@ EXPORTED = [
     "letkf_gpu_synchronize", "letkf_gpu_obs_operator", "letkf_gpu_local_obs",
     "letkf_gpu_last_trans", "letkf_gpu_core_batch", "letkf_gpu_get_stats",
     "letkf_gpu_last_error", "letkf_gpu_destroy", "letkf_gpu_launch_count",
-    "letkf_gpu_core_batch_noalloc",
+    "letkf_gpu_core_batch_noalloc", "letkf_decomp_dims",
     "letkf_init_gpu_", "letkf_set_obs_gpu_", "letkf_run_gpu_", "letkf_final_gpu_",
 ]
 
@@ -69,6 +69,7 @@ class Params(C.Structure):
         ("obs_polar_deg", C.c_double), ("gc_filter", C.c_int), ("gc_filter_vertical", C.c_int),
         ("max_obs", C.c_int), ("cube_n", C.c_int), ("cube_nz", C.c_int), ("overlap", C.c_int),
         ("h_mode", C.c_int), ("precision", C.c_int),
+        ("decomp_lat_blocks", C.c_int), ("decomp_lon_blocks", C.c_int),
     ]
 
 
@@ -86,6 +87,7 @@ class Stats(C.Structure):
         ("n_not_converged", C.c_int64), ("max_sweeps", C.c_int32), ("precision", C.c_int32),
         ("ms_h2d", C.c_double), ("ms_obs", C.c_double), ("ms_search", C.c_double),
         ("ms_core", C.c_double), ("ms_d2h", C.c_double), ("ms_total", C.c_double),
+        ("sum_sweeps", C.c_int64),
     ]
 
     def as_dict(self):
@@ -119,6 +121,7 @@ def load_library(path: str = LIB_PATH):
     L.letkf_gpu_destroy.argtypes = [vp]
     L.letkf_gpu_launch_count.restype = i64
     L.letkf_gpu_core_batch_noalloc.argtypes = [i32, C.c_double, i64, vp, vp, vp, vp, vp, vp, vp, vp]
+    L.letkf_decomp_dims.argtypes = [i32, C.POINTER(C.c_int), C.POINTER(C.c_int)]
     _lib = L
     return L
 
@@ -158,13 +161,24 @@ class ObsArrays:
                      var=p("var"), yo=p("yo"), rinv=p("rinv"))
 
 
+def decomp_dims(nranks: int):
+    """(lat_blocks, lon_blocks) of a DA group of nranks ranks (letkf_decomp_dims)."""
+    L = load_library()
+    a, b = C.c_int(), C.c_int()
+    rc = L.letkf_decomp_dims(nranks, C.byref(a), C.byref(b))
+    if rc != LETKF_OK:
+        raise LetkfError(rc, "letkf_decomp_dims")
+    return a.value, b.value
+
+
 class LetkfGPU:
     """One analysis context (grid + namelist parameters) on one GPU."""
 
     def __init__(self, glat, glon, nz, ens, *, nvar2d=1, nvar3d=3, hyai=None, hybi=None,
                  p0=1.0e5, ptop=219.4, ps_row=0, loc_dist_km, inflation, vert_dist=-999.0,
                  obs_polar_deg=91.0, gc_filter=1, gc_filter_vertical=1, max_obs=10000,
-                 cube_n=1, cube_nz=1, overlap=0, h_mode=1, precision=LETKF_PREC_FP64, device=0):
+                 cube_n=1, cube_nz=1, overlap=0, h_mode=1, precision=LETKF_PREC_FP64,
+                 decomp=(0, 0), device=0):
         L = load_library()
         self._glat = np.ascontiguousarray(glat, dtype=np.float32)
         self._glon = np.ascontiguousarray(glon, dtype=np.float32)
@@ -179,7 +193,8 @@ class LetkfGPU:
         prm = Params(loc_dist_km=loc_dist_km, vert_dist=vert_dist, inflation=inflation,
                      obs_polar_deg=obs_polar_deg, gc_filter=gc_filter,
                      gc_filter_vertical=gc_filter_vertical, max_obs=max_obs, cube_n=cube_n,
-                     cube_nz=cube_nz, overlap=overlap, h_mode=h_mode, precision=precision)
+                     cube_nz=cube_nz, overlap=overlap, h_mode=h_mode, precision=precision,
+                     decomp_lat_blocks=decomp[0], decomp_lon_blocks=decomp[1])
         h = C.c_void_p()
         rc = L.letkf_gpu_create(C.byref(h), C.byref(g), C.byref(prm), device)
         if rc != LETKF_OK:

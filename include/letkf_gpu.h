@@ -85,6 +85,16 @@ typedef struct letkf_params {
     int h_mode;                /* 0: hybrid log-p interpolation (obs_make.F90:233-381),
                                   1: level select (obs carries a model level)       */
     int precision;             /* LETKF_PREC_*                                      */
+    /* Observation sets.  0, 0: one logical block holding every observation
+     * once (each obs scanned once, in index order).  Otherwise the local
+     * lists are those of a DA group decomposed into decomp_lat_blocks x
+     * decomp_lon_blocks MPI blocks (module_da_parallel.F90:73-103, pro_info.F90:
+     * 96-125): each block holds the obs inside its lat/lon box
+     * (read_obs_mod.F90:73-165), and a column scans the blocks of its
+     * neighbour set (letkf_init.F90:100-341) in the reference's order, which
+     * reproduces a P-rank run's lists.  Needs cube_n 1 and overlap 0;
+     * letkf_decomp_dims gives the blocks of P ranks.                         */
+    int decomp_lat_blocks, decomp_lon_blocks;
 } letkf_params;
 
 /* Observations (the obs_list fields, read_obs_mod.F90:15-27, flattened). */
@@ -109,7 +119,15 @@ typedef struct letkf_stats {
     int32_t max_sweeps;        /* most Jacobi sweeps any cube needed                */
     int32_t precision;
     double ms_h2d, ms_obs, ms_search, ms_core, ms_d2h, ms_total;  /* device-event times */
+    int64_t sum_sweeps;        /* Jacobi sweeps summed over all cubes               */
 } letkf_stats;
+
+/* The lat x lon blocks of a DA group of nranks MPI ranks: MPI_Dims_create(
+ * nranks, 2) (the most balanced factor pair, larger first), whose first
+ * dimension splits longitude and second latitude
+ * (EnDNN/src/module_da_parallel.F90:73-103, 143).  No counterpart function in
+ * the reference, which asks MPI.  Returns LETKF_ERR_INVALID for nranks < 1.  */
+int letkf_decomp_dims(int nranks, int *lat_blocks, int *lon_blocks);
 
 /* Create a context on CUDA device `device` (the current device if < 0).
  * Copies the grid; replaces letkf_init.                                      */

@@ -11,6 +11,7 @@
 #include "letkf_oracle.h"
 
 #include <math.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 #ifdef _OPENMP
@@ -314,9 +315,18 @@ typedef struct {
     lat_key *keys;        /* obs sorted by latitude */
     double *s, *c, *yr;   /* sin/cos of obs latitude, obs longitude in radians */
     int64_t n;
+    /* decomposed mode: obs of each block (ascending), neighbour slots */
+    int nbx, nby;
+    int *bx_of_row, *by_of_col;        /* block of each lat row / lon column */
+    int64_t *blk_off;
+    int32_t *blk_obs;
+    int *slot_off;
+    int32_t *slot_blk;
 } obs_index;
 
-static void obs_index_build(const orc_obs *obs, obs_index *ix)
+static void decomp_build(const orc_config *cfg, const orc_obs *obs, obs_index *ix);
+
+static void obs_index_build(const orc_config *cfg, const orc_obs *obs, obs_index *ix)
 {
     int64_t o;
     ix->n = obs->nobs;
@@ -333,6 +343,13 @@ static void obs_index_build(const orc_obs *obs, obs_index *ix)
         ix->yr[o] = lat_rad(obs->lon[o]);
     }
     qsort(ix->keys, (size_t)obs->nobs, sizeof(lat_key), cmp_lat);
+    ix->nbx = ix->nby = 0;
+    ix->bx_of_row = ix->by_of_col = NULL;
+    ix->blk_off = NULL;
+    ix->blk_obs = NULL;
+    ix->slot_off = NULL;
+    ix->slot_blk = NULL;
+    if (cfg->dec_lat_blocks > 0 && cfg->dec_lon_blocks > 0) decomp_build(cfg, obs, ix);
 }
 
 static void obs_index_free(obs_index *ix)
@@ -341,6 +358,12 @@ static void obs_index_free(obs_index *ix)
     free(ix->s);
     free(ix->c);
     free(ix->yr);
+    free(ix->bx_of_row);
+    free(ix->by_of_col);
+    free(ix->blk_off);
+    free(ix->blk_obs);
+    free(ix->slot_off);
+    free(ix->slot_blk);
 }
 
 static int64_t lower_bound_lat(const obs_index *ix, double lat)
@@ -429,13 +452,256 @@ static int local_point(const orc_config *cfg, const orc_obs *obs, const obs_inde
     return nobsl;
 }
 
+
+/* ---- decomposed observation sets --------------------------------------- */
+
+int orc_decomp_dims(int nranks, int *lat_blocks, int *lon_blocks)
+{
+    int b, best = 1;
+    if (nranks < 1) return -1;
+    for (b = 1; (int64_t)b * b <= nranks; b++)
+        if (nranks % b == 0) best = b;
+    *lon_blocks = nranks / best;     /* dims(1) >= dims(2) */
+    *lat_blocks = best;
+    return 0;
+}
+
+/* pro_info_get_indx (DA/utils/pro_info.F90:96-125) along one axis: 1-based
+ * inclusive index range of block b (1-based) of n points in nb blocks, the
+ * first n mod nb blocks one point longer.                                   */
+static void block_range(int n, int nb, int b, int *s, int *e)
+{
+    int sec = n / nb, res = n % nb;
+    if (b - 1 < res) {
+        *s = (b - 1) * (sec + 1) + 1;
+        *e = *s + sec;
+    } else {
+        *s = (b - 1) * sec + res + 1;
+        *e = *s + sec - 1;
+    }
+}
+
+/* latlon_dist_r4, DA/utils/pro_info.F90:163-175: the distance in default
+ * (single) precision, with float pi and Earth radius.                       */
+static float latlon_dist_f32(float x1, float y1, float x2, float y2)
+{
+    const float pi = atanf(1.0f) * 4.0f, a = 6371.393f;
+    float v = cosf(x1 / 180.0f * pi) * cosf(x2 / 180.0f * pi) * cosf(y1 / 180.0f * pi - y2 / 180.0f * pi) +
+              sinf(x1 / 180.0f * pi) * sinf(x2 / 180.0f * pi);
+    if (v > 1.0f) v = 1.0f;
+    return a * acosf(v);
+}
+
+/* nearest_dist, DA/LETKF/src/letkf_init.F90:293-341 (1-based blocks). */
+static double nearest_dist(const orc_config *cfg, int bx1, int by1, int bx2, int by2)
+{
+    const int NX = cfg->dec_lat_blocks, NY = cfg->dec_lon_blocks;
+    int xs1, xe1, ys1, ye1, xs2, xe2, ys2, ye2, tx1, tx2;
+    float lat1, lat2;
+    block_range(cfg->nlat, NX, bx1, &xs1, &xe1);
+    block_range(cfg->nlon, NY, by1, &ys1, &ye1);
+    block_range(cfg->nlat, NX, bx2, &xs2, &xe2);
+    block_range(cfg->nlon, NY, by2, &ys2, &ye2);
+    if (bx1 > bx2) {
+        tx1 = xs1;
+        tx2 = xe2 + 1;
+    } else if (bx1 < bx2) {
+        tx1 = xe1 + 1;
+        tx2 = xs2;
+    } else if (bx1 > NX / 2) {
+        tx1 = xe1 + 1;
+        tx2 = xe2 + 1;
+    } else {
+        tx1 = xs1;
+        tx2 = xs2;
+    }
+    lat1 = glat_ext(cfg, tx1);
+    lat2 = glat_ext(cfg, tx2);
+    if (fabs((double)lat1) > cfg->obs_polar) lat1 = (float)(lat1 < 0 ? -cfg->obs_polar : cfg->obs_polar);
+    if (fabs((double)lat2) > cfg->obs_polar) lat2 = (float)(lat2 < 0 ? -cfg->obs_polar : cfg->obs_polar);
+    if (by1 == by2)
+        return (double)latlon_dist_f32(lat1, glon_ext(cfg, ys1), lat2, glon_ext(cfg, ys2));
+    {
+        float d1 = latlon_dist_f32(lat1, glon_ext(cfg, ys1), lat2, glon_ext(cfg, ye2 % cfg->nlon + 1));
+        float d2 = latlon_dist_f32(lat1, glon_ext(cfg, ye1 % cfg->nlon + 1), lat2, glon_ext(cfg, ys2));
+        return (double)(d1 < d2 ? d1 : d2);
+    }
+}
+
+/* comm_info_init, DA/LETKF/src/letkf_init.F90:100-291: the blocks whose obs
+ * a block's columns scan, in the order gen_yb_dis visits them (lat offsets
+ * -north_n..south_n, then lon offsets -west_n..east_n, wrapping in longitude).
+ * Blocks are compared against local_dist itself (the cut-off is 2 local_dist),
+ * as the reference does.                                                    */
+int orc_block_slots(const orc_config *cfg, int bx0, int by0, int32_t *blocks, int cap)
+{
+    const int NX = cfg->dec_lat_blocks, NY = cfg->dec_lon_blocks;
+    const int bx = bx0 + 1, by = by0 + 1;
+    int s_lat, e_lat, s_lon, e_lon, tx_s, tx_e, north_n = 0, south_n = 0, i, n = 0;
+    double x1, y1, x2, y2;
+    block_range(cfg->nlat, NX, bx, &s_lat, &e_lat);
+    block_range(cfg->nlon, NY, by, &s_lon, &e_lon);
+    x1 = glat_ext(cfg, s_lat);
+    y1 = glon_ext(cfg, s_lon);
+    y2 = y1;
+    for (i = bx - 1; i > 0; i--) {
+        block_range(cfg->nlat, NX, i, &tx_s, &tx_e);
+        x2 = glat_ext(cfg, tx_e + 1);
+        if (orc_latlon_dist(x1, y1, x2, y2) > cfg->local_dist) break;
+        north_n++;
+    }
+    x1 = glat_ext(cfg, e_lat + 1);
+    for (i = bx + 1; i <= NX; i++) {
+        block_range(cfg->nlat, NX, i, &tx_s, &tx_e);
+        x2 = glat_ext(cfg, tx_s);
+        if (orc_latlon_dist(x1, y1, x2, y2) > cfg->local_dist) break;
+        south_n++;
+    }
+    for (i = -north_n; i <= south_n; i++) {
+        const int tbx = bx + i;
+        int west = 0, east = 0, tby, j;
+        tby = by;
+        while (west <= (NY - 1) / 2) {
+            tby = (tby + NY - 2) % NY + 1;
+            if (nearest_dist(cfg, bx, by, tbx, tby) > cfg->local_dist) break;
+            west++;
+        }
+        tby = by;
+        while (east <= (NY - 1) / 2) {
+            tby = tby % NY + 1;
+            if (nearest_dist(cfg, bx, by, tbx, tby) > cfg->local_dist) break;
+            east++;
+        }
+        if (west + east > NY - 1) east--;
+        for (j = -west; j <= east; j++) {
+            const int lb = ((by - 1 + j) % NY + NY) % NY;
+            if (n < cap) blocks[n] = (int32_t)((tbx - 1) * NY + lb);
+            n++;
+        }
+    }
+    return n;
+}
+
+/* A block's box bound as the obs store's range query sees it: the float grid
+ * coordinate printed with five decimals ("%.5f", LIB/REDIS/src/
+ * redis_wrapper.c:4097-4117) and read back.                                 */
+static double box_bound(float v)
+{
+    char buf[64];
+    snprintf(buf, sizeof buf, "%.5f", (double)v);
+    return strtod(buf, NULL);
+}
+
+/* Obs of each block: inside the closed box [grid_lat(s), grid_lat(e+1)] x
+ * [grid_lon(s), grid_lon(e+1)] of the block (allocate_obslist / read_obs,
+ * DA/LETKF/src/read_obs_mod.F90:73-165,338-449, called from
+ * letkf_obs.F90:45-90), in ascending index order (the store's range query
+ * returns sorted ids).  An obs on a shared edge belongs to both blocks; one
+ * outside every box (south of the first row or west of the first column of
+ * centres) to none.                                                          */
+static void decomp_build(const orc_config *cfg, const orc_obs *obs, obs_index *ix)
+{
+    const int NX = cfg->dec_lat_blocks, NY = cfg->dec_lon_blocks, nb = NX * NY;
+    double *la0 = (double *)malloc(sizeof(double) * NX), *la1 = (double *)malloc(sizeof(double) * NX);
+    double *lo0 = (double *)malloc(sizeof(double) * NY), *lo1 = (double *)malloc(sizeof(double) * NY);
+    int64_t *cnt = (int64_t *)calloc((size_t)nb + 1, sizeof(int64_t));
+    int b, s, e, i, cap;
+    int64_t o;
+    ix->nbx = NX;
+    ix->nby = NY;
+    ix->bx_of_row = (int *)malloc(sizeof(int) * cfg->nlat);
+    ix->by_of_col = (int *)malloc(sizeof(int) * cfg->nlon);
+    for (b = 0; b < NX; b++) {
+        block_range(cfg->nlat, NX, b + 1, &s, &e);
+        la0[b] = box_bound(glat_ext(cfg, s));
+        la1[b] = box_bound(glat_ext(cfg, e + 1));
+        for (i = s; i <= e; i++) ix->bx_of_row[i - 1] = b;
+    }
+    for (b = 0; b < NY; b++) {
+        block_range(cfg->nlon, NY, b + 1, &s, &e);
+        lo0[b] = box_bound(glon_ext(cfg, s));
+        lo1[b] = box_bound(glon_ext(cfg, e + 1));
+        for (i = s; i <= e; i++) ix->by_of_col[i - 1] = b;
+    }
+    for (int pass = 0; pass < 2; pass++) {
+        if (pass == 1) {
+            ix->blk_off = (int64_t *)malloc(sizeof(int64_t) * (nb + 1));
+            ix->blk_off[0] = 0;
+            for (b = 0; b < nb; b++) ix->blk_off[b + 1] = ix->blk_off[b] + cnt[b];
+            ix->blk_obs = (int32_t *)malloc(sizeof(int32_t) * (ix->blk_off[nb] + 1));
+            memset(cnt, 0, sizeof(int64_t) * (nb + 1));
+        }
+        for (o = 0; o < obs->nobs; o++) {
+            int bxa, bya;
+            for (bxa = 0; bxa < NX; bxa++) {
+                if (!(obs->lat[o] >= la0[bxa] && obs->lat[o] <= la1[bxa])) continue;
+                for (bya = 0; bya < NY; bya++) {
+                    if (!(obs->lon[o] >= lo0[bya] && obs->lon[o] <= lo1[bya])) continue;
+                    b = bxa * NY + bya;
+                    if (pass == 1) ix->blk_obs[ix->blk_off[b] + cnt[b]] = (int32_t)o;
+                    cnt[b]++;
+                }
+            }
+        }
+    }
+    cap = 2 * nb + 2;
+    ix->slot_off = (int *)malloc(sizeof(int) * (nb + 1));
+    ix->slot_blk = (int32_t *)malloc(sizeof(int32_t) * (size_t)nb * cap);
+    ix->slot_off[0] = 0;
+    for (b = 0; b < nb; b++) {
+        int ns = orc_block_slots(cfg, b / NY, b % NY, ix->slot_blk + ix->slot_off[b], cap);
+        if (ns > cap) ns = cap;
+        ix->slot_off[b + 1] = ix->slot_off[b] + ns;
+    }
+    free(la0); free(la1); free(lo0); free(lo1); free(cnt);
+}
+
+/* gen_yb_dis over the neighbour blocks of block b (letkf_yb.F90:71-133). */
+static int local_point_dec(const orc_config *cfg, const orc_obs *obs, const obs_index *ix, int b,
+                           double clat, double clon, int32_t *idx, double *rloc)
+{
+    double s2 = sin(lat_rad(clat)), c2 = cos(lat_rad(clat)), y2r = lat_rad(clon);
+    int nobsl = 0, sl;
+    for (sl = ix->slot_off[b]; sl < ix->slot_off[b + 1]; sl++) {
+        const int32_t blk = ix->slot_blk[sl];
+        int64_t m;
+        for (m = ix->blk_off[blk]; m < ix->blk_off[blk + 1]; m++) {
+            const int32_t o = ix->blk_obs[m];
+            double dist, gc;
+            if (!(fabs(obs->lat[o]) <= cfg->obs_polar)) continue;
+            dist = dist_pre(ix->s[o], ix->c[o], ix->yr[o], s2, c2, y2r);
+            gc = cfg->gc_filter ? orc_schr2(dist * 1.0 / cfg->local_dist)
+                                : orc_schr(dist * 1.0 / cfg->local_dist);
+            if (gc > 0 || gc != gc) {
+                if (idx) idx[nobsl] = o;
+                if (rloc) rloc[nobsl] = gc;
+                nobsl++;
+                if (nobsl >= cfg->max_obs) return nobsl;
+            }
+        }
+    }
+    return nobsl;
+}
+
+/* Local list of the cube (sj..ej, si..ei) in either obs-set mode. */
+static int cube_list(const orc_config *cfg, const orc_obs *obs, const obs_index *ix,
+                     int sj, int ej, int si, int ei, int32_t *idx, double *rloc, int32_t *buf)
+{
+    double clat, clon;
+    orc_cube_center(cfg, sj, ej, si, ei, &clat, &clon);
+    if (ix->nbx > 0)
+        return local_point_dec(cfg, obs, ix, ix->bx_of_row[sj] * ix->nby + ix->by_of_col[si], clat,
+                               clon, idx, rloc);
+    return local_point(cfg, obs, ix, clat, clon, idx, rloc, buf);
+}
+
 int orc_local_obs_point(const orc_config *cfg, const orc_obs *obs, double clat, double clon,
                         int32_t *idx, double *rloc)
 {
     obs_index ix;
     int32_t *buf;
     int n;
-    obs_index_build(obs, &ix);
+    obs_index_build(cfg, obs, &ix);
     buf = (int32_t *)malloc(sizeof(int32_t) * (obs->nobs + 1));
     n = local_point(cfg, obs, &ix, clat, clon, idx, rloc, buf);
     free(buf);
@@ -448,17 +714,15 @@ int64_t orc_local_obs(const orc_config *cfg, const orc_obs *obs,
 {
     int64_t nc = orc_num_cubes(cfg), c, total;
     obs_index ix;
-    obs_index_build(obs, &ix);
+    obs_index_build(cfg, obs, &ix);
 #pragma omp parallel
     {
         int32_t *buf = (int32_t *)malloc(sizeof(int32_t) * (obs->nobs + 1));
 #pragma omp for schedule(dynamic, 16)
         for (c = 0; c < nc; c++) {
             int sj, ej, si, ei;
-            double clat, clon;
             orc_cube_bounds(cfg, c, &sj, &ej, &si, &ei);
-            orc_cube_center(cfg, sj, ej, si, ei, &clat, &clon);
-            offsets[c + 1] = local_point(cfg, obs, &ix, clat, clon, NULL, NULL, buf);
+            offsets[c + 1] = cube_list(cfg, obs, &ix, sj, ej, si, ei, NULL, NULL, buf);
         }
         free(buf);
     }
@@ -476,11 +740,9 @@ int64_t orc_local_obs(const orc_config *cfg, const orc_obs *obs,
 #pragma omp for schedule(dynamic, 16)
             for (c = 0; c < nc; c++) {
                 int sj, ej, si, ei;
-                double clat, clon;
                 orc_cube_bounds(cfg, c, &sj, &ej, &si, &ei);
-                orc_cube_center(cfg, sj, ej, si, ei, &clat, &clon);
-                local_point(cfg, obs, &ix, clat, clon, idx + offsets[c],
-                            rloc ? rloc + offsets[c] : NULL, buf);
+                cube_list(cfg, obs, &ix, sj, ej, si, ei, idx + offsets[c],
+                          rloc ? rloc + offsets[c] : NULL, buf);
             }
             free(buf);
         }
@@ -683,10 +945,8 @@ static void cube_core(const orc_config *cfg, const orc_obs *obs, const obs_index
                       double *dis, double *trans, double *w, int *fail)
 {
     int sj, ej, si, ei, p;
-    double clat, clon;
     orc_cube_bounds(cfg, cube, &sj, &ej, &si, &ei);
-    orc_cube_center(cfg, sj, ej, si, ei, &clat, &clon);
-    p = local_point(cfg, obs, ix, clat, clon, idx, rl, cbuf);
+    p = cube_list(cfg, obs, ix, sj, ej, si, ei, idx, rl, cbuf);
     gather_local(cfg->k, p, idx, yb, dep, obs, hx, rdi, dis);
     if (orc_letkf_core(cfg->k, p, hx, rdi, dis, rl, cfg->inflation, trans, w) != 0) *fail = 1;
 }
@@ -699,7 +959,7 @@ int orc_letkf_cubes(const orc_config *cfg, const orc_obs *obs, const double *yb,
     int64_t t;
     int fail = 0;
     obs_index ix;
-    obs_index_build(obs, &ix);
+    obs_index_build(cfg, obs, &ix);
 #pragma omp parallel reduction(| : fail)
     {
         int mo = cfg->max_obs;
@@ -742,7 +1002,7 @@ static int run_vertical(const orc_config *cfg, const orc_obs *obs, const double 
     int64_t nc = orc_num_cubes(cfg), cube, c;
     int fail = 0;
     obs_index ix;
-    obs_index_build(obs, &ix);
+    obs_index_build(cfg, obs, &ix);
 #pragma omp parallel reduction(| : fail)
     {
         int mo = cfg->max_obs;
@@ -760,10 +1020,9 @@ static int run_vertical(const orc_config *cfg, const orc_obs *obs, const double 
 #pragma omp for schedule(dynamic, 4)
         for (cube = 0; cube < nc; cube++) {
             int sj, ej, si, ei, p, o, kk, v, ii, jj;
-            double clat, clon, ps;
+            double ps;
             orc_cube_bounds(cfg, cube, &sj, &ej, &si, &ei);
-            orc_cube_center(cfg, sj, ej, si, ei, &clat, &clon);
-            p = local_point(cfg, obs, &ix, clat, clon, idx, rlh, cbuf);
+            p = cube_list(cfg, obs, &ix, sj, ej, si, ei, idx, rlh, cbuf);
             gather_local(k, p, idx, yb, dep, obs, hx, rdi, dis);
             for (o = 0; o < p; o++) lnp[o] = log(obs->ph[idx[o]]);
             {
@@ -850,7 +1109,7 @@ static int run_overlap(const orc_config *cfg, const orc_obs *obs, const double *
     obs_index ix;
     if (step <= 0) return -2;
     count = (double *)calloc((size_t)ncol, sizeof(double));
-    obs_index_build(obs, &ix);
+    obs_index_build(cfg, obs, &ix);
     memset(xa, 0, sizeof(double) * ncol * n * k);
     memset(axa, 0, sizeof(double) * ncol * n);
     for (i = 0; i < cfg->nlon; i += step) {
@@ -908,6 +1167,7 @@ int orc_letkf_run(const orc_config *cfg, const orc_obs *obs,
     double *yb = (double *)malloc(sizeof(double) * (obs->nobs * (int64_t)cfg->k + 1));
     double *dep = (double *)malloc(sizeof(double) * (obs->nobs + 1));
     rc = orc_obs_operator(cfg, xb, axb, obs, yb, dep);
+    if (rc == 0 && cfg->dec_lat_blocks > 0 && (cfg->cube_n != 1 || cfg->overlap != 0)) rc = -2;
     if (rc == 0) {
         if (cfg->overlap != 0)
             rc = run_overlap(cfg, obs, yb, dep, xb, axb, xa, axa);

@@ -52,6 +52,13 @@ typedef struct orc_config {
     int max_obs;                /* MAX_OBS                                             */
     int cube_n, cube_nz, overlap;
     int h_mode;                 /* 0: hybrid log-p vertical interpolation, 1: level select */
+    /* Observation-set mode.  0, 0: one logical block that holds every obs once
+     * (mode "global").  Otherwise the analysis emulates a DA run decomposed
+     * into dec_lat_blocks x dec_lon_blocks MPI blocks (mode "decomposed"):
+     * each block holds the obs inside its lat/lon box, and a column scans the
+     * blocks of its neighbour set in the reference's order.  Needs cube_n 1
+     * and overlap 0.                                                        */
+    int dec_lat_blocks, dec_lon_blocks;
 } orc_config;
 
 typedef struct orc_obs {
@@ -75,6 +82,15 @@ int orc_find_obs_grid(const orc_config *cfg, double lat, double lon,
  * Writes yb[obs][k] (perturbations) and dep[obs] = yo - mean(H xb).  */
 int orc_obs_operator(const orc_config *cfg, const double *xb, const double *axb,
                      const orc_obs *obs, double *yb, double *dep);
+
+/* MPI_Dims_create(nranks, 2) as the DA group decomposes the globe: the most
+ * balanced factor pair, larger first; dims(1) splits longitude and dims(2)
+ * latitude.  Returns 0, or -1 for nranks < 1.                               */
+int orc_decomp_dims(int nranks, int *lat_blocks, int *lon_blocks);
+
+/* Neighbour set of lat/lon block (bx, by) (0-based) in scan order: writes up
+ * to cap block ids (bx' * lon_blocks + by') and returns how many there are.  */
+int orc_block_slots(const orc_config *cfg, int bx, int by, int32_t *blocks, int cap);
 
 /* Cubes of the column loop (no overlap), ordered lon-block-major. */
 int64_t orc_num_cubes(const orc_config *cfg);

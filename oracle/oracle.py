@@ -34,7 +34,7 @@ class OrcConfig(C.Structure):
         ("local_dist", C.c_double), ("vert_dist", C.c_double), ("inflation", C.c_double),
         ("obs_polar", C.c_double), ("gc_filter", C.c_int), ("gc_filter_vertical", C.c_int),
         ("max_obs", C.c_int), ("cube_n", C.c_int), ("cube_nz", C.c_int), ("overlap", C.c_int),
-        ("h_mode", C.c_int),
+        ("h_mode", C.c_int), ("dec_lat_blocks", C.c_int), ("dec_lon_blocks", C.c_int),
     ]
 
 
@@ -77,7 +77,7 @@ class Oracle:
     """Oracle bound to one workload (see synthetic.Workload) and its parameters."""
 
     def __init__(self, w, *, vert_dist=-999.0, cube_n=1, cube_nz=1, overlap=0,
-                 gc_filter_vertical=1):
+                 gc_filter_vertical=1, decomp=(0, 0)):
         self.w = w
         self._keep = []
         k = lambda a, dt: self._hold(np.ascontiguousarray(a, dtype=dt))
@@ -93,7 +93,7 @@ class Oracle:
             vert_dist=vert_dist, inflation=w.inflation, obs_polar=w.obs_polar,
             gc_filter=w.gc_filter, gc_filter_vertical=gc_filter_vertical,
             max_obs=w.max_obs, cube_n=cube_n, cube_nz=cube_nz, overlap=overlap,
-            h_mode=w.h_mode)
+            h_mode=w.h_mode, dec_lat_blocks=decomp[0], dec_lon_blocks=decomp[1])
         o = w.obs
         self.olat = k(o["lat"], np.float64)
         self.olon = k(o["lon"], np.float64)
@@ -205,6 +205,22 @@ def letkf_core(hxens, rdiaginv, dep, rloc, inflation):
     if rc != 0:
         raise RuntimeError("oracle letkf_core: eigensolver did not converge")
     return np.asarray(trans), w
+
+
+def decomp_dims(nranks: int):
+    """(lat_blocks, lon_blocks) of an nranks-way DA decomposition."""
+    a, b = C.c_int(), C.c_int()
+    if lib().orc_decomp_dims(nranks, C.byref(a), C.byref(b)) != 0:
+        raise ValueError("nranks must be >= 1")
+    return a.value, b.value
+
+
+def block_slots(orc: "Oracle", bx: int, by: int):
+    """Neighbour blocks (ids bx' * lon_blocks + by') that block (bx, by) scans."""
+    cap = 4 * max(1, orc.cfg.dec_lat_blocks * orc.cfg.dec_lon_blocks) + 4
+    buf = np.empty(cap, dtype=np.int32)
+    n = lib().orc_block_slots(C.byref(orc.cfg), bx, by, _p(buf, C.c_int32), cap)
+    return buf[:n].copy()
 
 
 def num_threads() -> int:

@@ -87,3 +87,13 @@ def test_missing_library_fails_loudly(tmp_path):
             letkf.load_library(str(tmp_path / "nope.so"))
     finally:
         letkf._lib = saved
+
+
+def test_decomp_dims_matches_oracle_without_gpu():
+    letkf = pkg("letkf")
+    letkf.load_library()
+    from oracle import oracle as O
+    for p in range(1, 200):
+        assert letkf.decomp_dims(p) == O.decomp_dims(p), p
+    with pytest.raises(letkf.LetkfError):
+        letkf.decomp_dims(0)
