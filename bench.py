@@ -154,15 +154,16 @@ def fp64_peak_tflops(torch, dev):
 
 def mixed_pipe_bounds(w, sum_p, peaks_tflops, hbm_gbs):
     """Per-pipe lower bounds (ms) of the mixed core on the algorithmic work:
-    the two dense products on the tensor cores (2k^2 p and 2k^2 n per column;
-    the hi/lo split's extra products are implementation cost), the 13k^3
-    eigensolve and transform work on the FP32 pipe, g (2k p) on the FP64 pipe,
-    and the state and observation bytes on HBM."""
+    the products with the observations and the state on the tensor cores
+    (2k^2 p + 2k p for A and g, 2k^2 n for the update, per column; the hi/lo
+    split's extra products are implementation cost), the 13k^3 eigensolve and
+    transform work on the FP32 pipe, the FP64 work by design (wbar and the
+    mean increment), and the state and observation bytes on HBM."""
     k, n, ncol = w.k, w.n, w.ncol
     flops, nbytes = algorithmic_work(w, sum_p)
-    work = {"tensor": 2.0 * k * k * sum_p + 2.0 * k * k * n * ncol,
+    work = {"tensor": 2.0 * k * k * sum_p + 2.0 * k * sum_p + 2.0 * k * k * n * ncol,
             "fp32": 13.0 * k ** 3 * ncol,
-            "fp64": 2.0 * k * sum_p,
+            "fp64": mixed_fp64_flops(w, sum_p),
             "hbm": nbytes}
     ms = {"tensor": work["tensor"] / (peaks_tflops["bf16"] * 1e12) * 1e3,
           "fp32": work["fp32"] / (peaks_tflops["fp32"] * 1e12) * 1e3,
@@ -321,14 +322,12 @@ def _field_errors(w, xa, axa, xa_ref, axa_ref):
 
 
 def mixed_fp64_flops(w, sum_p):
-    """FP64 work the mixed form does by design per analysis: g (k p), the
-    FP64 copy of A' (k^2), wbar with one refinement step (five k x k
-    matrix-vector products: 5k^2) and the mean increment xb^T wbar (n k)
-    multiply-adds.  The eigensolve, T and the two large products are FP32 or
-    tensor-core work."""
+    """FP64 multiply-adds the mixed core does by design per analysis, times 2:
+    the FP64 copy of A' (k^2), wbar with one refinement step (five k x k
+    matrix-vector products) and the mean increment xb^T wbar (n k).  A, g,
+    the eigensolve, T and the update are tensor-core or FP32 work."""
     k, n, ncol = w.k, w.n, w.ncol
-    fma = k * sum_p + ncol * (k * k + 5 * k * k + n * k)
-    return 2.0 * fma
+    return 2.0 * ncol * (k * k + 5 * k * k + n * k)
 
 
 def run_ours(args, rank, world, local_rank):
@@ -449,9 +448,9 @@ def run_ours(args, rank, world, local_rank):
         roof = {"bound": pipe, "kernel": f"k_core_mixed<{w.k}>",
                 "achieved": achieved, "peak": peak, "unit": unit, "frac": achieved / peak,
                 "traffic": traffic, "kernel_ms": core,
-                "work": "algorithmic work per pipe: tensor 2k^2(p+n), FP32 13k^3, FP64 2kp "
-                        "(g), HBM state + obs bytes; the bound is the pipe with the largest "
-                        "work/peak time",
+                "work": "algorithmic work per pipe: tensor 2k^2(p+n) + 2kp, FP32 13k^3, FP64 "
+                        "wbar and xb^T wbar, HBM state + obs bytes; the bound is the pipe with "
+                        "the largest work/peak time",
                 "pipe_bound_ms": bound_ms, "pipe_work": work,
                 "peaks_tflops": {"bf16": pk["bf16"], "fp32_measured_sgemm": fp32_peak,
                                  "fp64_measured_dgemm": fp64_peak},

@@ -171,16 +171,15 @@ __device__ int lg_jacobi(T *W, T *nrm, typename LgVec2<T>::type *rot, int *s_rot
     return sweep;
 }
 
-// FP32 one-sided Jacobi for the mixed-precision form.  Pairs whose cosine
-// exceeds tol are rotated; the sweeps stop after one in which no cosine
-// exceeded tol_continue: cyclic Jacobi converges quadratically, so a sweep
-// whose largest cosine is below sqrt(tol) leaves the columns orthogonal to
-// about tol, and the extra sweep that would only confirm it is skipped.  Same round-robin
+// FP32 one-sided Jacobi for the mixed-precision form.  Same round-robin
 // scheme as lg_jacobi, but each lane of a pair group owns a contiguous run of
 // K/G rows, keeps the pair's rows in registers between the inner product and
 // the rotation, and moves them with vector shared-memory accesses; every lane
 // computes the rotation (FP32, cheap) so a step needs one barrier.  LD (the
 // column stride) must keep the rows of a lane aligned for the vector width.
+// Pairs whose cosine exceeds tol are rotated; the sweeps stop after one in
+// which no cosine exceeded tol_continue (>= tol; tol itself is the usual
+// choice, a larger value skips the last, confirming sweep).
 template <int K, int G, int LD>
 __device__ int lg_jacobi32(float *W, float *nrm, int *s_rot, float tol, float tol_continue, int max_sweeps)
 {

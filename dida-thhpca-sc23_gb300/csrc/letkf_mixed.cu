@@ -31,12 +31,6 @@
 #include "letkf_jacobi.cuh"
 #include "letkf_umma.cuh"
 
-// Largest column cosine after which the FP32 Jacobi runs another sweep
-// (tolerance 2e-6, quadratic convergence: sqrt(2e-6) ~ 1.4e-3).
-#ifndef LG_JACOBI32_CONTINUE
-#define LG_JACOBI32_CONTINUE 2e-6f
-#endif
-
 namespace {
 
 constexpr int kT = 256;
@@ -388,7 +382,7 @@ k_core_mixed(LgGrid g, LgParams prm, const double *__restrict__ yb, const float 
 
         LG_PHASE(1);
         // ---------------- phase 3: FP32 Jacobi -> Xhat (columns of W32) ----------------
-        const int sw = lg_jacobi32<K, C::G, C::LDW>(W32, nrm32, &s_rot, 2e-6f, LG_JACOBI32_CONTINUE, 24);
+        const int sw = lg_jacobi32<K, C::G, C::LDW>(W32, nrm32, &s_rot, 2e-6f, 2e-6f, 24);
         if (tid == 0) {
             atomicMax(&counters[LG_CNT_MAXSWEEP], (unsigned long long)sw);
             atomicAdd(&counters[LG_CNT_SUMSWEEP], (unsigned long long)sw);
