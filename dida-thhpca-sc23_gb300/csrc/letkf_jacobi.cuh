@@ -185,18 +185,23 @@ __device__ int lg_jacobi32(float *W, float *nrm, int *s_rot, float tol, float to
 {
     constexpr int NP = K / 2, RPL = K / G;
     constexpr int VW = (RPL % 4 == 0) ? 4 : ((RPL % 2 == 0) ? 2 : 1);
+    constexpr int NC = RPL / VW;                 // vector chunks per lane
     static_assert(K % G == 0, "rows per lane");
     static_assert(LD % VW == 0, "vector alignment of columns");
     const int tid = threadIdx.x;
     const int pair = tid / G, lane = tid % G;
+    const int warp = tid >> 5, wl = tid & 31;
     const bool act = pair < NP;
     const float tol2 = tol * tol, cont2 = tol_continue * tol_continue;
     int sweep;
     for (sweep = 1; sweep <= max_sweeps; sweep++) {
-        if (tid < K) {
+        // squared column norms, one warp per column
+        for (int j = warp; j < K; j += (int)(blockDim.x >> 5)) {
             float s = 0.0f;
-            for (int r = 0; r < K; r++) s += W[tid * LD + r] * W[tid * LD + r];
-            nrm[tid] = s;
+            for (int r = wl; r < K; r += 32) s = fmaf(W[j * LD + r], W[j * LD + r], s);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+            if (wl == 0) nrm[j] = s;
         }
         if (tid == 0) *s_rot = 0;
         __syncthreads();
@@ -207,23 +212,26 @@ __device__ int lg_jacobi32(float *W, float *nrm, int *s_rot, float tol, float to
                 const int q = (pair == 0) ? r : qr;
                 if (++pr == K - 1) pr = 0;
                 if (++qr == K - 1) qr = 0;
-                float *wp = W + p * LD + lane * RPL, *wq = W + q * LD + lane * RPL;
+                // lane rows: chunks c*G + lane of VW rows, so the G lanes of a
+                // pair read consecutive vectors (no bank conflicts for VW = 4)
+                float *wp = W + p * LD + lane * VW, *wq = W + q * LD + lane * VW;
                 float a[RPL], b[RPL];
 #pragma unroll
-                for (int i = 0; i < RPL; i += VW) {
+                for (int c = 0; c < NC; c++) {
+                    const int o = c * G * VW, i = c * VW;
                     if (VW == 4) {
-                        const float4 x = *reinterpret_cast<const float4 *>(wp + i);
-                        const float4 y = *reinterpret_cast<const float4 *>(wq + i);
+                        const float4 x = *reinterpret_cast<const float4 *>(wp + o);
+                        const float4 y = *reinterpret_cast<const float4 *>(wq + o);
                         a[i] = x.x; a[i + 1] = x.y; a[i + 2] = x.z; a[i + 3] = x.w;
                         b[i] = y.x; b[i + 1] = y.y; b[i + 2] = y.z; b[i + 3] = y.w;
                     } else if (VW == 2) {
-                        const float2 x = *reinterpret_cast<const float2 *>(wp + i);
-                        const float2 y = *reinterpret_cast<const float2 *>(wq + i);
+                        const float2 x = *reinterpret_cast<const float2 *>(wp + o);
+                        const float2 y = *reinterpret_cast<const float2 *>(wq + o);
                         a[i] = x.x; a[i + 1] = x.y;
                         b[i] = y.x; b[i + 1] = y.y;
                     } else {
-                        a[i] = wp[i];
-                        b[i] = wq[i];
+                        a[i] = wp[o];
+                        b[i] = wq[o];
                     }
                 }
                 float g0 = 0.0f, g1 = 0.0f;
@@ -247,16 +255,17 @@ __device__ int lg_jacobi32(float *W, float *nrm, int *s_rot, float tol, float to
                         b[i] = s * x + c * y;
                     }
 #pragma unroll
-                    for (int i = 0; i < RPL; i += VW) {
+                    for (int cc = 0; cc < NC; cc++) {
+                        const int o = cc * G * VW, i = cc * VW;
                         if (VW == 4) {
-                            *reinterpret_cast<float4 *>(wp + i) = make_float4(a[i], a[i + 1], a[i + 2], a[i + 3]);
-                            *reinterpret_cast<float4 *>(wq + i) = make_float4(b[i], b[i + 1], b[i + 2], b[i + 3]);
+                            *reinterpret_cast<float4 *>(wp + o) = make_float4(a[i], a[i + 1], a[i + 2], a[i + 3]);
+                            *reinterpret_cast<float4 *>(wq + o) = make_float4(b[i], b[i + 1], b[i + 2], b[i + 3]);
                         } else if (VW == 2) {
-                            *reinterpret_cast<float2 *>(wp + i) = make_float2(a[i], a[i + 1]);
-                            *reinterpret_cast<float2 *>(wq + i) = make_float2(b[i], b[i + 1]);
+                            *reinterpret_cast<float2 *>(wp + o) = make_float2(a[i], a[i + 1]);
+                            *reinterpret_cast<float2 *>(wq + o) = make_float2(b[i], b[i + 1]);
                         } else {
-                            wp[i] = a[i];
-                            wq[i] = b[i];
+                            wp[o] = a[i];
+                            wq[o] = b[i];
                         }
                     }
                     if (lane == 0) {
