@@ -148,6 +148,8 @@ int obs_and_search(letkf_ctx *ctx, const double *xb, const double *axb, const le
         const int64_t guess = ctx->ncubes * (int64_t)std::min(ctx->params.max_obs, 512);
         LG_CUDA(ctx->d_lidx.reserve((size_t)std::max<int64_t>(guess, 1)));
         LG_CUDA(ctx->d_lrloc.reserve((size_t)std::max<int64_t>(guess, 1)));
+        if (ctx->params.precision == LETKF_PREC_MIXED)
+            LG_CUDA(ctx->d_lmeta.reserve((size_t)std::max<int64_t>(guess, 1)));
         ctx->list_cap = std::max<int64_t>(guess, 1);
     }
     for (int attempt = 0; attempt < 3; attempt++) {
@@ -170,8 +172,10 @@ int obs_and_search(letkf_ctx *ctx, const double *xb, const double *axb, const le
         const int64_t cap = need + need / 16 + 1024;
         ctx->d_lidx.release();
         ctx->d_lrloc.release();
+        ctx->d_lmeta.release();
         LG_CUDA(ctx->d_lidx.reserve((size_t)cap));
         LG_CUDA(ctx->d_lrloc.reserve((size_t)cap));
+        if (ctx->params.precision == LETKF_PREC_MIXED) LG_CUDA(ctx->d_lmeta.reserve((size_t)cap));
         ctx->list_cap = cap;
         // the search counters start again; status keeps any obs error
         LG_CUDA(cudaMemsetAsync(ctx->d_counters.p, 0, sizeof(unsigned long long) * LG_CNT_N,

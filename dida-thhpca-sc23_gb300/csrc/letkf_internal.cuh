@@ -166,6 +166,10 @@ struct DevBuf {
         p = nullptr;
         n = 0;
     }
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    ~DevBuf() { release(); }
 };
 
 struct letkf_ctx {
@@ -201,6 +205,7 @@ struct letkf_ctx {
     DevBuf<int32_t> d_lcnt;
     DevBuf<int32_t> d_lidx;
     DevBuf<double> d_lrloc;
+    DevBuf<float2> d_lmeta;       // mixed form: (sqrt(rloc), sqrt(rdiaginv rloc) dep) per entry
     int64_t list_cap = 0;
     // decomposed observation sets (letkf_decomp.cu)
     int dec_nx = 0, dec_ny = 0, dec_nchunk = 0;

@@ -68,14 +68,29 @@ struct MCfg {
     static constexpr int LDW = K + 4;                  // padded column stride of the FP32 Jacobi
     static constexpr size_t AREA = 64 * 1024;          // tiles / FP32 scratch / P, R, Xhat
     static constexpr size_t B1 = sizeof(double) * K * K;
-    static constexpr size_t VEC = sizeof(double) * (7 * K + 128 + CH) +
-                                  sizeof(float) * (2 * K + CH) + sizeof(int) * CH;
+    // per-chunk observation index and factors, a ring of 3 chunks
+    static constexpr size_t VEC = sizeof(double) * (7 * K + 128) + sizeof(float) * (2 * K) +
+                                  3 * CH * (sizeof(int) + 2 * sizeof(float));
     static constexpr size_t SMEM = 1024 + AREA + B1 + VEC + 256;
+    // gathered FP32 observation rows of one chunk; two stages: the first in B1
+    // (free while A is built), the second after it in B1 or after the tiles
+    static constexpr size_t STAGE = (size_t)CH * K * sizeof(float);
+    static constexpr bool STAGE1_IN_B1 = 2 * STAGE <= B1;
     static_assert(2 * K <= 128, "stacked hi/lo rows must fit M = 128");
     static_assert(K % 16 == 0, "N must be a multiple of 16");
     static_assert(2 * TILE <= 49152, "A-build tiles must not reach the warm-start vectors");
     static_assert(K + 16 <= (int)TMEM_COLS, "A-build accumulator must fit the TMEM allocation");
+    static_assert(STAGE <= B1 && (STAGE1_IN_B1 || 2 * TILE + STAGE <= 49152), "gather stages must fit");
 };
+
+// 16-byte global -> shared copies that bypass the registers (cp.async, L2 only).
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void *src)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
 
 __device__ __forceinline__ uint32_t pack_bf16(float a, float b)
 {
@@ -117,9 +132,8 @@ __device__ __forceinline__ double block_sum(double v, double *red)
 
 template <int K>
 __global__ void __launch_bounds__(kT, 2)
-k_core_mixed(LgGrid g, LgParams prm, const double *__restrict__ yb, const float *__restrict__ ys32,
-             const double *__restrict__ dep, const float *__restrict__ rinvf,
-             const int32_t *__restrict__ lidx, const double *__restrict__ lrloc,
+k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32_t *__restrict__ lidx,
+             const float2 *__restrict__ lmeta,
              const int64_t *__restrict__ loff, const int32_t *__restrict__ lcnt, int64_t ncubes,
              const double *__restrict__ xb, const double *__restrict__ axb, double *__restrict__ xa,
              double *__restrict__ axa, double *__restrict__ trans_out, double *__restrict__ w_out,
@@ -137,11 +151,13 @@ k_core_mixed(LgGrid g, LgParams prm, const double *__restrict__ yb, const float 
     double *wbar = hco + K;
     double *misc = wbar + K;       // 2K
     double *inc = misc + 2 * K;    // 128
-    double *cd = inc + 128;        // CH
-    float *nrm32 = reinterpret_cast<float *>(cd + CH);             // K
+    float *nrm32 = reinterpret_cast<float *>(inc + 128);           // K
     float2 *rot32 = reinterpret_cast<float2 *>(nrm32 + K);          // K/2
-    float *sq32 = reinterpret_cast<float *>(rot32 + K / 2);         // CH
-    int *gidx = reinterpret_cast<int *>(sq32 + CH);                 // CH
+    int *mg = reinterpret_cast<int *>(rot32 + K / 2);               // 3 x CH obs indices
+    float *msq = reinterpret_cast<float *>(mg + 3 * CH);            // 3 x CH sqrt(rloc)
+    float *me = msq + 3 * CH;                                       // 3 x CH e
+    float *stage0 = reinterpret_cast<float *>(B1);
+    float *stage1 = C::STAGE1_IN_B1 ? stage0 + CH * K : reinterpret_cast<float *>(area + 2 * C::TILE);
     __shared__ uint64_t mbar[3];
     __shared__ uint32_t s_tmem;
     __shared__ int s_rot, s_ok;
@@ -223,52 +239,83 @@ k_core_mixed(LgGrid g, LgParams prm, const double *__restrict__ yb, const float 
                 *reinterpret_cast<uint4 *>(area + b * C::TILE + lg_sw128_offset(r, c)) = make_uint4(0, 0, 0, 0);
             }
         }
-        float *e32 = reinterpret_cast<float *>(cd);
+        // Chunk x's observation rows are gathered by cp.async into stage x & 1,
+        // two chunks ahead of the conversion; its list entries (index and the
+        // factors sqrt(rloc), e) sit in ring slot x % 3 and are read into
+        // registers one more chunk ahead.
         const int nch = (p + CH - 1) / CH;
+        auto load_meta = [&](int x, int &gi, float2 &mf) {      // tid < CH
+            const int o = x * CH + tid;
+            if (x < nch && o < p) {
+                gi = lidx[off + o];
+                mf = lmeta[off + o];
+            } else {
+                gi = -1;
+                mf = make_float2(0.0f, 0.0f);
+            }
+        };
+        auto put_meta = [&](int x, int gi, float2 mf) {
+            const int r = (x % 3) * CH + tid;
+            mg[r] = gi;
+            msq[r] = mf.x;
+            me[r] = mf.y;
+        };
+        auto issue_rows = [&](int x) {       // all threads; ring slot x % 3 is visible
+            float *st = (x & 1) ? stage1 : stage0;
+            const int *gs = mg + (x % 3) * CH;
+            constexpr int PPR = K / 4;        // 16-byte pieces per row
+            for (int q = tid; q < CH * PPR; q += kT) {
+                const int o = q / PPR, part = q % PPR;
+                const int gi = gs[o];
+                if (gi >= 0) cp_async16(lg_smem_u32(st + o * K + part * 4), ys32 + (int64_t)gi * K + part * 4);
+            }
+            cp_async_commit();               // one group per chunk, empty past the end
+        };
+        int pf_g = -1;
+        float2 pf_m = make_float2(0.0f, 0.0f);
+        if (nch > 0) {
+            if (tid < CH) {
+                int g0, g1;
+                float2 m0, m1;
+                load_meta(0, g0, m0);
+                load_meta(1, g1, m1);
+                load_meta(2, pf_g, pf_m);
+                put_meta(0, g0, m0);
+                put_meta(1, g1, m1);
+            }
+            __syncthreads();
+            issue_rows(0);
+            issue_rows(1);
+        }
         for (int ch = 0; ch < nch; ch++) {
             const int b = ch & 1;
+            const float *st = b ? stage1 : stage0;
+            const float *sq = msq + (ch % 3) * CH, *ev = me + (ch % 3) * CH;
+            cp_async_wait<1>();              // this chunk's rows (the next chunk's may be in flight)
+            __syncthreads();
             unsigned char *tile = area + b * C::TILE;
             if (!wait_bar(b)) {
                 failed = true;
                 break;
             }
             const int cnt = min(CH, p - ch * CH);
-            if (tid < CH) {
-                if (tid < cnt) {
-                    const int64_t li = off + (int64_t)ch * CH + tid;
-                    const int gi = lidx[li];
-                    const float rl = (float)lrloc[li];
-                    gidx[tid] = gi;
-                    sq32[tid] = sqrtf(rl);
-                    e32[tid] = sqrtf(rinvf[gi] * rl) * (float)dep[gi];
-                } else {
-                    gidx[tid] = 0;
-                    sq32[tid] = 0.0f;
-                    e32[tid] = 0.0f;
-                }
-            }
-            __syncthreads();
             for (int t = tid; t < K * 8 + 8; t += kT) {
                 float v[8];
-                int rh, rl;
+                uint4 hi, lo;
                 if (t < K * 8) {
                     const int m = t % K, c = t / K;
 #pragma unroll
                     for (int j = 0; j < 8; j++) {
                         const int o = 8 * c + j;
-                        v[j] = (o < cnt) ? ys32[(int64_t)gidx[o] * K + m] * sq32[o] : 0.0f;
+                        v[j] = (o < cnt) ? st[o * K + m] * sq[o] : 0.0f;
                     }
-                    rh = K + m;
-                    rl = m;
-                    uint4 hi, lo;
                     split8(v, hi, lo);
-                    *reinterpret_cast<uint4 *>(tile + lg_sw128_offset(rh, c)) = hi;
-                    *reinterpret_cast<uint4 *>(tile + lg_sw128_offset(rl, c)) = lo;
+                    *reinterpret_cast<uint4 *>(tile + lg_sw128_offset(K + m, c)) = hi;
+                    *reinterpret_cast<uint4 *>(tile + lg_sw128_offset(m, c)) = lo;
                 } else {
                     const int c = t - K * 8;
 #pragma unroll
-                    for (int j = 0; j < 8; j++) v[j] = e32[8 * c + j];
-                    uint4 hi, lo;
+                    for (int j = 0; j < 8; j++) v[j] = ev[8 * c + j];
                     split8(v, hi, lo);
                     *reinterpret_cast<uint4 *>(tile + lg_sw128_offset(2 * K, c)) = hi;
                     *reinterpret_cast<uint4 *>(tile + lg_sw128_offset(2 * K + 1, c)) = lo;
@@ -287,7 +334,15 @@ k_core_mixed(LgGrid g, LgParams prm, const double *__restrict__ yb, const float 
             }
             ncommit[b]++;
             pending[b] = true;
+            // refill this stage with chunk ch + 2 (its rows were read before the barrier)
+            if (tid < CH) {
+                put_meta(ch + 2, pf_g, pf_m);
+                load_meta(ch + 3, pf_g, pf_m);
+            }
+            __syncthreads();
+            issue_rows(ch + 2);
         }
+        cp_async_wait<0>();
         if (failed) break;
         if (!wait_bar(0) || !wait_bar(1)) {
             failed = true;
@@ -617,6 +672,7 @@ k_core_mixed(LgGrid g, LgParams prm, const double *__restrict__ yb, const float 
                ph_cyc[0], ph_cyc[1], ph_cyc[2], ph_cyc[3], ph_cyc[4], ph_cyc[5], ph_cyc[6]);
 #endif
     if (failed && tid == 0) atomicOr(status, LG_ST_TIMEOUT);
+    cp_async_wait<0>();
     // let any MMA still in flight finish before the TMEM is freed
     for (int b = 0; b < 3; b++) wait_bar(b);
     lg_tc_fence_before();
@@ -648,8 +704,8 @@ cudaError_t launch_mixed(letkf_ctx *ctx, const LgGrid &g, const double *xb, cons
     const unsigned blocks = (unsigned)(ctx->ncubes < want ? ctx->ncubes : want);
     lg_count_launch();
     k_core_mixed<K><<<blocks, kT, smem, ctx->stream>>>(
-        g, lg_params(ctx), ctx->d_yb.p, ctx->d_ys32.p, ctx->d_dep.p, ctx->d_rinvf.p, ctx->d_lidx.p,
-        ctx->d_lrloc.p, ctx->d_loff.p, ctx->d_lcnt.p, ctx->ncubes, xb, axb, xa, axa, trans_out, w_out,
+        g, lg_params(ctx), ctx->d_ys32.p, ctx->d_lidx.p, ctx->d_lmeta.p, ctx->d_loff.p, ctx->d_lcnt.p,
+        ctx->ncubes, xb, axb, xa, axa, trans_out, w_out,
         ctx->d_counters.p, ctx->d_status.p);
     return cudaGetLastError();
 }

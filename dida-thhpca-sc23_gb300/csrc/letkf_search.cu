@@ -126,10 +126,18 @@ __device__ void bitonic_sort(int32_t *keys, int n_pow2)
     }
 }
 
+// Observation terms the mixed form's list entries carry.
+struct LgListMeta {
+    const float *rinvf;       // R^-1 narrowed to float
+    const double *dep;        // departures
+    float2 *meta;             // out, mixed form only
+};
+
 // Reserve the cube's slot in the list pool with one atomic add and write its
 // kept obs (keys[0..nout), in list order) with their localization weights.
 __device__ void write_list(const int32_t *keys, int nout, bool truncated, int64_t cube, const CubeGeo &cg,
-                           const LgObsGeo &geo, const LgParams &prm, int32_t *__restrict__ lidx,
+                           const LgObsGeo &geo, const LgParams &prm, const LgListMeta &lm,
+                           int32_t *__restrict__ lidx,
                            double *__restrict__ lrloc, int64_t list_cap, int64_t *__restrict__ loff,
                            int32_t *__restrict__ lcnt, unsigned long long *__restrict__ counters,
                            unsigned *__restrict__ status, long long *s_off)
@@ -160,8 +168,12 @@ __device__ void write_list(const int32_t *keys, int nout, bool truncated, int64_
                 const float dx = q.x - cg.cx, dy = q.y - cg.cy, dz = q.z - cg.cz;
                 const float half = fminf(1.0f, 0.5f * sqrtf(dx * dx + dy * dy + dz * dz));
                 const float ri = 2.0f * asinf(half) * scale;
+                const float rl = prm.gc_filter ? lg_schr2f(ri) : (ri > 2.0f ? 0.0f : 1.0f);
                 lidx[off + i] = o;
-                lrloc[off + i] = prm.gc_filter ? (double)lg_schr2f(ri) : (ri > 2.0f ? 0.0 : 1.0);
+                lrloc[off + i] = (double)rl;
+                // the mixed core's per-entry factors: Yhat = y sqrt(rdiaginv) sqrt(rloc)
+                // and e = sqrt(rdiaginv rloc) dep (g = Yhat e)
+                lm.meta[off + i] = make_float2(sqrtf(rl), sqrtf(lm.rinvf[o] * rl) * (float)lm.dep[o]);
             }
         } else {
             for (int i = threadIdx.x; i < nout; i += kThreads) {
@@ -207,7 +219,7 @@ __device__ CubeGeo cube_geo(const LgGrid &g, const LgParams &prm, int64_t cube, 
 }
 
 __global__ void __launch_bounds__(kThreads)
-k_search(LgGrid g, LgParams prm, LgBuckets bk, LgObsGeo geo, int64_t nobs, int cap_sort,
+k_search(LgGrid g, LgParams prm, LgBuckets bk, LgObsGeo geo, LgListMeta lm, int64_t nobs, int cap_sort,
          int32_t *__restrict__ lidx, double *__restrict__ lrloc, int64_t list_cap,
          int64_t *__restrict__ loff, int32_t *__restrict__ lcnt,
          unsigned long long *__restrict__ counters, unsigned *__restrict__ status, int64_t ncubes)
@@ -291,7 +303,7 @@ k_search(LgGrid g, LgParams prm, LgBuckets bk, LgObsGeo geo, int64_t nobs, int c
             bitonic_sort(keys, np2);
             nout = min(c, prm.max_obs);
         }
-        write_list(keys, nout, nk > prm.max_obs, cube, cg, geo, prm, lidx, lrloc, list_cap, loff, lcnt,
+        write_list(keys, nout, nk > prm.max_obs, cube, cg, geo, prm, lm, lidx, lrloc, list_cap, loff, lcnt,
                    counters, status, &s_off);
         __syncthreads();
     }
@@ -306,7 +318,8 @@ k_search(LgGrid g, LgParams prm, LgBuckets bk, LgObsGeo geo, int64_t nobs, int c
 // totals); candidates whose float chord is near the antipode's take the
 // double test, where the reference keeps NaN distances.
 __global__ void __launch_bounds__(kThreads)
-k_search_dec(LgGrid g, LgParams prm, LgObsGeo geo, const double *__restrict__ olat, int NY, int nchunk,
+k_search_dec(LgGrid g, LgParams prm, LgObsGeo geo, LgListMeta lm, const double *__restrict__ olat, int NY,
+             int nchunk,
              const int *__restrict__ row_blk, const int *__restrict__ col_blk,
              const int *__restrict__ slot_off, const int *__restrict__ slot_blk,
              const int *__restrict__ blk_pos, const int *__restrict__ blk_obs, int32_t *__restrict__ lidx,
@@ -364,7 +377,7 @@ k_search_dec(LgGrid g, LgParams prm, LgObsGeo geo, const double *__restrict__ ol
                 __syncthreads();
             }
         }
-        write_list(keys, min(n, max_obs), n >= max_obs, cube, cg, geo, prm, lidx, lrloc, list_cap, loff,
+        write_list(keys, min(n, max_obs), n >= max_obs, cube, cg, geo, prm, lm, lidx, lrloc, list_cap, loff,
                    lcnt, counters, status, &s_off);
         __syncthreads();
     }
@@ -398,7 +411,7 @@ cudaError_t lg_launch_search(letkf_ctx *ctx, const LgGrid &g, int64_t nobs)
     const int64_t blocks = ctx->ncubes < (1 << 30) ? ctx->ncubes : (1 << 30);
     lg_count_launch();
     k_search<<<(unsigned)(blocks > 0 ? blocks : 1), kThreads, smem, ctx->stream>>>(
-        g, prm, bk, geo, nobs, cap, ctx->d_lidx.p, ctx->d_lrloc.p, ctx->list_cap, ctx->d_loff.p,
+        g, prm, bk, geo, LgListMeta{ctx->d_rinvf.p, ctx->d_dep.p, ctx->d_lmeta.p}, nobs, cap, ctx->d_lidx.p, ctx->d_lrloc.p, ctx->list_cap, ctx->d_loff.p,
         ctx->d_lcnt.p, ctx->d_counters.p, ctx->d_status.p, ctx->ncubes);
     return cudaGetLastError();
 }
@@ -414,7 +427,7 @@ cudaError_t lg_launch_search_dec(letkf_ctx *ctx, const LgGrid &g, const double *
     const int64_t blocks = ctx->ncubes < (1 << 30) ? ctx->ncubes : (1 << 30);
     lg_count_launch();
     k_search_dec<<<(unsigned)(blocks > 0 ? blocks : 1), kThreads, smem, ctx->stream>>>(
-        g, prm, geo, olat, ctx->dec_ny, ctx->dec_nchunk, ctx->d_dec_row_blk.p, ctx->d_dec_col_blk.p,
+        g, prm, geo, LgListMeta{ctx->d_rinvf.p, ctx->d_dep.p, ctx->d_lmeta.p}, olat, ctx->dec_ny, ctx->dec_nchunk, ctx->d_dec_row_blk.p, ctx->d_dec_col_blk.p,
         ctx->d_dec_slot_off.p, ctx->d_dec_slot_blk.p, ctx->d_dec_pos.p, ctx->d_dec_obs.p, ctx->d_lidx.p,
         ctx->d_lrloc.p, ctx->list_cap, ctx->d_loff.p, ctx->d_lcnt.p, ctx->d_counters.p, ctx->d_status.p,
         ctx->ncubes);
