@@ -69,7 +69,7 @@ struct MCfg {
     static constexpr size_t AREA = 64 * 1024;          // tiles / FP32 scratch / P, R, Xhat
     static constexpr size_t B1 = sizeof(double) * K * K;
     // per-chunk observation index and factors, a ring of 3 chunks
-    static constexpr size_t VEC = sizeof(double) * (7 * K + 128) + sizeof(float) * (2 * K) +
+    static constexpr size_t VEC = sizeof(double) * (4 * K + 128) + sizeof(float) * (2 * K) +
                                   3 * CH * (sizeof(int) + 2 * sizeof(float));
     static constexpr size_t SMEM = 1024 + AREA + B1 + VEC + 256;
     // gathered FP32 observation rows of one chunk; two stages: the first in B1
@@ -145,10 +145,7 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
     unsigned char *area = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     double *B1 = reinterpret_cast<double *>(area + C::AREA);
     double *gv = B1 + K * K;
-    double *lam = gv + K;
-    double *fco = lam + K;
-    double *hco = fco + K;
-    double *wbar = hco + K;
+    double *wbar = gv + K;
     double *misc = wbar + K;       // 2K
     double *inc = misc + 2 * K;    // 128
     float *nrm32 = reinterpret_cast<float *>(inc + 128);           // K
@@ -443,21 +440,28 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
             atomicAdd(&counters[LG_CNT_SUMSWEEP], (unsigned long long)sw);
             if (sw > 24) atomicAdd(&counters[LG_CNT_NOTCONV], 1ull);
         }
-        // lambda_j = |w_j| (A' is SPD, so the converged columns are lambda_j x_j)
-        if (tid < K) {
+        // lambda_j = |w_j| (A' is SPD, so the converged columns are lambda_j x_j),
+        // one warp per column
+        float *ilam32 = reinterpret_cast<float *>(misc);     // 1/lambda (misc: 2K doubles = 4K floats)
+        float *hc32 = ilam32 + K, *w32 = hc32 + K, *r32 = w32 + K;
+        for (int j = warp; j < K; j += kT / 32) {
             float s = 0.0f;
-            for (int r = 0; r < K; r++) s = fmaf(W32[tid * C::LDW + r], W32[tid * C::LDW + r], s);
-            nrm32[tid] = 1.0f / sqrtf(s);
-            lam[tid] = sqrt((double)s);
-            fco[tid] = sqrt((double)(K - 1) / lam[tid]);
+            for (int r = lane; r < K; r += 32) s = fmaf(W32[j * C::LDW + r], W32[j * C::LDW + r], s);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+            if (lane == 0) {
+                const float lamf = sqrtf(s);
+                nrm32[j] = 1.0f / lamf;
+                ilam32[j] = 1.0f / lamf;
+                hc32[j] = sqrtf((float)(K - 1) / lamf);   // f_j = sqrt((k-1)/lambda_j)
+            }
         }
         __syncthreads();
         LG_PHASE(2);
-        // ---------------- phase 4: X, wbar with one FP64 refinement step ------------------
-        // X by columns in FP32 (T, warm start) and FP64 (wbar).  W32 shares this
-        // memory, so the values pass through registers first.
+        // ---------------- phase 4: X, wbar with one refinement step ------------------------
+        // X by columns in FP32 (T, wbar, warm start).  W32 shares this memory, so
+        // the values pass through registers first.
         float *X32 = reinterpret_cast<float *>(area);            // X32[j*K + r] = x_j[r]
-        double *Xd = reinterpret_cast<double *>(area + 16384);   // the same in FP64
         {
             constexpr int PER = (K * K + kT - 1) / kT;
             float xv[PER];
@@ -470,39 +474,44 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
 #pragma unroll
             for (int q = 0; q < PER; q++) {
                 const int idx = tid + q * kT;
-                if (idx < K * K) {
-                    X32[idx] = xv[q];
-                    Xd[idx] = (double)xv[q];
-                }
+                if (idx < K * K) X32[idx] = xv[q];
             }
-            if (tid < K) nrm32[tid] = (float)fco[tid];       // f = sqrt((k-1)/lambda) for T
+            if (tid < K) {
+                nrm32[tid] = hc32[tid];                    // f for T
+                r32[tid] = (float)gv[tid];                 // right-hand side of the first solve
+            }
         }
         __syncthreads();
-        // wbar = X diag(1/lambda) X^T g, then wbar += X diag(1/lambda) X^T (g - A' wbar):
-        // the residual against the FP64 A' removes the FP32 eigenpairs' error from wbar
+        // wbar = X diag(1/lambda) X^T g in FP32, then one refinement step:
+        // wbar += X diag(1/lambda) X^T (g - A' wbar) with the residual in FP64
+        // against the FP64 A' (in B1).  The FP32 solve has a relative error of
+        // about eps32 kappa; the step leaves the error of the FP32 eigenpairs
+        // times that, far below the FP32 representation of A.
         for (int it = 0; it < 2; it++) {
-            const double *rhs = it == 0 ? gv : misc;
             for (int j = warp; j < K; j += kT / 32) {          // one warp per eigenvector
-                double dot = 0.0;
-                for (int l = lane; l < K; l += 32) dot += Xd[j * K + l] * rhs[l];
+                float d = 0.0f;
+                for (int l = lane; l < K; l += 32) d = fmaf(X32[j * K + l], r32[l], d);
 #pragma unroll
-                for (int o = 16; o > 0; o >>= 1) dot += __shfl_xor_sync(0xffffffffu, dot, o);
-                if (lane == 0) hco[j] = dot / lam[j];
+                for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+                if (lane == 0) hc32[j] = d * ilam32[j];
             }
             __syncthreads();
             if (tid < K) {
-                double s = 0.0;
-                for (int j = 0; j < K; j++) s += Xd[j * K + tid] * hco[j];
-                wbar[tid] = (it == 0 ? 0.0 : wbar[tid]) + s;
+                float a0 = 0.0f, a1 = 0.0f;
+                for (int j = 0; j < K; j += 2) {
+                    a0 = fmaf(X32[j * K + tid], hc32[j], a0);
+                    a1 = fmaf(X32[(j + 1) * K + tid], hc32[j + 1], a1);
+                }
+                wbar[tid] = (it == 0 ? 0.0 : wbar[tid]) + (double)(a0 + a1);
             }
             __syncthreads();
             if (it == 0) {
                 for (int i = warp; i < K; i += kT / 32) {      // one warp per row of A'
-                    double s = 0.0;
-                    for (int l = lane; l < K; l += 32) s += B1[i * K + l] * wbar[l];
+                    double d = 0.0;
+                    for (int l = lane; l < K; l += 32) d += B1[i * K + l] * wbar[l];
 #pragma unroll
-                    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-                    if (lane == 0) misc[i] = gv[i] - s;
+                    for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+                    if (lane == 0) r32[i] = (float)(gv[i] - d);
                 }
                 __syncthreads();
             }
@@ -510,6 +519,20 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
         LG_PHASE(3);
 
         // ---------------- phase 5: T in FP32 ------------------------------------------------
+        // start moving this cube's background state into L2 for the update
+        {
+            const int bjc = (int)(cube % prm.nbj), bic = (int)(cube / prm.nbj);
+            const int sj = bjc * prm.cube_n, ej = min(sj + prm.cube_n - 1, g.nlat - 1);
+            const int si = bic * prm.cube_n, ei = min(si + prm.cube_n - 1, g.nlon - 1);
+            const int64_t lines = ((int64_t)g.n * K * (int64_t)sizeof(double) + 127) / 128;
+            for (int ii = si; ii <= ei; ii++)
+                for (int jj = sj; jj <= ej; jj++) {
+                    const int64_t col = jj + (int64_t)g.nlat * ii;
+                    const char *base = reinterpret_cast<const char *>(xb + col * g.n * K);
+                    for (int64_t l = tid; l < lines; l += kT)
+                        asm volatile("prefetch.global.L2 [%0];" ::"l"(base + l * 128));
+                }
+        }
         // T = X diag(f) X^T only feeds the BF16 hi/lo tensor-core update (16
         // significant bits); FP32 eigenpairs give it to ~1e-7 relative.
         float *T32 = reinterpret_cast<float *>(B1);               // T, FP32, row-major
