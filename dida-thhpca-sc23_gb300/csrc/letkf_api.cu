@@ -100,7 +100,10 @@ int reserve_obs_work(letkf_ctx *ctx, int64_t no)
 {
     const size_t n = (size_t)std::max<int64_t>(no, 1);
     LG_CUDA(ctx->d_yb.reserve(n * ctx->k));
-    if (ctx->params.precision == LETKF_PREC_MIXED) LG_CUDA(ctx->d_ys32.reserve(n * ctx->k));
+    if (ctx->params.precision == LETKF_PREC_MIXED) {
+        LG_CUDA(ctx->d_ys32.reserve(n * ctx->k));
+        LG_CUDA(ctx->d_oef.reserve(n));
+    }
     LG_CUDA(ctx->d_dep.reserve(n));
     LG_CUDA(ctx->d_rinvf.reserve(n));
     LG_CUDA(ctx->d_os.reserve(n));
@@ -332,6 +335,7 @@ int letkf_gpu_create(letkf_ctx **out, const letkf_grid *grid, const letkf_params
         LG_CUDA(h2d(ctx->d_glat, glat.data(), glat.size(), ctx->stream));
         LG_CUDA(h2d(ctx->d_glon, glon.data(), glon.size(), ctx->stream));
         if (decomposed) LG_CUDA(lg_decomp_setup(ctx, glat, glon));
+        LG_CUDA(lg_launch_geo_tables(ctx));
         std::vector<double> zero(G.nz + 1, 0.0);
         LG_CUDA(h2d(ctx->d_hyai, G.hyai ? G.hyai : zero.data(), (size_t)G.nz + 1, ctx->stream));
         LG_CUDA(h2d(ctx->d_hybi, G.hybi ? G.hybi : zero.data(), (size_t)G.nz + 1, ctx->stream));

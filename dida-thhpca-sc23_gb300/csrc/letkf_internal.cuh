@@ -138,6 +138,15 @@ struct LgBuckets {
 };
 
 // Per-obs precomputed search data (original order).
+// Geometry of the cube centres for the search: sin/cos of the grid latitudes,
+// the grid longitudes in radians with their cos/sin, the cut-off angle and the
+// chord^2 band of the float prefilter.
+struct LgSearchGeo {
+    const double *row_s, *row_c;
+    const double *col_yr, *col_cos, *col_sin;
+    float theta, lo2, hi2;
+};
+
 struct LgObsGeo {
     const double *s, *c, *yr;   // sin, cos of latitude, longitude in radians
     const float4 *xyz;          // unit vector (x, y, z) and index bits, obs order
@@ -192,6 +201,8 @@ struct letkf_ctx {
     DevBuf<double> d_yb, d_dep;
     DevBuf<float> d_ys32;         // yb * sqrt(rinv) in FP32 (mixed precision)
     DevBuf<float> d_rinvf;
+    DevBuf<float> d_oef;          // mixed form: sqrt(rdiaginv) dep per obs
+    DevBuf<double> d_row_s, d_row_c, d_col_yr, d_col_cos, d_col_sin;   // search geometry tables
     DevBuf<double> d_os, d_oc, d_oyr;
     DevBuf<float4> d_oxyz;
     DevBuf<int> d_obucket;
@@ -241,6 +252,8 @@ cudaError_t lg_launch_obs_prepare(letkf_ctx *ctx, const LgGrid &g, const double 
                                   const int32_t *ovar, const double *oyo, const double *orinv);
 cudaError_t lg_launch_buckets(letkf_ctx *ctx, int64_t nobs);
 void lg_launch_scan_exclusive(const int *in, int *out, int n, cudaStream_t stream);
+cudaError_t lg_launch_geo_tables(letkf_ctx *ctx);
+LgSearchGeo lg_search_geo(letkf_ctx *ctx);
 cudaError_t lg_launch_search(letkf_ctx *ctx, const LgGrid &g, int64_t nobs);
 // decomposed observation sets (letkf_decomp.cu, letkf_search.cu)
 int lg_decomp_dims(int nranks, int &lat_blocks, int &lon_blocks);

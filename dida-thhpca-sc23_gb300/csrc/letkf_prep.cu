@@ -58,7 +58,7 @@ k_obs_prepare(LgGrid g, LgParams prm, const double *__restrict__ xb, const doubl
               const double *__restrict__ orinv, double *__restrict__ yb, double *__restrict__ dep,
               float *__restrict__ rinvf, double *__restrict__ os, double *__restrict__ oc,
               double *__restrict__ oyr, float4 *__restrict__ oxyz, int *__restrict__ obucket,
-              float *__restrict__ ys32,
+              float *__restrict__ ys32, float *__restrict__ oef,
               int nblat, int nblon, double cell_lat, double cell_lon, unsigned *status)
 {
     const int lane = threadIdx.x & 31;
@@ -86,6 +86,7 @@ k_obs_prepare(LgGrid g, LgParams prm, const double *__restrict__ xb, const doubl
             if (lane == 0) {
                 dep[o] = 0.0;
                 rinvf[o] = 0.0f;
+                if (oef) oef[o] = 0.0f;
                 obucket[o] = -1;
                 atomicOr(status, LG_ST_BAD_OBS);
             }
@@ -170,6 +171,8 @@ k_obs_prepare(LgGrid g, LgParams prm, const double *__restrict__ xb, const doubl
         if (lane == 0) {
             dep[o] = oyo[o] - mean;
             rinvf[o] = (float)orinv[o];
+            // the mixed form's departure factor: e = sqrt(rloc) sqrt(rdiaginv) dep
+            if (oef) oef[o] = sqrtf(rinvf[o]) * (float)dep[o];
             const double xr = lg_rad(lat), yr = lg_rad(lon);
             const double s = sin(xr), c = cos(xr);
             os[o] = s;
@@ -261,8 +264,66 @@ cudaError_t lg_launch_obs_prepare(letkf_ctx *ctx, const LgGrid &g, const double 
         g, prm, xb, axb, nobs, olat, olon, oph, olev, ovar, oyo, orinv, ctx->d_yb.p, ctx->d_dep.p,
         ctx->d_rinvf.p, ctx->d_os.p, ctx->d_oc.p, ctx->d_oyr.p, ctx->d_oxyz.p, ctx->d_obucket.p,
         ctx->params.precision == LETKF_PREC_MIXED ? ctx->d_ys32.p : nullptr,
+        ctx->params.precision == LETKF_PREC_MIXED ? ctx->d_oef.p : nullptr,
         ctx->nblat, ctx->nblon, ctx->cell_lat, ctx->cell_lon, ctx->d_status.p);
     return cudaGetLastError();
+}
+
+// Per-row and per-column geometry of the cube centres, with the same device
+// functions as the per-obs terms (the exact distance test uses both).
+__global__ void k_geo_tables(const float *__restrict__ glat, const float *__restrict__ glon, int nlat, int nlon,
+                             double *__restrict__ row_s, double *__restrict__ row_c, double *__restrict__ col_yr,
+                             double *__restrict__ col_cos, double *__restrict__ col_sin)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nlat + nlon; i += gridDim.x * blockDim.x) {
+        if (i < nlat) {
+            const double xr = lg_rad((double)glat[i]);
+            row_s[i] = sin(xr);
+            row_c[i] = cos(xr);
+        } else {
+            const int j = i - nlat;
+            const double yr = lg_rad((double)glon[j]);
+            col_yr[j] = yr;
+            col_cos[j] = cos(yr);
+            col_sin[j] = sin(yr);
+        }
+    }
+}
+
+cudaError_t lg_launch_geo_tables(letkf_ctx *ctx)
+{
+    cudaError_t e;
+    if ((e = ctx->d_row_s.reserve(ctx->nlat)) || (e = ctx->d_row_c.reserve(ctx->nlat)) ||
+        (e = ctx->d_col_yr.reserve(ctx->nlon)) || (e = ctx->d_col_cos.reserve(ctx->nlon)) ||
+        (e = ctx->d_col_sin.reserve(ctx->nlon)))
+        return e;
+    lg_count_launch();
+    k_geo_tables<<<grid_for(ctx->nlat + ctx->nlon, 256, 1024), 256, 0, ctx->stream>>>(
+        ctx->d_glat.p, ctx->d_glon.p, ctx->nlat, ctx->nlon, ctx->d_row_s.p, ctx->d_row_c.p, ctx->d_col_yr.p,
+        ctx->d_col_cos.p, ctx->d_col_sin.p);
+    return cudaGetLastError();
+}
+
+LgSearchGeo lg_search_geo(letkf_ctx *ctx)
+{
+    LgSearchGeo sg;
+    sg.row_s = ctx->d_row_s.p;
+    sg.row_c = ctx->d_row_c.p;
+    sg.col_yr = ctx->d_col_yr.p;
+    sg.col_cos = ctx->d_col_cos.p;
+    sg.col_sin = ctx->d_col_sin.p;
+    const double theta = 2.0 * ctx->params.loc_dist_km / LG_EARTH_A;
+    sg.theta = (float)theta;
+    if (theta > 0.01) {
+        const double a = 2.0 * std::sin(0.5 * theta * (1.0 - 1e-3));
+        const double b = 2.0 * std::sin(0.5 * theta * (1.0 + 1e-3));
+        sg.lo2 = (float)(a * a);
+        sg.hi2 = (float)(b * b);
+    } else {
+        sg.lo2 = -1.0f;           // every candidate takes the double test
+        sg.hi2 = 1.0e30f;
+    }
+    return sg;
 }
 
 void lg_launch_scan_exclusive(const int *in, int *out, int n, cudaStream_t stream)

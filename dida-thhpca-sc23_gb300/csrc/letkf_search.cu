@@ -24,6 +24,7 @@ namespace {
 
 constexpr int kMaxSeg = 128;
 constexpr int kThreads = 256;
+constexpr size_t kBitmapMaxBytes = 96 * 1024;   // obs-index bitmap of k_search_bitmap (786,432 obs)
 
 struct Seg {
     int b, e, exact;   // [b, e) in bucket order; exact: skip the float prefilter
@@ -36,11 +37,12 @@ struct CubeGeo {
 };
 
 __device__ __forceinline__ void add_lon_range(Seg *seg, int &ns, const LgBuckets &bk, int band,
-                                              double lon0, double lon1, int exact)
+                                              float lon0, float lon1, int exact)
 {
     const int nbl = bk.nblon;
     const int base = band * nbl;
-    int j0 = (int)floor(lon0 / bk.cell_lon), j1 = (int)floor(lon1 / bk.cell_lon);
+    const float cl = (float)bk.cell_lon;
+    int j0 = (int)floorf(lon0 / cl), j1 = (int)floorf(lon1 / cl);
     if (j1 - j0 + 1 >= nbl) {
         if (ns < kMaxSeg) seg[ns++] = {bk.start[base], bk.start[base + nbl], exact};
         return;
@@ -128,10 +130,58 @@ __device__ void bitonic_sort(int32_t *keys, int n_pow2)
 
 // Observation terms the mixed form's list entries carry.
 struct LgListMeta {
-    const float *rinvf;       // R^-1 narrowed to float
-    const double *dep;        // departures
+    const float *ef;          // sqrt(rdiaginv) dep per obs (mixed form)
     float2 *meta;             // out, mixed form only
 };
+
+// One list entry: the obs index and its localization weight (the reference's
+// double formula; FP32 from the unit-vector chord for the mixed form, which
+// also stores its per-entry factors).
+__device__ __forceinline__ void write_entry(int o, long long at, const CubeGeo &cg, const LgObsGeo &geo,
+                                            const LgParams &prm, const LgListMeta &lm,
+                                            int32_t *__restrict__ lidx, double *__restrict__ lrloc)
+{
+    if (prm.precision == LETKF_PREC_MIXED) {
+        // the selection used the reference's double formula where it mattered
+        const float scale = (float)(LG_EARTH_A / prm.local_dist);
+        const float4 q = geo.xyz[o];
+        const float dx = q.x - cg.cx, dy = q.y - cg.cy, dz = q.z - cg.cz;
+        const float half = fminf(1.0f, 0.5f * sqrtf(dx * dx + dy * dy + dz * dz));
+        const float ri = 2.0f * asinf(half) * scale;
+        const float rl = prm.gc_filter ? lg_schr2f(ri) : (ri > 2.0f ? 0.0f : 1.0f);
+        lidx[at] = o;
+        lrloc[at] = (double)rl;
+        // the mixed core's per-entry factors: Yhat = y sqrt(rdiaginv) sqrt(rloc)
+        // and e = sqrt(rdiaginv rloc) dep (g = Yhat e)
+        const float sr = sqrtf(rl);
+        lm.meta[at] = make_float2(sr, sr * lm.ef[o]);
+    } else {
+        const double dist = lg_dist(geo.s[o], geo.c[o], geo.yr[o], cg.s2, cg.c2, cg.y2r);
+        const double ri = lg_ri(dist, prm.local_dist);
+        lidx[at] = o;
+        lrloc[at] = prm.gc_filter ? lg_schr2(ri) : lg_schr(ri);
+    }
+}
+
+// Reserve the cube's slot in the list pool with one atomic add (thread 0;
+// the caller synchronizes before reading *s_off).
+__device__ __forceinline__ void reserve_list(int nout, bool truncated, int64_t cube, int64_t list_cap,
+                                             int64_t *__restrict__ loff, int32_t *__restrict__ lcnt,
+                                             unsigned long long *__restrict__ counters,
+                                             unsigned *__restrict__ status, long long *s_off)
+{
+    long long off = (long long)atomicAdd(&counters[LG_CNT_CURSOR], (unsigned long long)nout);
+    if (off + nout > list_cap) {
+        atomicOr(status, LG_ST_LIST_FULL);
+        off = -1;
+    }
+    *s_off = off;
+    loff[cube] = off < 0 ? 0 : off;
+    lcnt[cube] = off < 0 ? 0 : nout;
+    atomicAdd(&counters[LG_CNT_SUMP], (unsigned long long)nout);
+    atomicMax(&counters[LG_CNT_MAXP], (unsigned long long)nout);
+    if (truncated) atomicAdd(&counters[LG_CNT_TRUNC], 1ull);
+}
 
 // Reserve the cube's slot in the list pool with one atomic add and write its
 // kept obs (keys[0..nout), in list order) with their localization weights.
@@ -142,84 +192,79 @@ __device__ void write_list(const int32_t *keys, int nout, bool truncated, int64_
                            int32_t *__restrict__ lcnt, unsigned long long *__restrict__ counters,
                            unsigned *__restrict__ status, long long *s_off)
 {
-    if (threadIdx.x == 0) {
-        long long off = (long long)atomicAdd(&counters[LG_CNT_CURSOR], (unsigned long long)nout);
-        if (off + nout > list_cap) {
-            atomicOr(status, LG_ST_LIST_FULL);
-            off = -1;
-        }
-        *s_off = off;
-        loff[cube] = off < 0 ? 0 : off;
-        lcnt[cube] = off < 0 ? 0 : nout;
-        atomicAdd(&counters[LG_CNT_SUMP], (unsigned long long)nout);
-        atomicMax(&counters[LG_CNT_MAXP], (unsigned long long)nout);
-        if (truncated) atomicAdd(&counters[LG_CNT_TRUNC], 1ull);
-    }
+    if (threadIdx.x == 0) reserve_list(nout, truncated, cube, list_cap, loff, lcnt, counters, status, s_off);
     __syncthreads();
     const long long off = *s_off;
-    if (off >= 0) {
-        if (prm.precision == LETKF_PREC_MIXED) {
-            // FP32 weights from the chord of the unit vectors (the selection
-            // used the reference's double formula where it mattered)
-            const float scale = (float)(LG_EARTH_A / prm.local_dist);
-            for (int i = threadIdx.x; i < nout; i += kThreads) {
-                const int o = keys[i];
-                const float4 q = geo.xyz[o];
-                const float dx = q.x - cg.cx, dy = q.y - cg.cy, dz = q.z - cg.cz;
-                const float half = fminf(1.0f, 0.5f * sqrtf(dx * dx + dy * dy + dz * dz));
-                const float ri = 2.0f * asinf(half) * scale;
-                const float rl = prm.gc_filter ? lg_schr2f(ri) : (ri > 2.0f ? 0.0f : 1.0f);
-                lidx[off + i] = o;
-                lrloc[off + i] = (double)rl;
-                // the mixed core's per-entry factors: Yhat = y sqrt(rdiaginv) sqrt(rloc)
-                // and e = sqrt(rdiaginv rloc) dep (g = Yhat e)
-                lm.meta[off + i] = make_float2(sqrtf(rl), sqrtf(lm.rinvf[o] * rl) * (float)lm.dep[o]);
-            }
-        } else {
-            for (int i = threadIdx.x; i < nout; i += kThreads) {
-                const int o = keys[i];
-                const double dist = lg_dist(geo.s[o], geo.c[o], geo.yr[o], cg.s2, cg.c2, cg.y2r);
-                const double ri = lg_ri(dist, prm.local_dist);
-                lidx[off + i] = o;
-                lrloc[off + i] = prm.gc_filter ? lg_schr2(ri) : lg_schr(ri);
-            }
-        }
-    }
+    if (off >= 0)
+        for (int i = threadIdx.x; i < nout; i += kThreads) write_entry(keys[i], off + i, cg, geo, prm, lm, lidx, lrloc);
 }
 
 // Centre geometry of cube (as k_search's): unit vector, sin/cos, the chord
 // thresholds of the float prefilter.
-__device__ CubeGeo cube_geo(const LgGrid &g, const LgParams &prm, int64_t cube, double &clat, double &clon)
+__device__ CubeGeo cube_geo(const LgGrid &g, const LgParams &prm, const LgSearchGeo &sg, int64_t cube,
+                            float &clat, float &clon)
 {
     const int bj = (int)(cube % prm.nbj), bi = (int)(cube / prm.nbj);
     const int sj = bj * prm.cube_n, ej = min(sj + prm.cube_n - 1, g.nlat - 1);
     const int si = bi * prm.cube_n, ei = min(si + prm.cube_n - 1, g.nlon - 1);
     const int cj = ((sj + 1) + (ej + 1)) / 2 - 1, ci = ((si + 1) + (ei + 1)) / 2 - 1;
-    clat = (double)g.glat[cj];
-    clon = (double)g.glon[ci];
+    clat = g.glat[cj];
+    clon = g.glon[ci];
     CubeGeo cg;
-    const double xr = lg_rad(clat);
-    cg.s2 = sin(xr);
-    cg.c2 = cos(xr);
-    cg.y2r = lg_rad(clon);
-    cg.cx = (float)(cg.c2 * cos(cg.y2r));
-    cg.cy = (float)(cg.c2 * sin(cg.y2r));
+    cg.s2 = sg.row_s[cj];
+    cg.c2 = sg.row_c[cj];
+    cg.y2r = sg.col_yr[ci];
+    cg.cx = (float)(cg.c2 * sg.col_cos[ci]);
+    cg.cy = (float)(cg.c2 * sg.col_sin[ci]);
     cg.cz = (float)cg.s2;
-    const double theta = 2.0 * prm.local_dist / LG_EARTH_A;
-    if (theta > 0.01) {
-        const double a = 2.0 * sin(0.5 * theta * (1.0 - 1e-3));
-        const double b = 2.0 * sin(0.5 * theta * (1.0 + 1e-3));
-        cg.lo2 = (float)(a * a);
-        cg.hi2 = (float)(b * b);
-    } else {
-        cg.lo2 = -1.0f;           // every candidate takes the double test
-        cg.hi2 = 1.0e30f;
-    }
+    cg.lo2 = sg.lo2;
+    cg.hi2 = sg.hi2;
     return cg;
 }
 
+// Bucket segments of the cap of radius 2c around (clat, clon), plus the
+// buckets within 1e-6 rad of the antipode (exact test there).  FP32 with
+// margins of 1e-4 degrees (and the full circle of longitudes whenever the cap
+// comes within 1e-4 rad of a pole): the segments are a superset of the cap.
+__device__ int cap_segments(Seg *seg, const LgBuckets &bk, float clat, float clon, float theta)
+{
+    int ns = 0;
+    const float deg = 57.295779513f, cla = (float)bk.cell_lat;
+    const float band = (theta + 1e-6f) * deg + 1e-4f;
+    const int b0 = max(0, (int)floorf((clat - band + 90.0f) / cla));
+    const int b1 = min(bk.nblat - 1, (int)floorf((clat + band + 90.0f) / cla));
+    const float clat_r = clat / deg;
+    bool full = true;
+    float dlon = 360.0f;
+    if (fabsf(clat_r) + theta < 1.5707963f - 1e-4f) {
+        const float sv = sinf(theta) / cosf(clat_r);
+        if (sv < 1.0f - 1e-4f) {
+            full = false;
+            dlon = (asinf(sv) + 1e-6f) * deg + 1e-4f;
+        }
+    }
+    for (int b = b0; b <= b1; b++) {
+        if (full) add_lon_range(seg, ns, bk, b, 0.0f, 720.0f, 0);
+        else add_lon_range(seg, ns, bk, b, clon - dlon, clon + dlon, 0);
+    }
+    // buckets within 1e-6 rad of the antipode
+    {
+        const float alat = -clat, alon = fmodf(clon + 180.0f, 360.0f);
+        const float ad = 1e-6f * deg + 1e-4f;
+        const int a0 = max(0, (int)floorf((alat - ad + 90.0f) / cla));
+        const int a1 = min(bk.nblat - 1, (int)floorf((alat + ad + 90.0f) / cla));
+        const float ca = cosf(alat / deg);
+        for (int b = a0; b <= a1; b++) {
+            if (ca < 1e-3f) add_lon_range(seg, ns, bk, b, 0.0f, 720.0f, 1);
+            else add_lon_range(seg, ns, bk, b, alon - ad / ca, alon + ad / ca, 1);
+        }
+    }
+    return ns;
+}
+
 __global__ void __launch_bounds__(kThreads)
-k_search(LgGrid g, LgParams prm, LgBuckets bk, LgObsGeo geo, LgListMeta lm, int64_t nobs, int cap_sort,
+k_search(LgGrid g, LgParams prm, LgSearchGeo sgeo, LgBuckets bk, LgObsGeo geo, LgListMeta lm, int64_t nobs,
+         int cap_sort,
          int32_t *__restrict__ lidx, double *__restrict__ lrloc, int64_t list_cap,
          int64_t *__restrict__ loff, int32_t *__restrict__ lcnt,
          unsigned long long *__restrict__ counters, unsigned *__restrict__ status, int64_t ncubes)
@@ -232,42 +277,10 @@ k_search(LgGrid g, LgParams prm, LgBuckets bk, LgObsGeo geo, LgListMeta lm, int6
 
     for (int64_t cube = blockIdx.x; cube < ncubes; cube += gridDim.x) {
         if (threadIdx.x == 0) {
-            double clat, clon;
-            const CubeGeo cg = cube_geo(g, prm, cube, clat, clon);
-            const double theta = 2.0 * prm.local_dist / LG_EARTH_A;
+            float clat, clon;
+            const CubeGeo cg = cube_geo(g, prm, sgeo, cube, clat, clon);
             s_cg = cg;
-            // buckets of the cap
-            int ns = 0;
-            const double deg = 180.0 / M_PI;
-            const double band = (theta + 1e-6) * deg;
-            const int b0 = max(0, (int)floor((clat - band + 90.0) / bk.cell_lat));
-            const int b1 = min(bk.nblat - 1, (int)floor((clat + band + 90.0) / bk.cell_lat));
-            const double clat_r = clat / deg;
-            bool full = true;
-            double dlon = 360.0;
-            if (fabs(clat_r) + theta + 1e-6 < M_PI / 2 - 1e-6) {
-                const double sv = sin(theta) / cos(clat_r);
-                if (sv < 1.0) {
-                    full = false;
-                    dlon = (asin(sv) + 1e-6) * deg + 1e-9;
-                }
-            }
-            for (int b = b0; b <= b1; b++) {
-                if (full) add_lon_range(seg, ns, bk, b, 0.0, 720.0, 0);
-                else add_lon_range(seg, ns, bk, b, clon - dlon, clon + dlon, 0);
-            }
-            // buckets within 1e-6 rad of the antipode
-            {
-                const double alat = -clat, alon = fmod(clon + 180.0, 360.0);
-                const double ad = 1e-6 * deg + 1e-9;
-                const int a0 = max(0, (int)floor((alat - ad + 90.0) / bk.cell_lat));
-                const int a1 = min(bk.nblat - 1, (int)floor((alat + ad + 90.0) / bk.cell_lat));
-                const double ca = cos(alat / deg);
-                for (int b = a0; b <= a1; b++) {
-                    if (ca < 1e-3) add_lon_range(seg, ns, bk, b, 0.0, 720.0, 1);
-                    else add_lon_range(seg, ns, bk, b, alon - ad / ca, alon + ad / ca, 1);
-                }
-            }
+            int ns = cap_segments(seg, bk, clat, clon, sgeo.theta);
             if (ns >= kMaxSeg) atomicOr(status, LG_ST_SEGMENTS);
             s_ns = ns;
         }
@@ -309,6 +322,90 @@ k_search(LgGrid g, LgParams prm, LgBuckets bk, LgObsGeo geo, LgListMeta lm, int6
     }
 }
 
+// The search with the kept set held as a bitmap over observation indices
+// (when nobs/8 bytes fit in shared memory): each kept candidate sets its bit,
+// and one ordered pass over the bitmap yields the list in canonical (index)
+// order, so no sort is needed and no list length is limited by shared memory.
+__global__ void __launch_bounds__(kThreads)
+k_search_bitmap(LgGrid g, LgParams prm, LgSearchGeo sgeo, LgBuckets bk, LgObsGeo geo, LgListMeta lm,
+                int64_t nobs,
+                int32_t *__restrict__ lidx, double *__restrict__ lrloc, int64_t list_cap,
+                int64_t *__restrict__ loff, int32_t *__restrict__ lcnt,
+                unsigned long long *__restrict__ counters, unsigned *__restrict__ status, int64_t ncubes)
+{
+    extern __shared__ uint32_t bits[];
+    __shared__ Seg seg[kMaxSeg];
+    __shared__ int s_ns;
+    __shared__ CubeGeo s_cg;
+    __shared__ long long s_off;
+    __shared__ int s_warp[kThreads / 32];
+    const int nw = (int)((nobs + 31) / 32);
+    const int per = (nw + kThreads - 1) / kThreads;
+    const int w0 = min(nw, (int)threadIdx.x * per), w1 = min(nw, w0 + per);
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+    for (int64_t cube = blockIdx.x; cube < ncubes; cube += gridDim.x) {
+        for (int w = threadIdx.x; w < nw; w += kThreads) bits[w] = 0u;
+        if (threadIdx.x == 0) {
+            float clat, clon;
+            const CubeGeo cg = cube_geo(g, prm, sgeo, cube, clat, clon);
+            s_cg = cg;
+            const int ns = cap_segments(seg, bk, clat, clon, sgeo.theta);
+            if (ns >= kMaxSeg) atomicOr(status, LG_ST_SEGMENTS);
+            s_ns = ns;
+        }
+        __syncthreads();
+        const int ns = s_ns;
+        const CubeGeo cg = s_cg;
+        for (int si = 0; si < ns; si++) {
+            const Seg sg = seg[si];
+            for (int i = sg.b + threadIdx.x; i < sg.e; i += kThreads) {
+                const float4 p = bk.xyz[i];
+                if (keep_candidate(p, sg.exact, cg, geo, prm, &counters[LG_CNT_BORDER])) {
+                    const int o = __float_as_int(p.w);
+                    atomicOr(&bits[o >> 5], 1u << (o & 31));
+                }
+            }
+        }
+        __syncthreads();
+        // exclusive prefix of the kept counts of each thread's word range
+        int cnt = 0;
+        for (int w = w0; w < w1; w++) cnt += __popc(bits[w]);
+        int incl = cnt;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        if (lane == 31) s_warp[warp] = incl;
+        __syncthreads();
+        int before = incl - cnt, total = 0;
+#pragma unroll
+        for (int w = 0; w < kThreads / 32; w++) {
+            before += (w < warp) ? s_warp[w] : 0;
+            total += s_warp[w];
+        }
+        const int nout = min(total, prm.max_obs);
+        if (threadIdx.x == 0)
+            reserve_list(nout, total > prm.max_obs, cube, list_cap, loff, lcnt, counters, status, &s_off);
+        __syncthreads();
+        const long long off = s_off;
+        if (off >= 0) {
+            int pos = before;
+            for (int w = w0; w < w1 && pos < nout; w++) {
+                uint32_t m = bits[w];
+                while (m && pos < nout) {
+                    const int b = __ffs(m) - 1;
+                    m &= m - 1u;
+                    write_entry(w * 32 + b, off + pos, cg, geo, prm, lm, lidx, lrloc);
+                    pos++;
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
 // Decomposed observation sets: the cube's list is the scan of gen_yb_dis
 // (letkf_yb.F90:71-133) over the obs of its block's neighbour blocks, block
 // by block in the neighbour order and by index within a block, kept iff
@@ -318,7 +415,8 @@ k_search(LgGrid g, LgParams prm, LgBuckets bk, LgObsGeo geo, LgListMeta lm, int6
 // totals); candidates whose float chord is near the antipode's take the
 // double test, where the reference keeps NaN distances.
 __global__ void __launch_bounds__(kThreads)
-k_search_dec(LgGrid g, LgParams prm, LgObsGeo geo, LgListMeta lm, const double *__restrict__ olat, int NY,
+k_search_dec(LgGrid g, LgParams prm, LgSearchGeo sgeo, LgObsGeo geo, LgListMeta lm,
+             const double *__restrict__ olat, int NY,
              int nchunk,
              const int *__restrict__ row_blk, const int *__restrict__ col_blk,
              const int *__restrict__ slot_off, const int *__restrict__ slot_blk,
@@ -337,8 +435,8 @@ k_search_dec(LgGrid g, LgParams prm, LgObsGeo geo, LgListMeta lm, const double *
 
     for (int64_t cube = blockIdx.x; cube < ncubes; cube += gridDim.x) {
         if (threadIdx.x == 0) {
-            double clat, clon;
-            s_cg = cube_geo(g, prm, cube, clat, clon);
+            float clat, clon;
+            s_cg = cube_geo(g, prm, sgeo, cube, clat, clon);
             const int sj = (int)(cube % prm.nbj), si = (int)(cube / prm.nbj);   // cube_n is 1
             s_blk = row_blk[sj] * NY + col_blk[si];
         }
@@ -404,14 +502,26 @@ cudaError_t lg_launch_search(letkf_ctx *ctx, const LgGrid &g, int64_t nobs)
     bk.idx = ctx->d_bidx.p;
     bk.xyz = ctx->d_bxyz.p;
     LgObsGeo geo{ctx->d_os.p, ctx->d_oc.p, ctx->d_oyr.p, ctx->d_oxyz.p};
+    const int64_t blocks = ctx->ncubes < (1 << 30) ? ctx->ncubes : (1 << 30);
+    const size_t bitmap_bytes = sizeof(uint32_t) * (size_t)((nobs + 31) / 32 > 0 ? (nobs + 31) / 32 : 1);
+    if (bitmap_bytes <= kBitmapMaxBytes) {
+        cudaError_t e = cudaFuncSetAttribute(k_search_bitmap, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)bitmap_bytes);
+        if (e != cudaSuccess) return e;
+        lg_count_launch();
+        k_search_bitmap<<<(unsigned)(blocks > 0 ? blocks : 1), kThreads, bitmap_bytes, ctx->stream>>>(
+            g, prm, lg_search_geo(ctx), bk, geo, LgListMeta{ctx->d_oef.p, ctx->d_lmeta.p}, nobs, ctx->d_lidx.p,
+            ctx->d_lrloc.p, ctx->list_cap, ctx->d_loff.p, ctx->d_lcnt.p, ctx->d_counters.p, ctx->d_status.p,
+            ctx->ncubes);
+        return cudaGetLastError();
+    }
     const int cap = lg_search_cap(prm.max_obs);
     const size_t smem = sizeof(int32_t) * cap;
     cudaError_t e = cudaFuncSetAttribute(k_search, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    const int64_t blocks = ctx->ncubes < (1 << 30) ? ctx->ncubes : (1 << 30);
     lg_count_launch();
     k_search<<<(unsigned)(blocks > 0 ? blocks : 1), kThreads, smem, ctx->stream>>>(
-        g, prm, bk, geo, LgListMeta{ctx->d_rinvf.p, ctx->d_dep.p, ctx->d_lmeta.p}, nobs, cap, ctx->d_lidx.p, ctx->d_lrloc.p, ctx->list_cap, ctx->d_loff.p,
+        g, prm, lg_search_geo(ctx), bk, geo, LgListMeta{ctx->d_oef.p, ctx->d_lmeta.p}, nobs, cap, ctx->d_lidx.p, ctx->d_lrloc.p, ctx->list_cap, ctx->d_loff.p,
         ctx->d_lcnt.p, ctx->d_counters.p, ctx->d_status.p, ctx->ncubes);
     return cudaGetLastError();
 }
@@ -427,7 +537,7 @@ cudaError_t lg_launch_search_dec(letkf_ctx *ctx, const LgGrid &g, const double *
     const int64_t blocks = ctx->ncubes < (1 << 30) ? ctx->ncubes : (1 << 30);
     lg_count_launch();
     k_search_dec<<<(unsigned)(blocks > 0 ? blocks : 1), kThreads, smem, ctx->stream>>>(
-        g, prm, geo, LgListMeta{ctx->d_rinvf.p, ctx->d_dep.p, ctx->d_lmeta.p}, olat, ctx->dec_ny, ctx->dec_nchunk, ctx->d_dec_row_blk.p, ctx->d_dec_col_blk.p,
+        g, prm, lg_search_geo(ctx), geo, LgListMeta{ctx->d_oef.p, ctx->d_lmeta.p}, olat, ctx->dec_ny, ctx->dec_nchunk, ctx->d_dec_row_blk.p, ctx->d_dec_col_blk.p,
         ctx->d_dec_slot_off.p, ctx->d_dec_slot_blk.p, ctx->d_dec_pos.p, ctx->d_dec_obs.p, ctx->d_lidx.p,
         ctx->d_lrloc.p, ctx->list_cap, ctx->d_loff.p, ctx->d_lcnt.p, ctx->d_counters.p, ctx->d_status.p,
         ctx->ncubes);

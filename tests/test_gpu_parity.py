@@ -211,6 +211,23 @@ def test_overflow_selection_beyond_shared_memory(letkf, synthetic):
     assert_fields(xa, xa_o, w)
 
 
+@pytest.mark.parametrize("loc_km", [300.0, 1500.0])
+def test_search_without_the_bitmap(letkf, synthetic, loc_km):
+    # more than 786,432 obs: the search keeps its candidates in a sorted key
+    # buffer instead of an index bitmap; at 1500 km more obs are kept than that
+    # buffer holds (threshold-search path)
+    w = synthetic.generate("manyobs", 7.5, 1, 4, 800_000, loc_km, 1.1, 9, lmax_noise=4)
+    ctx = letkf.LetkfGPU.from_workload(w)
+    xa, axa = ctx.run(w.xb, w.axb, w.obs)
+    orc = O.Oracle(w)
+    compare_lists(ctx, orc)
+    if loc_km > 1000.0:
+        assert ctx.stats()["n_truncated"] > 0
+    else:
+        xa_o, axa_o = orc.run()
+        assert_fields(xa, xa_o, w)
+
+
 def test_bad_observation_is_rejected(letkf, synthetic):
     w = synthetic.small_case(nlat=8, nlon=16, nz=2, k=8, nobs=50, seed=3)
     w.obs["lat"] = w.obs["lat"].copy()
