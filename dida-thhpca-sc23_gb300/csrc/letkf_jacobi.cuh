@@ -283,3 +283,136 @@ __device__ int lg_jacobi32(float *W, float *nrm, int *s_rot, float tol, float to
     }
     return sweep;
 }
+
+// FP32 one-sided Jacobi with a hierarchical parallel ordering (K a power of
+// two): the K columns are split into halves; for K/2 steps the K/2 slots each
+// hold one column of the first half fixed in registers and rotate it against
+// the second half's columns, which move one slot per step, so every step
+// moves one column per slot through shared memory instead of two.  Then each
+// half is split again (two sub-problems of K/2 columns side by side), and so on
+// down to pairs: K/2 + K/4 + ... + 1 = K-1 steps cover every pair once per
+// sweep, as the round-robin ordering does.  Columns are stored back into W
+// (column j at W[j*LD ..]) after every level.  The moving columns pass through
+// buffers that reuse W's memory while the columns live in registers.
+// Returns the sweeps used, or max_sweeps+1 if not converged.
+template <int K, int G, int LD>
+__device__ int lg_jacobi32h(float *W, int *s_rot, float tol, int max_sweeps)
+{
+    constexpr int NS = K / 2, RPL = K / G;
+    constexpr int VW = (RPL % 4 == 0) ? 4 : ((RPL % 2 == 0) ? 2 : 1);
+    constexpr int NC = RPL / VW;
+    static_assert((K & (K - 1)) == 0, "K must be a power of two");
+    static_assert(K % G == 0 && LD % VW == 0, "rows per lane");
+    static_assert(2 * NS * K + 2 * NS + 2 * NS <= K * LD, "moving-column buffers must fit in W");
+    const int tid = threadIdx.x;
+    const int slot = tid / G, lane = tid % G;
+    const bool act = slot < NS;
+    const float tol2 = tol * tol;
+    float *buf = W;                                   // [2][NS][K] moving rows
+    float *bnrm = W + 2 * NS * K;                      // [2][NS] their squared norms
+    int *bid = reinterpret_cast<int *>(bnrm + 2 * NS);  // [2][NS] their column ids
+    float F[RPL], M[RPL];
+
+    auto ld = [&](const float *src, float *r) {
+#pragma unroll
+        for (int c = 0; c < NC; c++) {
+            const int o = (c * G + lane) * VW, i = c * VW;
+            if (VW == 4) {
+                const float4 x = *reinterpret_cast<const float4 *>(src + o);
+                r[i] = x.x; r[i + 1] = x.y; r[i + 2] = x.z; r[i + 3] = x.w;
+            } else if (VW == 2) {
+                const float2 x = *reinterpret_cast<const float2 *>(src + o);
+                r[i] = x.x; r[i + 1] = x.y;
+            } else {
+                r[i] = src[o];
+            }
+        }
+    };
+    auto st = [&](float *dst, const float *r) {
+#pragma unroll
+        for (int c = 0; c < NC; c++) {
+            const int o = (c * G + lane) * VW, i = c * VW;
+            if (VW == 4) *reinterpret_cast<float4 *>(dst + o) = make_float4(r[i], r[i + 1], r[i + 2], r[i + 3]);
+            else if (VW == 2) *reinterpret_cast<float2 *>(dst + o) = make_float2(r[i], r[i + 1]);
+            else dst[o] = r[i];
+        }
+    };
+    auto dot = [&](const float *x, const float *y) {
+        float d0 = 0.0f, d1 = 0.0f;
+#pragma unroll
+        for (int i = 0; i < RPL; i += 2) {
+            d0 = fmaf(x[i], y[i], d0);
+            if (i + 1 < RPL) d1 = fmaf(x[i + 1], y[i + 1], d1);
+        }
+        float d = d0 + d1;
+#pragma unroll
+        for (int o = G / 2; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
+        return d;
+    };
+
+    int sweep;
+    for (sweep = 1; sweep <= max_sweeps; sweep++) {
+        if (tid == 0) *s_rot = 0;
+        for (int B = K; B >= 2; B >>= 1) {
+            const int half = B / 2, u = slot / half, i = slot % half;
+            const int fc = u * B + i;
+            int mc = u * B + half + i;
+            __syncthreads();                           // W holds every column
+            if (act) {
+                ld(W + fc * LD, F);
+                ld(W + mc * LD, M);
+            }
+            float fa = 0.0f, mb = 0.0f;
+            if (act) {
+                fa = dot(F, F);
+                mb = dot(M, M);
+            }
+            __syncthreads();                           // W becomes the moving-column buffers
+            for (int t = 0; t < half; t++) {
+                if (act) {
+                    const float gam = dot(F, M);
+                    if (gam * gam > tol2 * (fa * mb)) {
+                        float c, s, tt;
+                        lg_rotation(fa, mb, gam, c, s, tt);
+#pragma unroll
+                        for (int r = 0; r < RPL; r++) {
+                            const float x = F[r], y = M[r];
+                            F[r] = c * x - s * y;
+                            M[r] = s * x + c * y;
+                        }
+                        fa = fa - tt * gam;
+                        mb = mb + tt * gam;
+                        if (lane == 0) *s_rot = 1;
+                    }
+                }
+                if (t == half - 1) break;
+                // pass the moving column to the previous slot of the group
+                const int par = t & 1;
+                if (act) {
+                    st(buf + (par * NS + slot) * K, M);
+                    if (lane == 0) {
+                        bnrm[par * NS + slot] = mb;
+                        bid[par * NS + slot] = mc;
+                    }
+                }
+                __syncthreads();
+                if (act) {
+                    const int src = u * half + (i + 1) % half;
+                    ld(buf + (par * NS + src) * K, M);
+                    mb = bnrm[par * NS + src];
+                    mc = bid[par * NS + src];
+                }
+            }
+            __syncthreads();                           // every read of the buffers is done
+            if (act) {
+                st(W + fc * LD, F);
+                st(W + mc * LD, M);
+            }
+        }
+        __syncthreads();
+        const int rotated = *s_rot;
+        __syncthreads();
+        if (!rotated) break;
+    }
+    return sweep;
+}

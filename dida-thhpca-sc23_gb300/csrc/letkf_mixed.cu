@@ -31,6 +31,13 @@
 #include "letkf_jacobi.cuh"
 #include "letkf_umma.cuh"
 
+// Column-cosine tolerance of the FP32 Jacobi.  It bounds the eigenvectors'
+// orthogonality error, which reaches T (BF16 hi/lo in the update, ~1e-5
+// relative) scaled by about one half.
+#ifndef LG_MIXED_JACOBI_TOL
+#define LG_MIXED_JACOBI_TOL 2e-6f
+#endif
+
 namespace {
 
 constexpr int kT = 256;
@@ -434,7 +441,9 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
 
         LG_PHASE(1);
         // ---------------- phase 3: FP32 Jacobi -> Xhat (columns of W32) ----------------
-        const int sw = lg_jacobi32<K, C::G, C::LDW>(W32, nrm32, &s_rot, 2e-6f, 2e-6f, 24);
+        int sw;
+        if constexpr ((K & (K - 1)) == 0) sw = lg_jacobi32h<K, C::G, C::LDW>(W32, &s_rot, LG_MIXED_JACOBI_TOL, 24);
+        else sw = lg_jacobi32<K, C::G, C::LDW>(W32, nrm32, &s_rot, LG_MIXED_JACOBI_TOL, LG_MIXED_JACOBI_TOL, 24);
         if (tid == 0) {
             atomicMax(&counters[LG_CNT_MAXSWEEP], (unsigned long long)sw);
             atomicAdd(&counters[LG_CNT_SUMSWEEP], (unsigned long long)sw);
