@@ -430,9 +430,11 @@ def run_ours(args, rank, world, local_rank):
     fp64_peak = fp64_peak_tflops(torch, dev)
     flops, nbytes = algorithmic_work(w, st["sum_p"])
     core = statistics.mean(res[head][1])
+    # DRAM bytes per full launch of the dominant kernel, from the committed ncu
+    # summary of a 2-degree capture scaled by the column count
     traffic = None
-    tfile = os.path.join(REPO, "profiles", "core_fp64_cfg1_2deg.md")
-    if head == "fp64" and os.path.exists(tfile):
+    tfile = os.path.join(REPO, "profiles", f"core_{head}_cfg1_2deg.md")
+    if args.config in (1, 2) and args.grid_res in (None, 1.0) and os.path.exists(tfile):
         import re
         m = re.search(r"bytes_per_full_launch:\s*([0-9.eE+]+)", open(tfile).read())
         traffic = float(m.group(1)) if m else None

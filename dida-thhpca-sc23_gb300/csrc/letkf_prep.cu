@@ -312,11 +312,16 @@ LgSearchGeo lg_search_geo(letkf_ctx *ctx)
     sg.col_yr = ctx->d_col_yr.p;
     sg.col_cos = ctx->d_col_cos.p;
     sg.col_sin = ctx->d_col_sin.p;
+    // the squared chord of two unit vectors rounded to float is within ~4e-6
+    // relative of the true one for cut-off angles above 0.05 rad, so
+    // candidates more than 2e-5 relative inside or outside the cut-off are
+    // decided by the float test and only the band between (and every
+    // candidate of a smaller cap) takes the reference's double formula
     const double theta = 2.0 * ctx->params.loc_dist_km / LG_EARTH_A;
     sg.theta = (float)theta;
-    if (theta > 0.01) {
-        const double a = 2.0 * std::sin(0.5 * theta * (1.0 - 1e-3));
-        const double b = 2.0 * std::sin(0.5 * theta * (1.0 + 1e-3));
+    if (theta > 0.05) {
+        const double a = 2.0 * std::sin(0.5 * theta * (1.0 - 2e-5));
+        const double b = 2.0 * std::sin(0.5 * theta * (1.0 + 2e-5));
         sg.lo2 = (float)(a * a);
         sg.hi2 = (float)(b * b);
     } else {

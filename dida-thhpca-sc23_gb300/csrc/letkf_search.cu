@@ -8,14 +8,19 @@
 //      the few buckets at the antipode, where rounding can make acos return
 //      NaN and schr2(NaN) = 1 keeps the obs, as in the reference);
 //   2. a float chord-length test classifies candidates that are clearly
-//      inside or outside (a 1e-3 relative margin around 2c); only candidates
+//      inside or outside (a 2e-5 relative margin around 2c); only candidates
 //      in the margin get the reference's double-precision formula;
-//   3. kept obs indices are sorted in shared memory (bitonic), which restores
-//      canonical order, and cut at max_obs (if more are kept than shared
-//      memory holds, a threshold search finds the max_obs-th smallest index);
+//   3. canonical order: while a bitmap over all obs indices fits shared
+//      memory (k_search_bitmap, up to 786,432 obs), every kept obs sets its
+//      bit and one ordered pass over the bitmap lists them by index; above
+//      that (k_search), kept indices are sorted in shared memory (bitonic),
+//      and if more are kept than shared memory holds, a threshold search
+//      finds the max_obs-th smallest index; lists stop at max_obs;
 //   4. the localization weight of every kept obs is computed with the
-//      reference's double formula and the list is written at a slot reserved
-//      with one atomic add.
+//      reference's double formula (FP32 from the chord for the mixed form)
+//      and the list is written at a slot reserved with one atomic add.
+// The decomposed observation sets (k_search_dec) scan the blocks of the
+// cube's neighbour set instead of the buckets.
 #include <climits>
 
 #include "letkf_internal.cuh"
