@@ -101,7 +101,7 @@ int reserve_obs_work(letkf_ctx *ctx, int64_t no)
     const size_t n = (size_t)std::max<int64_t>(no, 1);
     LG_CUDA(ctx->d_yb.reserve(n * ctx->k));
     if (ctx->params.precision == LETKF_PREC_MIXED) {
-        LG_CUDA(ctx->d_ys32.reserve(n * ctx->k));
+        LG_CUDA(ctx->d_ys32.reserve((n > 0 ? n : 1) * ctx->k));
         LG_CUDA(ctx->d_oef.reserve(n));
     }
     LG_CUDA(ctx->d_dep.reserve(n));
@@ -202,6 +202,7 @@ void fill_stats(letkf_ctx *ctx, const unsigned long long *cnt)
     s.n_not_converged = (int64_t)cnt[LG_CNT_NOTCONV];
     s.max_sweeps = (int32_t)cnt[LG_CNT_MAXSWEEP];
     s.sum_sweeps = (int64_t)cnt[LG_CNT_SUMSWEEP];
+    s.n_ill_conditioned = (int64_t)cnt[LG_CNT_ILLCOND];
     s.precision = ctx->params.precision;
 }
 

@@ -40,6 +40,7 @@ enum {
     LG_CNT_NOTCONV,
     LG_CNT_MAXSWEEP,
     LG_CNT_SUMSWEEP,
+    LG_CNT_ILLCOND,
     LG_CNT_N
 };
 

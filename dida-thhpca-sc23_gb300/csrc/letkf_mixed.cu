@@ -466,6 +466,21 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
             }
         }
         __syncthreads();
+        // condition number check: the FP32 eigenpairs are accurate to about
+        // eps32 * lambda_max / lambda_min
+        if (warp == 0) {
+            float lo = 3.0e38f, hi = 0.0f;
+            for (int j = lane; j < K; j += 32) {
+                lo = fminf(lo, ilam32[j]);
+                hi = fmaxf(hi, ilam32[j]);
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+                hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+            }
+            if (lane == 0 && hi > 1.0e4f * lo) atomicAdd(&counters[LG_CNT_ILLCOND], 1ull);
+        }
         LG_PHASE(2);
         // ---------------- phase 4: X, wbar with one refinement step ------------------------
         // X by columns in FP32 (T, wbar, warm start).  W32 shares this memory, so

@@ -87,7 +87,7 @@ class Stats(C.Structure):
         ("n_not_converged", C.c_int64), ("max_sweeps", C.c_int32), ("precision", C.c_int32),
         ("ms_h2d", C.c_double), ("ms_obs", C.c_double), ("ms_search", C.c_double),
         ("ms_core", C.c_double), ("ms_d2h", C.c_double), ("ms_total", C.c_double),
-        ("sum_sweeps", C.c_int64),
+        ("sum_sweeps", C.c_int64), ("n_ill_conditioned", C.c_int64),
     ]
 
     def as_dict(self):

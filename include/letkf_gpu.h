@@ -120,6 +120,8 @@ typedef struct letkf_stats {
     int32_t precision;
     double ms_h2d, ms_obs, ms_search, ms_core, ms_d2h, ms_total;  /* device-event times */
     int64_t sum_sweeps;        /* Jacobi sweeps summed over all cubes               */
+    int64_t n_ill_conditioned; /* mixed form: cubes whose A' has lambda_max/lambda_min
+                                  above 1e4, where the FP32 eigenpairs lose digits    */
 } letkf_stats;
 
 /* The lat x lon blocks of a DA group of nranks MPI ranks: MPI_Dims_create(

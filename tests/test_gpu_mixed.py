@@ -90,4 +90,6 @@ def test_mixed_config1_vs_fp64(letkf, synthetic):
     errs = assert_mixed(xa16, axa16, xa64, axa64, w)
     st = mx.stats()
     assert st["n_borderline"] == 0
+    # A' stays well conditioned at this size (lambda_max / lambda_min < 1e4)
+    assert st["n_ill_conditioned"] == 0 and st["n_not_converged"] == 0
     print("config1 mixed vs fp64:", errs)
