@@ -260,8 +260,9 @@ def run_reference(args, rank, world):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * t, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"config{args.config}: 1deg 360x180x32, k=64, 200k clustered obs, "
-                               f"c=400 km, rho=1.08 (sample of {ns} columns per step)"},
+        "config": {"workload": f"config{args.config} ({w.name}): {w.nlon}x{w.nlat}x{w.nz}, k={w.k}, "
+                               f"{w.obs['lat'].size} obs, c={w.loc_dist_km:g} km, rho={w.inflation:g} "
+                               f"(sample of {ns} columns per step)"},
         "cpu_baseline": {"value": value, "unit": "columns/s", "cores": O.num_threads(),
                          "kind": "port",
                          "sample": f"{ns} of {nc} columns per step; H over all obs pro rata; "
@@ -511,6 +512,155 @@ def run_ours(args, rank, world, local_rank):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------------------
+def run_ours_batch(args, rank, world, local_rank):
+    """Configuration 3, the batching form: eight instances of different grids
+    and ensemble sizes in one CUDA graph (each instance on its own stream, the
+    mixed core's work queue autotuned per instance).  k = 96 instances run the
+    FP64 form (the mixed core covers k <= 64).  `value` = columns of all
+    instances per second of graph replay."""
+    import torch
+    dev = torch.device("cuda", local_rank)
+    torch.cuda.set_device(dev)
+    synthetic = pkg("synthetic")
+    letkf = pkg("letkf")
+    pkg("build").build()
+    letkf.load_library()
+    tdist = None
+    if world > 1:
+        import torch.distributed as tdist
+    t_gen = time.perf_counter()
+    ws = [synthetic.config(3, i) for i in range(len(synthetic.INSTANCES_3))]
+    t_gen = time.perf_counter() - t_gen
+    # one non-default stream for the contexts, the graph replays, the copies and
+    # the timing events
+    stream = torch.cuda.Stream(dev)
+    keys = ("lat", "lon", "ph", "lev", "var", "yo", "rinv")
+    ctxs, bufs, forms = [], [], []
+    for w in ws:
+        mixed = w.k <= 64
+        ctx = letkf.LetkfGPU.from_workload(w, device=local_rank,
+                                           precision=letkf.LETKF_PREC_MIXED if mixed else letkf.LETKF_PREC_FP64)
+        ctx.set_stream(stream.cuda_stream)
+        xb = torch.from_numpy(w.xb).to(dev)
+        axb = torch.from_numpy(w.axb).to(dev)
+        obs = letkf.ObsArrays({k: torch.from_numpy(np.ascontiguousarray(w.obs[k])).to(dev) for k in keys},
+                              device=True)
+        b = (xb, axb, obs, torch.empty_like(xb), torch.empty_like(axb))
+        chunk = ctx.autotune_device(*b) if mixed else None
+        ctxs.append(ctx)
+        bufs.append(b)
+        forms.append({"grid": f"{w.nlat}x{w.nlon}", "k": w.k, "obs": int(w.obs["lat"].size),
+                      "form": "mixed" if mixed else "fp64", "sched_chunk": chunk})
+    torch.cuda.synchronize()
+    # the instances one after another (no graph), for reference
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for ctx, b in zip(ctxs, bufs):
+        ctx.run_device(*b)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms_seq = e0.elapsed_time(e1)
+    for ctx, f in zip(ctxs, forms):
+        st = ctx.stats()
+        f["sum_p"], f["ms_core_sequential"] = st["sum_p"], st["ms_core"]
+    batch = letkf.Batch(ctxs, [b[0] for b in bufs], [b[1] for b in bufs], [b[2] for b in bufs],
+                        [b[3] for b in bufs], [b[4] for b in bufs])
+    sh = stream.cuda_stream
+    for _ in range(args.warmup):
+        batch.launch(sh)
+    batch.sync(sh)
+    gpu_uuid = str(torch.cuda.get_device_properties(dev).uuid)
+    clocks = ClockSampler(gpu_uuid if gpu_uuid.startswith("GPU-") else f"GPU-{gpu_uuid}")
+    if world > 1:
+        tdist.barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    time.sleep(0.3)
+    n0 = letkf.launch_count()
+    e0.record(stream)
+    for _ in range(args.steps):
+        batch.launch(sh)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    clk = clocks.stop()
+    launches = letkf.launch_count() - n0
+    batch.sync(sh)
+    ms = e0.elapsed_time(e1) / args.steps
+    if world > 1:
+        ms = _max_over_ranks(torch, tdist, dev, ms)
+    ncol = sum(w.ncol for w in ws)
+    value = whole_job_columns_per_s(world, ncol, ms)
+    # end to end: each step copies every instance's inputs in from pinned host
+    # memory, replays the graph and copies every analysis out
+    host_in, host_out = [], []
+    for w, b in zip(ws, bufs):
+        pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
+        host_in.append([pin(w.xb), pin(w.axb)] + [pin(w.obs[k]) for k in keys])
+        host_out.append([torch.empty(b[3].shape, dtype=torch.float64, pin_memory=True),
+                         torch.empty(b[4].shape, dtype=torch.float64, pin_memory=True)])
+    dev_in = [[b[0], b[1]] + [b[2]._keep[k] for k in keys] for b in bufs]
+    h2d = sum(t.numel() * t.element_size() for hs in host_in for t in hs)
+    d2h = sum(t.numel() * t.element_size() for hs in host_out for t in hs)
+    e2e_steps = max(1, min(args.steps, 3))
+    torch.cuda.synchronize()
+    e0.record(stream)
+    with torch.cuda.stream(stream):
+        for _ in range(e2e_steps):
+            for hs, ds in zip(host_in, dev_in):
+                for h, d in zip(hs, ds):
+                    d.copy_(h, non_blocking=True)
+            batch.launch(sh)
+            for hs, b in zip(host_out, bufs):
+                hs[0].copy_(b[3], non_blocking=True)
+                hs[1].copy_(b[4], non_blocking=True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    batch.sync(sh)
+    ms_e2e = e0.elapsed_time(e1) / e2e_steps
+    if world > 1:
+        ms_e2e = _max_over_ranks(torch, tdist, dev, ms_e2e)
+    if rank != 0:
+        return
+    peaks = measured_peaks()
+    flops = nbytes = 0.0
+    for w, ctx in zip(ws, ctxs):
+        f_, b_ = algorithmic_work(w, ctx.stats()["sum_p"])
+        flops += f_
+        nbytes += b_
+    fp64_peak = fp64_peak_tflops(torch, dev)
+    line = {
+        "metric": METRIC, "value": value, "unit": "columns/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "bf16 hi/lo tensor products + f32 eigen + f64 mean (k<=64); f64 (k=96)",
+        "data": "synthetic (seeded; no public dataset for this path)",
+        "config": {"workload": "config3: 8 instances 90x180..240x480 x32, k in {32,48,64,96}, "
+                               "20k-400k obs, one CUDA graph",
+                   "instances": forms, "columns": ncol,
+                   "l2": "inputs larger than L2", "parallelism": f"replicas x{world}"},
+        "sequential_ms": ms_seq,
+        "graph_speedup_vs_sequential": ms_seq / ms,
+        "e2e": {"value": whole_job_columns_per_s(world, ncol, ms_e2e), "unit": "columns/s",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches,
+        "roofline": {"bound": "fp64", "achieved": flops / (ms * 1e-3) / 1e12, "peak": fp64_peak,
+                     "unit": "TFLOP/s", "frac": flops / (ms * 1e-3) / 1e12 / fp64_peak, "traffic": None,
+                     "work": "algorithmic FLOPs of all instances per replay against the measured "
+                             "FP64 DGEMM rate (FP64-equivalent)"},
+        "roofline_hbm_step": {"achieved": nbytes / (ms * 1e-3) / 1e9, "peak": peaks.get("hbm_gbs", 6800.0),
+                              "unit": "GB/s", "frac": nbytes / (ms * 1e-3) / 1e9 / peaks.get("hbm_gbs", 6800.0),
+                              "algorithmic_bytes": nbytes},
+        "clocks": clk,
+        "workload_generation_s": t_gen,
+    }
+    if not args.no_cpu_baseline and world == 1:
+        line["cpu_baseline"] = cpu_baseline(ws[4], args.cpu_seconds, "config3 instance 4 (1 deg, k=64)")
+        line["cpu_baseline"]["cpu"] = cpu_model()
+    print(json.dumps(line), flush=True)
+    batch.close()
+
+
 def main():
     args = parse_args()
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -525,7 +675,10 @@ def main():
         torch.cuda.set_device(local_rank)
         tdist.init_process_group("nccl")
     try:
-        run_ours(args, rank, world, local_rank)
+        if args.config == 3:
+            run_ours_batch(args, rank, world, local_rank)
+        else:
+            run_ours(args, rank, world, local_rank)
     finally:
         if world > 1:
             import torch.distributed as tdist

@@ -191,6 +191,33 @@ int obs_and_search(letkf_ctx *ctx, const double *xb, const double *axb, const le
     return set_err(ctx, LETKF_ERR_ALLOC, "local observation lists did not fit");
 }
 
+// The whole analysis on device pointers with no host synchronization, for
+// capture into a CUDA graph.  Every buffer must already be sized for these
+// inputs by an earlier run (the list pool cannot grow here: a list pool that
+// is too small shows as LETKF_ERR_ALLOC when the status is read).
+int enqueue_run(letkf_ctx *ctx, const double *xb, const double *axb, const letkf_obs *obs, double *xa,
+                double *axa)
+{
+    if (ctx->dec_nx > 0)
+        return set_err(ctx, LETKF_ERR_UNSUPPORTED, "decomposed observation sets are not captured in graphs");
+    int rc = reset_status(ctx);
+    if (rc) return rc;
+    ObsDev od;
+    rc = stage_obs(ctx, obs, false, od);
+    if (rc) return rc;
+    const int64_t no = obs->nobs;
+    const LgGrid g = lg_grid(ctx);
+    LG_CUDA(lg_launch_obs_prepare(ctx, g, xb, axb, no, od.lat, od.lon, od.ph, od.lev, od.var, od.yo,
+                                  od.rinv));
+    LG_CUDA(lg_launch_buckets(ctx, no));
+    LG_CUDA(lg_launch_search(ctx, g, no));
+    if (ctx->params.precision == LETKF_PREC_MIXED)
+        LG_CUDA(lg_launch_core_mixed(ctx, g, xb, axb, xa, axa, ctx->d_trans.p != nullptr));
+    else
+        LG_CUDA(lg_launch_core_fp64(ctx, g, xb, axb, xa, axa, ctx->d_trans.p != nullptr));
+    return LETKF_OK;
+}
+
 void fill_stats(letkf_ctx *ctx, const unsigned long long *cnt)
 {
     letkf_stats &s = ctx->stats;
@@ -203,6 +230,7 @@ void fill_stats(letkf_ctx *ctx, const unsigned long long *cnt)
     s.max_sweeps = (int32_t)cnt[LG_CNT_MAXSWEEP];
     s.sum_sweeps = (int64_t)cnt[LG_CNT_SUMSWEEP];
     s.n_ill_conditioned = (int64_t)cnt[LG_CNT_ILLCOND];
+    s.sched_chunk = ctx->sched_chunk;
     s.precision = ctx->params.precision;
 }
 
@@ -761,6 +789,186 @@ void letkf_final_gpu_(int *ierr)
 {
     *ierr = letkf_gpu_destroy(g_fctx);
     g_fctx = nullptr;
+}
+
+int letkf_gpu_autotune(letkf_ctx *ctx, const double *xb, const double *axb, const letkf_obs *obs,
+                       double *xa, double *axa, int flags)
+{
+    if (!ctx) return LETKF_ERR_INVALID;
+    if (ctx->params.precision != LETKF_PREC_MIXED)
+        return letkf_gpu_run(ctx, xb, axb, obs, xa, axa, flags);
+    // chunk sizes of the mixed core's work queue: small chunks balance the
+    // load, large ones keep more cubes warm-started; the fastest core wins
+    static const int cand[] = {8, 16, 32, 64};
+    int best = 0;
+    double best_ms = 1e300;
+    for (int c : cand) {
+        ctx->sched_chunk = c;
+        const int rc = letkf_gpu_run(ctx, xb, axb, obs, xa, axa, flags);
+        if (rc != LETKF_OK && rc != LETKF_ERR_NOT_CONVERGED) return rc;
+        if (flags == LETKF_DEVICE_PTRS) LG_CUDA(cudaStreamSynchronize(ctx->stream));
+        if (ctx->stats.ms_core < best_ms) {
+            best_ms = ctx->stats.ms_core;
+            best = c;
+        }
+    }
+    ctx->sched_chunk = best;
+    ctx->stats.sched_chunk = best;
+    return LETKF_OK;
+}
+
+}  // extern "C"
+
+struct letkf_batch {
+    int n = 0;
+    std::vector<letkf_ctx *> ctx;
+    std::vector<cudaStream_t> streams;
+    std::vector<cudaEvent_t> joins;
+    cudaStream_t origin = nullptr;
+    cudaEvent_t fork = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int64_t launches = 0;
+    std::string last_error;
+};
+
+namespace {
+
+void batch_release(letkf_batch *b)
+{
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    for (auto e : b->joins)
+        if (e) cudaEventDestroy(e);
+    for (auto s : b->streams)
+        if (s) cudaStreamDestroy(s);
+    if (b->fork) cudaEventDestroy(b->fork);
+    if (b->origin) cudaStreamDestroy(b->origin);
+    delete b;
+}
+
+}  // namespace
+
+extern "C" {
+
+int letkf_batch_create(letkf_batch **out, int n, letkf_ctx *const *ctxs, const double *const *xb,
+                       const double *const *axb, const letkf_obs *obs, double *const *xa, double *const *axa)
+{
+    if (!out || n < 1 || !ctxs || !xb || !axb || !obs || !xa || !axa) return LETKF_ERR_INVALID;
+    *out = nullptr;
+    for (int i = 0; i < n; i++)
+        if (!ctxs[i] || ctxs[i]->device != ctxs[0]->device) return LETKF_ERR_INVALID;
+    for (int i = 0; i < n; i++)
+        if (ctxs[i]->dec_nx > 0)
+            return set_err(ctxs[i], LETKF_ERR_UNSUPPORTED,
+                           "decomposed observation sets are not captured in graphs");
+    // one analysis of each instance outside the graph sizes every buffer
+    for (int i = 0; i < n; i++) {
+        const int rc = letkf_gpu_run(ctxs[i], xb[i], axb[i], &obs[i], xa[i], axa[i], LETKF_DEVICE_PTRS);
+        if (rc != LETKF_OK && rc != LETKF_ERR_NOT_CONVERGED) return rc;
+        if (letkf_gpu_synchronize(ctxs[i]) != LETKF_OK) return LETKF_ERR_CUDA;
+    }
+    letkf_batch *b = new letkf_batch();
+    b->n = n;
+    b->ctx.assign(ctxs, ctxs + n);
+    b->streams.assign(n, nullptr);
+    b->joins.assign(n, nullptr);
+    std::vector<cudaStream_t> saved(n, nullptr);
+    auto fail = [&](int rc) {
+        for (int i = 0; i < n; i++)
+            if (saved[i]) ctxs[i]->stream = saved[i];
+        batch_release(b);
+        return rc;
+    };
+    if (cudaSetDevice(ctxs[0]->device) != cudaSuccess) return fail(LETKF_ERR_CUDA);
+    if (cudaStreamCreateWithFlags(&b->origin, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming) != cudaSuccess)
+        return fail(LETKF_ERR_CUDA);
+    for (int i = 0; i < n; i++)
+        if (cudaStreamCreateWithFlags(&b->streams[i], cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&b->joins[i], cudaEventDisableTiming) != cudaSuccess)
+            return fail(LETKF_ERR_CUDA);
+    // every instance on its own stream, forked from and joined to the origin
+    const int64_t l0 = g_launches.load();
+    if (cudaStreamBeginCapture(b->origin, cudaStreamCaptureModeRelaxed) != cudaSuccess)
+        return fail(LETKF_ERR_CUDA);
+    int rc = LETKF_OK;
+    if (cudaEventRecord(b->fork, b->origin) != cudaSuccess) rc = LETKF_ERR_CUDA;
+    for (int i = 0; i < n && rc == LETKF_OK; i++) {
+        saved[i] = ctxs[i]->stream;
+        ctxs[i]->stream = b->streams[i];
+        if (cudaStreamWaitEvent(b->streams[i], b->fork, 0) != cudaSuccess) rc = LETKF_ERR_CUDA;
+        if (rc == LETKF_OK) rc = enqueue_run(ctxs[i], xb[i], axb[i], &obs[i], xa[i], axa[i]);
+        if (rc == LETKF_OK && (cudaEventRecord(b->joins[i], b->streams[i]) != cudaSuccess ||
+                               cudaStreamWaitEvent(b->origin, b->joins[i], 0) != cudaSuccess))
+            rc = LETKF_ERR_CUDA;
+    }
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(b->origin, &graph);
+    for (int i = 0; i < n; i++)
+        if (saved[i]) {
+            ctxs[i]->stream = saved[i];
+            saved[i] = nullptr;
+        }
+    if (rc != LETKF_OK) {
+        if (graph) cudaGraphDestroy(graph);
+        return fail(rc);
+    }
+    if (ec != cudaSuccess || !graph) return fail(LETKF_ERR_CUDA);
+    b->graph = graph;
+    if (cudaGraphInstantiate(&b->exec, graph, 0) != cudaSuccess) return fail(LETKF_ERR_CUDA);
+    b->launches = g_launches.load() - l0;
+    *out = b;
+    return LETKF_OK;
+}
+
+int letkf_batch_launch(letkf_batch *b, void *stream)
+{
+    if (!b || !b->exec) return LETKF_ERR_INVALID;
+    const cudaError_t e = cudaGraphLaunch(b->exec, stream ? (cudaStream_t)stream : b->origin);
+    if (e != cudaSuccess) {
+        b->last_error = cudaGetErrorString(e);
+        return LETKF_ERR_CUDA;
+    }
+    g_launches.fetch_add(b->launches, std::memory_order_relaxed);
+    return LETKF_OK;
+}
+
+int letkf_batch_sync(letkf_batch *b, void *stream)
+{
+    if (!b) return LETKF_ERR_INVALID;
+    cudaError_t e = cudaStreamSynchronize(stream ? (cudaStream_t)stream : b->origin);
+    if (e != cudaSuccess) {
+        b->last_error = cudaGetErrorString(e);
+        return LETKF_ERR_CUDA;
+    }
+    int worst = LETKF_OK;
+    for (letkf_ctx *ctx : b->ctx) {
+        unsigned st = 0;
+        unsigned long long cnt[LG_CNT_N] = {};
+        const int rc = read_status(ctx, st, cnt);
+        if (rc) return rc;
+        fill_stats(ctx, cnt);
+        int r = LETKF_OK;
+        if (st & LG_ST_LIST_FULL) r = set_err(ctx, LETKF_ERR_ALLOC, "local observation lists did not fit");
+        else if (st & LG_ST_BAD_OBS) r = set_err(ctx, LETKF_ERR_INVALID, "bad observation");
+        else if (st & LG_ST_TIMEOUT) r = set_err(ctx, LETKF_ERR_TIMEOUT, "a bounded wait on the tensor cores ran out");
+        else if (st & LG_ST_SEGMENTS) r = set_err(ctx, LETKF_ERR_UNSUPPORTED, "localization cap spans too many buckets");
+        else if (st & LG_ST_NOT_CONV) r = set_err(ctx, LETKF_ERR_NOT_CONVERGED, "eigensolve did not converge");
+        if (worst == LETKF_OK) worst = r;
+    }
+    return worst;
+}
+
+int64_t letkf_batch_launches(letkf_batch *b) { return b ? b->launches : 0; }
+
+int letkf_batch_destroy(letkf_batch *b)
+{
+    if (!b) return LETKF_OK;
+    cudaSetDevice(b->ctx.empty() ? 0 : b->ctx[0]->device);
+    if (b->origin) cudaStreamSynchronize(b->origin);
+    batch_release(b);
+    return LETKF_OK;
 }
 
 }  // extern "C"

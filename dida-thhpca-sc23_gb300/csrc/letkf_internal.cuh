@@ -41,6 +41,7 @@ enum {
     LG_CNT_MAXSWEEP,
     LG_CNT_SUMSWEEP,
     LG_CNT_ILLCOND,
+    LG_CNT_QUEUE,         // work-queue cursor of the mixed core
     LG_CNT_N
 };
 
@@ -225,6 +226,9 @@ struct letkf_ctx {
     DevBuf<int> d_dec_row_blk, d_dec_col_blk;    // lat block of each row, lon block of each column
     DevBuf<int> d_dec_slot_off, d_dec_slot_blk;  // neighbour blocks of each block, scan order
     DevBuf<int> d_dec_cnt, d_dec_pos, d_dec_obs; // per (block, chunk) counts, offsets; obs of blocks
+    // mixed core schedule (0: defaults) and its work queue
+    int sched_chunk = 0, sched_p0 = 0;
+    DevBuf<int> d_queue;
     // per-cube results
     DevBuf<double> d_trans, d_w;
     // core_batch staging

@@ -140,7 +140,7 @@ __device__ __forceinline__ double block_sum(double v, double *red)
 template <int K>
 __global__ void __launch_bounds__(kT, 2)
 k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32_t *__restrict__ lidx,
-             const float2 *__restrict__ lmeta,
+             const float2 *__restrict__ lmeta, const int *__restrict__ queue, int nchunks, int chunk,
              const int64_t *__restrict__ loff, const int32_t *__restrict__ lcnt, int64_t ncubes,
              const double *__restrict__ xb, const double *__restrict__ axb, double *__restrict__ xa,
              double *__restrict__ axa, double *__restrict__ trans_out, double *__restrict__ w_out,
@@ -218,13 +218,23 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
     long long ph_cyc[7] = {0, 0, 0, 0, 0, 0, 0};
     long long ph_last = clock64();
 #endif
-    // each CTA takes a contiguous run of cubes (neighbours along latitude), so
-    // a cube's eigenvectors are a good start for the next one
-    const int64_t per_cta = (ncubes + gridDim.x - 1) / gridDim.x;
-    const int64_t cube_begin = (int64_t)blockIdx.x * per_cta;
-    const int64_t cube_end = min(ncubes, cube_begin + per_cta);
+    // Work queue: chunks of `chunk` consecutive cubes (neighbours along
+    // latitude, so a cube's eigenvectors are a good start for the next one),
+    // taken heaviest first (queue order) by an atomic cursor.
+    __shared__ int s_chunk;
+    for (;;) {
+    if (tid == 0) {
+        const unsigned long long q = atomicAdd(&counters[LG_CNT_QUEUE], 1ull);
+        s_chunk = q < (unsigned long long)nchunks ? queue[q] : -1;
+    }
+    __syncthreads();
+    const int ck = s_chunk;
+    __syncthreads();
+    if (ck < 0) break;
+    const int cube_begin = ck * chunk;
+    const int cube_end = (int)min(ncubes, (int64_t)cube_begin + chunk);
     bool have_prev = false;
-    for (int64_t cube = cube_begin; cube < cube_end; cube++) {
+    for (int cube = cube_begin; cube < cube_end; cube++) {
         const int64_t off = loff[cube];
         const int p = lcnt[cube];
         LG_PHASE(6);
@@ -602,9 +612,9 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
         if (trans_out) {
             for (int idx = tid; idx < K * K; idx += kT) {
                 const int i = idx % K, j = idx / K;
-                trans_out[cube * K * K + idx] = (double)T32[i * K + j] + wbar[i];
+                trans_out[(int64_t)cube * K * K + idx] = (double)T32[i * K + j] + wbar[i];
             }
-            if (tid < K) w_out[cube * K + tid] = wbar[tid];
+            if (tid < K) w_out[(int64_t)cube * K + tid] = wbar[tid];
         }
 
         LG_PHASE(4);
@@ -712,6 +722,8 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
         if (failed) break;
         have_prev = true;
     }
+    if (failed) break;
+    }
 #ifdef LG_PHASE_CLOCKS
     if (blockIdx.x == 0 && tid == 0)
         printf("phase cycles cta0: A-build %lld, A'-form %lld, jacobi32 %lld, X/wbar %lld, T %lld, "
@@ -726,6 +738,47 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
     __syncthreads();
     lg_tc_fence_after();
     if (warp == 0) lg_tmem_dealloc(tmem, C::TMEM_COLS);
+}
+
+constexpr int kQueueMax = 8192;      // chunks one queue-building CTA sorts in shared memory
+
+// The work queue of the mixed core: chunk weights sum(p + p0) over each
+// chunk's cubes (p0: the per-cube work that does not grow with p, in
+// observation equivalents), sorted heaviest first (bitonic, one CTA).
+__global__ void __launch_bounds__(1024)
+k_chunk_queue(const int32_t *__restrict__ lcnt, int64_t ncubes, int chunk, int nchunks, int p0,
+              int *__restrict__ queue)
+{
+    extern __shared__ unsigned long long qkeys[];
+    int np2 = 1;
+    while (np2 < nchunks) np2 <<= 1;
+    for (int i = threadIdx.x; i < np2; i += blockDim.x) {
+        unsigned long long key = 0ull;
+        if (i < nchunks) {
+            unsigned long long w = 0;
+            const int64_t c0 = (int64_t)i * chunk, c1 = min(ncubes, c0 + chunk);
+            for (int64_t c = c0; c < c1; c++) w += (unsigned long long)(lcnt[c] + p0);
+            key = (w << 32) | (unsigned)i;
+        }
+        qkeys[i] = key;
+    }
+    __syncthreads();
+    for (int k2 = 2; k2 <= np2; k2 <<= 1)
+        for (int j = k2 >> 1; j > 0; j >>= 1) {
+            for (int i = threadIdx.x; i < np2; i += blockDim.x) {
+                const int ixj = i ^ j;
+                if (ixj > i) {
+                    const unsigned long long a = qkeys[i], b = qkeys[ixj];
+                    const bool desc = (i & k2) == 0;
+                    if ((a < b) == desc) {
+                        qkeys[i] = b;
+                        qkeys[ixj] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    for (int i = threadIdx.x; i < nchunks; i += blockDim.x) queue[i] = (int)(qkeys[i] & 0xffffffffull);
 }
 
 template <int K>
@@ -746,12 +799,29 @@ cudaError_t launch_mixed(letkf_ctx *ctx, const LgGrid &g, const double *xb, cons
     // two CTAs per SM when their shared memory fits (registers are capped at
     // 128 per thread by the launch bounds, so two 256-thread CTAs fit)
     const int per_sm = (2 * (smem + 1024) <= (size_t)smem_sm) ? 2 : 1;
+    // work queue (chunks of consecutive cubes, heaviest first)
+    int chunk = ctx->sched_chunk > 0 ? ctx->sched_chunk : 16;
+    while ((ctx->ncubes + chunk - 1) / chunk > kQueueMax) chunk *= 2;
+    const int nchunks = (int)((ctx->ncubes + chunk - 1) / chunk);
+    e = ctx->d_queue.reserve((size_t)nchunks);
+    if (e != cudaSuccess) return e;
+    int np2 = 1;
+    while (np2 < nchunks) np2 <<= 1;
+    const size_t qsmem = sizeof(unsigned long long) * np2;
+    e = cudaFuncSetAttribute(k_chunk_queue, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)qsmem);
+    if (e != cudaSuccess) return e;
+    lg_count_launch();
+    k_chunk_queue<<<1, 1024, qsmem, ctx->stream>>>(ctx->d_lcnt.p, ctx->ncubes, chunk, nchunks,
+                                                   ctx->sched_p0 > 0 ? ctx->sched_p0 : 4400, ctx->d_queue.p);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
     // persistent grid: each CTA allocates its tensor memory once
     const int64_t want = (int64_t)nsm * per_sm;
-    const unsigned blocks = (unsigned)(ctx->ncubes < want ? ctx->ncubes : want);
+    const unsigned blocks = (unsigned)(nchunks < want ? nchunks : want);
     lg_count_launch();
     k_core_mixed<K><<<blocks, kT, smem, ctx->stream>>>(
-        g, lg_params(ctx), ctx->d_ys32.p, ctx->d_lidx.p, ctx->d_lmeta.p, ctx->d_loff.p, ctx->d_lcnt.p,
+        g, lg_params(ctx), ctx->d_ys32.p, ctx->d_lidx.p, ctx->d_lmeta.p, ctx->d_queue.p, nchunks, chunk,
+        ctx->d_loff.p, ctx->d_lcnt.p,
         ctx->ncubes, xb, axb, xa, axa, trans_out, w_out,
         ctx->d_counters.p, ctx->d_status.p);
     return cudaGetLastError();

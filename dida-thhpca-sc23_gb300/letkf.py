@@ -42,7 +42,9 @@ EXPORTED = [
     "letkf_gpu_synchronize", "letkf_gpu_obs_operator", "letkf_gpu_local_obs",
     "letkf_gpu_last_trans", "letkf_gpu_core_batch", "letkf_gpu_get_stats",
     "letkf_gpu_last_error", "letkf_gpu_destroy", "letkf_gpu_launch_count",
-    "letkf_gpu_core_batch_noalloc", "letkf_decomp_dims",
+    "letkf_gpu_core_batch_noalloc", "letkf_decomp_dims", "letkf_gpu_autotune",
+    "letkf_batch_create", "letkf_batch_launch", "letkf_batch_sync", "letkf_batch_launches",
+    "letkf_batch_destroy",
     "letkf_init_gpu_", "letkf_set_obs_gpu_", "letkf_run_gpu_", "letkf_final_gpu_",
 ]
 
@@ -88,6 +90,7 @@ class Stats(C.Structure):
         ("ms_h2d", C.c_double), ("ms_obs", C.c_double), ("ms_search", C.c_double),
         ("ms_core", C.c_double), ("ms_d2h", C.c_double), ("ms_total", C.c_double),
         ("sum_sweeps", C.c_int64), ("n_ill_conditioned", C.c_int64),
+        ("sched_chunk", C.c_int32), ("reserved", C.c_int32),
     ]
 
     def as_dict(self):
@@ -122,6 +125,14 @@ def load_library(path: str = LIB_PATH):
     L.letkf_gpu_launch_count.restype = i64
     L.letkf_gpu_core_batch_noalloc.argtypes = [i32, C.c_double, i64, vp, vp, vp, vp, vp, vp, vp, vp]
     L.letkf_decomp_dims.argtypes = [i32, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+    L.letkf_gpu_autotune.argtypes = [vp, vp, vp, C.POINTER(Obs), vp, vp, i32]
+    L.letkf_batch_create.argtypes = [C.POINTER(vp), i32, C.POINTER(vp), C.POINTER(vp), C.POINTER(vp),
+                                     C.POINTER(Obs), C.POINTER(vp), C.POINTER(vp)]
+    L.letkf_batch_launch.argtypes = [vp, vp]
+    L.letkf_batch_sync.argtypes = [vp, vp]
+    L.letkf_batch_launches.argtypes = [vp]
+    L.letkf_batch_launches.restype = i64
+    L.letkf_batch_destroy.argtypes = [vp]
     _lib = L
     return L
 
@@ -159,6 +170,47 @@ class ObsArrays:
             n = int(t["lat"].size)
         self.c = Obs(nobs=n, lat=p("lat"), lon=p("lon"), ph=p("ph"), lev=p("lev"),
                      var=p("var"), yo=p("yo"), rinv=p("rinv"))
+
+
+class Batch:
+    """One CUDA graph over the analyses of several contexts (letkf_batch_*):
+    device tensors in and out, replayed on the same tensors."""
+
+    def __init__(self, ctxs, xb, axb, obs, xa, axa):
+        L = load_library()
+        n = len(ctxs)
+        vpa = lambda vals: (C.c_void_p * n)(*vals)
+        self._obs = (Obs * n)(*[o.c for o in obs])
+        self._keep = (ctxs, xb, axb, obs, xa, axa)
+        h = C.c_void_p()
+        rc = L.letkf_batch_create(C.byref(h), n, vpa([c.h.value for c in ctxs]),
+                                  vpa([t.data_ptr() for t in xb]), vpa([t.data_ptr() for t in axb]),
+                                  self._obs, vpa([t.data_ptr() for t in xa]), vpa([t.data_ptr() for t in axa]))
+        if rc != LETKF_OK:
+            raise LetkfError(rc, "letkf_batch_create")
+        self.h, self.L = h, L
+        self.launches = int(L.letkf_batch_launches(h))
+
+    def launch(self, stream_handle=None):
+        rc = self.L.letkf_batch_launch(self.h, stream_handle)
+        if rc != LETKF_OK:
+            raise LetkfError(rc, "letkf_batch_launch")
+
+    def sync(self, stream_handle=None):
+        rc = self.L.letkf_batch_sync(self.h, stream_handle)
+        if rc != LETKF_OK:
+            raise LetkfError(rc, "letkf_batch_sync")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.letkf_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def decomp_dims(nranks: int):
@@ -255,6 +307,13 @@ class LetkfGPU:
         rc = self.L.letkf_gpu_run(self.h, xb.data_ptr(), axb.data_ptr(), C.byref(obs.c),
                                   xa.data_ptr(), axa.data_ptr(), LETKF_DEVICE_PTRS)
         self._check(rc, "letkf_gpu_run")
+
+    def autotune_device(self, xb, axb, obs: ObsArrays, xa, axa):
+        """letkf_gpu_autotune on device tensors; returns the chosen chunk size."""
+        rc = self.L.letkf_gpu_autotune(self.h, xb.data_ptr(), axb.data_ptr(), C.byref(obs.c),
+                                       xa.data_ptr(), axa.data_ptr(), LETKF_DEVICE_PTRS)
+        self._check(rc, "letkf_gpu_autotune")
+        return self.stats()["sched_chunk"]
 
     def obs_operator(self, xb, axb, obs):
         xb = _f64(xb)

@@ -122,6 +122,8 @@ typedef struct letkf_stats {
     int64_t sum_sweeps;        /* Jacobi sweeps summed over all cubes               */
     int64_t n_ill_conditioned; /* mixed form: cubes whose A' has lambda_max/lambda_min
                                   above 1e4, where the FP32 eigenpairs lose digits    */
+    int32_t sched_chunk;       /* mixed form: cubes per work-queue chunk (0: default 16) */
+    int32_t reserved;
 } letkf_stats;
 
 /* The lat x lon blocks of a DA group of nranks MPI ranks: MPI_Dims_create(
@@ -203,6 +205,39 @@ int letkf_gpu_core_batch(letkf_ctx *ctx, int64_t nb, const int64_t *offsets,
 int letkf_gpu_core_batch_noalloc(int ens, double inflation, int64_t nb, const int64_t *offsets,
                                  const double *hxens, const float *rdiaginv, const double *dep,
                                  const double *rloc, double *trans, double *w, void *stream);
+
+/* Autotuner of the mixed form's schedule: runs the analysis (as
+ * letkf_gpu_run) once per candidate chunk size of the core's work queue
+ * (8, 16, 32, 64 consecutive cubes per chunk; chunks are taken heaviest
+ * first) and keeps the one with the fastest core for the context's later
+ * runs (letkf_stats.sched_chunk).  xa/axa hold the last run's analysis.
+ * For the FP64 form it is one letkf_gpu_run.  No counterpart in the
+ * reference.                                                                 */
+int letkf_gpu_autotune(letkf_ctx *ctx, const double *xb, const double *axb, const letkf_obs *obs,
+                       double *xa, double *axa, int flags);
+
+/* One CUDA graph over the analyses of several contexts (the batching form:
+ * instances of different grids and ensemble sizes, each on its own stream
+ * forked from and joined to one origin).  No counterpart in the reference.
+ * All pointers are device memory; obs holds n observation sets.  The call
+ * first runs each analysis once outside the graph to size every buffer for
+ * these inputs, then captures them; letkf_batch_launch replays the graph on
+ * the same pointers (refresh the inputs in place between launches) and
+ * returns at once, letkf_batch_sync waits for it and reports the worst
+ * status of the contexts (their stats are updated; a list pool too small for
+ * new inputs shows as LETKF_ERR_ALLOC: create the batch again).  Contexts with
+ * decomposed observation sets are not captured (LETKF_ERR_UNSUPPORTED).
+ * Do not run a captured context by itself while its batch may be running.   */
+typedef struct letkf_batch letkf_batch;
+int letkf_batch_create(letkf_batch **batch, int n, letkf_ctx *const *ctxs, const double *const *xb,
+                       const double *const *axb, const letkf_obs *obs, double *const *xa,
+                       double *const *axa);
+/* stream: a cudaStream_t for the replay (NULL: the batch's own stream);
+ * letkf_batch_sync waits for the same stream.                               */
+int letkf_batch_launch(letkf_batch *batch, void *stream);
+int letkf_batch_sync(letkf_batch *batch, void *stream);
+int64_t letkf_batch_launches(letkf_batch *batch);   /* kernels per replay */
+int letkf_batch_destroy(letkf_batch *batch);
 
 int letkf_gpu_get_stats(letkf_ctx *ctx, letkf_stats *stats);
 const char *letkf_gpu_last_error(letkf_ctx *ctx);
