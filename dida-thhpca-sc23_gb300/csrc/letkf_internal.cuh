@@ -270,6 +270,11 @@ cudaError_t lg_launch_core_fp64(letkf_ctx *ctx, const LgGrid &g, const double *x
                                 const double *axb, double *xa, double *axa, bool keep_trans);
 cudaError_t lg_launch_core_mixed(letkf_ctx *ctx, const LgGrid &g, const double *xb,
                                  const double *axb, double *xa, double *axa, bool keep_trans);
+// the mixed core for k = 96, 128 (letkf_mixed_wide.cu) and the work queue
+// both mixed kernels take (letkf_mixed.cu)
+cudaError_t lg_launch_core_mixed_wide(letkf_ctx *ctx, const LgGrid &g, const double *xb, const double *axb,
+                                      double *xa, double *axa, double *trans_out, double *w_out);
+cudaError_t lg_build_chunk_queue(letkf_ctx *ctx, int &chunk, int &nchunks);
 cudaError_t lg_launch_core_batch_fp64(letkf_ctx *ctx, int64_t nb, const int64_t *d_off,
                                       const double *d_hx, const float *d_rdi,
                                       const double *d_dep, const double *d_rloc,

@@ -29,6 +29,7 @@
 
 #include "letkf_internal.cuh"
 #include "letkf_jacobi.cuh"
+#include "letkf_mixed_util.cuh"
 #include "letkf_umma.cuh"
 
 // Column-cosine tolerance of the FP32 Jacobi.  It bounds the eigenvectors'
@@ -89,39 +90,6 @@ struct MCfg {
     static_assert(K + 16 <= (int)TMEM_COLS, "A-build accumulator must fit the TMEM allocation");
     static_assert(STAGE <= B1 && (STAGE1_IN_B1 || 2 * TILE + STAGE <= 49152), "gather stages must fit");
 };
-
-// 16-byte global -> shared copies that bypass the registers (cp.async, L2 only).
-__device__ __forceinline__ void cp_async16(uint32_t dst, const void *src)
-{
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
-}
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
-
-__device__ __forceinline__ uint32_t pack_bf16(float a, float b)
-{
-    __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
-    return *reinterpret_cast<uint32_t *>(&h);
-}
-
-// hi/lo BF16 split of 8 floats into two 16-byte chunks.
-__device__ __forceinline__ void split8(const float *v, uint4 &hi, uint4 &lo)
-{
-    uint32_t h[4], l[4];
-#pragma unroll
-    for (int j = 0; j < 4; j++) {
-        const __nv_bfloat16 h0 = __float2bfloat16_rn(v[2 * j]), h1 = __float2bfloat16_rn(v[2 * j + 1]);
-        const float r0 = v[2 * j] - __bfloat162float(h0), r1 = v[2 * j + 1] - __bfloat162float(h1);
-        __nv_bfloat162 hh;
-        hh.x = h0;
-        hh.y = h1;
-        h[j] = *reinterpret_cast<uint32_t *>(&hh);
-        l[j] = pack_bf16(r0, r1);
-    }
-    hi = make_uint4(h[0], h[1], h[2], h[3]);
-    lo = make_uint4(l[0], l[1], l[2], l[3]);
-}
 
 __device__ __forceinline__ double block_sum(double v, double *red)
 {
@@ -781,6 +749,31 @@ k_chunk_queue(const int32_t *__restrict__ lcnt, int64_t ncubes, int chunk, int n
     for (int i = threadIdx.x; i < nchunks; i += blockDim.x) queue[i] = (int)(qkeys[i] & 0xffffffffull);
 }
 
+}  // namespace
+
+// Build the mixed core's work queue for the cubes of the last search: chunks
+// of `chunk` consecutive cubes (the context's schedule, 16 by default, grown
+// until at most kQueueMax chunks), heaviest first, into ctx->d_queue.
+cudaError_t lg_build_chunk_queue(letkf_ctx *ctx, int &chunk, int &nchunks)
+{
+    chunk = ctx->sched_chunk > 0 ? ctx->sched_chunk : 16;
+    while ((ctx->ncubes + chunk - 1) / chunk > kQueueMax) chunk *= 2;
+    nchunks = (int)((ctx->ncubes + chunk - 1) / chunk);
+    cudaError_t e = ctx->d_queue.reserve((size_t)nchunks);
+    if (e != cudaSuccess) return e;
+    int np2 = 1;
+    while (np2 < nchunks) np2 <<= 1;
+    const size_t qsmem = sizeof(unsigned long long) * np2;
+    e = cudaFuncSetAttribute(k_chunk_queue, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)qsmem);
+    if (e != cudaSuccess) return e;
+    lg_count_launch();
+    k_chunk_queue<<<1, 1024, qsmem, ctx->stream>>>(ctx->d_lcnt.p, ctx->ncubes, chunk, nchunks,
+                                                   ctx->sched_p0 > 0 ? ctx->sched_p0 : 4400, ctx->d_queue.p);
+    return cudaGetLastError();
+}
+
+namespace {
+
 template <int K>
 cudaError_t launch_mixed(letkf_ctx *ctx, const LgGrid &g, const double *xb, const double *axb,
                          double *xa, double *axa, double *trans_out, double *w_out)
@@ -800,20 +793,8 @@ cudaError_t launch_mixed(letkf_ctx *ctx, const LgGrid &g, const double *xb, cons
     // 128 per thread by the launch bounds, so two 256-thread CTAs fit)
     const int per_sm = (2 * (smem + 1024) <= (size_t)smem_sm) ? 2 : 1;
     // work queue (chunks of consecutive cubes, heaviest first)
-    int chunk = ctx->sched_chunk > 0 ? ctx->sched_chunk : 16;
-    while ((ctx->ncubes + chunk - 1) / chunk > kQueueMax) chunk *= 2;
-    const int nchunks = (int)((ctx->ncubes + chunk - 1) / chunk);
-    e = ctx->d_queue.reserve((size_t)nchunks);
-    if (e != cudaSuccess) return e;
-    int np2 = 1;
-    while (np2 < nchunks) np2 <<= 1;
-    const size_t qsmem = sizeof(unsigned long long) * np2;
-    e = cudaFuncSetAttribute(k_chunk_queue, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)qsmem);
-    if (e != cudaSuccess) return e;
-    lg_count_launch();
-    k_chunk_queue<<<1, 1024, qsmem, ctx->stream>>>(ctx->d_lcnt.p, ctx->ncubes, chunk, nchunks,
-                                                   ctx->sched_p0 > 0 ? ctx->sched_p0 : 4400, ctx->d_queue.p);
-    e = cudaGetLastError();
+    int chunk = 0, nchunks = 0;
+    e = lg_build_chunk_queue(ctx, chunk, nchunks);
     if (e != cudaSuccess) return e;
     // persistent grid: each CTA allocates its tensor memory once
     const int64_t want = (int64_t)nsm * per_sm;
@@ -829,7 +810,7 @@ cudaError_t launch_mixed(letkf_ctx *ctx, const LgGrid &g, const double *xb, cons
 
 }  // namespace
 
-bool lg_mixed_supports(int k) { return k == 32 || k == 48 || k == 64; }
+bool lg_mixed_supports(int k) { return k == 32 || k == 48 || k == 64 || k == 96 || k == 128; }
 
 cudaError_t lg_launch_core_mixed(letkf_ctx *ctx, const LgGrid &g, const double *xb, const double *axb,
                                  double *xa, double *axa, bool keep_trans)
@@ -840,6 +821,8 @@ cudaError_t lg_launch_core_mixed(letkf_ctx *ctx, const LgGrid &g, const double *
     case 32: return launch_mixed<32>(ctx, g, xb, axb, xa, axa, tr, w);
     case 48: return launch_mixed<48>(ctx, g, xb, axb, xa, axa, tr, w);
     case 64: return launch_mixed<64>(ctx, g, xb, axb, xa, axa, tr, w);
+    case 96:
+    case 128: return lg_launch_core_mixed_wide(ctx, g, xb, axb, xa, axa, tr, w);
     default: return cudaErrorInvalidValue;
     }
 }

@@ -1,0 +1,40 @@
+// letkf_mixed_util.cuh -- small device helpers shared by the mixed-precision
+// core kernels: BF16 hi/lo splitting and cp.async row copies.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <stdint.h>
+
+// 16-byte global -> shared copies that bypass the registers (cp.async, L2 only).
+__device__ __forceinline__ void cp_async16(uint32_t dst, const void *src)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory"); }
+
+__device__ __forceinline__ uint32_t pack_bf16(float a, float b)
+{
+    __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+    return *reinterpret_cast<uint32_t *>(&h);
+}
+
+// hi/lo BF16 split of 8 floats into two 16-byte chunks.
+__device__ __forceinline__ void split8(const float *v, uint4 &hi, uint4 &lo)
+{
+    uint32_t h[4], l[4];
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        const __nv_bfloat16 h0 = __float2bfloat16_rn(v[2 * j]), h1 = __float2bfloat16_rn(v[2 * j + 1]);
+        const float r0 = v[2 * j] - __bfloat162float(h0), r1 = v[2 * j + 1] - __bfloat162float(h1);
+        __nv_bfloat162 hh;
+        hh.x = h0;
+        hh.y = h1;
+        h[j] = *reinterpret_cast<uint32_t *>(&hh);
+        l[j] = pack_bf16(r0, r1);
+    }
+    hi = make_uint4(h[0], h[1], h[2], h[3]);
+    lo = make_uint4(l[0], l[1], l[2], l[3]);
+}
+

@@ -35,7 +35,7 @@ def assert_mixed(xa, axa, xa_ref, axa_ref, w):
     return errs
 
 
-@pytest.mark.parametrize("k", [32, 48, 64])
+@pytest.mark.parametrize("k", [32, 48, 64, 96, 128])
 def test_mixed_small_cases_vs_oracle(letkf, synthetic, k):
     w = synthetic.small_case(nlat=12, nlon=24, nz=4, k=k, nobs=900, loc_dist_km=900.0, seed=100 + k)
     ctx = letkf.LetkfGPU.from_workload(w, precision=letkf.LETKF_PREC_MIXED)
@@ -58,8 +58,9 @@ def test_mixed_no_observations(letkf, synthetic):
     assert np.max(np.abs(xa - np.sqrt(w.inflation) * w.xb)) <= 1e-4 * np.abs(w.xb).max()
 
 
-def test_mixed_transforms_close_to_fp64(letkf, synthetic):
-    w = synthetic.small_case(nlat=10, nlon=20, nz=3, k=64, nobs=1500, loc_dist_km=1000.0, seed=31)
+@pytest.mark.parametrize("k", [64, 96, 128])
+def test_mixed_transforms_close_to_fp64(letkf, synthetic, k):
+    w = synthetic.small_case(nlat=10, nlon=20, nz=3, k=k, nobs=1500, loc_dist_km=1000.0, seed=31)
     fp = letkf.LetkfGPU.from_workload(w)
     mx = letkf.LetkfGPU.from_workload(w, precision=letkf.LETKF_PREC_MIXED)
     fp.keep_trans(True)
@@ -71,6 +72,20 @@ def test_mixed_transforms_close_to_fp64(letkf, synthetic):
     t16, w16 = mx.last_trans(cubes)
     assert np.max(np.abs(t16 - t64)) <= 1e-4 * np.abs(t64).max()
     assert np.max(np.abs(w16 - w64)) <= 1e-3 * np.abs(w64).max()
+
+
+def test_mixed_wide_ensemble_vs_fp64(letkf, synthetic):
+    # k = 96 (two accumulators, two member tiles) on a 2-degree grid with
+    # clustered obs, warm starts along every chunk
+    w = synthetic.generate("k96", 2.0, 8, 96, 60_000, 500.0, 1.08, 96,
+                           boxes=((0.0, 60.0, -10.0, 30.0),), box_factor=4.0)
+    fp = letkf.LetkfGPU.from_workload(w)
+    mx = letkf.LetkfGPU.from_workload(w, precision=letkf.LETKF_PREC_MIXED)
+    xa64, axa64 = fp.run(w.xb, w.axb, w.obs)
+    xa16, axa16 = mx.run(w.xb, w.axb, w.obs)
+    assert_mixed(xa16, axa16, xa64, axa64, w)
+    st = mx.stats()
+    assert st["n_not_converged"] == 0 and st["max_p"] > 1000
 
 
 def test_mixed_config0_vs_oracle(letkf, synthetic):
