@@ -133,12 +133,9 @@ int reset_status(letkf_ctx *ctx)
     return LETKF_OK;
 }
 
-// H, buckets and local lists for the staged observations; grows the list
-// storage and repeats the search if it was too small.
-int obs_and_search(letkf_ctx *ctx, const double *xb, const double *axb, const letkf_obs *obs,
-                   const ObsDev &od, unsigned long long *cnt)
+// H and the observation buckets for the staged observations.
+int obs_prepare(letkf_ctx *ctx, const double *xb, const double *axb, const ObsDev &od, int64_t no)
 {
-    const int64_t no = obs->nobs;
     const LgGrid g = lg_grid(ctx);
     int rc = reserve_obs_work(ctx, no);
     if (rc) return rc;
@@ -146,49 +143,164 @@ int obs_and_search(letkf_ctx *ctx, const double *xb, const double *axb, const le
                                   od.rinv));
     LG_CUDA(lg_launch_buckets(ctx, no));
     if (ctx->dec_nx > 0) LG_CUDA(lg_launch_block_members(ctx, no, od.lat, od.lon));
-    LG_CUDA(cudaEventRecord(ctx->ev[2], ctx->stream));
+    return LETKF_OK;
+}
+
+size_t list_entry_bytes(const letkf_ctx *ctx)
+{
+    return sizeof(int32_t) + sizeof(double) + (ctx->params.precision == LETKF_PREC_MIXED ? sizeof(float2) : 0);
+}
+
+// Entries the list pool may hold: the caller's limit, else the device's free
+// memory plus the pool's own, less 1 GiB for the rest of the run.
+int64_t pool_limit(letkf_ctx *ctx)
+{
+    if (ctx->list_limit > 0) return ctx->list_limit;
+    size_t fr = 0, tot = 0;
+    if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) return std::max<int64_t>(ctx->list_cap, 1);
+    const size_t held = ctx->d_lidx.n * sizeof(int32_t) + ctx->d_lrloc.n * sizeof(double) +
+                        ctx->d_lmeta.n * sizeof(float2);
+    const size_t keep = (size_t)1 << 30;
+    const size_t avail = fr + held > keep ? fr + held - keep : 0;
+    return std::max<int64_t>((int64_t)(avail / list_entry_bytes(ctx)), 1);
+}
+
+void release_pool(letkf_ctx *ctx)
+{
+    ctx->d_lidx.release();
+    ctx->d_lrloc.release();
+    ctx->d_lmeta.release();
+    ctx->list_cap = 0;
+}
+
+// A list pool of at least cap entries (a larger one that is held is kept).
+int size_pool(letkf_ctx *ctx, int64_t cap)
+{
+    if (cap <= ctx->list_cap && ctx->d_lidx.p) return LETKF_OK;
+    release_pool(ctx);
+    LG_CUDA(ctx->d_lidx.reserve((size_t)cap));
+    LG_CUDA(ctx->d_lrloc.reserve((size_t)cap));
+    if (ctx->params.precision == LETKF_PREC_MIXED) LG_CUDA(ctx->d_lmeta.reserve((size_t)cap));
+    ctx->list_cap = cap;
+    return LETKF_OK;
+}
+
+cudaError_t launch_search(letkf_ctx *ctx, const ObsDev &od, int64_t no)
+{
+    const LgGrid g = lg_grid(ctx);
+    return ctx->dec_nx > 0 ? lg_launch_search_dec(ctx, g, od.lat) : lg_launch_search(ctx, g, no);
+}
+
+cudaError_t launch_core(letkf_ctx *ctx, const double *xb, const double *axb, double *xa, double *axa)
+{
+    const LgGrid g = lg_grid(ctx);
+    const bool keep = ctx->d_trans.p != nullptr;
+    return ctx->params.precision == LETKF_PREC_MIXED ? lg_launch_core_mixed(ctx, g, xb, axb, xa, axa, keep)
+                                                     : lg_launch_core_fp64(ctx, g, xb, axb, xa, axa, keep);
+}
+
+// Zero the list cursor and the work-queue cursor (the counters that restart
+// with every window; the others sum over the windows).
+int restart_cursors(letkf_ctx *ctx)
+{
+    LG_CUDA(cudaMemsetAsync(ctx->d_counters.p + LG_CNT_CURSOR, 0, sizeof(unsigned long long), ctx->stream));
+    LG_CUDA(cudaMemsetAsync(ctx->d_counters.p + LG_CNT_QUEUE, 0, sizeof(unsigned long long), ctx->stream));
+    return LETKF_OK;
+}
+
+// Local lists and the analysis of cubes range0 .. range1-1.  One search over
+// the range gives every cube's list length; when the lists fit the pool (grown
+// up to the limit if needed) one core launch follows, else the range is cut
+// into consecutive windows whose lists fit and each window is searched again
+// and analysed.  ev[3] is recorded after the first search.
+int search_and_core(letkf_ctx *ctx, const double *xb, const double *axb, double *xa, double *axa,
+                    const ObsDev &od, int64_t no, unsigned long long *cnt)
+{
+    const int64_t c0 = ctx->range0, c1 = ctx->range1;
+    int rc = LETKF_OK;
+    // a pool from before a smaller limit was set is given back
+    if (ctx->list_limit > 0 && ctx->list_cap > ctx->list_limit) release_pool(ctx);
+    const int64_t limit = pool_limit(ctx);
     if (ctx->list_cap == 0) {
-        const int64_t guess = ctx->ncubes * (int64_t)std::min(ctx->params.max_obs, 512);
-        LG_CUDA(ctx->d_lidx.reserve((size_t)std::max<int64_t>(guess, 1)));
-        LG_CUDA(ctx->d_lrloc.reserve((size_t)std::max<int64_t>(guess, 1)));
-        if (ctx->params.precision == LETKF_PREC_MIXED)
-            LG_CUDA(ctx->d_lmeta.reserve((size_t)std::max<int64_t>(guess, 1)));
-        ctx->list_cap = std::max<int64_t>(guess, 1);
+        const int64_t guess = (c1 - c0) * (int64_t)std::min(ctx->params.max_obs, 512);
+        rc = size_pool(ctx, std::max<int64_t>(std::min(guess, limit), 1));
+        if (rc) return rc;
     }
-    for (int attempt = 0; attempt < 3; attempt++) {
-        if (ctx->dec_nx > 0)
-            LG_CUDA(lg_launch_search_dec(ctx, g, od.lat));
-        else
-            LG_CUDA(lg_launch_search(ctx, g, no));
+    ctx->lists_whole = false;
+    ctx->win0 = c0;
+    ctx->win1 = c1;
+    bool fits = false;
+    for (int attempt = 0; attempt < 2; attempt++) {
+        LG_CUDA(launch_search(ctx, od, no));
         unsigned st = 0;
         rc = read_status(ctx, st, cnt);
         if (rc) return rc;
         if (st & LG_ST_SEGMENTS)
             return set_err(ctx, LETKF_ERR_UNSUPPORTED, "localization cap spans too many buckets");
-        if (!(st & LG_ST_LIST_FULL)) {
-            if (st & LG_ST_BAD_OBS)
-                return set_err(ctx, LETKF_ERR_INVALID,
-                               "observation outside the grid or with a bad variable/level/pressure");
-            return LETKF_OK;
-        }
+        if (st & LG_ST_BAD_OBS)
+            return set_err(ctx, LETKF_ERR_INVALID,
+                           "observation outside the grid or with a bad variable/level/pressure");
+        fits = !(st & LG_ST_LIST_FULL);
+        if (fits) break;
+        // every cube's length is known now: restart the counters and either
+        // grow the pool to hold all lists or go through windows
+        rc = reset_status(ctx);
+        if (rc) return rc;
         const int64_t need = (int64_t)cnt[LG_CNT_CURSOR];
-        const int64_t cap = need + need / 16 + 1024;
-        ctx->d_lidx.release();
-        ctx->d_lrloc.release();
-        ctx->d_lmeta.release();
-        LG_CUDA(ctx->d_lidx.reserve((size_t)cap));
-        LG_CUDA(ctx->d_lrloc.reserve((size_t)cap));
-        if (ctx->params.precision == LETKF_PREC_MIXED) LG_CUDA(ctx->d_lmeta.reserve((size_t)cap));
-        ctx->list_cap = cap;
-        // the search counters start again; status keeps any obs error
-        LG_CUDA(cudaMemsetAsync(ctx->d_counters.p, 0, sizeof(unsigned long long) * LG_CNT_N,
-                                ctx->stream));
-        unsigned keep = st & LG_ST_BAD_OBS;
-        LG_CUDA(cudaMemcpyAsync(ctx->d_status.p, &keep, sizeof(unsigned), cudaMemcpyHostToDevice,
-                                ctx->stream));
-        LG_CUDA(cudaStreamSynchronize(ctx->stream));
+        const int64_t grown = need + need / 16 + 1024;
+        if (attempt > 0 || grown > limit) break;
+        rc = size_pool(ctx, grown);
+        if (rc) return rc;
     }
-    return set_err(ctx, LETKF_ERR_ALLOC, "local observation lists did not fit");
+    LG_CUDA(cudaEventRecord(ctx->ev[3], ctx->stream));
+    if (fits) {
+        LG_CUDA(launch_core(ctx, xb, axb, xa, axa));
+        ctx->last_windows = 1;
+        ctx->lists_whole = c0 == 0 && c1 == ctx->ncubes;
+        return LETKF_OK;
+    }
+    std::vector<int32_t> need((size_t)(c1 - c0));
+    LG_CUDA(cudaMemcpyAsync(need.data(), ctx->d_lneed.p + c0, sizeof(int32_t) * need.size(),
+                            cudaMemcpyDeviceToHost, ctx->stream));
+    LG_CUDA(cudaStreamSynchronize(ctx->stream));
+    // windows end on multiples of the mixed core's chunk size (so that every
+    // cube keeps its chunk); the pool holds at least the heaviest chunk
+    const int64_t align = ctx->params.precision == LETKF_PREC_MIXED ? lg_run_chunk(ctx) : 1;
+    std::vector<int64_t> unit;   // list entries of each aligned group of cubes
+    for (int64_t c = c0; c < c1;) {
+        const int64_t e = std::min(c1, (c / align + 1) * align);
+        int64_t s = 0;
+        for (int64_t i = c; i < e; i++) s += need[(size_t)(i - c0)];
+        unit.push_back(s);
+        c = e;
+    }
+    int64_t heaviest = 1;
+    for (int64_t s : unit) heaviest = std::max(heaviest, s);
+    rc = size_pool(ctx, std::max(limit, heaviest));
+    if (rc) return rc;
+    std::vector<int64_t> bounds{c0};
+    int64_t acc = 0, at = c0;
+    for (int64_t s : unit) {
+        if (acc + s > ctx->list_cap) {
+            bounds.push_back(at);
+            acc = 0;
+        }
+        acc += s;
+        at = std::min(c1, (at / align + 1) * align);
+    }
+    bounds.push_back(c1);
+    for (size_t w = 0; w + 1 < bounds.size(); w++) {
+        rc = restart_cursors(ctx);
+        if (rc) return rc;
+        ctx->win0 = bounds[w];
+        ctx->win1 = bounds[w + 1];
+        LG_CUDA(launch_search(ctx, od, no));
+        LG_CUDA(launch_core(ctx, xb, axb, xa, axa));
+    }
+    ctx->win0 = c0;
+    ctx->win1 = c1;
+    ctx->last_windows = (int)(bounds.size() - 1);
+    return LETKF_OK;
 }
 
 // The whole analysis on device pointers with no host synchronization, for
@@ -206,22 +318,19 @@ int enqueue_run(letkf_ctx *ctx, const double *xb, const double *axb, const letkf
     rc = stage_obs(ctx, obs, false, od);
     if (rc) return rc;
     const int64_t no = obs->nobs;
-    const LgGrid g = lg_grid(ctx);
-    LG_CUDA(lg_launch_obs_prepare(ctx, g, xb, axb, no, od.lat, od.lon, od.ph, od.lev, od.var, od.yo,
-                                  od.rinv));
-    LG_CUDA(lg_launch_buckets(ctx, no));
-    LG_CUDA(lg_launch_search(ctx, g, no));
-    if (ctx->params.precision == LETKF_PREC_MIXED)
-        LG_CUDA(lg_launch_core_mixed(ctx, g, xb, axb, xa, axa, ctx->d_trans.p != nullptr));
-    else
-        LG_CUDA(lg_launch_core_fp64(ctx, g, xb, axb, xa, axa, ctx->d_trans.p != nullptr));
+    rc = obs_prepare(ctx, xb, axb, od, no);
+    if (rc) return rc;
+    ctx->win0 = ctx->range0;
+    ctx->win1 = ctx->range1;
+    LG_CUDA(launch_search(ctx, od, no));
+    LG_CUDA(launch_core(ctx, xb, axb, xa, axa));
     return LETKF_OK;
 }
 
 void fill_stats(letkf_ctx *ctx, const unsigned long long *cnt)
 {
     letkf_stats &s = ctx->stats;
-    s.ncubes = ctx->ncubes;
+    s.ncubes = ctx->range1 - ctx->range0;
     s.sum_p = (int64_t)cnt[LG_CNT_SUMP];
     s.max_p = (int64_t)cnt[LG_CNT_MAXP];
     s.n_truncated = (int64_t)cnt[LG_CNT_TRUNC];
@@ -231,6 +340,7 @@ void fill_stats(letkf_ctx *ctx, const unsigned long long *cnt)
     s.sum_sweeps = (int64_t)cnt[LG_CNT_SUMSWEEP];
     s.n_ill_conditioned = (int64_t)cnt[LG_CNT_ILLCOND];
     s.sched_chunk = ctx->sched_chunk;
+    s.n_windows = ctx->last_windows;
     s.precision = ctx->params.precision;
 }
 
@@ -276,6 +386,7 @@ LgParams lg_params(letkf_ctx *ctx)
     p.precision = q.precision;
     p.nbj = ctx->nbj;
     p.nbi = ctx->nbi;
+    p.cube0 = ctx->win0;
     return p;
 }
 
@@ -351,6 +462,8 @@ int letkf_gpu_create(letkf_ctx **out, const letkf_grid *grid, const letkf_params
     ctx->nbj = (G.nlat + P.cube_n - 1) / P.cube_n;
     ctx->nbi = (G.nlon + P.cube_n - 1) / P.cube_n;
     ctx->ncubes = (int64_t)ctx->nbj * ctx->nbi;
+    ctx->range0 = ctx->win0 = 0;
+    ctx->range1 = ctx->win1 = ctx->ncubes;
     ctx->have_hybrid = G.hyai && G.hybi;
 
     int rc = LETKF_OK;
@@ -382,6 +495,7 @@ int letkf_gpu_create(letkf_ctx **out, const letkf_grid *grid, const letkf_params
         LG_CUDA(ctx->d_bstart.reserve(nb + 1));
         LG_CUDA(ctx->d_loff.reserve((size_t)ctx->ncubes));
         LG_CUDA(ctx->d_lcnt.reserve((size_t)ctx->ncubes));
+        LG_CUDA(ctx->d_lneed.reserve((size_t)ctx->ncubes));
         LG_CUDA(ctx->d_status.reserve(1));
         LG_CUDA(ctx->d_counters.reserve(LG_CNT_N));
         LG_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -413,6 +527,31 @@ int letkf_gpu_set_keep_trans(letkf_ctx *ctx, int keep)
         ctx->d_trans.release();
         ctx->d_w.release();
     }
+    return LETKF_OK;
+}
+
+int letkf_gpu_set_list_limit(letkf_ctx *ctx, int64_t max_entries)
+{
+    if (!ctx) return LETKF_ERR_INVALID;
+    if (max_entries < 0) return set_err(ctx, LETKF_ERR_INVALID, "negative list limit");
+    ctx->list_limit = max_entries;
+    return LETKF_OK;
+}
+
+int letkf_gpu_set_cube_range(letkf_ctx *ctx, int64_t first, int64_t count)
+{
+    if (!ctx) return LETKF_ERR_INVALID;
+    if (count < 0) {
+        ctx->range0 = 0;
+        ctx->range1 = ctx->ncubes;
+        return LETKF_OK;
+    }
+    if (first < 0 || count < 1 || first > ctx->ncubes - count)
+        return set_err(ctx, LETKF_ERR_INVALID, "cube range outside the grid");
+    if (ctx->params.cube_n > 1 && (first % ctx->nbj != 0 || count % ctx->nbj != 0))
+        return set_err(ctx, LETKF_ERR_INVALID, "with cube_n > 1 the range must be whole longitude strips");
+    ctx->range0 = first;
+    ctx->range1 = first + count;
     return LETKF_OK;
 }
 
@@ -448,23 +587,31 @@ int letkf_gpu_run(letkf_ctx *ctx, const double *xb, const double *axb, const let
     if (rc) return rc;
     LG_CUDA(cudaEventRecord(ctx->ev[1], ctx->stream));
     unsigned long long cnt[LG_CNT_N] = {};
-    rc = obs_and_search(ctx, dxb, daxb, obs, od, cnt);
+    rc = obs_prepare(ctx, dxb, daxb, od, obs->nobs);
     if (rc) return rc;
-    LG_CUDA(cudaEventRecord(ctx->ev[3], ctx->stream));
-    const LgGrid g = lg_grid(ctx);
-    if (ctx->params.precision == LETKF_PREC_MIXED)
-        LG_CUDA(lg_launch_core_mixed(ctx, g, dxb, daxb, dxa, daxa, ctx->d_trans.p != nullptr));
-    else
-        LG_CUDA(lg_launch_core_fp64(ctx, g, dxb, daxb, dxa, daxa, ctx->d_trans.p != nullptr));
+    LG_CUDA(cudaEventRecord(ctx->ev[2], ctx->stream));
+    rc = search_and_core(ctx, dxb, daxb, dxa, daxa, od, obs->nobs, cnt);
+    if (rc) return rc;
     LG_CUDA(cudaEventRecord(ctx->ev[4], ctx->stream));
     if (host) {
-        LG_CUDA(cudaMemcpyAsync(xa, dxa, sizeof(double) * nstate, cudaMemcpyDeviceToHost, ctx->stream));
-        LG_CUDA(cudaMemcpyAsync(axa, daxa, sizeof(double) * nmean, cudaMemcpyDeviceToHost, ctx->stream));
+        // the columns of the analysed cubes: with cube_n 1 the cubes
+        // themselves, else whole longitude strips of them
+        int64_t col0 = ctx->range0, col1 = ctx->range1;
+        if (ctx->params.cube_n > 1) {
+            col0 = ctx->range0 / ctx->nbj * ctx->params.cube_n * ctx->nlat;
+            col1 = std::min<int64_t>(ctx->range1 / ctx->nbj * ctx->params.cube_n, ctx->nlon) * ctx->nlat;
+        }
+        const size_t per_s = (size_t)ctx->n * ctx->k, per_m = (size_t)ctx->n;
+        LG_CUDA(cudaMemcpyAsync(xa + col0 * per_s, dxa + col0 * per_s, sizeof(double) * (col1 - col0) * per_s,
+                                cudaMemcpyDeviceToHost, ctx->stream));
+        LG_CUDA(cudaMemcpyAsync(axa + col0 * per_m, daxa + col0 * per_m, sizeof(double) * (col1 - col0) * per_m,
+                                cudaMemcpyDeviceToHost, ctx->stream));
     }
     LG_CUDA(cudaEventRecord(ctx->ev[5], ctx->stream));
     unsigned st = 0;
     rc = read_status(ctx, st, cnt);
     if (rc) return rc;
+    if (st & LG_ST_LIST_FULL) return set_err(ctx, LETKF_ERR_ALLOC, "local observation lists did not fit");
     fill_stats(ctx, cnt);
     ctx->stats.ms_h2d = elapsed(ctx->ev[0], ctx->ev[1]);
     ctx->stats.ms_obs = elapsed(ctx->ev[1], ctx->ev[2]);
@@ -528,6 +675,8 @@ int letkf_gpu_local_obs(letkf_ctx *ctx, int64_t *offsets, int32_t *idx, double *
 {
     if (!ctx || !offsets) return LETKF_ERR_INVALID;
     if (!ctx->have_run) return set_err(ctx, LETKF_ERR_STATE, "no run yet");
+    if (!ctx->lists_whole)
+        return set_err(ctx, LETKF_ERR_STATE, "the last run kept no complete lists (cube windows or a cube range)");
     const int64_t nc = ctx->ncubes;
     std::vector<int64_t> off(nc);
     std::vector<int32_t> cnt(nc);

@@ -83,7 +83,7 @@ k_core_fp64(LgGrid g, LgParams prm, RowSrc src, const int64_t *__restrict__ loff
         lg_decode_block(bok[m] ? b : 0, bi[m], bj[m]);
     }
 
-    for (int64_t cube = blockIdx.x; cube < ncubes; cube += gridDim.x) {
+    for (int64_t cube = prm.cube0 + blockIdx.x; cube < ncubes; cube += gridDim.x) {
         const int64_t off = loff[cube];
         const int p = lcnt[cube];
 
@@ -290,35 +290,38 @@ k_core_fp64(LgGrid g, LgParams prm, RowSrc src, const int64_t *__restrict__ loff
 
 template <int K>
 cudaError_t launch_k(letkf_ctx *ctx, const LgGrid &g, const RowSrc &src, const int64_t *loff,
-                     const int32_t *lcnt, int64_t ncubes, const double *xb, const double *axb,
+                     const int32_t *lcnt, int64_t cube0, int64_t ncubes, const double *xb, const double *axb,
                      double *xa, double *axa, double *trans_out, double *w_out)
 {
     const size_t smem = Cfg<K>::SMEM;
     cudaError_t e = cudaFuncSetAttribute(k_core_fp64<K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return e;
-    if (ncubes <= 0) return cudaSuccess;
-    const unsigned blocks = (unsigned)(ncubes < (1 << 30) ? ncubes : (1 << 30));
+    if (ncubes <= cube0) return cudaSuccess;
+    const int64_t nwin = ncubes - cube0;
+    const unsigned blocks = (unsigned)(nwin < (1 << 30) ? nwin : (1 << 30));
+    LgParams prm = lg_params(ctx);
+    prm.cube0 = cube0;
     lg_count_launch();
-    k_core_fp64<K><<<blocks, kT, smem, ctx->stream>>>(g, lg_params(ctx), src, loff, lcnt, ncubes, xb,
+    k_core_fp64<K><<<blocks, kT, smem, ctx->stream>>>(g, prm, src, loff, lcnt, ncubes, xb,
                                                       axb, xa, axa, trans_out, w_out,
                                                       ctx->d_counters.p, ctx->d_status.p);
     return cudaGetLastError();
 }
 
 cudaError_t dispatch(letkf_ctx *ctx, const LgGrid &g, const RowSrc &src, const int64_t *loff,
-                     const int32_t *lcnt, int64_t ncubes, const double *xb, const double *axb,
+                     const int32_t *lcnt, int64_t cube0, int64_t ncubes, const double *xb, const double *axb,
                      double *xa, double *axa, double *trans_out, double *w_out)
 {
     switch (g.k) {
-    case 32: return launch_k<32>(ctx, g, src, loff, lcnt, ncubes, xb, axb, xa, axa, trans_out, w_out);
-    case 48: return launch_k<48>(ctx, g, src, loff, lcnt, ncubes, xb, axb, xa, axa, trans_out, w_out);
-    case 64: return launch_k<64>(ctx, g, src, loff, lcnt, ncubes, xb, axb, xa, axa, trans_out, w_out);
-    case 96: return launch_k<96>(ctx, g, src, loff, lcnt, ncubes, xb, axb, xa, axa, trans_out, w_out);
-    case 128: return launch_k<128>(ctx, g, src, loff, lcnt, ncubes, xb, axb, xa, axa, trans_out, w_out);
-    case 4: return launch_k<4>(ctx, g, src, loff, lcnt, ncubes, xb, axb, xa, axa, trans_out, w_out);
-    case 8: return launch_k<8>(ctx, g, src, loff, lcnt, ncubes, xb, axb, xa, axa, trans_out, w_out);
-    case 16: return launch_k<16>(ctx, g, src, loff, lcnt, ncubes, xb, axb, xa, axa, trans_out, w_out);
+    case 32: return launch_k<32>(ctx, g, src, loff, lcnt, cube0, ncubes, xb, axb, xa, axa, trans_out, w_out);
+    case 48: return launch_k<48>(ctx, g, src, loff, lcnt, cube0, ncubes, xb, axb, xa, axa, trans_out, w_out);
+    case 64: return launch_k<64>(ctx, g, src, loff, lcnt, cube0, ncubes, xb, axb, xa, axa, trans_out, w_out);
+    case 96: return launch_k<96>(ctx, g, src, loff, lcnt, cube0, ncubes, xb, axb, xa, axa, trans_out, w_out);
+    case 128: return launch_k<128>(ctx, g, src, loff, lcnt, cube0, ncubes, xb, axb, xa, axa, trans_out, w_out);
+    case 4: return launch_k<4>(ctx, g, src, loff, lcnt, cube0, ncubes, xb, axb, xa, axa, trans_out, w_out);
+    case 8: return launch_k<8>(ctx, g, src, loff, lcnt, cube0, ncubes, xb, axb, xa, axa, trans_out, w_out);
+    case 16: return launch_k<16>(ctx, g, src, loff, lcnt, cube0, ncubes, xb, axb, xa, axa, trans_out, w_out);
     default: return cudaErrorInvalidValue;
     }
 }
@@ -340,7 +343,7 @@ cudaError_t lg_launch_core_fp64(letkf_ctx *ctx, const LgGrid &g, const double *x
     src.rinvf = ctx->d_rinvf.p;
     src.lidx = ctx->d_lidx.p;
     src.lrloc = ctx->d_lrloc.p;
-    return dispatch(ctx, g, src, ctx->d_loff.p, ctx->d_lcnt.p, ctx->ncubes, xb, axb, xa, axa,
+    return dispatch(ctx, g, src, ctx->d_loff.p, ctx->d_lcnt.p, ctx->win0, ctx->win1, xb, axb, xa, axa,
                     keep_trans ? ctx->d_trans.p : nullptr, keep_trans ? ctx->d_w.p : nullptr);
 }
 
@@ -356,7 +359,7 @@ cudaError_t lg_launch_core_batch_fp64(letkf_ctx *ctx, int64_t nb, const int64_t 
     src.bdep = d_dep;
     src.brloc = d_rloc;
     LgGrid g = lg_grid(ctx);
-    return dispatch(ctx, g, src, d_off, ctx->d_lcnt.p, nb, nullptr, nullptr, nullptr, nullptr,
+    return dispatch(ctx, g, src, d_off, ctx->d_lcnt.p, 0, nb, nullptr, nullptr, nullptr, nullptr,
                     d_trans, d_w);
 }
 

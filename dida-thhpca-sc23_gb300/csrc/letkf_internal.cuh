@@ -128,6 +128,7 @@ struct LgParams {
     double local_dist, vert_dist, inflation, obs_polar;
     int gc_filter, gc_filter_vertical, max_obs, cube_n, cube_nz, overlap, h_mode, precision;
     int nbj, nbi;         // cube counts along lat and lon
+    int64_t cube0;        // first cube of the launch's window
 };
 
 // Lat-lon bucket grid of the observations.
@@ -191,6 +192,8 @@ struct letkf_ctx {
     int nlat = 0, nlon = 0, nz = 0, nvar2d = 0, nvar3d = 0, k = 0, n = 0, ps_row = 0;
     double p0 = 0, ptop = 0;
     int64_t ncol = 0, ncubes = 0;
+    int64_t win0 = 0, win1 = 0;       // cube window of the current search and core launches
+    int64_t range0 = 0, range1 = 0;   // cubes a run analyses (letkf_gpu_set_cube_range)
     int nbj = 0, nbi = 0;
     bool have_hybrid = false;
 
@@ -219,7 +222,11 @@ struct letkf_ctx {
     DevBuf<int32_t> d_lidx;
     DevBuf<double> d_lrloc;
     DevBuf<float2> d_lmeta;       // mixed form: (sqrt(rloc), sqrt(rdiaginv rloc) dep) per entry
+    DevBuf<int32_t> d_lneed;      // each cube's list length from the last search
     int64_t list_cap = 0;
+    int64_t list_limit = 0;       // most list entries the pool may hold (0: from free memory)
+    bool lists_whole = false;     // the pool holds every cube's list of the last run
+    int last_windows = 0;         // cube windows of the last run
     // decomposed observation sets (letkf_decomp.cu)
     int dec_nx = 0, dec_ny = 0, dec_nchunk = 0;
     DevBuf<double> d_dec_box;                    // lat0[nx], lat1[nx], lon0[ny], lon1[ny]
@@ -275,6 +282,7 @@ cudaError_t lg_launch_core_mixed(letkf_ctx *ctx, const LgGrid &g, const double *
 cudaError_t lg_launch_core_mixed_wide(letkf_ctx *ctx, const LgGrid &g, const double *xb, const double *axb,
                                       double *xa, double *axa, double *trans_out, double *w_out);
 cudaError_t lg_build_chunk_queue(letkf_ctx *ctx, int &chunk, int &nchunks);
+int lg_run_chunk(const letkf_ctx *ctx);
 cudaError_t lg_launch_core_batch_fp64(letkf_ctx *ctx, int64_t nb, const int64_t *d_off,
                                       const double *d_hx, const float *d_rdi,
                                       const double *d_dep, const double *d_rloc,

@@ -199,8 +199,11 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
     const int ck = s_chunk;
     __syncthreads();
     if (ck < 0) break;
-    const int cube_begin = ck * chunk;
-    const int cube_end = (int)min(ncubes, (int64_t)cube_begin + chunk);
+    // chunks are aligned to multiples of `chunk` in cube numbering; the
+    // first and last chunk of a window may be partial
+    const int64_t chunk_at = prm.cube0 / chunk * chunk + (int64_t)ck * chunk;
+    const int cube_begin = (int)max(chunk_at, prm.cube0);
+    const int cube_end = (int)min(ncubes, chunk_at + chunk);
     bool have_prev = false;
     for (int cube = cube_begin; cube < cube_end; cube++) {
         const int64_t off = loff[cube];
@@ -714,9 +717,10 @@ constexpr int kQueueMax = 8192;      // chunks one queue-building CTA sorts in s
 // chunk's cubes (p0: the per-cube work that does not grow with p, in
 // observation equivalents), sorted heaviest first (bitonic, one CTA).
 __global__ void __launch_bounds__(1024)
-k_chunk_queue(const int32_t *__restrict__ lcnt, int64_t ncubes, int chunk, int nchunks, int p0,
+k_chunk_queue(const int32_t *__restrict__ lcnt, int64_t win0, int64_t win1, int chunk, int nchunks, int p0,
               int *__restrict__ queue)
 {
+    const int64_t base = win0 / chunk * chunk;
     extern __shared__ unsigned long long qkeys[];
     int np2 = 1;
     while (np2 < nchunks) np2 <<= 1;
@@ -724,7 +728,8 @@ k_chunk_queue(const int32_t *__restrict__ lcnt, int64_t ncubes, int chunk, int n
         unsigned long long key = 0ull;
         if (i < nchunks) {
             unsigned long long w = 0;
-            const int64_t c0 = (int64_t)i * chunk, c1 = min(ncubes, c0 + chunk);
+            const int64_t c0 = max(win0, base + (int64_t)i * chunk);
+            const int64_t c1 = min(win1, base + (int64_t)(i + 1) * chunk);
             for (int64_t c = c0; c < c1; c++) w += (unsigned long long)(lcnt[c] + p0);
             key = (w << 32) | (unsigned)i;
         }
@@ -751,14 +756,28 @@ k_chunk_queue(const int32_t *__restrict__ lcnt, int64_t ncubes, int chunk, int n
 
 }  // namespace
 
-// Build the mixed core's work queue for the cubes of the last search: chunks
-// of `chunk` consecutive cubes (the context's schedule, 16 by default, grown
-// until at most kQueueMax chunks), heaviest first, into ctx->d_queue.
+// Cubes per work-queue chunk for the run's cube range: the context's
+// schedule (16 by default), grown until any window of the range takes at most
+// kQueueMax chunks.  One size for every window of a run keeps each cube's
+// chunk (and so its eigenvector warm start) the same however the range is
+// windowed.
+int lg_run_chunk(const letkf_ctx *ctx)
+{
+    const int64_t n = ctx->range1 - ctx->range0;
+    int chunk = ctx->sched_chunk > 0 ? ctx->sched_chunk : 16;
+    while ((n + chunk - 1) / chunk + 1 > kQueueMax) chunk *= 2;
+    return chunk;
+}
+
+// Build the mixed core's work queue for the cubes of the last search (the
+// window win0 .. win1 - 1): the chunks of lg_run_chunk cubes that meet the
+// window (aligned to multiples of the chunk size in cube numbering), heaviest
+// first, into ctx->d_queue.
 cudaError_t lg_build_chunk_queue(letkf_ctx *ctx, int &chunk, int &nchunks)
 {
-    chunk = ctx->sched_chunk > 0 ? ctx->sched_chunk : 16;
-    while ((ctx->ncubes + chunk - 1) / chunk > kQueueMax) chunk *= 2;
-    nchunks = (int)((ctx->ncubes + chunk - 1) / chunk);
+    chunk = lg_run_chunk(ctx);
+    const int64_t base = ctx->win0 / chunk * chunk;
+    nchunks = (int)((ctx->win1 - base + chunk - 1) / chunk);
     cudaError_t e = ctx->d_queue.reserve((size_t)nchunks);
     if (e != cudaSuccess) return e;
     int np2 = 1;
@@ -767,7 +786,7 @@ cudaError_t lg_build_chunk_queue(letkf_ctx *ctx, int &chunk, int &nchunks)
     e = cudaFuncSetAttribute(k_chunk_queue, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)qsmem);
     if (e != cudaSuccess) return e;
     lg_count_launch();
-    k_chunk_queue<<<1, 1024, qsmem, ctx->stream>>>(ctx->d_lcnt.p, ctx->ncubes, chunk, nchunks,
+    k_chunk_queue<<<1, 1024, qsmem, ctx->stream>>>(ctx->d_lcnt.p, ctx->win0, ctx->win1, chunk, nchunks,
                                                    ctx->sched_p0 > 0 ? ctx->sched_p0 : 4400, ctx->d_queue.p);
     return cudaGetLastError();
 }
@@ -782,7 +801,7 @@ cudaError_t launch_mixed(letkf_ctx *ctx, const LgGrid &g, const double *xb, cons
     cudaError_t e = cudaFuncSetAttribute(k_core_mixed<K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return e;
-    if (ctx->ncubes <= 0) return cudaSuccess;
+    if (ctx->win1 <= ctx->win0) return cudaSuccess;
     e = cudaFuncSetAttribute(k_core_mixed<K>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     if (e != cudaSuccess) return e;
     int dev = 0, nsm = 0, smem_sm = 0;
@@ -803,7 +822,7 @@ cudaError_t launch_mixed(letkf_ctx *ctx, const LgGrid &g, const double *xb, cons
     k_core_mixed<K><<<blocks, kT, smem, ctx->stream>>>(
         g, lg_params(ctx), ctx->d_ys32.p, ctx->d_lidx.p, ctx->d_lmeta.p, ctx->d_queue.p, nchunks, chunk,
         ctx->d_loff.p, ctx->d_lcnt.p,
-        ctx->ncubes, xb, axb, xa, axa, trans_out, w_out,
+        ctx->win1, xb, axb, xa, axa, trans_out, w_out,
         ctx->d_counters.p, ctx->d_status.p);
     return cudaGetLastError();
 }

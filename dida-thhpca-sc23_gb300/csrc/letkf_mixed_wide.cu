@@ -123,8 +123,11 @@ k_core_mixed_wide(LgGrid g, LgParams prm, const float *__restrict__ ys32, const 
     const int ck = s_chunk;
     __syncthreads();
     if (ck < 0) break;
-    const int cube_begin = ck * chunk;
-    const int cube_end = (int)min(ncubes, (int64_t)cube_begin + chunk);
+    // chunks are aligned to multiples of `chunk` in cube numbering; the
+    // first and last chunk of a window may be partial
+    const int64_t chunk_at = prm.cube0 / chunk * chunk + (int64_t)ck * chunk;
+    const int cube_begin = (int)max(chunk_at, prm.cube0);
+    const int cube_end = (int)min(ncubes, chunk_at + chunk);
     bool have_prev = false;
     for (int cube = cube_begin; cube < cube_end; cube++) {
         const int64_t off = loff[cube];
@@ -610,7 +613,7 @@ cudaError_t launch_wide(letkf_ctx *ctx, const LgGrid &g, const double *xb, const
     cudaError_t e = cudaFuncSetAttribute(k_core_mixed_wide<K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return e;
-    if (ctx->ncubes <= 0) return cudaSuccess;
+    if (ctx->win1 <= ctx->win0) return cudaSuccess;
     int dev = 0, nsm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
@@ -622,7 +625,7 @@ cudaError_t launch_wide(letkf_ctx *ctx, const LgGrid &g, const double *xb, const
     lg_count_launch();
     k_core_mixed_wide<K><<<blocks, kTW, smem, ctx->stream>>>(
         g, lg_params(ctx), ctx->d_ys32.p, ctx->d_lidx.p, ctx->d_lmeta.p, ctx->d_queue.p, nchunks, chunk,
-        ctx->d_loff.p, ctx->d_lcnt.p, ctx->ncubes, xb, axb, xa, axa, trans_out, w_out, ctx->d_counters.p,
+        ctx->d_loff.p, ctx->d_lcnt.p, ctx->win1, xb, axb, xa, axa, trans_out, w_out, ctx->d_counters.p,
         ctx->d_status.p);
     return cudaGetLastError();
 }

@@ -137,6 +137,7 @@ __device__ void bitonic_sort(int32_t *keys, int n_pow2)
 struct LgListMeta {
     const float *ef;          // sqrt(rdiaginv) dep per obs (mixed form)
     float2 *meta;             // out, mixed form only
+    int32_t *need;            // out: each cube's list length, written even when the pool is full
 };
 
 // One list entry: the obs index and its localization weight (the reference's
@@ -172,9 +173,11 @@ __device__ __forceinline__ void write_entry(int o, long long at, const CubeGeo &
 // the caller synchronizes before reading *s_off).
 __device__ __forceinline__ void reserve_list(int nout, bool truncated, int64_t cube, int64_t list_cap,
                                              int64_t *__restrict__ loff, int32_t *__restrict__ lcnt,
+                                             int32_t *__restrict__ need,
                                              unsigned long long *__restrict__ counters,
                                              unsigned *__restrict__ status, long long *s_off)
 {
+    need[cube] = nout;
     long long off = (long long)atomicAdd(&counters[LG_CNT_CURSOR], (unsigned long long)nout);
     if (off + nout > list_cap) {
         atomicOr(status, LG_ST_LIST_FULL);
@@ -197,7 +200,8 @@ __device__ void write_list(const int32_t *keys, int nout, bool truncated, int64_
                            int32_t *__restrict__ lcnt, unsigned long long *__restrict__ counters,
                            unsigned *__restrict__ status, long long *s_off)
 {
-    if (threadIdx.x == 0) reserve_list(nout, truncated, cube, list_cap, loff, lcnt, counters, status, s_off);
+    if (threadIdx.x == 0)
+        reserve_list(nout, truncated, cube, list_cap, loff, lcnt, lm.need, counters, status, s_off);
     __syncthreads();
     const long long off = *s_off;
     if (off >= 0)
@@ -280,7 +284,7 @@ k_search(LgGrid g, LgParams prm, LgSearchGeo sgeo, LgBuckets bk, LgObsGeo geo, L
     __shared__ CubeGeo s_cg;
     __shared__ long long s_off;
 
-    for (int64_t cube = blockIdx.x; cube < ncubes; cube += gridDim.x) {
+    for (int64_t cube = prm.cube0 + blockIdx.x; cube < ncubes; cube += gridDim.x) {
         if (threadIdx.x == 0) {
             float clat, clon;
             const CubeGeo cg = cube_geo(g, prm, sgeo, cube, clat, clon);
@@ -349,7 +353,7 @@ k_search_bitmap(LgGrid g, LgParams prm, LgSearchGeo sgeo, LgBuckets bk, LgObsGeo
     const int w0 = min(nw, (int)threadIdx.x * per), w1 = min(nw, w0 + per);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
-    for (int64_t cube = blockIdx.x; cube < ncubes; cube += gridDim.x) {
+    for (int64_t cube = prm.cube0 + blockIdx.x; cube < ncubes; cube += gridDim.x) {
         for (int w = threadIdx.x; w < nw; w += kThreads) bits[w] = 0u;
         if (threadIdx.x == 0) {
             float clat, clon;
@@ -392,7 +396,8 @@ k_search_bitmap(LgGrid g, LgParams prm, LgSearchGeo sgeo, LgBuckets bk, LgObsGeo
         }
         const int nout = min(total, prm.max_obs);
         if (threadIdx.x == 0)
-            reserve_list(nout, total > prm.max_obs, cube, list_cap, loff, lcnt, counters, status, &s_off);
+            reserve_list(nout, total > prm.max_obs, cube, list_cap, loff, lcnt, lm.need, counters, status,
+                         &s_off);
         __syncthreads();
         const long long off = s_off;
         if (off >= 0) {
@@ -438,7 +443,7 @@ k_search_dec(LgGrid g, LgParams prm, LgSearchGeo sgeo, LgObsGeo geo, LgListMeta 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int max_obs = prm.max_obs;
 
-    for (int64_t cube = blockIdx.x; cube < ncubes; cube += gridDim.x) {
+    for (int64_t cube = prm.cube0 + blockIdx.x; cube < ncubes; cube += gridDim.x) {
         if (threadIdx.x == 0) {
             float clat, clon;
             s_cg = cube_geo(g, prm, sgeo, cube, clat, clon);
@@ -507,7 +512,8 @@ cudaError_t lg_launch_search(letkf_ctx *ctx, const LgGrid &g, int64_t nobs)
     bk.idx = ctx->d_bidx.p;
     bk.xyz = ctx->d_bxyz.p;
     LgObsGeo geo{ctx->d_os.p, ctx->d_oc.p, ctx->d_oyr.p, ctx->d_oxyz.p};
-    const int64_t blocks = ctx->ncubes < (1 << 30) ? ctx->ncubes : (1 << 30);
+    const int64_t nwin = ctx->win1 - ctx->win0;
+    const int64_t blocks = nwin < (1 << 30) ? nwin : (1 << 30);
     const size_t bitmap_bytes = sizeof(uint32_t) * (size_t)((nobs + 31) / 32 > 0 ? (nobs + 31) / 32 : 1);
     if (bitmap_bytes <= kBitmapMaxBytes) {
         cudaError_t e = cudaFuncSetAttribute(k_search_bitmap, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -515,9 +521,9 @@ cudaError_t lg_launch_search(letkf_ctx *ctx, const LgGrid &g, int64_t nobs)
         if (e != cudaSuccess) return e;
         lg_count_launch();
         k_search_bitmap<<<(unsigned)(blocks > 0 ? blocks : 1), kThreads, bitmap_bytes, ctx->stream>>>(
-            g, prm, lg_search_geo(ctx), bk, geo, LgListMeta{ctx->d_oef.p, ctx->d_lmeta.p}, nobs, ctx->d_lidx.p,
+            g, prm, lg_search_geo(ctx), bk, geo, LgListMeta{ctx->d_oef.p, ctx->d_lmeta.p, ctx->d_lneed.p}, nobs, ctx->d_lidx.p,
             ctx->d_lrloc.p, ctx->list_cap, ctx->d_loff.p, ctx->d_lcnt.p, ctx->d_counters.p, ctx->d_status.p,
-            ctx->ncubes);
+            ctx->win1);
         return cudaGetLastError();
     }
     const int cap = lg_search_cap(prm.max_obs);
@@ -526,8 +532,8 @@ cudaError_t lg_launch_search(letkf_ctx *ctx, const LgGrid &g, int64_t nobs)
     if (e != cudaSuccess) return e;
     lg_count_launch();
     k_search<<<(unsigned)(blocks > 0 ? blocks : 1), kThreads, smem, ctx->stream>>>(
-        g, prm, lg_search_geo(ctx), bk, geo, LgListMeta{ctx->d_oef.p, ctx->d_lmeta.p}, nobs, cap, ctx->d_lidx.p, ctx->d_lrloc.p, ctx->list_cap, ctx->d_loff.p,
-        ctx->d_lcnt.p, ctx->d_counters.p, ctx->d_status.p, ctx->ncubes);
+        g, prm, lg_search_geo(ctx), bk, geo, LgListMeta{ctx->d_oef.p, ctx->d_lmeta.p, ctx->d_lneed.p}, nobs, cap, ctx->d_lidx.p, ctx->d_lrloc.p, ctx->list_cap, ctx->d_loff.p,
+        ctx->d_lcnt.p, ctx->d_counters.p, ctx->d_status.p, ctx->win1);
     return cudaGetLastError();
 }
 
@@ -539,12 +545,13 @@ cudaError_t lg_launch_search_dec(letkf_ctx *ctx, const LgGrid &g, const double *
     const size_t smem = sizeof(int32_t) * cap;
     cudaError_t e = cudaFuncSetAttribute(k_search_dec, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    const int64_t blocks = ctx->ncubes < (1 << 30) ? ctx->ncubes : (1 << 30);
+    const int64_t nwin = ctx->win1 - ctx->win0;
+    const int64_t blocks = nwin < (1 << 30) ? nwin : (1 << 30);
     lg_count_launch();
     k_search_dec<<<(unsigned)(blocks > 0 ? blocks : 1), kThreads, smem, ctx->stream>>>(
-        g, prm, lg_search_geo(ctx), geo, LgListMeta{ctx->d_oef.p, ctx->d_lmeta.p}, olat, ctx->dec_ny, ctx->dec_nchunk, ctx->d_dec_row_blk.p, ctx->d_dec_col_blk.p,
+        g, prm, lg_search_geo(ctx), geo, LgListMeta{ctx->d_oef.p, ctx->d_lmeta.p, ctx->d_lneed.p}, olat, ctx->dec_ny, ctx->dec_nchunk, ctx->d_dec_row_blk.p, ctx->d_dec_col_blk.p,
         ctx->d_dec_slot_off.p, ctx->d_dec_slot_blk.p, ctx->d_dec_pos.p, ctx->d_dec_obs.p, ctx->d_lidx.p,
         ctx->d_lrloc.p, ctx->list_cap, ctx->d_loff.p, ctx->d_lcnt.p, ctx->d_counters.p, ctx->d_status.p,
-        ctx->ncubes);
+        ctx->win1);
     return cudaGetLastError();
 }

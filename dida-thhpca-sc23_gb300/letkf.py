@@ -44,7 +44,7 @@ EXPORTED = [
     "letkf_gpu_last_error", "letkf_gpu_destroy", "letkf_gpu_launch_count",
     "letkf_gpu_core_batch_noalloc", "letkf_decomp_dims", "letkf_gpu_autotune",
     "letkf_batch_create", "letkf_batch_launch", "letkf_batch_sync", "letkf_batch_launches",
-    "letkf_batch_destroy",
+    "letkf_batch_destroy", "letkf_gpu_set_list_limit", "letkf_gpu_set_cube_range",
     "letkf_init_gpu_", "letkf_set_obs_gpu_", "letkf_run_gpu_", "letkf_final_gpu_",
 ]
 
@@ -90,7 +90,7 @@ class Stats(C.Structure):
         ("ms_h2d", C.c_double), ("ms_obs", C.c_double), ("ms_search", C.c_double),
         ("ms_core", C.c_double), ("ms_d2h", C.c_double), ("ms_total", C.c_double),
         ("sum_sweeps", C.c_int64), ("n_ill_conditioned", C.c_int64),
-        ("sched_chunk", C.c_int32), ("reserved", C.c_int32),
+        ("sched_chunk", C.c_int32), ("n_windows", C.c_int32),
     ]
 
     def as_dict(self):
@@ -133,6 +133,8 @@ def load_library(path: str = LIB_PATH):
     L.letkf_batch_launches.argtypes = [vp]
     L.letkf_batch_launches.restype = i64
     L.letkf_batch_destroy.argtypes = [vp]
+    L.letkf_gpu_set_list_limit.argtypes = [vp, i64]
+    L.letkf_gpu_set_cube_range.argtypes = [vp, i64, i64]
     _lib = L
     return L
 
@@ -288,6 +290,15 @@ class LetkfGPU:
 
     def keep_trans(self, keep: bool = True):
         self._check(self.L.letkf_gpu_set_keep_trans(self.h, int(keep)), "set_keep_trans")
+
+    def set_list_limit(self, max_entries: int = 0):
+        """Most local-list entries held at once (0: from free memory); runs
+        whose lists exceed it go through consecutive cube windows."""
+        self._check(self.L.letkf_gpu_set_list_limit(self.h, int(max_entries)), "set_list_limit")
+
+    def set_cube_range(self, first: int = 0, count: int = -1):
+        """Analyse only cubes first .. first+count-1 (count < 0: all)."""
+        self._check(self.L.letkf_gpu_set_cube_range(self.h, int(first), int(count)), "set_cube_range")
 
     def run(self, xb, axb, obs, xa=None, axa=None, allow_not_converged=False):
         """Host arrays in, host arrays out (letkf_run)."""

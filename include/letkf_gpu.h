@@ -123,7 +123,8 @@ typedef struct letkf_stats {
     int64_t n_ill_conditioned; /* mixed form: cubes whose A' has lambda_max/lambda_min
                                   above 1e4, where the FP32 eigenpairs lose digits    */
     int32_t sched_chunk;       /* mixed form: cubes per work-queue chunk (0: default 16) */
-    int32_t reserved;
+    int32_t n_windows;         /* consecutive cube windows the run was split into
+                                  (1 when every local list fit the list pool)        */
 } letkf_stats;
 
 /* The lat x lon blocks of a DA group of nranks MPI ranks: MPI_Dims_create(
@@ -151,6 +152,28 @@ int letkf_gpu_set_stream(letkf_ctx *ctx, void *stream);
  * stream (call letkf_gpu_synchronize before reading the outputs).           */
 int letkf_gpu_run(letkf_ctx *ctx, const double *xb, const double *axb, const letkf_obs *obs,
                   double *xa, double *axa, int flags);
+
+/* Most local-list entries (obs of one cube's list) the list pool may hold;
+ * 0 (the default) sizes it from the device's free memory.  When the lists of
+ * all analysed cubes do not fit, a run searches and analyses the cubes in
+ * consecutive windows whose lists fit (letkf_stats.n_windows), with the same
+ * results; letkf_gpu_local_obs then has no lists to return.  No counterpart
+ * in the reference, whose ranks each hold their own sub-domain's lists.     */
+int letkf_gpu_set_list_limit(letkf_ctx *ctx, int64_t max_entries);
+
+/* Analyse only cubes first .. first+count-1 (count < 0: every cube), as one
+ * DA rank analyses its own sub-domain (letkf_run's nx x ny arrays,
+ * letkf.F90:169-176); cube = lat block + (lat blocks) * lon block, so with
+ * cube_n 1 the cubes are the columns.  The observation operator still reads
+ * the whole background.  Columns of other cubes are not written (host
+ * pointers: not copied back).  With cube_n > 1, first and count must be
+ * multiples of the number of lat blocks (whole longitude strips).  The local
+ * lists of a range run are not kept for letkf_gpu_local_obs.  The mixed form
+ * warm-starts each cube's eigensolve from the cube before it in the same
+ * work-queue chunk, so a range that cuts a chunk starts that chunk's first
+ * cube cold (results then agree with a whole run to FP32 eigensolve
+ * precision); windows never cut a chunk.                                     */
+int letkf_gpu_set_cube_range(letkf_ctx *ctx, int64_t first, int64_t count);
 
 /* Keep (1) or drop (0) every cube's trans and w of the following runs in
  * device memory (ncubes * ens * (ens+1) doubles) for letkf_gpu_last_trans. */
