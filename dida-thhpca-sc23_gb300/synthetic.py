@@ -281,9 +281,26 @@ def _make_obs(rng, glat, glon, nz, hyai, hybi, truth, nobs, boxes=(), box_factor
     return dict(lat=lat, lon=lon, ph=ph, lev=lev, var=var, yo=yo, rinv=rinv)
 
 
+def _members_on_device(basis, coef2d, device, chunk_cols=1 << 16):
+    """xb = basis @ coef as a float64 torch tensor [ncol][n*k] on `device`,
+    built a block of columns at a time (the host never holds the ensemble)."""
+    import torch
+    ncol = basis.shape[0]
+    coef_d = torch.from_numpy(np.ascontiguousarray(coef2d)).to(device)
+    xb = torch.empty((ncol, coef2d.shape[1]), dtype=torch.float64, device=device)
+    for c0 in range(0, ncol, chunk_cols):
+        c1 = min(ncol, c0 + chunk_cols)
+        b = torch.from_numpy(np.ascontiguousarray(basis[c0:c1])).to(device)
+        torch.matmul(b, coef_d, out=xb[c0:c1])
+    return xb
+
+
 def generate(name, res_deg, nz, k, nobs, loc_dist_km, inflation, seed,
-             boxes=(), box_factor=1.0, lmax_noise=12, noise_len_km=2000.0):
-    """Build one analysis instance (see the module docstring for the recipe)."""
+             boxes=(), box_factor=1.0, lmax_noise=12, noise_len_km=2000.0, device=None):
+    """Build one analysis instance (see the module docstring for the recipe).
+    With a torch `device` the members xb are built there (a torch float64
+    tensor [ncol][n][k]) from the same random draws, for ensembles larger than
+    host memory; everything else stays on the host."""
     rng = np.random.Generator(np.random.PCG64(seed))
     glat, glon = make_grid(res_deg)
     hyai, hybi = hybrid_coefficients(nz)
@@ -301,7 +318,11 @@ def generate(name, res_deg, nz, k, nobs, loc_dist_km, inflation, seed,
     coef = rng.standard_normal((basis_t.shape[0], n, k))
     coef -= coef.mean(axis=2, keepdims=True)      # sample mean removed (linear)
     coef *= spec[:, None, None] * std[None, :, None]
-    xb = (basis_t.T @ coef.reshape(basis_t.shape[0], n * k)).reshape(ncol, n, k)
+    if device is None:
+        xb = (basis_t.T @ coef.reshape(basis_t.shape[0], n * k)).reshape(ncol, n, k)
+    else:
+        xb = _members_on_device(basis, coef.reshape(basis_t.shape[0], n * k), device).view(ncol, n, k)
+    del basis, basis_t
     obs = _make_obs(rng, glat, glon, nz, hyai, hybi, truth, nobs, boxes, box_factor)
     return Workload(name=name, glat=glat, glon=glon, nz=nz, k=k, hyai=hyai, hybi=hybi,
                     xb=xb, axb=axb, truth=truth, obs=obs, loc_dist_km=loc_dist_km,
@@ -320,10 +341,18 @@ INSTANCES_3 = [  # (res_deg, k, nobs, radius_km, inflation)
 ]
 
 
-def config(cfg: int, instance: int = 0, nobs: int | None = None, res_deg: float | None = None):
-    """Workload of a benchmark configuration (0, 1, 2 and the instances of 3).
-    nobs overrides the observation count and res_deg the grid spacing (smaller
-    cases with the same observation density, e.g. for profiling)."""
+def config(cfg: int, instance: int = 0, nobs: int | None = None, res_deg: float | None = None,
+           device=None):
+    """Workload of a benchmark configuration (0, 1, 2, the instances of 3, and
+    4).  nobs overrides the observation count and res_deg the grid spacing
+    (smaller cases with the same observation density when both are scaled,
+    e.g. for profiling).  device: build the members on this torch device
+    (configuration 4's ensemble, 103 GB in float64, is built only there)."""
+    if cfg == 4:
+        res = res_deg or 0.25
+        no = nobs if nobs is not None else int(round(4_000_000 * (0.25 / res) ** 2))
+        return generate("cfg4", res, 32, 128, no, 250.0, 1.05, 4000, boxes=CLUSTERS_4,
+                        box_factor=10.0, device=device)
     seed = 1000 * cfg + instance
     if cfg == 0:
         return generate("cfg0", res_deg or 2.0, 32, 32, nobs or 20_000, 500.0, 1.1, seed)
