@@ -208,11 +208,21 @@ int restart_cursors(letkf_ctx *ctx)
     return LETKF_OK;
 }
 
+// The list length of every cube of the run's range from the last search.
+int read_need(letkf_ctx *ctx, std::vector<int32_t> &need)
+{
+    need.resize((size_t)(ctx->range1 - ctx->range0));
+    LG_CUDA(cudaMemcpyAsync(need.data(), ctx->d_lneed.p + ctx->range0, sizeof(int32_t) * need.size(),
+                            cudaMemcpyDeviceToHost, ctx->stream));
+    LG_CUDA(cudaStreamSynchronize(ctx->stream));
+    return LETKF_OK;
+}
+
 // Local lists and the analysis of cubes range0 .. range1-1.  One search over
 // the range gives every cube's list length; when the lists fit the pool (grown
 // up to the limit if needed) one core launch follows, else the range is cut
 // into consecutive windows whose lists fit and each window is searched again
-// and analysed.  ev[3] is recorded after the first search.
+// and analysed.  ev[3] is recorded after the first search (or count).
 int search_and_core(letkf_ctx *ctx, const double *xb, const double *axb, double *xa, double *axa,
                     const ObsDev &od, int64_t no, unsigned long long *cnt)
 {
@@ -229,9 +239,18 @@ int search_and_core(letkf_ctx *ctx, const double *xb, const double *axb, double 
     ctx->lists_whole = false;
     ctx->win0 = c0;
     ctx->win1 = c1;
+    // a run after one that needed windows counts first: one pass that only
+    // counts gives every list length, so no full search fills a pool that is
+    // too small
+    const bool count_first = ctx->last_windows > 1;
+    std::vector<int32_t> need;
     bool fits = false;
     for (int attempt = 0; attempt < 2; attempt++) {
-        LG_CUDA(launch_search(ctx, od, no));
+        ctx->count_pass = count_first && attempt == 0;
+        const cudaError_t e = launch_search(ctx, od, no);
+        const bool counted = ctx->count_pass;
+        ctx->count_pass = false;
+        LG_CUDA(e);
         unsigned st = 0;
         rc = read_status(ctx, st, cnt);
         if (rc) return rc;
@@ -240,17 +259,23 @@ int search_and_core(letkf_ctx *ctx, const double *xb, const double *axb, double 
         if (st & LG_ST_BAD_OBS)
             return set_err(ctx, LETKF_ERR_INVALID,
                            "observation outside the grid or with a bad variable/level/pressure");
-        fits = !(st & LG_ST_LIST_FULL);
+        fits = !counted && !(st & LG_ST_LIST_FULL);
         if (fits) break;
         // every cube's length is known now: restart the counters and either
         // grow the pool to hold all lists or go through windows
         rc = reset_status(ctx);
         if (rc) return rc;
-        const int64_t need = (int64_t)cnt[LG_CNT_CURSOR];
-        const int64_t grown = need + need / 16 + 1024;
-        if (attempt > 0 || grown > limit) break;
-        rc = size_pool(ctx, grown);
+        int64_t total = (int64_t)cnt[LG_CNT_CURSOR];
+        if (counted) {
+            rc = read_need(ctx, need);
+            if (rc) return rc;
+            total = 0;
+            for (int32_t v : need) total += v;
+        }
+        if (attempt > 0 || total > limit) break;
+        rc = size_pool(ctx, std::min(limit, total + total / 16 + 1024));
         if (rc) return rc;
+        need.clear();
     }
     LG_CUDA(cudaEventRecord(ctx->ev[3], ctx->stream));
     if (fits) {
@@ -259,10 +284,10 @@ int search_and_core(letkf_ctx *ctx, const double *xb, const double *axb, double 
         ctx->lists_whole = c0 == 0 && c1 == ctx->ncubes;
         return LETKF_OK;
     }
-    std::vector<int32_t> need((size_t)(c1 - c0));
-    LG_CUDA(cudaMemcpyAsync(need.data(), ctx->d_lneed.p + c0, sizeof(int32_t) * need.size(),
-                            cudaMemcpyDeviceToHost, ctx->stream));
-    LG_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (need.empty()) {
+        rc = read_need(ctx, need);
+        if (rc) return rc;
+    }
     // windows end on multiples of the mixed core's chunk size (so that every
     // cube keeps its chunk); the pool holds at least the heaviest chunk
     const int64_t align = ctx->params.precision == LETKF_PREC_MIXED ? lg_run_chunk(ctx) : 1;
@@ -387,6 +412,7 @@ LgParams lg_params(letkf_ctx *ctx)
     p.nbj = ctx->nbj;
     p.nbi = ctx->nbi;
     p.cube0 = ctx->win0;
+    p.count_only = ctx->count_pass ? 1 : 0;
     return p;
 }
 

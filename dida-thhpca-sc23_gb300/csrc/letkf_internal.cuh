@@ -129,6 +129,7 @@ struct LgParams {
     int gc_filter, gc_filter_vertical, max_obs, cube_n, cube_nz, overlap, h_mode, precision;
     int nbj, nbi;         // cube counts along lat and lon
     int64_t cube0;        // first cube of the launch's window
+    int count_only;       // search: only each cube's list length (LgListMeta::need)
 };
 
 // Lat-lon bucket grid of the observations.
@@ -227,6 +228,7 @@ struct letkf_ctx {
     int64_t list_limit = 0;       // most list entries the pool may hold (0: from free memory)
     bool lists_whole = false;     // the pool holds every cube's list of the last run
     int last_windows = 0;         // cube windows of the last run
+    bool count_pass = false;      // the next search only counts (lg_params.count_only)
     // decomposed observation sets (letkf_decomp.cu)
     int dec_nx = 0, dec_ny = 0, dec_nchunk = 0;
     DevBuf<double> d_dec_box;                    // lat0[nx], lat1[nx], lon0[ny], lon1[ny]

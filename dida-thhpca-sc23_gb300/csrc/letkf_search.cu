@@ -14,13 +14,18 @@
 //      memory (k_search_bitmap, up to 786,432 obs), every kept obs sets its
 //      bit and one ordered pass over the bitmap lists them by index; above
 //      that (k_search), kept indices are sorted in shared memory (bitonic),
-//      and if more are kept than shared memory holds, a threshold search
-//      finds the max_obs-th smallest index; lists stop at max_obs;
+//      and if more are kept than shared memory holds, a histogram of the kept
+//      indices by their high bits (2048 bins, filled in the first pass) gives
+//      the bin of the max_obs-th smallest index, and a second pass collects
+//      the indices up to that bin (a threshold search inside the bin when
+//      even those overflow shared memory); lists stop at max_obs;
 //   4. the localization weight of every kept obs is computed with the
 //      reference's double formula (FP32 from the chord for the mixed form)
 //      and the list is written at a slot reserved with one atomic add.
 // The decomposed observation sets (k_search_dec) scan the blocks of the
-// cube's neighbour set instead of the buckets.
+// cube's neighbour set instead of the buckets.  A count-only launch
+// (LgParams::count_only) writes each cube's list length and nothing else:
+// the first step of a run whose lists are cut into windows.
 #include <climits>
 
 #include "letkf_internal.cuh"
@@ -30,6 +35,7 @@ namespace {
 constexpr int kMaxSeg = 128;
 constexpr int kThreads = 256;
 constexpr size_t kBitmapMaxBytes = 96 * 1024;   // obs-index bitmap of k_search_bitmap (786,432 obs)
+constexpr int kHistBins = 2048;                   // k_search: kept indices by high bits
 
 struct Seg {
     int b, e, exact;   // [b, e) in bucket order; exact: skip the float prefilter
@@ -87,12 +93,14 @@ __device__ __forceinline__ bool keep_candidate(const float4 &p, int exact, const
 }
 
 // One pass over all candidate segments.
-//   mode 0: append every kept index (up to cap) and count them
+//   mode 0: append every kept index (up to cap), count them and, with hist,
+//           count them by bin o >> shift
 //   mode 1: count kept indices below `thr`
 //   mode 2: append kept indices below `thr`
 __device__ int scan_pass(int mode, int thr, const Seg *seg, int ns, const LgBuckets &bk,
                          const CubeGeo &cg, const LgObsGeo &geo, const LgParams &prm,
-                         int32_t *keys, int cap, int *s_count, unsigned long long *border)
+                         int32_t *keys, int cap, int *s_count, unsigned long long *border,
+                         int *hist = nullptr, int shift = 0)
 {
     if (threadIdx.x == 0) *s_count = 0;
     __syncthreads();
@@ -105,12 +113,46 @@ __device__ int scan_pass(int mode, int thr, const Seg *seg, int ns, const LgBuck
             if (!keep_candidate(p, s.exact, cg, geo, prm, mode == 0 ? border : nullptr)) continue;
             const int pos = atomicAdd(s_count, 1);
             if (mode != 1 && pos < cap) keys[pos] = o;
+            if (hist) atomicAdd(&hist[o >> shift], 1);
         }
     }
     __syncthreads();
     const int c = *s_count;
     __syncthreads();
     return c;
+}
+
+// The bin where the running count of hist[0..kHistBins) reaches target
+// (the total is at least target >= 1) and the count up to and including it.
+__device__ void hist_select(const int *hist, int target, int *s_bin, int *s_through, int *s_warp)
+{
+    constexpr int per = kHistBins / kThreads;
+    const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+    int loc = 0;
+#pragma unroll
+    for (int i = 0; i < per; i++) loc += hist[t * per + i];
+    int incl = loc;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    if (lane == 31) s_warp[warp] = incl;
+    __syncthreads();
+    int before = incl - loc;
+    for (int w = 0; w < warp; w++) before += s_warp[w];
+    if (before < target && before + loc >= target) {
+        int run = before;
+        for (int i = 0; i < per; i++) {
+            run += hist[t * per + i];
+            if (run >= target) {
+                *s_bin = t * per + i;
+                *s_through = run;
+                break;
+            }
+        }
+    }
+    __syncthreads();
 }
 
 __device__ void bitonic_sort(int32_t *keys, int n_pow2)
@@ -278,13 +320,18 @@ k_search(LgGrid g, LgParams prm, LgSearchGeo sgeo, LgBuckets bk, LgObsGeo geo, L
          int64_t *__restrict__ loff, int32_t *__restrict__ lcnt,
          unsigned long long *__restrict__ counters, unsigned *__restrict__ status, int64_t ncubes)
 {
-    extern __shared__ int32_t keys[];
+    extern __shared__ int32_t keys[];   // cap_sort keys, then kHistBins bins
+    int *hist = keys + cap_sort;
     __shared__ Seg seg[kMaxSeg];
-    __shared__ int s_ns, s_count;
+    __shared__ int s_ns, s_count, s_bin, s_through;
+    __shared__ int s_warp[kThreads / 32];
     __shared__ CubeGeo s_cg;
     __shared__ long long s_off;
+    int shift = 0;
+    while (((nobs - 1) >> shift) >= kHistBins) shift++;
 
     for (int64_t cube = prm.cube0 + blockIdx.x; cube < ncubes; cube += gridDim.x) {
+        for (int i = threadIdx.x; i < kHistBins; i += kThreads) hist[i] = 0;
         if (threadIdx.x == 0) {
             float clat, clon;
             const CubeGeo cg = cube_geo(g, prm, sgeo, cube, clat, clon);
@@ -298,7 +345,12 @@ k_search(LgGrid g, LgParams prm, LgSearchGeo sgeo, LgBuckets bk, LgObsGeo geo, L
         const CubeGeo cg = s_cg;
 
         int nk = scan_pass(0, 0, seg, ns, bk, cg, geo, prm, keys, cap_sort, &s_count,
-                           &counters[LG_CNT_BORDER]);
+                           &counters[LG_CNT_BORDER], hist, shift);
+        if (prm.count_only) {
+            if (threadIdx.x == 0) lm.need[cube] = min(nk, prm.max_obs);
+            __syncthreads();
+            continue;
+        }
         int nout;
         if (nk <= cap_sort) {
             int np2 = 1;
@@ -308,8 +360,16 @@ k_search(LgGrid g, LgParams prm, LgSearchGeo sgeo, LgBuckets bk, LgObsGeo geo, L
             bitonic_sort(keys, np2);
             nout = min(nk, prm.max_obs);
         } else {
-            // smallest threshold T with max_obs kept indices below it
-            int lo = 1, hi = (int)nobs;
+            // the histogram bin that holds the max_obs-th smallest kept index
+            hist_select(hist, prm.max_obs, &s_bin, &s_through, s_warp);
+            const int bin = s_bin;
+            const int thr = (int)min((int64_t)(bin + 1) << shift, nobs);
+            int lo = thr, hi = thr;
+            if (s_through > cap_sort) {
+                // even the indices up to that bin overflow: the smallest
+                // threshold T inside the bin with max_obs kept indices below it
+                lo = (bin << shift) + 1;
+            }
             while (lo < hi) {
                 const int mid = lo + (hi - lo) / 2;
                 const int c = scan_pass(1, mid, seg, ns, bk, cg, geo, prm, keys, cap_sort, &s_count,
@@ -395,6 +455,11 @@ k_search_bitmap(LgGrid g, LgParams prm, LgSearchGeo sgeo, LgBuckets bk, LgObsGeo
             total += s_warp[w];
         }
         const int nout = min(total, prm.max_obs);
+        if (prm.count_only) {
+            if (threadIdx.x == 0) lm.need[cube] = nout;
+            __syncthreads();
+            continue;
+        }
         if (threadIdx.x == 0)
             reserve_list(nout, total > prm.max_obs, cube, list_cap, loff, lcnt, lm.need, counters, status,
                          &s_off);
@@ -485,8 +550,12 @@ k_search_dec(LgGrid g, LgParams prm, LgSearchGeo sgeo, LgObsGeo geo, LgListMeta 
                 __syncthreads();
             }
         }
-        write_list(keys, min(n, max_obs), n >= max_obs, cube, cg, geo, prm, lm, lidx, lrloc, list_cap, loff,
-                   lcnt, counters, status, &s_off);
+        if (prm.count_only) {
+            if (threadIdx.x == 0) lm.need[cube] = min(n, max_obs);
+        } else {
+            write_list(keys, min(n, max_obs), n >= max_obs, cube, cg, geo, prm, lm, lidx, lrloc, list_cap,
+                       loff, lcnt, counters, status, &s_off);
+        }
         __syncthreads();
     }
 }
@@ -527,7 +596,7 @@ cudaError_t lg_launch_search(letkf_ctx *ctx, const LgGrid &g, int64_t nobs)
         return cudaGetLastError();
     }
     const int cap = lg_search_cap(prm.max_obs);
-    const size_t smem = sizeof(int32_t) * cap;
+    const size_t smem = sizeof(int32_t) * (cap + kHistBins);
     cudaError_t e = cudaFuncSetAttribute(k_search, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     lg_count_launch();

@@ -228,6 +228,27 @@ def test_search_without_the_bitmap(letkf, synthetic, loc_km):
         assert_fields(xa, xa_o, w)
 
 
+
+def test_search_threshold_inside_a_histogram_bin(letkf, synthetic):
+    # more than 786,432 obs, indexed by distance from one column (after 100
+    # far ones): that column's kept indices fill whole bins of the search's
+    # index histogram, so the bin holding its max_obs-th kept index runs past
+    # the key buffer (2048 keys for max_obs 2000) and the threshold search
+    # inside that bin is taken; other columns take the plain histogram path
+    w = synthetic.generate("binfill", 7.5, 1, 4, 800_000, 1500.0, 1.1, 10, lmax_noise=4)
+    lat0, lon0 = np.deg2rad(float(w.glat[10])), np.deg2rad(float(w.glon[20]))
+    la, lo = np.deg2rad(w.obs["lat"]), np.deg2rad(w.obs["lon"])
+    cosd = np.sin(la) * np.sin(lat0) + np.cos(la) * np.cos(lat0) * np.cos(lo - lon0)
+    by_dist = np.argsort(-cosd, kind="stable")
+    order = np.concatenate([by_dist[-100:], by_dist[:-100]])
+    for key in w.obs:
+        w.obs[key] = np.ascontiguousarray(w.obs[key][order])
+    w.max_obs = 2000
+    ctx = letkf.LetkfGPU.from_workload(w)
+    ctx.run(w.xb, w.axb, w.obs)
+    assert ctx.stats()["n_truncated"] > 0
+    compare_lists(ctx, O.Oracle(w))
+
 def test_bad_observation_is_rejected(letkf, synthetic):
     w = synthetic.small_case(nlat=8, nlon=16, nz=2, k=8, nobs=50, seed=3)
     w.obs["lat"] = w.obs["lat"].copy()
