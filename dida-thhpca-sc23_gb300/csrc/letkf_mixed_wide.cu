@@ -28,6 +28,22 @@ namespace {
 
 constexpr int kTW = 256;
 
+// Optional per-phase cycle counts of CTA 0 (built with -DLG_PHASE_CLOCKS).
+#ifdef LG_PHASE_CLOCKS
+#define LGW_PHASE(i)                                                 \
+    do {                                                             \
+        if (tid == 0) {                                              \
+            const long long now_ = clock64();                        \
+            ph_cyc[i] += now_ - ph_last;                             \
+            ph_last = now_;                                          \
+        }                                                            \
+    } while (0)
+#else
+#define LGW_PHASE(i) \
+    do {             \
+    } while (0)
+#endif
+
 constexpr size_t r1024(size_t b) { return (b + 1023) & ~(size_t)1023; }
 constexpr size_t zmax(size_t a, size_t b) { return a > b ? a : b; }
 
@@ -114,6 +130,10 @@ k_core_mixed_wide(LgGrid g, LgParams prm, const float *__restrict__ ys32, const 
         return ok != 0;
     };
 
+#ifdef LG_PHASE_CLOCKS
+    long long ph_cyc[7] = {0, 0, 0, 0, 0, 0, 0};
+    long long ph_last = clock64();
+#endif
     for (;;) {
     if (tid == 0) {
         const unsigned long long q = atomicAdd(&counters[LG_CNT_QUEUE], 1ull);
@@ -132,6 +152,7 @@ k_core_mixed_wide(LgGrid g, LgParams prm, const float *__restrict__ ys32, const 
     for (int cube = cube_begin; cube < cube_end; cube++) {
         const int64_t off = loff[cube];
         const int p = lcnt[cube];
+        LGW_PHASE(6);
 
         // ---------------- phase 1: A and g on the tensor cores ----------------------
         // rows K..127 and 130+K..TROWS-1 of both tiles stay zero
@@ -249,6 +270,7 @@ k_core_mixed_wide(LgGrid g, LgParams prm, const float *__restrict__ ys32, const 
             break;
         }
         lg_tc_fence_after();
+        LGW_PHASE(0);
 
         // ---------------- phase 2: A = 0.5 (S + S^T), S = HH + 2 LH; g -------------------
         float *S = reinterpret_cast<float *>(RA);
@@ -324,6 +346,7 @@ k_core_mixed_wide(LgGrid g, LgParams prm, const float *__restrict__ ys32, const 
             }
         }
         __syncthreads();
+        LGW_PHASE(1);
 
         // ---------------- phase 3: FP32 Jacobi -> X (columns of W32) --------------------
         int sw;
@@ -334,6 +357,7 @@ k_core_mixed_wide(LgGrid g, LgParams prm, const float *__restrict__ ys32, const 
             atomicAdd(&counters[LG_CNT_SUMSWEEP], (unsigned long long)sw);
             if (sw > 24) atomicAdd(&counters[LG_CNT_NOTCONV], 1ull);
         }
+        LGW_PHASE(2);
         float *ilam32 = reinterpret_cast<float *>(misc);
         float *hc32 = ilam32 + K, *r32 = hc32 + 2 * K;
         for (int j = warp; j < K; j += kTW / 32) {
@@ -402,6 +426,8 @@ k_core_mixed_wide(LgGrid g, LgParams prm, const float *__restrict__ ys32, const 
                 __syncthreads();
             }
         }
+
+        LGW_PHASE(3);
 
         // ---------------- phase 5: T in FP32 ------------------------------------------------
         {
@@ -480,6 +506,8 @@ k_core_mixed_wide(LgGrid g, LgParams prm, const float *__restrict__ ys32, const 
             }
             if (tid < K) w_out[(int64_t)cube * K + tid] = wbar[tid];
         }
+
+        LGW_PHASE(4);
 
         // ---------------- phase 6: xa = xb^T (T + wbar 1^T) -------------------------------
         // T tiles (B operand, N = K rows) along members: hi tiles 0, 1 then lo tiles 0, 1
@@ -593,9 +621,16 @@ k_core_mixed_wide(LgGrid g, LgParams prm, const float *__restrict__ ys32, const 
             }
         if (failed) break;
         have_prev = true;
+        LGW_PHASE(5);
     }
     if (failed) break;
     }
+#ifdef LG_PHASE_CLOCKS
+    if (blockIdx.x == 0 && tid == 0)
+        printf("wide phase cycles cta0: A-build %lld, A'-form %lld, jacobi32 %lld, X/wbar %lld, T %lld, "
+               "update %lld, loop %lld\n",
+               ph_cyc[0], ph_cyc[1], ph_cyc[2], ph_cyc[3], ph_cyc[4], ph_cyc[5], ph_cyc[6]);
+#endif
     if (failed && tid == 0) atomicOr(status, LG_ST_TIMEOUT);
     cp_async_wait<0>();
     for (int b = 0; b < 3; b++) wait_bar(b);
