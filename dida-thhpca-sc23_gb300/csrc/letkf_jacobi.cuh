@@ -46,6 +46,32 @@ __device__ __forceinline__ void lg_rotation(float al, float be, float gam, float
     s = c * t;
 }
 
+// Packed pairs of FP32 (the f32x2 arithmetic of sm_100 and later): two
+// independent IEEE single-precision operations per instruction.
+__device__ __forceinline__ unsigned long long lg_pk2(float a, float b)
+{
+    unsigned long long r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ void lg_upk2(unsigned long long r, float &a, float &b)
+{
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(a), "=f"(b) : "l"(r));
+}
+__device__ __forceinline__ unsigned long long lg_ffma2(unsigned long long a, unsigned long long b,
+                                                       unsigned long long c)
+{
+    unsigned long long d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+__device__ __forceinline__ unsigned long long lg_fmul2(unsigned long long a, unsigned long long b)
+{
+    unsigned long long d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+
 __device__ __forceinline__ void lg_decode_block(int b, int &bi, int &bj)
 {
     int i = (int)((sqrtf(8.0f * (float)b + 1.0f) - 1.0f) * 0.5f);
@@ -293,23 +319,27 @@ __device__ int lg_jacobi32(float *W, float *nrm, int *s_rot, float tol, float to
 // down to pairs: K/2 + K/4 + ... + 1 = K-1 steps cover every pair once per
 // sweep, as the round-robin ordering does.  Columns are stored back into W
 // (column j at W[j*LD ..]) after every level.  The moving columns pass through
-// buffers that reuse W's memory while the columns live in registers.
+// buffers that reuse W's memory while the columns live in registers (slot
+// stride BS: with G = 4 lanes two slots share a quarter-warp of 16-byte
+// accesses, so BS = K + 16 puts them on disjoint bank halves); their norms and
+// ids go to `extra` (4 * (K/2) words; by default right after the buffers).
+// The inner products and rotations use packed f32x2 arithmetic.
 // Returns the sweeps used, or max_sweeps+1 if not converged.
-template <int K, int G, int LD>
-__device__ int lg_jacobi32h(float *W, int *s_rot, float tol, int max_sweeps)
+template <int K, int G, int LD, int BS = K>
+__device__ int lg_jacobi32h(float *W, int *s_rot, float tol, int max_sweeps, float *extra = nullptr)
 {
     constexpr int NS = K / 2, RPL = K / G;
     constexpr int VW = (RPL % 4 == 0) ? 4 : ((RPL % 2 == 0) ? 2 : 1);
     constexpr int NC = RPL / VW;
     static_assert((K & (K - 1)) == 0, "K must be a power of two");
-    static_assert(K % G == 0 && LD % VW == 0, "rows per lane");
-    static_assert(2 * NS * K + 2 * NS + 2 * NS <= K * LD, "moving-column buffers must fit in W");
+    static_assert(K % G == 0 && LD % VW == 0 && BS % VW == 0 && RPL % 2 == 0, "rows per lane");
+    static_assert(2 * NS * BS <= K * LD, "moving-column buffers must fit in W");
     const int tid = threadIdx.x;
     const int slot = tid / G, lane = tid % G;
     const bool act = slot < NS;
     const float tol2 = tol * tol;
-    float *buf = W;                                   // [2][NS][K] moving rows
-    float *bnrm = W + 2 * NS * K;                      // [2][NS] their squared norms
+    float *buf = W;                                   // [2][NS] moving columns, stride BS
+    float *bnrm = extra ? extra : W + 2 * NS * BS;     // [2][NS] their squared norms
     int *bid = reinterpret_cast<int *>(bnrm + 2 * NS);  // [2][NS] their column ids
     float F[RPL], M[RPL];
 
@@ -338,13 +368,16 @@ __device__ int lg_jacobi32h(float *W, int *s_rot, float tol, int max_sweeps)
         }
     };
     auto dot = [&](const float *x, const float *y) {
-        float d0 = 0.0f, d1 = 0.0f;
+        unsigned long long a0 = 0ull, a1 = 0ull;
 #pragma unroll
-        for (int i = 0; i < RPL; i += 2) {
-            d0 = fmaf(x[i], y[i], d0);
-            if (i + 1 < RPL) d1 = fmaf(x[i + 1], y[i + 1], d1);
+        for (int i = 0; i < RPL; i += 4) {
+            a0 = lg_ffma2(lg_pk2(x[i], x[i + 1]), lg_pk2(y[i], y[i + 1]), a0);
+            if (i + 3 < RPL) a1 = lg_ffma2(lg_pk2(x[i + 2], x[i + 3]), lg_pk2(y[i + 2], y[i + 3]), a1);
         }
-        float d = d0 + d1;
+        float p0, p1, p2, p3;
+        lg_upk2(a0, p0, p1);
+        lg_upk2(a1, p2, p3);
+        float d = (p0 + p1) + (p2 + p3);
 #pragma unroll
         for (int o = G / 2; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
         return d;
@@ -374,11 +407,12 @@ __device__ int lg_jacobi32h(float *W, int *s_rot, float tol, int max_sweeps)
                     if (gam * gam > tol2 * (fa * mb)) {
                         float c, s, tt;
                         lg_rotation(fa, mb, gam, c, s, tt);
+                        const unsigned long long c2 = lg_pk2(c, c), s2 = lg_pk2(s, s), ns2 = lg_pk2(-s, -s);
 #pragma unroll
-                        for (int r = 0; r < RPL; r++) {
-                            const float x = F[r], y = M[r];
-                            F[r] = c * x - s * y;
-                            M[r] = s * x + c * y;
+                        for (int r = 0; r < RPL; r += 2) {
+                            const unsigned long long x = lg_pk2(F[r], F[r + 1]), y = lg_pk2(M[r], M[r + 1]);
+                            lg_upk2(lg_ffma2(c2, x, lg_fmul2(ns2, y)), F[r], F[r + 1]);
+                            lg_upk2(lg_ffma2(s2, x, lg_fmul2(c2, y)), M[r], M[r + 1]);
                         }
                         fa = fa - tt * gam;
                         mb = mb + tt * gam;
@@ -389,7 +423,7 @@ __device__ int lg_jacobi32h(float *W, int *s_rot, float tol, int max_sweeps)
                 // pass the moving column to the previous slot of the group
                 const int par = t & 1;
                 if (act) {
-                    st(buf + (par * NS + slot) * K, M);
+                    st(buf + (par * NS + slot) * BS, M);
                     if (lane == 0) {
                         bnrm[par * NS + slot] = mb;
                         bid[par * NS + slot] = mc;
@@ -398,7 +432,7 @@ __device__ int lg_jacobi32h(float *W, int *s_rot, float tol, int max_sweeps)
                 __syncthreads();
                 if (act) {
                     const int src = u * half + (i + 1) % half;
-                    ld(buf + (par * NS + src) * K, M);
+                    ld(buf + (par * NS + src) * BS, M);
                     mb = bnrm[par * NS + src];
                     mc = bid[par * NS + src];
                 }

@@ -61,12 +61,15 @@ struct WCfg {
     static constexpr int NB = K + 16;                    // A-build N: Yhat_hi, e_hi, e_lo, zeros
     static constexpr int TROWS = (128 + NB > 256) ? 128 + NB : 256;
     static constexpr int TILE = TROWS * 128;
-    static constexpr int LDW = K + 4;                    // Jacobi column stride
+    // Jacobi column stride and moving-buffer stride: K + 16 puts the two slots
+    // of a quarter-warp on disjoint bank halves (hierarchical ordering)
+    static constexpr int LDW = ((K & (K - 1)) == 0) ? K + 16 : K + 4;
+    static constexpr int JEXTRA = 2 * K;                 // moving-column norms and ids after W
     static constexpr int LDS = K + 1;                    // S staging row stride
     static constexpr size_t STAGE = (size_t)CH * K * sizeof(float);
     static constexpr size_t TBSUB = (size_t)K * 128;     // one T tile along members (K rows)
     static constexpr size_t RV = r1024((size_t)K * K * sizeof(float));
-    static constexpr size_t RA = r1024(zmax(zmax((size_t)K * LDW, (size_t)K * LDS) * sizeof(float), 4 * TBSUB));
+    static constexpr size_t RA = r1024(zmax(zmax((size_t)K * LDW + JEXTRA, (size_t)K * LDS) * sizeof(float), 4 * TBSUB));
     static constexpr size_t RB = r1024(zmax(zmax((size_t)K * K * sizeof(float), 65536),
                                             2 * TILE + 2 * STAGE > RA ? 2 * TILE + 2 * STAGE - RA : 0));
     static constexpr size_t VEC = sizeof(double) * (4 * K + 128) + sizeof(float) * (2 * K) +
@@ -350,7 +353,8 @@ k_core_mixed_wide(LgGrid g, LgParams prm, const float *__restrict__ ys32, const 
 
         // ---------------- phase 3: FP32 Jacobi -> X (columns of W32) --------------------
         int sw;
-        if constexpr ((K & (K - 1)) == 0) sw = lg_jacobi32h<K, C::G, C::LDW>(W32, &s_rot, LG_MIXED_JACOBI_TOL, 24);
+        if constexpr ((K & (K - 1)) == 0)
+            sw = lg_jacobi32h<K, C::G, C::LDW, C::LDW>(W32, &s_rot, LG_MIXED_JACOBI_TOL, 24, W32 + K * C::LDW);
         else sw = lg_jacobi32<K, C::G, C::LDW>(W32, nrm32, &s_rot, LG_MIXED_JACOBI_TOL, LG_MIXED_JACOBI_TOL, 24);
         if (tid == 0) {
             atomicMax(&counters[LG_CNT_MAXSWEEP], (unsigned long long)sw);
