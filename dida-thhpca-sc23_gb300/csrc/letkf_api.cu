@@ -143,6 +143,10 @@ int obs_prepare(letkf_ctx *ctx, const double *xb, const double *axb, const ObsDe
                                   od.rinv));
     LG_CUDA(lg_launch_buckets(ctx, no));
     if (ctx->dec_nx > 0) LG_CUDA(lg_launch_block_members(ctx, no, od.lat, od.lon));
+    if (ctx->params.overlap == 0 && ctx->params.vert_dist > 0.0) {
+        LG_CUDA(ctx->d_olnp.reserve((size_t)std::max<int64_t>(no, 1)));
+        LG_CUDA(lg_launch_obs_lnp(ctx, no, od.ph));
+    }
     return LETKF_OK;
 }
 
@@ -194,6 +198,9 @@ cudaError_t launch_search(letkf_ctx *ctx, const ObsDev &od, int64_t no)
 cudaError_t launch_core(letkf_ctx *ctx, const double *xb, const double *axb, double *xa, double *axa)
 {
     const LgGrid g = lg_grid(ctx);
+    // overlapped cubes: each cube's trans now, the columns' averages after
+    // the last window (lg_launch_overlap_update)
+    if (ctx->params.overlap > 0) return lg_launch_core_fp64(ctx, g, nullptr, nullptr, nullptr, nullptr, true);
     const bool keep = ctx->d_trans.p != nullptr;
     return ctx->params.precision == LETKF_PREC_MIXED ? lg_launch_core_mixed(ctx, g, xb, axb, xa, axa, keep)
                                                      : lg_launch_core_fp64(ctx, g, xb, axb, xa, axa, keep);
@@ -337,6 +344,8 @@ int enqueue_run(letkf_ctx *ctx, const double *xb, const double *axb, const letkf
 {
     if (ctx->dec_nx > 0)
         return set_err(ctx, LETKF_ERR_UNSUPPORTED, "decomposed observation sets are not captured in graphs");
+    if (ctx->params.overlap > 0 || ctx->params.vert_dist > 0.0)
+        return set_err(ctx, LETKF_ERR_UNSUPPORTED, "overlapped cubes and vertical localization are not captured in graphs");
     int rc = reset_status(ctx);
     if (rc) return rc;
     ObsDev od;
@@ -411,6 +420,7 @@ LgParams lg_params(letkf_ctx *ctx)
     p.precision = q.precision;
     p.nbj = ctx->nbj;
     p.nbi = ctx->nbi;
+    p.cube_step = q.cube_n - q.overlap;
     p.cube0 = ctx->win0;
     p.count_only = ctx->count_pass ? 1 : 0;
     return p;
@@ -463,7 +473,8 @@ int letkf_gpu_create(letkf_ctx **out, const letkf_grid *grid, const letkf_params
                        (int64_t)P.decomp_lat_blocks * P.decomp_lon_blocks > 65535))
         return LETKF_ERR_INVALID;
     if (decomposed && P.cube_n != 1) return LETKF_ERR_UNSUPPORTED;
-    if (P.overlap != 0 || P.vert_dist > 0.0) return LETKF_ERR_UNSUPPORTED;
+    // the overlapped-cube and vertical-localization modes run in the FP64 form
+    if ((P.overlap != 0 || P.vert_dist > 0.0) && P.precision != LETKF_PREC_FP64) return LETKF_ERR_UNSUPPORTED;
     if (P.precision == LETKF_PREC_MIXED && !lg_mixed_supports(G.ens)) return LETKF_ERR_UNSUPPORTED;
 
     int ndev = 0;
@@ -485,8 +496,10 @@ int letkf_gpu_create(letkf_ctx **out, const letkf_grid *grid, const letkf_params
     ctx->p0 = G.p0;
     ctx->ptop = G.ptop;
     ctx->ncol = (int64_t)G.nlat * G.nlon;
-    ctx->nbj = (G.nlat + P.cube_n - 1) / P.cube_n;
-    ctx->nbi = (G.nlon + P.cube_n - 1) / P.cube_n;
+    // cubes start every cube_n - overlap points (letkf_compute.F90:150-160)
+    const int step = P.cube_n - P.overlap;
+    ctx->nbj = (G.nlat + step - 1) / step;
+    ctx->nbi = (G.nlon + step - 1) / step;
     ctx->ncubes = (int64_t)ctx->nbj * ctx->nbi;
     ctx->range0 = ctx->win0 = 0;
     ctx->range1 = ctx->win1 = ctx->ncubes;
@@ -546,6 +559,8 @@ int letkf_gpu_set_stream(letkf_ctx *ctx, void *stream)
 int letkf_gpu_set_keep_trans(letkf_ctx *ctx, int keep)
 {
     if (!ctx) return LETKF_ERR_INVALID;
+    if (keep && ctx->params.overlap == 0 && ctx->params.vert_dist > 0.0)
+        return set_err(ctx, LETKF_ERR_UNSUPPORTED, "vertical localization solves one problem per level block");
     if (keep) {
         LG_CUDA(ctx->d_trans.reserve((size_t)ctx->ncubes * ctx->k * ctx->k));
         LG_CUDA(ctx->d_w.reserve((size_t)ctx->ncubes * ctx->k));
@@ -590,6 +605,8 @@ int letkf_gpu_run(letkf_ctx *ctx, const double *xb, const double *axb, const let
         return set_err(ctx, LETKF_ERR_INVALID, "bad flags");
     int rc = check_obs(ctx, obs);
     if (rc) return rc;
+    if (ctx->params.overlap > 0 && (ctx->range0 != 0 || ctx->range1 != ctx->ncubes))
+        return set_err(ctx, LETKF_ERR_UNSUPPORTED, "overlapped cubes average over neighbouring cubes: no cube range");
     LG_CUDA(cudaSetDevice(ctx->device));
     const bool host = flags == LETKF_HOST_PTRS;
     const size_t nstate = (size_t)ctx->ncol * ctx->n * ctx->k, nmean = (size_t)ctx->ncol * ctx->n;
@@ -616,8 +633,13 @@ int letkf_gpu_run(letkf_ctx *ctx, const double *xb, const double *axb, const let
     rc = obs_prepare(ctx, dxb, daxb, od, obs->nobs);
     if (rc) return rc;
     LG_CUDA(cudaEventRecord(ctx->ev[2], ctx->stream));
+    if (ctx->params.overlap > 0) {
+        LG_CUDA(ctx->d_trans.reserve((size_t)ctx->ncubes * ctx->k * ctx->k));
+        LG_CUDA(ctx->d_w.reserve((size_t)ctx->ncubes * ctx->k));
+    }
     rc = search_and_core(ctx, dxb, daxb, dxa, daxa, od, obs->nobs, cnt);
     if (rc) return rc;
+    if (ctx->params.overlap > 0) LG_CUDA(lg_launch_overlap_update(ctx, lg_grid(ctx), dxb, daxb, dxa, daxa));
     LG_CUDA(cudaEventRecord(ctx->ev[4], ctx->stream));
     if (host) {
         // the columns of the analysed cubes: with cube_n 1 the cubes

@@ -18,6 +18,17 @@
 //
 // The reference forms Pa and the k x p matrix Pa*Yhat^T (:129-195); the
 // products here are the same quantities in O(k p + k^3) instead of O(k^2 p).
+//
+// Vertical localization (letkf_compute_nooverlap_vertical,
+// letkf_compute.F90:358-526; gen_yb_dis_vertical and vertical_localization,
+// letkf_yb.F90:137-243): per cube, every block of cube_nz levels solves its
+// own problem with rloc = rloc_h * gc(|ln p_c - ln p_obs| / vert_dist), where
+// ln p_c is the log of the block's centre-level pressure at the cube centre
+// (ps2alnp, obs_make.F90:418-437, from the mean surface pressure), and
+// updates only that block's rows (the 2-D variables with the last block).
+// Overlapped cubes (letkf_compute and xb_add2_xa, letkf_compute.F90:128-228,
+// 304-354): the core writes each cube's trans and k_overlap_update averages
+// the updated columns over the cubes that cover them.
 #include "letkf_internal.cuh"
 #include "letkf_jacobi.cuh"
 
@@ -42,6 +53,7 @@ struct RowSrc {
     bool batch;
     // analysis run: global obs arrays + local lists
     const double *yb, *dep;
+    const double *olnp;         // ln(ph) per obs (vertical localization) or null
     const float *rinvf;
     const int32_t *lidx;
     const double *lrloc;
@@ -83,9 +95,28 @@ k_core_fp64(LgGrid g, LgParams prm, RowSrc src, const int64_t *__restrict__ loff
         lg_decode_block(bok[m] ? b : 0, bi[m], bj[m]);
     }
 
+    const bool vertical = !src.batch && src.olnp != nullptr;
+    const int nvb = vertical ? (g.nz + prm.cube_nz - 1) / prm.cube_nz : 1;
     for (int64_t cube = prm.cube0 + blockIdx.x; cube < ncubes; cube += gridDim.x) {
         const int64_t off = loff[cube];
         const int p = lcnt[cube];
+        const int bjc = (int)(cube % prm.nbj), bic = (int)(cube / prm.nbj);
+        const int sj = bjc * prm.cube_step, ej = min(sj + prm.cube_n - 1, g.nlat - 1);
+        const int si = bic * prm.cube_step, ei = min(si + prm.cube_n - 1, g.nlon - 1);
+        for (int vb = 0; vb < nvb; vb++) {
+        // vertical block vb: levels sk..ek, centre level ck; ln p of the
+        // centre level at the cube centre from the mean surface pressure
+        const int sk = vb * prm.cube_nz, ek = min(sk + prm.cube_nz - 1, g.nz - 1);
+        double alnp = 0.0;
+        if (vertical) {
+            const int ck = ((sk + 1) + (ek + 1)) / 2 - 1;
+            const int cj = ((sj + 1) + (ej + 1)) / 2 - 1, ci = ((si + 1) + (ei + 1)) / 2 - 1;
+            const double ps = axb[(cj + (int64_t)g.nlat * ci) * g.n + g.ps_row];
+            const double pt = g.ptop, dp = g.p0 - g.ptop;
+            const double p_lo = g.hyai[ck] * dp + g.hybi[ck] * (ps - pt) + pt;
+            const double p_hi = g.hyai[ck + 1] * dp + g.hybi[ck + 1] * (ps - pt) + pt;
+            alnp = log(0.5 * (p_lo + p_hi));
+        }
 
         // ---- A = Yhat Yhat^T (lower blocks), g = Yhat (s .* dep)
         double acc[MB][16];
@@ -108,6 +139,10 @@ k_core_fp64(LgGrid g, LgParams prm, RowSrc src, const int64_t *__restrict__ loff
                     rdi = (double)src.rinvf[gi];
                     rl = src.lrloc[li];
                     d = src.dep[gi];
+                    if (vertical) {
+                        const double z = fabs(alnp - src.olnp[gi]) / prm.vert_dist;
+                        rl = rl * (prm.gc_filter_vertical ? lg_schr2(z) : lg_schr(z));
+                    }
                 }
                 const double sc = sqrt(rdi * rl);     // rrloc (letkf_core.F90:64-66)
                 scl[tid] = sc;
@@ -238,17 +273,28 @@ k_core_fp64(LgGrid g, LgParams prm, RowSrc src, const int64_t *__restrict__ loff
         }
 
         // ---- xa = trans^T xb + axb for every column of the cube, then mean removal
+        // (vertical blocks: the rows of the block's levels of each 3-D
+        // variable, and the 2-D variables with the last block)
         const int n = g.n;
-        const int bjc = (int)(cube % prm.nbj), bic = (int)(cube / prm.nbj);
-        const int sj = bjc * prm.cube_n, ej = min(sj + prm.cube_n - 1, g.nlat - 1);
-        const int si = bic * prm.cube_n, ei = min(si + prm.cube_n - 1, g.nlon - 1);
+        const int nruns = vertical ? g.nvar2d + g.nvar3d : 1;
         for (int ii = si; ii <= ei; ii++)
             for (int jj = sj; jj <= ej; jj++) {
                 const int64_t c = jj + (int64_t)g.nlat * ii;
                 const double *xbc = xb + c * n * K;
                 double *xac = xa + c * n * K;
-                for (int r0 = 0; r0 < n; r0 += CH) {
-                    const int R = min(CH, n - r0);
+                for (int run = 0; run < nruns; run++) {
+                int rs = 0, re = n - 1;
+                if (vertical) {
+                    if (run < g.nvar2d) {
+                        if (ek != g.nz - 1) continue;
+                        rs = re = run;
+                    } else {
+                        rs = g.nvar2d + (run - g.nvar2d) * g.nz + sk;
+                        re = g.nvar2d + (run - g.nvar2d) * g.nz + ek;
+                    }
+                }
+                for (int r0 = rs; r0 <= re; r0 += CH) {
+                    const int R = min(CH, re - r0 + 1);
                     for (int idx = tid; idx < R * K; idx += kT) S[idx] = xbc[(int64_t)r0 * K + idx];
                     __syncthreads();
                     double out[C::NO];
@@ -284,8 +330,99 @@ k_core_fp64(LgGrid g, LgParams prm, RowSrc src, const int64_t *__restrict__ loff
                         xac[(int64_t)r0 * K + idx] = S[idx] - sd[idx / K];
                     __syncthreads();
                 }
+                }
             }
+        }
     }
+}
+
+// Overlapped cubes (xb_add2_xa, letkf_compute.F90:304-354, and the final
+// division by the cover count, :206-226): per column, over the cubes that
+// cover it in the reference's loop order (longitude start outer, latitude
+// start inner): dist = axb + xb^T trans, xa += dist - mean(dist),
+// axa += mean(dist); then xa and axa are divided by the number of cubes.
+// One CTA per column; trans (with w, column-major) is staged in shared
+// memory row-major with a padded stride; warps take rows, lanes members.
+template <int K>
+__global__ void __launch_bounds__(kT)
+k_overlap_update(LgGrid g, LgParams prm, const double *__restrict__ trans, const double *__restrict__ xb,
+                 const double *__restrict__ axb, double *__restrict__ xa, double *__restrict__ axa)
+{
+    extern __shared__ double Ts[];               // Ts[l * (K + 1) + e] = trans(l, e)
+    constexpr int LDT = K + 1, PER = (K + 31) / 32;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int n = g.n, step = prm.cube_step, cn = prm.cube_n;
+    const int64_t ncol = (int64_t)g.nlat * g.nlon;
+    for (int64_t c = blockIdx.x; c < ncol; c += gridDim.x) {
+        const int jj = (int)(c % g.nlat), ii = (int)(c / g.nlat);
+        for (int idx = tid; idx < n * K; idx += kT) xa[c * n * K + idx] = 0.0;
+        for (int r = tid; r < n; r += kT) axa[c * n + r] = 0.0;
+        // cube starts i0 (j0) are multiples of step with i0 <= ii <= i0 + cube_n - 1
+        const int i_lo = max(0, (ii - cn + 1 + step - 1) / step), i_hi = ii / step;
+        const int j_lo = max(0, (jj - cn + 1 + step - 1) / step), j_hi = jj / step;
+        int count = 0;
+        for (int bi = i_lo; bi <= i_hi; bi++)
+            for (int bj = j_lo; bj <= j_hi; bj++) {
+                const int64_t cube = bj + (int64_t)prm.nbj * bi;
+                __syncthreads();
+                for (int idx = tid; idx < K * K; idx += kT) {
+                    const int l = idx % K, e = idx / K;
+                    Ts[l * LDT + e] = trans[cube * K * K + idx];
+                }
+                __syncthreads();
+                for (int r = warp; r < n; r += kT / 32) {
+                    const double *x = xb + (c * n + r) * K;
+                    const double ab = axb[c * n + r];
+                    double dist[PER];
+                    double sum = 0.0;
+#pragma unroll
+                    for (int q = 0; q < PER; q++) {
+                        const int e = lane + 32 * q;
+                        double s = 0.0;
+                        if (e < K)
+                            for (int l = 0; l < K; l++) s += x[l] * Ts[l * LDT + e];
+                        dist[q] = ab + s;
+                        if (e < K) sum += dist[q];
+                    }
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+                    const double mean = sum / K;
+#pragma unroll
+                    for (int q = 0; q < PER; q++) {
+                        const int e = lane + 32 * q;
+                        if (e < K) xa[(c * n + r) * K + e] += dist[q] - mean;
+                    }
+                    if (lane == 0) axa[c * n + r] += mean;
+                }
+                count++;
+            }
+        __syncthreads();
+        const double cnt = (double)count;
+        for (int idx = tid; idx < n * K; idx += kT) xa[c * n * K + idx] = xa[c * n * K + idx] / cnt;
+        for (int r = tid; r < n; r += kT) axa[c * n + r] = axa[c * n + r] / cnt;
+        __syncthreads();
+    }
+}
+
+template <int K>
+cudaError_t launch_overlap(letkf_ctx *ctx, const LgGrid &g, const double *xb, const double *axb, double *xa,
+                           double *axa)
+{
+    const size_t smem = sizeof(double) * (size_t)K * (K + 1);
+    cudaError_t e = cudaFuncSetAttribute(k_overlap_update<K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    const int64_t ncol = (int64_t)g.nlat * g.nlon;
+    const unsigned blocks = (unsigned)(ncol < (1 << 30) ? ncol : (1 << 30));
+    lg_count_launch();
+    k_overlap_update<K><<<blocks, kT, smem, ctx->stream>>>(g, lg_params(ctx), ctx->d_trans.p, xb, axb, xa, axa);
+    return cudaGetLastError();
+}
+
+__global__ void k_obs_lnp(int64_t nobs, const double *__restrict__ oph, double *__restrict__ olnp)
+{
+    for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < nobs; o += (int64_t)gridDim.x * blockDim.x)
+        olnp[o] = log(oph[o]);
 }
 
 template <int K>
@@ -343,8 +480,35 @@ cudaError_t lg_launch_core_fp64(letkf_ctx *ctx, const LgGrid &g, const double *x
     src.rinvf = ctx->d_rinvf.p;
     src.lidx = ctx->d_lidx.p;
     src.lrloc = ctx->d_lrloc.p;
+    src.olnp = (ctx->params.overlap == 0 && ctx->params.vert_dist > 0.0) ? ctx->d_olnp.p : nullptr;
     return dispatch(ctx, g, src, ctx->d_loff.p, ctx->d_lcnt.p, ctx->win0, ctx->win1, xb, axb, xa, axa,
                     keep_trans ? ctx->d_trans.p : nullptr, keep_trans ? ctx->d_w.p : nullptr);
+}
+
+cudaError_t lg_launch_overlap_update(letkf_ctx *ctx, const LgGrid &g, const double *xb, const double *axb,
+                                     double *xa, double *axa)
+{
+    switch (g.k) {
+    case 4: return launch_overlap<4>(ctx, g, xb, axb, xa, axa);
+    case 8: return launch_overlap<8>(ctx, g, xb, axb, xa, axa);
+    case 16: return launch_overlap<16>(ctx, g, xb, axb, xa, axa);
+    case 32: return launch_overlap<32>(ctx, g, xb, axb, xa, axa);
+    case 48: return launch_overlap<48>(ctx, g, xb, axb, xa, axa);
+    case 64: return launch_overlap<64>(ctx, g, xb, axb, xa, axa);
+    case 96: return launch_overlap<96>(ctx, g, xb, axb, xa, axa);
+    case 128: return launch_overlap<128>(ctx, g, xb, axb, xa, axa);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t lg_launch_obs_lnp(letkf_ctx *ctx, int64_t nobs, const double *oph)
+{
+    if (nobs <= 0) return cudaSuccess;
+    const int64_t want = (nobs + 255) / 256;
+    const unsigned blocks = (unsigned)(want < 4096 ? want : 4096);
+    lg_count_launch();
+    k_obs_lnp<<<blocks, 256, 0, ctx->stream>>>(nobs, oph, ctx->d_olnp.p);
+    return cudaGetLastError();
 }
 
 cudaError_t lg_launch_core_batch_fp64(letkf_ctx *ctx, int64_t nb, const int64_t *d_off,

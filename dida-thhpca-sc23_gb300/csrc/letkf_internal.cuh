@@ -128,6 +128,7 @@ struct LgParams {
     double local_dist, vert_dist, inflation, obs_polar;
     int gc_filter, gc_filter_vertical, max_obs, cube_n, cube_nz, overlap, h_mode, precision;
     int nbj, nbi;         // cube counts along lat and lon
+    int cube_step;        // grid points between cube starts (cube_n - overlap)
     int64_t cube0;        // first cube of the launch's window
     int count_only;       // search: only each cube's list length (LgListMeta::need)
 };
@@ -205,6 +206,7 @@ struct letkf_ctx {
     DevBuf<double> d_olat, d_olon, d_oph, d_oyo, d_orinv;
     DevBuf<int32_t> d_olev, d_ovar;
     DevBuf<double> d_yb, d_dep;
+    DevBuf<double> d_olnp;        // vertical localization: ln(ph) per obs
     DevBuf<float> d_ys32;         // yb * sqrt(rinv) in FP32 (mixed precision)
     DevBuf<float> d_rinvf;
     DevBuf<float> d_oef;          // mixed form: sqrt(rdiaginv) dep per obs
@@ -275,6 +277,11 @@ cudaError_t lg_decomp_setup(letkf_ctx *ctx, const std::vector<float> &glat_ext,
                             const std::vector<float> &glon_ext);
 cudaError_t lg_launch_block_members(letkf_ctx *ctx, int64_t nobs, const double *olat, const double *olon);
 cudaError_t lg_launch_search_dec(letkf_ctx *ctx, const LgGrid &g, const double *olat);
+// Overlapped cubes: every column's analysis is the average over the cubes
+// that cover it, from the cubes' trans (with w) in ctx->d_trans.
+cudaError_t lg_launch_overlap_update(letkf_ctx *ctx, const LgGrid &g, const double *xb, const double *axb,
+                                     double *xa, double *axa);
+cudaError_t lg_launch_obs_lnp(letkf_ctx *ctx, int64_t nobs, const double *oph);
 cudaError_t lg_launch_core_fp64(letkf_ctx *ctx, const LgGrid &g, const double *xb,
                                 const double *axb, double *xa, double *axa, bool keep_trans);
 cudaError_t lg_launch_core_mixed(letkf_ctx *ctx, const LgGrid &g, const double *xb,

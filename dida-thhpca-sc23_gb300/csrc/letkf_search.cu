@@ -256,8 +256,8 @@ __device__ CubeGeo cube_geo(const LgGrid &g, const LgParams &prm, const LgSearch
                             float &clat, float &clon)
 {
     const int bj = (int)(cube % prm.nbj), bi = (int)(cube / prm.nbj);
-    const int sj = bj * prm.cube_n, ej = min(sj + prm.cube_n - 1, g.nlat - 1);
-    const int si = bi * prm.cube_n, ei = min(si + prm.cube_n - 1, g.nlon - 1);
+    const int sj = bj * prm.cube_step, ej = min(sj + prm.cube_n - 1, g.nlat - 1);
+    const int si = bi * prm.cube_step, ei = min(si + prm.cube_n - 1, g.nlon - 1);
     const int cj = ((sj + 1) + (ej + 1)) / 2 - 1, ci = ((si + 1) + (ei + 1)) / 2 - 1;
     clat = g.glat[cj];
     clon = g.glon[ci];

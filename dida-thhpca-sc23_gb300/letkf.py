@@ -258,7 +258,8 @@ class LetkfGPU:
         self.nlat, self.nlon, self.nz, self.k = self._glat.size, self._glon.size, nz, ens
         self.n = nvar2d + nvar3d * nz
         self.cube_n = cube_n
-        self.ncubes = (-(-self.nlat // cube_n)) * (-(-self.nlon // cube_n))
+        step = cube_n - overlap                  # cubes start every cube_n - overlap points
+        self.ncubes = (-(-self.nlat // step)) * (-(-self.nlon // step))
 
     @classmethod
     def from_workload(cls, w, **kw):
