@@ -596,6 +596,70 @@ int letkf_gpu_set_cube_range(letkf_ctx *ctx, int64_t first, int64_t count)
     return LETKF_OK;
 }
 
+}  // extern "C"
+
+int lg_set_err(letkf_ctx *ctx, int code, const char *msg) { return set_err(ctx, code, msg); }
+int lg_reset_status(letkf_ctx *ctx) { return reset_status(ctx); }
+int lg_read_status(letkf_ctx *ctx, unsigned &status, unsigned long long *cnt)
+{
+    return read_status(ctx, status, cnt);
+}
+
+int lg_check_run(letkf_ctx *ctx, const letkf_obs *obs)
+{
+    int rc = check_obs(ctx, obs);
+    if (rc) return rc;
+    if (ctx->params.overlap > 0 && (ctx->range0 != 0 || ctx->range1 != ctx->ncubes))
+        return set_err(ctx, LETKF_ERR_UNSUPPORTED, "overlapped cubes average over neighbouring cubes: no cube range");
+    return LETKF_OK;
+}
+
+int lg_run_analysis(letkf_ctx *ctx, const letkf_obs *obs, bool host_obs, const double *dxb,
+                    const double *daxb, double *dxa, double *daxa, unsigned long long *cnt)
+{
+    ObsDev od;
+    int rc = stage_obs(ctx, obs, host_obs, od);
+    if (rc) return rc;
+    LG_CUDA(cudaEventRecord(ctx->ev[1], ctx->stream));
+    rc = obs_prepare(ctx, dxb, daxb, od, obs->nobs);
+    if (rc) return rc;
+    LG_CUDA(cudaEventRecord(ctx->ev[2], ctx->stream));
+    if (ctx->params.overlap > 0) {
+        LG_CUDA(ctx->d_trans.reserve((size_t)ctx->ncubes * ctx->k * ctx->k));
+        LG_CUDA(ctx->d_w.reserve((size_t)ctx->ncubes * ctx->k));
+    }
+    rc = search_and_core(ctx, dxb, daxb, dxa, daxa, od, obs->nobs, cnt);
+    if (rc) return rc;
+    if (ctx->params.overlap > 0) LG_CUDA(lg_launch_overlap_update(ctx, lg_grid(ctx), dxb, daxb, dxa, daxa));
+    LG_CUDA(cudaEventRecord(ctx->ev[4], ctx->stream));
+    return LETKF_OK;
+}
+
+int lg_finish_run(letkf_ctx *ctx, const letkf_obs *obs, unsigned long long *cnt)
+{
+    LG_CUDA(cudaEventRecord(ctx->ev[5], ctx->stream));
+    unsigned st = 0;
+    int rc = read_status(ctx, st, cnt);
+    if (rc) return rc;
+    if (st & LG_ST_LIST_FULL) return set_err(ctx, LETKF_ERR_ALLOC, "local observation lists did not fit");
+    fill_stats(ctx, cnt);
+    ctx->stats.ms_h2d = elapsed(ctx->ev[0], ctx->ev[1]);
+    ctx->stats.ms_obs = elapsed(ctx->ev[1], ctx->ev[2]);
+    ctx->stats.ms_search = elapsed(ctx->ev[2], ctx->ev[3]);
+    ctx->stats.ms_core = elapsed(ctx->ev[3], ctx->ev[4]);
+    ctx->stats.ms_d2h = elapsed(ctx->ev[4], ctx->ev[5]);
+    ctx->stats.ms_total = elapsed(ctx->ev[0], ctx->ev[5]);
+    ctx->have_run = true;
+    ctx->last_nobs = obs->nobs;
+    if (st & LG_ST_TIMEOUT)
+        return set_err(ctx, LETKF_ERR_TIMEOUT, "a bounded wait on the tensor cores ran out");
+    if (st & LG_ST_NOT_CONV)
+        return set_err(ctx, LETKF_ERR_NOT_CONVERGED, "an eigensolve reached its sweep limit");
+    return LETKF_OK;
+}
+
+extern "C" {
+
 int letkf_gpu_run(letkf_ctx *ctx, const double *xb, const double *axb, const letkf_obs *obs,
                   double *xa, double *axa, int flags)
 {
@@ -603,10 +667,8 @@ int letkf_gpu_run(letkf_ctx *ctx, const double *xb, const double *axb, const let
     if (!xb || !axb || !xa || !axa) return set_err(ctx, LETKF_ERR_INVALID, "NULL state pointer");
     if (flags != LETKF_HOST_PTRS && flags != LETKF_DEVICE_PTRS)
         return set_err(ctx, LETKF_ERR_INVALID, "bad flags");
-    int rc = check_obs(ctx, obs);
+    int rc = lg_check_run(ctx, obs);
     if (rc) return rc;
-    if (ctx->params.overlap > 0 && (ctx->range0 != 0 || ctx->range1 != ctx->ncubes))
-        return set_err(ctx, LETKF_ERR_UNSUPPORTED, "overlapped cubes average over neighbouring cubes: no cube range");
     LG_CUDA(cudaSetDevice(ctx->device));
     const bool host = flags == LETKF_HOST_PTRS;
     const size_t nstate = (size_t)ctx->ncol * ctx->n * ctx->k, nmean = (size_t)ctx->ncol * ctx->n;
@@ -625,22 +687,9 @@ int letkf_gpu_run(letkf_ctx *ctx, const double *xb, const double *axb, const let
         dxa = ctx->d_xa.p;
         daxa = ctx->d_axa.p;
     }
-    ObsDev od;
-    rc = stage_obs(ctx, obs, host, od);
-    if (rc) return rc;
-    LG_CUDA(cudaEventRecord(ctx->ev[1], ctx->stream));
     unsigned long long cnt[LG_CNT_N] = {};
-    rc = obs_prepare(ctx, dxb, daxb, od, obs->nobs);
+    rc = lg_run_analysis(ctx, obs, host, dxb, daxb, dxa, daxa, cnt);
     if (rc) return rc;
-    LG_CUDA(cudaEventRecord(ctx->ev[2], ctx->stream));
-    if (ctx->params.overlap > 0) {
-        LG_CUDA(ctx->d_trans.reserve((size_t)ctx->ncubes * ctx->k * ctx->k));
-        LG_CUDA(ctx->d_w.reserve((size_t)ctx->ncubes * ctx->k));
-    }
-    rc = search_and_core(ctx, dxb, daxb, dxa, daxa, od, obs->nobs, cnt);
-    if (rc) return rc;
-    if (ctx->params.overlap > 0) LG_CUDA(lg_launch_overlap_update(ctx, lg_grid(ctx), dxb, daxb, dxa, daxa));
-    LG_CUDA(cudaEventRecord(ctx->ev[4], ctx->stream));
     if (host) {
         // the columns of the analysed cubes: with cube_n 1 the cubes
         // themselves, else whole longitude strips of them
@@ -655,25 +704,7 @@ int letkf_gpu_run(letkf_ctx *ctx, const double *xb, const double *axb, const let
         LG_CUDA(cudaMemcpyAsync(axa + col0 * per_m, daxa + col0 * per_m, sizeof(double) * (col1 - col0) * per_m,
                                 cudaMemcpyDeviceToHost, ctx->stream));
     }
-    LG_CUDA(cudaEventRecord(ctx->ev[5], ctx->stream));
-    unsigned st = 0;
-    rc = read_status(ctx, st, cnt);
-    if (rc) return rc;
-    if (st & LG_ST_LIST_FULL) return set_err(ctx, LETKF_ERR_ALLOC, "local observation lists did not fit");
-    fill_stats(ctx, cnt);
-    ctx->stats.ms_h2d = elapsed(ctx->ev[0], ctx->ev[1]);
-    ctx->stats.ms_obs = elapsed(ctx->ev[1], ctx->ev[2]);
-    ctx->stats.ms_search = elapsed(ctx->ev[2], ctx->ev[3]);
-    ctx->stats.ms_core = elapsed(ctx->ev[3], ctx->ev[4]);
-    ctx->stats.ms_d2h = elapsed(ctx->ev[4], ctx->ev[5]);
-    ctx->stats.ms_total = elapsed(ctx->ev[0], ctx->ev[5]);
-    ctx->have_run = true;
-    ctx->last_nobs = obs->nobs;
-    if (st & LG_ST_TIMEOUT)
-        return set_err(ctx, LETKF_ERR_TIMEOUT, "a bounded wait on the tensor cores ran out");
-    if (st & LG_ST_NOT_CONV)
-        return set_err(ctx, LETKF_ERR_NOT_CONVERGED, "an eigensolve reached its sweep limit");
-    return LETKF_OK;
+    return lg_finish_run(ctx, obs, cnt);
 }
 
 int letkf_gpu_synchronize(letkf_ctx *ctx)

@@ -29,6 +29,7 @@
 #define LG_ST_NOT_CONV     4u   // an eigensolve hit its sweep limit
 #define LG_ST_SEGMENTS     8u   // a cap needed more bucket segments than the search holds
 #define LG_ST_TIMEOUT     16u   // a bounded wait on the tensor cores ran out
+#define LG_ST_BAD_STATE   32u   // a background member is NaN (members entry point)
 
 // Counters in ctx->d_counters.
 enum {
@@ -202,6 +203,7 @@ struct letkf_ctx {
     DevBuf<float> d_glat, d_glon;
     DevBuf<double> d_hyai, d_hybi;
     DevBuf<double> d_xb, d_axb, d_xa, d_axa;          // host-pointer runs
+    DevBuf<double> d_spb, d_spa;                      // members entry point: spreads
     // observations
     DevBuf<double> d_olat, d_olon, d_oph, d_oyo, d_orinv;
     DevBuf<int32_t> d_olev, d_ovar;
@@ -282,6 +284,18 @@ cudaError_t lg_launch_search_dec(letkf_ctx *ctx, const LgGrid &g, const double *
 cudaError_t lg_launch_overlap_update(letkf_ctx *ctx, const LgGrid &g, const double *xb, const double *axb,
                                      double *xa, double *axa);
 cudaError_t lg_launch_obs_lnp(letkf_ctx *ctx, int64_t nobs, const double *oph);
+
+// The analysis of letkf_gpu_run on device state: observations staged (host or
+// device pointers), H, search and core (cube windows), overlapped-cube
+// averaging; events 1-4 recorded.  lg_finish_run records event 5, reads the
+// status and counters, fills the stats and maps the status to a return code.
+int lg_run_analysis(letkf_ctx *ctx, const letkf_obs *obs, bool host_obs, const double *dxb,
+                    const double *daxb, double *dxa, double *daxa, unsigned long long *cnt);
+int lg_finish_run(letkf_ctx *ctx, const letkf_obs *obs, unsigned long long *cnt);
+int lg_check_run(letkf_ctx *ctx, const letkf_obs *obs);
+int lg_reset_status(letkf_ctx *ctx);
+int lg_read_status(letkf_ctx *ctx, unsigned &status, unsigned long long *cnt);
+int lg_set_err(letkf_ctx *ctx, int code, const char *msg);
 cudaError_t lg_launch_core_fp64(letkf_ctx *ctx, const LgGrid &g, const double *xb,
                                 const double *axb, double *xa, double *axa, bool keep_trans);
 cudaError_t lg_launch_core_mixed(letkf_ctx *ctx, const LgGrid &g, const double *xb,

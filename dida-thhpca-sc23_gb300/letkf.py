@@ -44,7 +44,7 @@ EXPORTED = [
     "letkf_gpu_last_error", "letkf_gpu_destroy", "letkf_gpu_launch_count",
     "letkf_gpu_core_batch_noalloc", "letkf_decomp_dims", "letkf_gpu_autotune",
     "letkf_batch_create", "letkf_batch_launch", "letkf_batch_sync", "letkf_batch_launches",
-    "letkf_batch_destroy", "letkf_gpu_set_list_limit", "letkf_gpu_set_cube_range",
+    "letkf_batch_destroy", "letkf_gpu_set_list_limit", "letkf_gpu_set_cube_range", "letkf_gpu_run_members",
     "letkf_init_gpu_", "letkf_set_obs_gpu_", "letkf_run_gpu_", "letkf_final_gpu_",
 ]
 
@@ -73,6 +73,10 @@ class Params(C.Structure):
         ("h_mode", C.c_int), ("precision", C.c_int),
         ("decomp_lat_blocks", C.c_int), ("decomp_lon_blocks", C.c_int),
     ]
+
+
+class Blend(C.Structure):
+    _fields_ = [("gamma1", C.c_double), ("gamma2", C.c_double), ("polar_lat_deg", C.c_double)]
 
 
 class Obs(C.Structure):
@@ -135,6 +139,7 @@ def load_library(path: str = LIB_PATH):
     L.letkf_batch_destroy.argtypes = [vp]
     L.letkf_gpu_set_list_limit.argtypes = [vp, i64]
     L.letkf_gpu_set_cube_range.argtypes = [vp, i64, i64]
+    L.letkf_gpu_run_members.argtypes = [vp, vp, C.POINTER(Obs), C.POINTER(Blend), vp, vp, vp, i32]
     _lib = L
     return L
 
@@ -313,6 +318,19 @@ class LetkfGPU:
         if not (allow_not_converged and rc == LETKF_ERR_NOT_CONVERGED):
             self._check(rc, "letkf_gpu_run")
         return xa, axa
+
+    def run_members(self, xb_in, obs, gamma1=0.0, gamma2=1.0, polar_lat_deg=90.0):
+        """run_da_parallel on the GPU: full members in (host arrays), analysis
+        members and the background and analysis spreads out."""
+        xin = _f64(xb_in)
+        xout = np.empty_like(xin)
+        sb = np.empty(xin.shape[:-1])
+        sa = np.empty(xin.shape[:-1])
+        o = obs if isinstance(obs, ObsArrays) else ObsArrays(obs)
+        bl = Blend(gamma1=gamma1, gamma2=gamma2, polar_lat_deg=polar_lat_deg)
+        self._check(self.L.letkf_gpu_run_members(self.h, _ptr(xin), C.byref(o.c), C.byref(bl), _ptr(xout),
+                                                  _ptr(sb), _ptr(sa), LETKF_HOST_PTRS), "run_members")
+        return xout, sb, sa
 
     def run_device(self, xb, axb, obs: ObsArrays, xa, axa):
         """Device tensors (torch, this GPU) in and out."""

@@ -153,6 +153,29 @@ int letkf_gpu_set_stream(letkf_ctx *ctx, void *stream);
 int letkf_gpu_run(letkf_ctx *ctx, const double *xb, const double *axb, const letkf_obs *obs,
                   double *xa, double *axa, int flags);
 
+/* The caller's conversion around letkf_run (run_da_parallel,
+ * EnDNN/src/module_da_parallel.F90:163-261), for letkf_gpu_run_members.     */
+typedef struct letkf_blend {
+    double gamma1, gamma2;     /* gamma1, gamma2 (da_namelist_mod.F90:39-40): the
+                                  analysis members are gamma1 (axb + xb) +
+                                  gamma2 (axa + xa) (:230-231)                     */
+    double polar_lat_deg;      /* da_polar_letkf_lat: columns with |grid_lat| above it
+                                  keep the background (:222, :242-251)            */
+} letkf_blend;
+
+/* run_da_parallel's body on the device: full background members
+ * xb_in [col][row][member] in; the mean and perturbations formed (dnn2letkf,
+ * module_da_parallel.F90:184-204: mean = sum / real(ens); a NaN member returns
+ * LETKF_ERR_INVALID before any analysis), the analysis of letkf_gpu_run, and
+ * the blend and spreads (letkf2dnn, :214-258): xa_out [col][row][member] the
+ * analysis members, spread_b and spread_a [col][row] the background and
+ * analysis spreads sqrt(sum d^2 / ens).  Every cube is analysed (no cube
+ * range).  With LETKF_HOST_PTRS all arrays, observations included, are host
+ * memory; with LETKF_DEVICE_PTRS all are device memory.                     */
+int letkf_gpu_run_members(letkf_ctx *ctx, const double *xb_in, const letkf_obs *obs,
+                          const letkf_blend *blend, double *xa_out, double *spread_b,
+                          double *spread_a, int flags);
+
 /* Most local-list entries (obs of one cube's list) the list pool may hold;
  * 0 (the default) sizes it from the device's free memory.  When the lists of
  * all analysed cubes do not fit, a run searches and analyses the cubes in

@@ -1180,3 +1180,65 @@ int orc_letkf_run(const orc_config *cfg, const orc_obs *obs,
     free(dep);
     return rc;
 }
+
+/* dnn2letkf: DA/EnDNN/src/module_da_parallel.F90:184-204.  axb = sum(xin)/real(ens)
+ * (the member count as a default real, exact here), xb = xin - axb.  A NaN
+ * member stops the reference (:188-193); here the call returns -1.          */
+int orc_members_split(const orc_config *cfg, const double *xin, double *xb, double *axb)
+{
+    const int k = cfg->k, n = state_rows(cfg);
+    const int64_t rows = (int64_t)cfg->nlat * cfg->nlon * n;
+    int64_t r;
+    int bad = 0;
+#pragma omp parallel for schedule(static) reduction(| : bad)
+    for (r = 0; r < rows; r++) {
+        const double *x = xin + r * k;
+        double s = 0.0;
+        int e;
+        for (e = 0; e < k; e++) {
+            if (isnan(x[e])) bad = 1;
+            s = s + x[e];
+        }
+        s = s / (double)(float)k;
+        axb[r] = s;
+        for (e = 0; e < k; e++) xb[r * k + e] = x[e] - s;
+    }
+    return bad ? -1 : 0;
+}
+
+/* letkf2dnn: DA/EnDNN/src/module_da_parallel.F90:214-258 (the halo branch
+ * does not apply to one global block).  grid_lat is the float grid.         */
+void orc_members_blend(const orc_config *cfg, double gamma1, double gamma2, double polar_lat,
+                       const double *xb, const double *axb, const double *xa, const double *axa,
+                       double *xout, double *spread_b, double *spread_a)
+{
+    const int k = cfg->k, n = state_rows(cfg);
+    const int64_t ncol = (int64_t)cfg->nlat * cfg->nlon;
+    int64_t c;
+#pragma omp parallel for schedule(static)
+    for (c = 0; c < ncol; c++) {
+        const double lat = (double)cfg->glat[c % cfg->nlat];
+        int r, e;
+        for (r = 0; r < n; r++) {
+            const int64_t row = c * n + r;
+            const double *b = xb + row * k, *a = xa + row * k;
+            double *o = xout + row * k;
+            double sb = 0.0, sa = 0.0;
+            if (fabs(lat) <= polar_lat) {
+                for (e = 0; e < k; e++) o[e] = gamma1 * (axb[row] + b[e]) + gamma2 * (axa[row] + a[e]);
+                for (e = 0; e < k; e++) {
+                    sb = sb + b[e] * b[e];
+                    sa = sa + (o[e] - axa[row]) * (o[e] - axa[row]);
+                }
+            } else {
+                for (e = 0; e < k; e++) o[e] = b[e] + axb[row];
+                for (e = 0; e < k; e++) {
+                    sb = sb + b[e] * b[e];
+                    sa = sa + b[e] * b[e];
+                }
+            }
+            spread_b[row] = sqrt(sb / (double)(float)k);
+            spread_a[row] = sqrt(sa / (double)(float)k);
+        }
+    }
+}

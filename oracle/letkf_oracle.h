@@ -133,6 +133,18 @@ int orc_letkf_cubes(const orc_config *cfg, const orc_obs *obs, const double *yb,
 /* Number of OpenMP threads the library will use. */
 int orc_num_threads(void);
 
+/* The caller's conversion around letkf_run (run_da_parallel,
+ * DA/EnDNN/src/module_da_parallel.F90:184-258), for the members entry point.
+ * members_split: full members xin [col][n][k] -> perturbations xb and mean
+ * axb (sum over members / real(ens)); returns -1 if a member is NaN.
+ * members_blend: xout = gamma1 (axb + xb) + gamma2 (axa + xa) where
+ * |grid_lat| <= polar_lat, else xb + axb; spread_b = sqrt(sum xb^2 / ens),
+ * spread_a = sqrt(sum (xout - axa)^2 / ens) (= spread_b where polar).     */
+int orc_members_split(const orc_config *cfg, const double *xin, double *xb, double *axb);
+void orc_members_blend(const orc_config *cfg, double gamma1, double gamma2, double polar_lat,
+                       const double *xb, const double *axb, const double *xa, const double *axa,
+                       double *xout, double *spread_b, double *spread_a);
+
 #ifdef __cplusplus
 }
 #endif

@@ -168,6 +168,30 @@ class Oracle:
         return xa, axa
 
 
+def members_split(orc: "Oracle", xin):
+    """dnn2letkf (module_da_parallel.F90:184-204): full members -> (xb, axb)."""
+    x = np.ascontiguousarray(xin, dtype=np.float64)
+    xb = np.empty_like(x)
+    axb = np.empty(x.shape[:-1])
+    rc = lib().orc_members_split(C.byref(orc.cfg), _p(x, C.c_double), _p(xb, C.c_double),
+                                 _p(axb, C.c_double))
+    if rc != 0:
+        raise RuntimeError("NaN in the background members")
+    return xb, axb
+
+
+def members_blend(orc: "Oracle", gamma1, gamma2, polar_lat, xb, axb, xa, axa):
+    """letkf2dnn (module_da_parallel.F90:214-258): -> (xa_out, spread_b, spread_a)."""
+    arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (xb, axb, xa, axa)]
+    xout = np.empty_like(arrs[0])
+    sb = np.empty_like(arrs[1])
+    sa = np.empty_like(arrs[1])
+    lib().orc_members_blend(C.byref(orc.cfg), C.c_double(gamma1), C.c_double(gamma2),
+                            C.c_double(polar_lat), *[_p(a, C.c_double) for a in arrs],
+                            _p(xout, C.c_double), _p(sb, C.c_double), _p(sa, C.c_double))
+    return xout, sb, sa
+
+
 def schr2(ri: float) -> float:
     return lib().orc_schr2(ri)
 
