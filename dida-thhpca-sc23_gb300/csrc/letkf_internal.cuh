@@ -209,6 +209,10 @@ struct letkf_ctx {
     DevBuf<int32_t> d_olev, d_ovar;
     DevBuf<double> d_yb, d_dep;
     DevBuf<double> d_olnp;        // vertical localization: ln(ph) per obs
+    // observations built on the device from raw obs-store buffers (letkf_ingest.cu)
+    DevBuf<double> d_plat, d_plon, d_pph, d_pyo, d_prinv;
+    DevBuf<int32_t> d_plev, d_pvar, d_pvarof;
+    DevBuf<float> d_raw;
     DevBuf<float> d_ys32;         // yb * sqrt(rinv) in FP32 (mixed precision)
     DevBuf<float> d_rinvf;
     DevBuf<float> d_oef;          // mixed form: sqrt(rdiaginv) dep per obs

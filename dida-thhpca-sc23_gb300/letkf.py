@@ -45,6 +45,8 @@ EXPORTED = [
     "letkf_gpu_core_batch_noalloc", "letkf_decomp_dims", "letkf_gpu_autotune",
     "letkf_batch_create", "letkf_batch_launch", "letkf_batch_sync", "letkf_batch_launches",
     "letkf_batch_destroy", "letkf_gpu_set_list_limit", "letkf_gpu_set_cube_range", "letkf_gpu_run_members",
+    "letkf_struct_atm2endnn", "letkf_struct_endnn2atm", "letkf_struct_atm2endnn_a", "letkf_struct_endnn2atm_a",
+    "letkf_gpu_obs_from_records", "letkf_gpu_obs_regular",
     "letkf_init_gpu_", "letkf_set_obs_gpu_", "letkf_run_gpu_", "letkf_final_gpu_",
 ]
 
@@ -140,6 +142,12 @@ def load_library(path: str = LIB_PATH):
     L.letkf_gpu_set_list_limit.argtypes = [vp, i64]
     L.letkf_gpu_set_cube_range.argtypes = [vp, i64, i64]
     L.letkf_gpu_run_members.argtypes = [vp, vp, C.POINTER(Obs), C.POINTER(Blend), vp, vp, vp, i32]
+    L.letkf_gpu_obs_from_records.argtypes = [vp, i64, i32, i32, vp, vp, vp, vp, vp, vp, C.POINTER(Obs), i32]
+    L.letkf_gpu_obs_regular.argtypes = [vp, i32, i32, i32, i32] + [vp] * 11 + [C.POINTER(Obs), i32]
+    L.letkf_struct_atm2endnn.argtypes = [i32] * 8 + [vp, vp, vp]
+    L.letkf_struct_endnn2atm.argtypes = [i32] * 8 + [vp, vp, vp]
+    L.letkf_struct_atm2endnn_a.argtypes = [i32] * 5 + [vp, vp, vp]
+    L.letkf_struct_endnn2atm_a.argtypes = [i32] * 5 + [vp, vp, vp]
     _lib = L
     return L
 
@@ -177,6 +185,43 @@ class ObsArrays:
             n = int(t["lat"].size)
         self.c = Obs(nobs=n, lat=p("lat"), lon=p("lon"), ph=p("ph"), lev=p("lev"),
                      var=p("var"), yo=p("yo"), rinv=p("rinv"))
+
+    @classmethod
+    def empty_view(cls):
+        """A view whose pointers the library fills (device memory it owns)."""
+        v = cls.__new__(cls)
+        v.device = True
+        v._keep = None
+        v.c = Obs()
+        return v
+
+    def to_host(self) -> dict:
+        """Copies of a device view's arrays (through the CUDA runtime)."""
+        cudart = _cudart()
+        n = int(self.c.nobs)
+        out = {}
+        for key, dt in (("lat", np.float64), ("lon", np.float64), ("ph", np.float64), ("lev", np.int32),
+                        ("var", np.int32), ("yo", np.float64), ("rinv", np.float64)):
+            a = np.empty(n, dtype=dt)
+            ptr = getattr(self.c, key)
+            if n and ptr:
+                rc = cudart.cudaMemcpy(C.c_void_p(a.ctypes.data), C.c_void_p(ptr), C.c_size_t(a.nbytes), 2)
+                if rc != 0:
+                    raise LetkfError(LETKF_ERR_CUDA, f"cudaMemcpy {rc}")
+            out[key] = a
+        return out
+
+
+_CUDART = None
+
+
+def _cudart():
+    global _CUDART
+    if _CUDART is None:
+        home = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+        _CUDART = C.CDLL(os.path.join(home, "lib64", "libcudart.so"))
+        _CUDART.cudaMemcpy.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t, C.c_int]
+    return _CUDART
 
 
 class Batch:
@@ -332,6 +377,35 @@ class LetkfGPU:
                                                   _ptr(sb), _ptr(sa), LETKF_HOST_PTRS), "run_members")
         return xout, sb, sa
 
+    def obs_from_records(self, lon, lat, lev, val, var_of, nz=1, randn=None):
+        """Build observations on the device from obs-store records (host
+        float32 arrays); returns an ObsArrays view of device memory."""
+        f = lambda a: None if a is None else np.ascontiguousarray(a, dtype=np.float32)
+        lon, lat, lev, val, randn = f(lon), f(lat), f(lev), f(val), f(randn)
+        vo = np.ascontiguousarray(var_of, dtype=np.int32)
+        nrec, nvar = lon.size, vo.size
+        view = ObsArrays.empty_view()
+        self._check(self.L.letkf_gpu_obs_from_records(self.h, nrec, nvar, nz, _ptr(lon), _ptr(lat), _ptr(lev),
+                                                      _ptr(val), None if randn is None else _ptr(randn),
+                                                      _ptr(vo), C.byref(view.c), LETKF_HOST_PTRS),
+                    "obs_from_records")
+        return view
+
+    def obs_regular(self, latn, lats, lonw, lone, r, nw, sw, ne, se, var_of, randn=None):
+        """Build a regular obs grid on the device (host float32 arrays in
+        C order: r [nz][nvar], corners [nlon_o][nlat_o][nz][nvar+1], randn
+        [nobs][nz][nvar]); returns an ObsArrays view of device memory."""
+        f = lambda a: None if a is None else np.ascontiguousarray(a, dtype=np.float32)
+        arrs = [f(a) for a in (latn, lats, lonw, lone, r, nw, sw, ne, se)]
+        randn = f(randn)
+        vo = np.ascontiguousarray(var_of, dtype=np.int32)
+        nlon_o, nlat_o, nz, _ = arrs[5].shape
+        view = ObsArrays.empty_view()
+        self._check(self.L.letkf_gpu_obs_regular(self.h, nlat_o, nlon_o, nz, vo.size, *[_ptr(a) for a in arrs],
+                                                 None if randn is None else _ptr(randn), _ptr(vo),
+                                                 C.byref(view.c), LETKF_HOST_PTRS), "obs_regular")
+        return view
+
     def run_device(self, xb, axb, obs: ObsArrays, xa, axa):
         """Device tensors (torch, this GPU) in and out."""
         rc = self.L.letkf_gpu_run(self.h, xb.data_ptr(), axb.data_ptr(), C.byref(obs.c),
@@ -389,6 +463,51 @@ class LetkfGPU:
         s = Stats()
         self._check(self.L.letkf_gpu_get_stats(self.h, C.byref(s)), "get_stats")
         return s.as_dict()
+
+
+def struct_atm2endnn(xb, xb2, ens_start=1, n_start=1, stream=None):
+    """struct_atm2endnn on device tensors: xb is the Fortran array
+    xb(ens, ny, nx, n), i.e. a C-order tensor [n][nx][ny][ens]; xb2 is
+    xb2(ens_max, n_max, nx, ny), a C-order tensor [ny][nx][n_max][ens_max]."""
+    n, nx, ny, ens = xb.shape
+    ny2, nx2, n_max, ens_max = xb2.shape
+    assert (nx2, ny2) == (nx, ny)
+    rc = load_library().letkf_struct_atm2endnn(ens, n, nx, ny, ens_max, n_max, ens_start, n_start,
+                                               xb.data_ptr(), xb2.data_ptr(), stream)
+    if rc != LETKF_OK:
+        raise LetkfError(rc, "letkf_struct_atm2endnn")
+
+
+def struct_endnn2atm(xb, xb2, ens_start=1, n_start=1, stream=None):
+    """struct_endnn2atm on device tensors: xb [ny][nx][n_max][ens_max] ->
+    xb2 [n][nx][ny][ens] (xb2 is the Fortran xb2(ens, ny, nx, n))."""
+    ny, nx, n_max, ens_max = xb.shape
+    n, nx2, ny2, ens = xb2.shape
+    assert (nx2, ny2) == (nx, ny)
+    rc = load_library().letkf_struct_endnn2atm(ens, n, nx, ny, ens_max, n_max, ens_start, n_start,
+                                               xb.data_ptr(), xb2.data_ptr(), stream)
+    if rc != LETKF_OK:
+        raise LetkfError(rc, "letkf_struct_endnn2atm")
+
+
+def struct_atm2endnn_a(axb, axb2, n_start=1, stream=None):
+    """struct_atm2endnn_a: axb [n][nx][ny] -> axb2 [ny][nx][n_max]."""
+    n, nx, ny = axb.shape
+    n_max = axb2.shape[2]
+    rc = load_library().letkf_struct_atm2endnn_a(n, nx, ny, n_max, n_start, axb.data_ptr(), axb2.data_ptr(),
+                                                 stream)
+    if rc != LETKF_OK:
+        raise LetkfError(rc, "letkf_struct_atm2endnn_a")
+
+
+def struct_endnn2atm_a(axb, axb2, n_start=1, stream=None):
+    """struct_endnn2atm_a: axb [ny][nx][n_max] -> axb2 [n][nx][ny]."""
+    ny, nx, n_max = axb.shape
+    n = axb2.shape[0]
+    rc = load_library().letkf_struct_endnn2atm_a(n, nx, ny, n_max, n_start, axb.data_ptr(), axb2.data_ptr(),
+                                                 stream)
+    if rc != LETKF_OK:
+        raise LetkfError(rc, "letkf_struct_endnn2atm_a")
 
 
 def launch_count() -> int:

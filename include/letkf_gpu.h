@@ -176,6 +176,53 @@ int letkf_gpu_run_members(letkf_ctx *ctx, const double *xb_in, const letkf_obs *
                           const letkf_blend *blend, double *xa_out, double *spread_b,
                           double *spread_a, int flags);
 
+/* Observations built on the device from the obs store's raw buffers, in the
+ * canonical flat order (obs, level, variable) that gen_yb_dis scans
+ * (letkf_yb.F90:71-113).  Both write the context's observation buffers and
+ * fill *obs with device pointers into them (valid until the next build or
+ * letkf_gpu_destroy), for letkf_gpu_run with LETKF_DEVICE_PTRS.  The float
+ * inputs are host (LETKF_HOST_PTRS) or device (LETKF_DEVICE_PTRS) memory;
+ * var_of[nvar] (host) maps each payload variable to a state variable index.
+ * randn may be NULL (no perturbation).
+ *
+ * Records (read_obs, read_obs_mod.F90:339-448): lon, lat, lev[nrec] and
+ * val[nrec][2 nvar + 1] = value, sigma per variable, then pressure;
+ * randn[nvar][nrec] the N(0,1) draws of the perturbation.  nz = 1 for
+ * single-level types; for profile types (ADPUPA, GPSRO) nz levels per
+ * profile, whose records hold lev = 1..nz in order (else LETKF_ERR_INVALID).
+ * yo = value + randn * sigma and rinv = 1 / sigma^2 in single precision.   */
+int letkf_gpu_obs_from_records(letkf_ctx *ctx, int64_t nrec, int nvar, int nz, const float *lon,
+                               const float *lat, const float *lev, const float *val, const float *randn,
+                               const int32_t *var_of, letkf_obs *obs, int flags);
+
+/* Regular obs grid (read_obs_regular, read_obs_mod.F90:451-651): cell edges
+ * latn, lats [nlat_o] and lonw, lone [nlon_o]; sigma r(nvar, nz); four corner
+ * fields nw, sw, ne, se (nvar + 1, nz, nlat_o, nlon_o) in Fortran order
+ * (pressure first, then the variables); randn(nvar, nz, nlat_o * nlon_o).
+ * Obs at the cell centres, longitude outer and latitude inner; values and
+ * pressure the four-corner average; yo = value + randn / sqrt(rinv).         */
+int letkf_gpu_obs_regular(letkf_ctx *ctx, int nlat_o, int nlon_o, int nz, int nvar, const float *latn,
+                          const float *lats, const float *lonw, const float *lone, const float *r,
+                          const float *nw, const float *sw, const float *ne, const float *se,
+                          const float *randn, const int32_t *var_of, letkf_obs *obs, int flags);
+
+/* The coupler's layout transforms (EnDNN/src/data_trans.F90:1-70) on device
+ * memory, so the state never goes through the host between the model and the
+ * analysis.  nx = latitudes, ny = longitudes; ens_start and n_start are
+ * 1-based as in the reference.  atm2endnn: xb(ens, ny, nx, n) (Fortran order)
+ * into members ens_start.. and rows n_start.. of xb2(ens_max, n_max, nx, ny)
+ * (the [col][row][member] layout of letkf_gpu_run); endnn2atm: back.  The _a
+ * forms move the mean, axb(ny, nx, n) <-> axb2(n_max, nx, ny).  Work is
+ * queued on `stream` (a cudaStream_t; NULL = the default stream).           */
+int letkf_struct_atm2endnn(int ens, int n, int nx, int ny, int ens_max, int n_max, int ens_start,
+                           int n_start, const double *xb, double *xb2, void *stream);
+int letkf_struct_endnn2atm(int ens, int n, int nx, int ny, int ens_max, int n_max, int ens_start,
+                           int n_start, const double *xb, double *xb2, void *stream);
+int letkf_struct_atm2endnn_a(int n, int nx, int ny, int n_max, int n_start, const double *axb,
+                             double *axb2, void *stream);
+int letkf_struct_endnn2atm_a(int n, int nx, int ny, int n_max, int n_start, const double *axb,
+                             double *axb2, void *stream);
+
 /* Most local-list entries (obs of one cube's list) the list pool may hold;
  * 0 (the default) sizes it from the device's free memory.  When the lists of
  * all analysed cubes do not fit, a run searches and analyses the cubes in

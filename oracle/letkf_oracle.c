@@ -1242,3 +1242,136 @@ void orc_members_blend(const orc_config *cfg, double gamma1, double gamma2, doub
         }
     }
 }
+
+/* struct_atm2endnn: DA/EnDNN/src/data_trans.F90:2-18, with the Fortran index
+ * maps written out: xb(e, j, i, nn) is xb[e + ens*(j + ny*(i + nx*nn))] and
+ * xb2(e, nn, i, j) is xb2[e + ens_max*(nn + n_max*(i + nx*j))].             */
+#define XB1(e, j, i, nn) xb[(e) + (int64_t)ens * ((j) + (int64_t)ny * ((i) + (int64_t)nx * (nn)))]
+#define XB2(e, nn, i, j) xb2[(e) + (int64_t)ens_max * ((nn) + (int64_t)n_max * ((i) + (int64_t)nx * (j)))]
+void orc_struct_atm2endnn(int ens, int n, int nx, int ny, int ens_max, int n_max, int ens_start,
+                          int n_start, const double *xb, double *xb2)
+{
+    int nn, i, j, e;
+    for (nn = n_start; nn <= n_start + n - 1; nn++)
+        for (i = 1; i <= nx; i++)
+            for (j = 1; j <= ny; j++)
+                for (e = 1; e <= ens; e++)
+                    XB2(ens_start + e - 2, nn - 1, i - 1, j - 1) = XB1(e - 1, j - 1, i - 1, nn - n_start);
+}
+
+/* struct_endnn2atm: data_trans.F90:21-38.  The first array is the
+ * analysis-side one (the reference's xb), the second the model-side one.     */
+void orc_struct_endnn2atm(int ens, int n, int nx, int ny, int ens_max, int n_max, int ens_start,
+                          int n_start, const double *xb2, double *xb)
+{
+    int nn, i, j, e;
+    for (j = 1; j <= ny; j++)
+        for (i = 1; i <= nx; i++)
+            for (nn = 1; nn <= n; nn++)
+                for (e = 1; e <= ens; e++)
+                    XB1(e - 1, j - 1, i - 1, nn - 1) = XB2(ens_start + e - 2, nn + n_start - 2, i - 1, j - 1);
+}
+#undef XB1
+#undef XB2
+
+/* struct_atm2endnn_a / struct_endnn2atm_a: data_trans.F90:41-70.           */
+void orc_struct_atm2endnn_a(int n, int nx, int ny, int n_max, int n_start, const double *axb, double *axb2)
+{
+    int nn, i, j;
+    for (nn = n_start; nn <= n_start + n - 1; nn++)
+        for (i = 1; i <= nx; i++)
+            for (j = 1; j <= ny; j++)
+                axb2[(nn - 1) + (int64_t)n_max * ((i - 1) + (int64_t)nx * (j - 1))] =
+                    axb[(j - 1) + (int64_t)ny * ((i - 1) + (int64_t)nx * (nn - n_start))];
+}
+
+void orc_struct_endnn2atm_a(int n, int nx, int ny, int n_max, int n_start, const double *axb, double *axb2)
+{
+    int nn, i, j;
+    for (j = 1; j <= ny; j++)
+        for (i = 1; i <= nx; i++)
+            for (nn = 1; nn <= n; nn++)
+                axb2[(j - 1) + (int64_t)ny * ((i - 1) + (int64_t)nx * (nn - 1))] =
+                    axb[(nn + n_start - 2) + (int64_t)n_max * ((i - 1) + (int64_t)nx * (j - 1))];
+}
+
+/* read_obs (read_obs_mod.F90:388-441): val_buf(2*nvar+1, obs_num) real(4),
+ * val = val_buf(2n-1) + randn * val_buf(2n) and obs_rinv = 1.0/val_buf(2n)**2
+ * in real(4); a record with lev_buf == 1 starts a profile (:401-423), whose
+ * level-1 record gives lat/lon; entry (prof, lev, n) of the flat list is
+ * (prof*nz + lev-1)*nvar + n.                                                */
+int64_t orc_obs_from_records(int64_t nrec, int nvar, int nz, const float *lon, const float *lat,
+                             const float *lev, const float *val, const float *randn, const int32_t *var_of,
+                             double *olat, double *olon, double *oph, int32_t *olev, int32_t *ovar,
+                             double *oyo, double *orinv)
+{
+    const int nv = 2 * nvar + 1;
+    int64_t r, indx = -1;
+    int n;
+    if (nrec % nz != 0) return -1;
+    for (r = 0; r < nrec; r++) {
+        int level;
+        if (nz == 1) {
+            indx = r;
+            level = 1;
+        } else {
+            if (lev[r] == 1.0f) indx++;
+            level = (int)lev[r];
+            if (indx < 0 || level != (int)(r % nz) + 1) return -1;
+        }
+        for (n = 0; n < nvar; n++) {
+            const int64_t e = (indx * nz + (level - 1)) * nvar + n;
+            const float v = val[r * nv + 2 * n], sg = val[r * nv + 2 * n + 1];
+            const float z = randn ? randn[(int64_t)n * nrec + r] : 0.0f;
+            const float yo = v + z * sg;
+            const float ri = 1.0f / (sg * sg);
+            const int64_t r1 = indx * nz;
+            olat[e] = (double)lat[r1];
+            olon[e] = (double)lon[r1];
+            oph[e] = (double)val[r * nv + 2 * nvar];
+            olev[e] = level;
+            ovar[e] = var_of[n];
+            oyo[e] = (double)yo;
+            orinv[e] = (double)ri;
+        }
+    }
+    return nrec * nvar;
+}
+
+/* read_obs_regular (read_obs_mod.F90:506-627): centres (latn+lats)/2.0,
+ * (lonw+lone)/2.0 in real(4), lon outer and lat inner; obs_rinv =
+ * 1.0/r(n,k)**2 in real(4) stored as real(8); yo_tmp = (nw+sw+ne+se)/4.0 in
+ * real(4); ph = yo_tmp(1); dis_yo = yo_tmp(n+1) + randn/sqrt(obs_rinv).     */
+int64_t orc_obs_regular(int nlat_o, int nlon_o, int nz, int nvar, const float *latn, const float *lats,
+                        const float *lonw, const float *lone, const float *r, const float *nw,
+                        const float *sw, const float *ne, const float *se, const float *randn,
+                        const int32_t *var_of, double *olat, double *olon, double *oph, int32_t *olev,
+                        int32_t *ovar, double *oyo, double *orinv)
+{
+    const int64_t nobs = (int64_t)nlat_o * nlon_o;
+    int i, j, k, n;
+    for (i = 0; i < nlon_o; i++)
+        for (j = 0; j < nlat_o; j++) {
+            const int64_t o = j + (int64_t)nlat_o * i;
+            for (k = 0; k < nz; k++)
+                for (n = 0; n < nvar; n++) {
+                    const int64_t e = (o * nz + k) * nvar + n;
+#define CORNER(f, q) f[(int64_t)(q) + (int64_t)(nvar + 1) * (k + (int64_t)nz * (j + (int64_t)nlat_o * i))]
+                    const float avg_p = (((CORNER(nw, 0) + CORNER(sw, 0)) + CORNER(ne, 0)) + CORNER(se, 0)) / 4.0f;
+                    const float avg_v = (((CORNER(nw, n + 1) + CORNER(sw, n + 1)) + CORNER(ne, n + 1)) +
+                                         CORNER(se, n + 1)) / 4.0f;
+#undef CORNER
+                    const float sg = r[n + (int64_t)nvar * k];
+                    const double rinv = (double)(1.0f / (sg * sg));
+                    const double z = randn ? (double)randn[n + (int64_t)nvar * (k + (int64_t)nz * o)] : 0.0;
+                    olat[e] = (double)((latn[j] + lats[j]) / 2.0f);
+                    olon[e] = (double)((lonw[i] + lone[i]) / 2.0f);
+                    oph[e] = (double)avg_p;
+                    olev[e] = k + 1;
+                    ovar[e] = var_of[n];
+                    oyo[e] = (double)avg_v + z / sqrt(rinv);
+                    orinv[e] = rinv;
+                }
+        }
+    return nobs * nz * nvar;
+}

@@ -141,6 +141,27 @@ int orc_num_threads(void);
  * |grid_lat| <= polar_lat, else xb + axb; spread_b = sqrt(sum xb^2 / ens),
  * spread_a = sqrt(sum (xout - axa)^2 / ens) (= spread_b where polar).     */
 int orc_members_split(const orc_config *cfg, const double *xin, double *xb, double *axb);
+/* Observations from the obs store's raw buffers (read_obs and
+ * read_obs_regular, DA/LETKF/src/read_obs_mod.F90:339-651), flattened in the
+ * (obs, level, variable) order of gen_yb_dis; arrays as letkf_obs.  Returns
+ * the entry count, or -1 for a profile whose records are not levels 1..nz.  */
+int64_t orc_obs_from_records(int64_t nrec, int nvar, int nz, const float *lon, const float *lat,
+                             const float *lev, const float *val, const float *randn, const int32_t *var_of,
+                             double *olat, double *olon, double *oph, int32_t *olev, int32_t *ovar,
+                             double *oyo, double *orinv);
+int64_t orc_obs_regular(int nlat_o, int nlon_o, int nz, int nvar, const float *latn, const float *lats,
+                        const float *lonw, const float *lone, const float *r, const float *nw,
+                        const float *sw, const float *ne, const float *se, const float *randn,
+                        const int32_t *var_of, double *olat, double *olon, double *oph, int32_t *olev,
+                        int32_t *ovar, double *oyo, double *orinv);
+/* The coupler's layout transforms, EnDNN/src/data_trans.F90:1-70 (Fortran
+ * arrays, 1-based ens_start / n_start).                                       */
+void orc_struct_atm2endnn(int ens, int n, int nx, int ny, int ens_max, int n_max, int ens_start,
+                          int n_start, const double *xb, double *xb2);
+void orc_struct_endnn2atm(int ens, int n, int nx, int ny, int ens_max, int n_max, int ens_start,
+                          int n_start, const double *xb, double *xb2);
+void orc_struct_atm2endnn_a(int n, int nx, int ny, int n_max, int n_start, const double *axb, double *axb2);
+void orc_struct_endnn2atm_a(int n, int nx, int ny, int n_max, int n_start, const double *axb, double *axb2);
 void orc_members_blend(const orc_config *cfg, double gamma1, double gamma2, double polar_lat,
                        const double *xb, const double *axb, const double *xa, const double *axa,
                        double *xout, double *spread_b, double *spread_a);

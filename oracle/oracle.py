@@ -192,6 +192,89 @@ def members_blend(orc: "Oracle", gamma1, gamma2, polar_lat, xb, axb, xa, axa):
     return xout, sb, sa
 
 
+def _obs_out(m):
+    return {"lat": np.empty(m), "lon": np.empty(m), "ph": np.empty(m), "lev": np.empty(m, np.int32),
+            "var": np.empty(m, np.int32), "yo": np.empty(m), "rinv": np.empty(m)}
+
+
+def _obs_ptrs(o):
+    return [_p(o["lat"], C.c_double), _p(o["lon"], C.c_double), _p(o["ph"], C.c_double),
+            _p(o["lev"], C.c_int32), _p(o["var"], C.c_int32), _p(o["yo"], C.c_double),
+            _p(o["rinv"], C.c_double)]
+
+
+def obs_from_records(lon, lat, lev, val, var_of, nz=1, randn=None):
+    """read_obs (read_obs_mod.F90:388-441) flattened: -> obs dict."""
+    f = lambda a: np.ascontiguousarray(a, dtype=np.float32)
+    lon, lat, lev, val = f(lon), f(lat), f(lev), f(val)
+    rn = None if randn is None else f(randn)
+    vo = np.ascontiguousarray(var_of, dtype=np.int32)
+    out = _obs_out(lon.size * vo.size)
+    L = lib()
+    L.orc_obs_from_records.restype = C.c_int64
+    m = L.orc_obs_from_records(C.c_int64(lon.size), vo.size, nz, _p(lon, C.c_float), _p(lat, C.c_float),
+                               _p(lev, C.c_float), _p(val, C.c_float),
+                               None if rn is None else _p(rn, C.c_float), _p(vo, C.c_int32), *_obs_ptrs(out))
+    if m < 0:
+        raise ValueError("profile records must hold levels 1..nz in order")
+    return out
+
+
+def obs_regular(latn, lats, lonw, lone, r, nw, sw, ne, se, var_of, randn=None):
+    """read_obs_regular (read_obs_mod.F90:506-627) flattened: -> obs dict.
+    C-order arrays: r [nz][nvar], corners [nlon_o][nlat_o][nz][nvar+1],
+    randn [nobs][nz][nvar]."""
+    f = lambda a: np.ascontiguousarray(a, dtype=np.float32)
+    arrs = [f(a) for a in (latn, lats, lonw, lone, r, nw, sw, ne, se)]
+    rn = None if randn is None else f(randn)
+    vo = np.ascontiguousarray(var_of, dtype=np.int32)
+    nlon_o, nlat_o, nz, _ = arrs[5].shape
+    out = _obs_out(nlat_o * nlon_o * nz * vo.size)
+    L = lib()
+    L.orc_obs_regular.restype = C.c_int64
+    L.orc_obs_regular(nlat_o, nlon_o, nz, vo.size, *[_p(a, C.c_float) for a in arrs],
+                      None if rn is None else _p(rn, C.c_float), _p(vo, C.c_int32), *_obs_ptrs(out))
+    return out
+
+
+def struct_atm2endnn(xb, ens_max, n_max, ens_start=1, n_start=1, xb2=None):
+    """struct_atm2endnn (data_trans.F90:2-18): xb C-order [n][nx][ny][ens]
+    (Fortran xb(ens, ny, nx, n)) into xb2 C-order [ny][nx][n_max][ens_max]."""
+    n, nx, ny, ens = xb.shape
+    src = np.ascontiguousarray(xb, dtype=np.float64)
+    out = np.zeros((ny, nx, n_max, ens_max)) if xb2 is None else xb2
+    lib().orc_struct_atm2endnn(ens, n, nx, ny, ens_max, n_max, ens_start, n_start, _p(src, C.c_double),
+                               _p(out, C.c_double))
+    return out
+
+
+def struct_endnn2atm(xb2, ens, n, ens_start=1, n_start=1):
+    """struct_endnn2atm (data_trans.F90:21-38): xb2 [ny][nx][n_max][ens_max] ->
+    xb [n][nx][ny][ens]."""
+    ny, nx, n_max, ens_max = xb2.shape
+    src = np.ascontiguousarray(xb2, dtype=np.float64)
+    out = np.empty((n, nx, ny, ens))
+    lib().orc_struct_endnn2atm(ens, n, nx, ny, ens_max, n_max, ens_start, n_start, _p(src, C.c_double),
+                               _p(out, C.c_double))
+    return out
+
+
+def struct_atm2endnn_a(axb, n_max, n_start=1, axb2=None):
+    n, nx, ny = axb.shape
+    src = np.ascontiguousarray(axb, dtype=np.float64)
+    out = np.zeros((ny, nx, n_max)) if axb2 is None else axb2
+    lib().orc_struct_atm2endnn_a(n, nx, ny, n_max, n_start, _p(src, C.c_double), _p(out, C.c_double))
+    return out
+
+
+def struct_endnn2atm_a(axb2, n, n_start=1):
+    ny, nx, n_max = axb2.shape
+    src = np.ascontiguousarray(axb2, dtype=np.float64)
+    out = np.empty((n, nx, ny))
+    lib().orc_struct_endnn2atm_a(n, nx, ny, n_max, n_start, _p(src, C.c_double), _p(out, C.c_double))
+    return out
+
+
 def schr2(ri: float) -> float:
     return lib().orc_schr2(ri)
 
