@@ -450,3 +450,166 @@ __device__ int lg_jacobi32h(float *W, int *s_rot, float tol, int max_sweeps, flo
     }
     return sweep;
 }
+
+// FP32 one-sided Jacobi with the hierarchical ordering over blocks of two
+// columns (K = 64 or 128, 256 threads): the K/4 slots each hold a fixed block
+// (F1, F2) and a moving block (M1, M2), G = 1024/K lanes per slot and K/G rows
+// per lane; a step does the four rotations between the two blocks, (F1, M1)
+// with (F2, M2) and then (F1, M2) with (F2, M1), each pair of rotations with
+// interleaved inner products, and the last level also rotates the pairs
+// inside the two blocks.  K/2 - 1 steps cover every pair once per sweep, so
+// the moving columns go through half as many passes as in lg_jacobi32h.  A
+// moving block passes to the next slot of its group by warp shuffles; where a
+// group spans warps, every 32/G steps the warps hand their moving blocks on
+// through shared memory (buffers reuse W while the columns are in registers,
+// slot stride 2 BS, alternating by hand-over parity) with one block barrier.
+// Norms and block ids of the handed-on blocks go to `extra` (6 * K/4 words).
+// Returns the sweeps used, or max_sweeps+1 if not converged.
+template <int K, int LD, int BS>
+__device__ int lg_jacobi32b2(float *W, float *extra, int *s_rot, float tol, int max_sweeps)
+{
+    constexpr int NB = K / 2, NSL = NB / 2, G = 256 / NSL, RPL = K / G, SPW = 32 / G;
+    constexpr int VW = (RPL % 4 == 0) ? 4 : 2, NC = RPL / VW;
+    static_assert(K == 64 || K == 128, "block-2 ordering for K = 64 and 128");
+    static_assert(2 * NSL * 2 * BS <= K * LD && LD % VW == 0 && BS % VW == 0, "moving-block buffers fit in W");
+    const int tid = threadIdx.x;
+    const int slot = tid / G, lane = tid % G;
+    const int lw = tid & 31, ws = lw / G, wl = lw % G;
+    const float tol2 = tol * tol;
+    float *buf = W;                                    // [2][NSL][2 columns][BS]
+    float *bn = extra;                                 // [2][NSL][2] squared norms
+    int *bid = reinterpret_cast<int *>(bn + 4 * NSL);  // [2][NSL] block ids
+    float F1[RPL], F2[RPL], M1[RPL], M2[RPL];
+    auto ld = [&](const float *src, float *r) {
+#pragma unroll
+        for (int c = 0; c < NC; c++) {
+            const int o = (c * G + lane) * VW, i = c * VW;
+            if constexpr (VW == 4) {
+                const float4 x = *reinterpret_cast<const float4 *>(src + o);
+                r[i] = x.x; r[i + 1] = x.y; r[i + 2] = x.z; r[i + 3] = x.w;
+            } else {
+                const float2 x = *reinterpret_cast<const float2 *>(src + o);
+                r[i] = x.x; r[i + 1] = x.y;
+            }
+        }
+    };
+    auto st = [&](float *dst, const float *r) {
+#pragma unroll
+        for (int c = 0; c < NC; c++) {
+            const int o = (c * G + lane) * VW, i = c * VW;
+            if constexpr (VW == 4) *reinterpret_cast<float4 *>(dst + o) = make_float4(r[i], r[i + 1], r[i + 2], r[i + 3]);
+            else *reinterpret_cast<float2 *>(dst + o) = make_float2(r[i], r[i + 1]);
+        }
+    };
+    auto pdot = [&](const float *x, const float *y) {
+        unsigned long long a = 0ull;
+#pragma unroll
+        for (int i = 0; i < RPL; i += 2) a = lg_ffma2(lg_pk2(x[i], x[i + 1]), lg_pk2(y[i], y[i + 1]), a);
+        float p0, p1;
+        lg_upk2(a, p0, p1);
+        return p0 + p1;
+    };
+    auto red2 = [&](float &a, float &b) {
+#pragma unroll
+        for (int o = G / 2; o > 0; o >>= 1) {
+            a += __shfl_xor_sync(0xffffffffu, a, o);
+            b += __shfl_xor_sync(0xffffffffu, b, o);
+        }
+    };
+    bool rotated_any = false;
+    auto apply = [&](float *X, float *Y, float &nx, float &ny, float gam) {
+        if (gam * gam > tol2 * (nx * ny)) {
+            float c, s, tt;
+            lg_rotation(nx, ny, gam, c, s, tt);
+            const unsigned long long c2 = lg_pk2(c, c), s2 = lg_pk2(s, s), ns2 = lg_pk2(-s, -s);
+#pragma unroll
+            for (int r = 0; r < RPL; r += 2) {
+                const unsigned long long x = lg_pk2(X[r], X[r + 1]), y = lg_pk2(Y[r], Y[r + 1]);
+                lg_upk2(lg_ffma2(c2, x, lg_fmul2(ns2, y)), X[r], X[r + 1]);
+                lg_upk2(lg_ffma2(s2, x, lg_fmul2(c2, y)), Y[r], Y[r + 1]);
+            }
+            nx = nx - tt * gam;
+            ny = ny + tt * gam;
+            rotated_any = true;
+        }
+    };
+    // two independent rotations with their inner products reduced together
+    auto rot2 = [&](float *X1, float *Y1, float &nx1, float &ny1, float *X2, float *Y2, float &nx2, float &ny2) {
+        float g1 = pdot(X1, Y1), g2 = pdot(X2, Y2);
+        red2(g1, g2);
+        apply(X1, Y1, nx1, ny1, g1);
+        apply(X2, Y2, nx2, ny2, g2);
+    };
+    int sweep, moves = 0;
+    for (sweep = 1; sweep <= max_sweeps; sweep++) {
+        if (tid == 0) *s_rot = 0;
+        rotated_any = false;
+        for (int B = NB; B >= 2; B >>= 1) {            // B blocks per group
+            const int half = B / 2, u = slot / half, i = slot % half;
+            const int fb = u * B + i;
+            int mbk = u * B + half + i;
+            __syncthreads();                           // W holds every column
+            ld(W + (2 * fb) * LD, F1);
+            ld(W + (2 * fb + 1) * LD, F2);
+            ld(W + (2 * mbk) * LD, M1);
+            ld(W + (2 * mbk + 1) * LD, M2);
+            float f1 = pdot(F1, F1), f2 = pdot(F2, F2), m1 = pdot(M1, M1), m2 = pdot(M2, M2);
+            red2(f1, f2);
+            red2(m1, m2);
+            __syncthreads();                           // W becomes the hand-over buffers
+            for (int t = 0; t < half; t++) {
+                rot2(F1, M1, f1, m1, F2, M2, f2, m2);
+                rot2(F1, M2, f1, m2, F2, M1, f2, m1);
+                if (B == 2) rot2(F1, F2, f1, f2, M1, M2, m1, m2);
+                if (t == half - 1) break;
+                const bool handover = half > SPW && (t + 1) % SPW == 0;
+                if (!handover) {
+                    // the next slot of the group inside the warp (cyclic)
+                    const int gs = half < SPW ? half : SPW;
+                    const int gbase = (ws / gs) * gs;
+                    const int src = (gbase + (ws - gbase + 1) % gs) * G + wl;
+#pragma unroll
+                    for (int r = 0; r < RPL; r++) {
+                        M1[r] = __shfl_sync(0xffffffffu, M1[r], src);
+                        M2[r] = __shfl_sync(0xffffffffu, M2[r], src);
+                    }
+                    m1 = __shfl_sync(0xffffffffu, m1, src);
+                    m2 = __shfl_sync(0xffffffffu, m2, src);
+                    mbk = __shfl_sync(0xffffffffu, mbk, src);
+                } else {
+                    // the same slot of the next warp of the group
+                    const int par = moves & 1;
+                    moves++;
+                    const int gw = i / SPW, nw = half / SPW;
+                    const int ss = u * half + ((gw + 1) % nw) * SPW + ws;
+                    float *mine = buf + (size_t)(par * NSL + slot) * 2 * BS;
+                    st(mine, M1);
+                    st(mine + BS, M2);
+                    if (lane == 0) {
+                        bn[(par * NSL + slot) * 2] = m1;
+                        bn[(par * NSL + slot) * 2 + 1] = m2;
+                        bid[par * NSL + slot] = mbk;
+                    }
+                    __syncthreads();
+                    const float *theirs = buf + (size_t)(par * NSL + ss) * 2 * BS;
+                    ld(theirs, M1);
+                    ld(theirs + BS, M2);
+                    m1 = bn[(par * NSL + ss) * 2];
+                    m2 = bn[(par * NSL + ss) * 2 + 1];
+                    mbk = bid[par * NSL + ss];
+                }
+            }
+            __syncthreads();                           // every read of the buffers is done
+            st(W + (2 * fb) * LD, F1);
+            st(W + (2 * fb + 1) * LD, F2);
+            st(W + (2 * mbk) * LD, M1);
+            st(W + (2 * mbk + 1) * LD, M2);
+        }
+        if (rotated_any && lane == 0) *s_rot = 1;
+        __syncthreads();
+        const int rotated = *s_rot;
+        __syncthreads();
+        if (!rotated) break;
+    }
+    return sweep;
+}
