@@ -213,6 +213,9 @@ struct letkf_ctx {
     DevBuf<double> d_plat, d_plon, d_pph, d_pyo, d_prinv;
     DevBuf<int32_t> d_plev, d_pvar, d_pvarof;
     DevBuf<float> d_raw;
+    // staged mixed core (k = 64): per cube A, X (k x k FP32), g (FP64), lambda
+    DevBuf<float> d_mA, d_mX, d_mlam;
+    DevBuf<double> d_mg;
     DevBuf<float> d_ys32;         // yb * sqrt(rinv) in FP32 (mixed precision)
     DevBuf<float> d_rinvf;
     DevBuf<float> d_oef;          // mixed form: sqrt(rdiaginv) dep per obs

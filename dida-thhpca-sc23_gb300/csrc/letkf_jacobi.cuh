@@ -613,3 +613,92 @@ __device__ int lg_jacobi32b2(float *W, float *extra, int *s_rot, float tol, int 
     }
     return sweep;
 }
+
+// FP32 one-sided Jacobi of one K x K problem by one warp (K = 64): lane l
+// owns a column pair in registers, so the inner products need no reduction
+// and a step needs no barrier; the hierarchical ordering passes the moving
+// column to the next lane of its group by shuffles, and the columns are
+// re-dealt through W (column j at W[j*LD ..], this warp's own memory) at each
+// level.  Returns the sweeps used, or max_sweeps+1 if not converged.
+template <int K, int LD>
+__device__ int lg_jacobi32w(float *W, float tol, int max_sweeps)
+{
+    constexpr int NS = K / 2;
+    static_assert(NS == 32 && LD % 4 == 0, "one lane per column pair");
+    const int lane = threadIdx.x & 31;
+    const float tol2 = tol * tol;
+    float F[K], M[K];
+    auto ldc = [&](int col, float *r) {
+        const float4 *src = reinterpret_cast<const float4 *>(W + col * LD);
+#pragma unroll
+        for (int c = 0; c < K / 4; c++) {
+            const float4 x = src[c];
+            r[4 * c] = x.x; r[4 * c + 1] = x.y; r[4 * c + 2] = x.z; r[4 * c + 3] = x.w;
+        }
+    };
+    auto stc = [&](int col, const float *r) {
+        float4 *dst = reinterpret_cast<float4 *>(W + col * LD);
+#pragma unroll
+        for (int c = 0; c < K / 4; c++) dst[c] = make_float4(r[4 * c], r[4 * c + 1], r[4 * c + 2], r[4 * c + 3]);
+    };
+    auto dot = [&](const float *x, const float *y) {
+        unsigned long long a[4] = {0ull, 0ull, 0ull, 0ull};
+#pragma unroll
+        for (int i = 0; i < K; i += 8) {
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+                a[q] = lg_ffma2(lg_pk2(x[i + 2 * q], x[i + 2 * q + 1]), lg_pk2(y[i + 2 * q], y[i + 2 * q + 1]), a[q]);
+        }
+        float s = 0.0f;
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            float p0, p1;
+            lg_upk2(a[q], p0, p1);
+            s += p0 + p1;
+        }
+        return s;
+    };
+    int sweep;
+    for (sweep = 1; sweep <= max_sweeps; sweep++) {
+        bool rot = false;
+        for (int B = K; B >= 2; B >>= 1) {
+            const int half = B / 2, u = lane / half, i = lane % half;
+            const int fc = u * B + i;
+            int mc = u * B + half + i;
+            __syncwarp();
+            ldc(fc, F);
+            ldc(mc, M);
+            float fa = dot(F, F), mb = dot(M, M);
+            for (int t = 0; t < half; t++) {
+                const float gam = dot(F, M);
+                if (gam * gam > tol2 * (fa * mb)) {
+                    float c, s, tt;
+                    lg_rotation(fa, mb, gam, c, s, tt);
+                    const unsigned long long c2 = lg_pk2(c, c), s2 = lg_pk2(s, s), ns2 = lg_pk2(-s, -s);
+#pragma unroll
+                    for (int r = 0; r < K; r += 2) {
+                        const unsigned long long x = lg_pk2(F[r], F[r + 1]), y = lg_pk2(M[r], M[r + 1]);
+                        lg_upk2(lg_ffma2(c2, x, lg_fmul2(ns2, y)), F[r], F[r + 1]);
+                        lg_upk2(lg_ffma2(s2, x, lg_fmul2(c2, y)), M[r], M[r + 1]);
+                    }
+                    fa = fa - tt * gam;
+                    mb = mb + tt * gam;
+                    rot = true;
+                }
+                if (t == half - 1) break;
+                // the moving column of the next lane of the group
+                const int src = u * half + (i + 1) % half;
+#pragma unroll
+                for (int r = 0; r < K; r++) M[r] = __shfl_sync(0xffffffffu, M[r], src);
+                mb = __shfl_sync(0xffffffffu, mb, src);
+                mc = __shfl_sync(0xffffffffu, mc, src);
+            }
+            __syncwarp();
+            stc(fc, F);
+            stc(mc, M);
+        }
+        if (!__any_sync(0xffffffffu, rot)) break;
+    }
+    __syncwarp();
+    return sweep;
+}

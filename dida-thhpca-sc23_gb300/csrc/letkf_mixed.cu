@@ -105,14 +105,20 @@ __device__ __forceinline__ double block_sum(double v, double *red)
     return t;
 }
 
-template <int K>
+// ST selects the stages a launch runs: 0 all of them; 1 the A build only
+// (A without the diagonal shift and g to mA, mgv); 2 from the eigenpairs on
+// (X and lambda from mX, mlam, written by k_eig_warp).  The intermediates
+// are indexed by cube - prm.cube0.
+template <int K, int ST>
 __global__ void __launch_bounds__(kT, 2)
 k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32_t *__restrict__ lidx,
              const float2 *__restrict__ lmeta, const int *__restrict__ queue, int nchunks, int chunk,
              const int64_t *__restrict__ loff, const int32_t *__restrict__ lcnt, int64_t ncubes,
              const double *__restrict__ xb, const double *__restrict__ axb, double *__restrict__ xa,
              double *__restrict__ axa, double *__restrict__ trans_out, double *__restrict__ w_out,
-             unsigned long long *__restrict__ counters, unsigned *__restrict__ status)
+             unsigned long long *__restrict__ counters, unsigned *__restrict__ status,
+             float *__restrict__ mA, double *__restrict__ mgv, const float *__restrict__ mX,
+             const float *__restrict__ mlam)
 {
     using C = MCfg<K>;
     constexpr int CH = C::CH;
@@ -209,7 +215,21 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
         const int64_t off = loff[cube];
         const int p = lcnt[cube];
         LG_PHASE(6);
+        const int64_t ci = cube - prm.cube0;                 // index of the stage intermediates
+        constexpr int LDD = K + 1;                             // padded rows: conflict-free both ways
+        float *Dhh = reinterpret_cast<float *>(area);
+        float *Dlh = Dhh + K * LDD;
+        float *W32 = reinterpret_cast<float *>(area);          // FP32 Jacobi columns (stride LDW)
+        float *A32 = W32 + K * C::LDW;                          // A' in FP32 (warm start)
+        float *Vprev = reinterpret_cast<float *>(area + 49152); // previous cube's X by rows, FP32
+        float *X32 = reinterpret_cast<float *>(area);            // X32[j*K + r] = x_j[r]
+        float *ilam32 = reinterpret_cast<float *>(misc);     // 1/lambda (misc: 2K doubles = 4K floats)
+        float *hc32 = ilam32 + K, *w32 = hc32 + K, *r32 = w32 + K;
+        const double cdiag = (double)(K - 1) / prm.inflation;
+        (void)w32;
+        (void)ci;
 
+        if (ST != 2) {
         // ---------------- phase 1: A and g on the tensor cores ----------------------
         // Tile rows: Yhat_lo (0..K-1), Yhat_hi (K..2K-1), e_hi (2K), e_lo (2K+1),
         // zeros to TROWS.  The A operand is rows 0..127, the B operand rows
@@ -337,12 +357,6 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
 
         LG_PHASE(0);
         // ---------------- phase 2: A' = HH + LH + LH^T + (k-1)/rho I -------------------
-        constexpr int LDD = K + 1;                             // padded rows: conflict-free both ways
-        float *Dhh = reinterpret_cast<float *>(area);
-        float *Dlh = Dhh + K * LDD;
-        float *W32 = reinterpret_cast<float *>(area);          // FP32 Jacobi columns (stride LDW)
-        float *A32 = W32 + K * C::LDW;                          // A' in FP32 (warm start)
-        float *Vprev = reinterpret_cast<float *>(area + 49152); // previous cube's X by rows, FP32
         if (warp < 4) {
             const int row = warp * 32 + lane;
             const uint32_t tl = tmem + ((uint32_t)(warp * 32) << 16);
@@ -377,15 +391,37 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
         __syncthreads();
         // A = HH + LH + LH^T is formed in FP32 (the accumulators are FP32), then
         // A' = A + (k-1)/rho I in FP64 and in FP32 for the Jacobi
-        if (tid < K) gv[tid] = misc[K + tid] + misc[tid];
-        const double cdiag = (double)(K - 1) / prm.inflation;
+        if (tid < K) {
+            gv[tid] = misc[K + tid] + misc[tid];
+            if (ST == 1) mgv[ci * K + tid] = gv[tid];
+        }
         for (int idx = tid; idx < K * K; idx += kT) {
             const int i = idx / K, j = idx % K;
             const float a32 = 0.5f * (Dhh[i * LDD + j] + Dhh[j * LDD + i]) + (Dlh[i * LDD + j] + Dlh[j * LDD + i]);
             const double a = (double)a32 + (i == j ? cdiag : 0.0);
             B1[idx] = a;
+            if (ST == 1) mA[ci * K * K + idx] = a32;
         }
         __syncthreads();                                   // Dhh/Dlh are dead
+        }
+        if (ST == 1) continue;
+        if (ST == 2) {
+            // this cube's g, A' and eigenpairs from the build and eigensolve launches
+            if (tid < K) gv[tid] = mgv[ci * K + tid];
+            for (int idx = tid; idx < K * K; idx += kT) {
+                const int i = idx / K, j = idx % K;
+                B1[idx] = (double)mA[ci * K * K + idx] + (i == j ? cdiag : 0.0);
+            }
+            for (int idx = tid; idx < K * K / 4; idx += kT)
+                reinterpret_cast<float4 *>(X32)[idx] = reinterpret_cast<const float4 *>(mX + ci * K * K)[idx];
+            if (tid < K) {
+                const float lamf = mlam[ci * K + tid];
+                ilam32[tid] = 1.0f / lamf;
+                hc32[tid] = sqrtf((float)(K - 1) / lamf);
+            }
+            __syncthreads();
+        }
+        if (ST == 0) {
         if (!have_prev) {
             // cold start: the Jacobi works on A' itself
             for (int idx = tid; idx < K * K; idx += kT) W32[(idx / K) * C::LDW + idx % K] = (float)B1[idx];
@@ -434,8 +470,6 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
         }
         // lambda_j = |w_j| (A' is SPD, so the converged columns are lambda_j x_j),
         // one warp per column
-        float *ilam32 = reinterpret_cast<float *>(misc);     // 1/lambda (misc: 2K doubles = 4K floats)
-        float *hc32 = ilam32 + K, *w32 = hc32 + K, *r32 = w32 + K;
         for (int j = warp; j < K; j += kT / 32) {
             float s = 0.0f;
             for (int r = lane; r < K; r += 32) s = fmaf(W32[j * C::LDW + r], W32[j * C::LDW + r], s);
@@ -468,7 +502,6 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
         // ---------------- phase 4: X, wbar with one refinement step ------------------------
         // X by columns in FP32 (T, wbar, warm start).  W32 shares this memory, so
         // the values pass through registers first.
-        float *X32 = reinterpret_cast<float *>(area);            // X32[j*K + r] = x_j[r]
         {
             constexpr int PER = (K * K + kT - 1) / kT;
             float xv[PER];
@@ -483,10 +516,11 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
                 const int idx = tid + q * kT;
                 if (idx < K * K) X32[idx] = xv[q];
             }
-            if (tid < K) {
-                nrm32[tid] = hc32[tid];                    // f for T
-                r32[tid] = (float)gv[tid];                 // right-hand side of the first solve
-            }
+        }
+        }
+        if (tid < K) {
+            nrm32[tid] = hc32[tid];                    // f for T
+            r32[tid] = (float)gv[tid];                 // right-hand side of the first solve
         }
         __syncthreads();
         // wbar = X diag(1/lambda) X^T g in FP32, then one refinement step:
@@ -563,10 +597,11 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
                 }
             }
             // keep X by rows for the next cube's warm start
-            for (int idx = tid; idx < K * K; idx += kT) {
-                const int r = idx / K, j = idx % K;
-                Vprev[idx] = X32[j * K + r];
-            }
+            if (ST == 0)
+                for (int idx = tid; idx < K * K; idx += kT) {
+                    const int r = idx / K, j = idx % K;
+                    Vprev[idx] = X32[j * K + r];
+                }
             // B1 (A') was last read before the previous barrier
 #pragma unroll
             for (int m = 0; m < C::ML; m++) {
@@ -795,38 +830,207 @@ cudaError_t lg_build_chunk_queue(letkf_ctx *ctx, int &chunk, int &nchunks)
 
 namespace {
 
+// Eigenpairs of A' = A + (k-1)/rho I for the cubes cube0 .. cube_end-1, one
+// warp per eigenproblem (the staged form of k_core_mixed): each lane owns a
+// column pair of the one-sided Jacobi in registers (lg_jacobi32w), so a step
+// needs no block barrier and moves columns by shuffles.  The cubes go in runs
+// of R consecutive cubes aligned to multiples of R in cube numbering (the
+// work-queue chunks); inside a run each cube starts from the previous one's
+// eigenvectors, W = A' V_prev, the first cold from W = A'.  Writes x_j
+// (columns, FP32, [j][r]) and lambda_j, and the sweep and conditioning
+// counters.
 template <int K>
-cudaError_t launch_mixed(letkf_ctx *ctx, const LgGrid &g, const double *xb, const double *axb,
-                         double *xa, double *axa, double *trans_out, double *w_out)
+__global__ void __launch_bounds__(kT, 1)
+k_eig_warp(int64_t cube0, int64_t cube_end, int R, double cdiag, float tol, const float *__restrict__ mA,
+           float *__restrict__ mX, float *__restrict__ mlam, unsigned long long *__restrict__ counters)
+{
+    constexpr int LDW = K + 4, NS = K / 2;
+    static_assert(NS == 32, "one lane per column pair");
+    extern __shared__ float smw[];
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    float *Wp = smw + (size_t)warp * K * LDW;           // this warp's columns
+    const int64_t base = cube0 / R * R;
+    const int64_t nruns = (cube_end - base + R - 1) / R;
+    const int64_t nw = (int64_t)gridDim.x * (kT / 32);
+    const float cd = (float)cdiag;
+    for (int64_t run = blockIdx.x * (int64_t)(kT / 32) + warp; run < nruns; run += nw) {
+        const int64_t c0 = max(cube0, base + run * R), c1 = min(cube_end, base + (run + 1) * R);
+        for (int64_t c = c0; c < c1; c++) {
+            const float *Ac = mA + (c - cube0) * K * K;
+            // W columns lane and lane + NS into Wp (each lane reads and writes
+            // only its own two columns)
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const int j = lane + h * NS;
+                float4 *dst = reinterpret_cast<float4 *>(Wp + j * LDW);
+                if (c == c0) {
+                    // cold: column j of A' is row j (A' symmetric)
+                    const float4 *row = reinterpret_cast<const float4 *>(Ac + j * K);
+#pragma unroll
+                    for (int q = 0; q < K / 4; q++) {
+                        float4 x = row[q];
+                        if (4 * q == (j & ~3)) {
+                            const int r = j & 3;
+                            if (r == 0) x.x += cd; else if (r == 1) x.y += cd; else if (r == 2) x.z += cd; else x.w += cd;
+                        }
+                        dst[q] = x;
+                    }
+                } else {
+                    // warm: w_j = A' v_j = sum_l A[l][:] v_j[l] + cd v_j (A symmetric;
+                    // all lanes read the same row of A at once, each its own v_j[l])
+                    const float *vj = Wp + j * LDW;
+                    unsigned long long acc[K / 2];
+#pragma unroll
+                    for (int q = 0; q < K / 4; q++) {
+                        const float4 x = reinterpret_cast<const float4 *>(vj)[q];
+                        acc[2 * q] = lg_pk2(cd * x.x, cd * x.y);
+                        acc[2 * q + 1] = lg_pk2(cd * x.z, cd * x.w);
+                    }
+#pragma unroll 1
+                    for (int l = 0; l < K; l++) {
+                        const float4 *row = reinterpret_cast<const float4 *>(Ac + l * K);
+                        const float vl = vj[l];
+                        const unsigned long long v2 = lg_pk2(vl, vl);
+#pragma unroll
+                        for (int q = 0; q < K / 4; q++) {
+                            const float4 x = row[q];
+                            acc[2 * q] = lg_ffma2(lg_pk2(x.x, x.y), v2, acc[2 * q]);
+                            acc[2 * q + 1] = lg_ffma2(lg_pk2(x.z, x.w), v2, acc[2 * q + 1]);
+                        }
+                    }
+#pragma unroll
+                    for (int q = 0; q < K / 4; q++) {
+                        float a, b, cc, d;
+                        lg_upk2(acc[2 * q], a, b);
+                        lg_upk2(acc[2 * q + 1], cc, d);
+                        dst[q] = make_float4(a, b, cc, d);
+                    }
+                }
+            }
+            __syncwarp();
+            const int sw = lg_jacobi32w<K, LDW>(Wp, tol, 24);
+            // lambda_j = |w_j|, x_j = w_j / lambda_j (kept in Wp for the next cube)
+            float lo = 3.0e38f, hi = 0.0f;
+#pragma unroll
+            for (int h = 0; h < 2; h++) {
+                const int j = lane + h * NS;
+                float4 *col = reinterpret_cast<float4 *>(Wp + j * LDW);
+                float s = 0.0f;
+#pragma unroll
+                for (int q = 0; q < K / 4; q++) {
+                    const float4 x = col[q];
+                    s = fmaf(x.x, x.x, fmaf(x.y, x.y, fmaf(x.z, x.z, fmaf(x.w, x.w, s))));
+                }
+                const float lamf = sqrtf(s), il = 1.0f / lamf;
+                float4 *out = reinterpret_cast<float4 *>(mX + (c - cube0) * K * K + j * K);
+#pragma unroll
+                for (int q = 0; q < K / 4; q++) {
+                    float4 x = col[q];
+                    x.x *= il; x.y *= il; x.z *= il; x.w *= il;
+                    col[q] = x;
+                    out[q] = x;
+                }
+                mlam[(c - cube0) * K + j] = lamf;
+                lo = fminf(lo, lamf);
+                hi = fmaxf(hi, lamf);
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+                hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+            }
+            if (lane == 0) {
+                atomicMax(&counters[LG_CNT_MAXSWEEP], (unsigned long long)sw);
+                atomicAdd(&counters[LG_CNT_SUMSWEEP], (unsigned long long)sw);
+                if (sw > 24) atomicAdd(&counters[LG_CNT_NOTCONV], 1ull);
+                if (hi > 1.0e4f * lo) atomicAdd(&counters[LG_CNT_ILLCOND], 1ull);
+            }
+            __syncwarp();
+        }
+    }
+}
+
+// Most cubes one staged launch sequence holds intermediates for (A, X: 2 k^2
+// floats, g: k doubles, lambda: k floats per cube); a multiple of every
+// work-queue chunk size.
+constexpr int64_t kStagedCubes = 1 << 17;
+
+template <int K, int ST>
+cudaError_t launch_stage(letkf_ctx *ctx, const LgGrid &g, const double *xb, const double *axb, double *xa,
+                         double *axa, double *trans_out, double *w_out, int chunk, int nchunks, int nsm)
 {
     const size_t smem = MCfg<K>::SMEM;
-    cudaError_t e = cudaFuncSetAttribute(k_core_mixed<K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaError_t e = cudaFuncSetAttribute(k_core_mixed<K, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                          (int)smem);
     if (e != cudaSuccess) return e;
-    if (ctx->win1 <= ctx->win0) return cudaSuccess;
-    e = cudaFuncSetAttribute(k_core_mixed<K>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    e = cudaFuncSetAttribute(k_core_mixed<K, ST>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     if (e != cudaSuccess) return e;
-    int dev = 0, nsm = 0, smem_sm = 0;
+    int dev = 0, smem_sm = 0;
     cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
     // two CTAs per SM when their shared memory fits (registers are capped at
     // 128 per thread by the launch bounds, so two 256-thread CTAs fit)
     const int per_sm = (2 * (smem + 1024) <= (size_t)smem_sm) ? 2 : 1;
-    // work queue (chunks of consecutive cubes, heaviest first)
-    int chunk = 0, nchunks = 0;
-    e = lg_build_chunk_queue(ctx, chunk, nchunks);
-    if (e != cudaSuccess) return e;
     // persistent grid: each CTA allocates its tensor memory once
     const int64_t want = (int64_t)nsm * per_sm;
     const unsigned blocks = (unsigned)(nchunks < want ? nchunks : want);
+    // the CTAs take chunks with the queue cursor
+    e = cudaMemsetAsync(ctx->d_counters.p + LG_CNT_QUEUE, 0, sizeof(unsigned long long), ctx->stream);
+    if (e != cudaSuccess) return e;
     lg_count_launch();
-    k_core_mixed<K><<<blocks, kT, smem, ctx->stream>>>(
+    k_core_mixed<K, ST><<<blocks, kT, smem, ctx->stream>>>(
         g, lg_params(ctx), ctx->d_ys32.p, ctx->d_lidx.p, ctx->d_lmeta.p, ctx->d_queue.p, nchunks, chunk,
-        ctx->d_loff.p, ctx->d_lcnt.p,
-        ctx->win1, xb, axb, xa, axa, trans_out, w_out,
-        ctx->d_counters.p, ctx->d_status.p);
+        ctx->d_loff.p, ctx->d_lcnt.p, ctx->win1, xb, axb, xa, axa, trans_out, w_out, ctx->d_counters.p,
+        ctx->d_status.p, ctx->d_mA.p, ctx->d_mg.p, ctx->d_mX.p, ctx->d_mlam.p);
     return cudaGetLastError();
+}
+
+template <int K>
+cudaError_t launch_mixed(letkf_ctx *ctx, const LgGrid &g, const double *xb, const double *axb,
+                         double *xa, double *axa, double *trans_out, double *w_out)
+{
+    if (ctx->win1 <= ctx->win0) return cudaSuccess;
+    int dev = 0, nsm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    int chunk = 0, nchunks = 0;
+    if constexpr (K != 64) {
+        // one launch: A build, eigensolve and update per cube
+        cudaError_t e = lg_build_chunk_queue(ctx, chunk, nchunks);
+        if (e != cudaSuccess) return e;
+        return launch_stage<K, 0>(ctx, g, xb, axb, xa, axa, trans_out, w_out, chunk, nchunks, nsm);
+    } else {
+        // staged: the A build (work queue), the eigenproblems one warp each,
+        // the update (work queue), over blocks of at most kStagedCubes cubes
+        const int64_t w0 = ctx->win0, w1 = ctx->win1;
+        const int R = lg_run_chunk(ctx);
+        const size_t ew = (size_t)K * (K + 4) * sizeof(float) * (kT / 32);
+        cudaError_t e = cudaFuncSetAttribute(k_eig_warp<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ew);
+        for (int64_t b0 = w0; b0 < w1 && e == cudaSuccess; b0 += kStagedCubes) {
+            const int64_t b1 = min(w1, b0 + kStagedCubes), nb = b1 - b0;
+            ctx->win0 = b0;
+            ctx->win1 = b1;
+            if ((e = ctx->d_mA.reserve((size_t)nb * K * K)) != cudaSuccess) break;
+            if ((e = ctx->d_mX.reserve((size_t)nb * K * K)) != cudaSuccess) break;
+            if ((e = ctx->d_mg.reserve((size_t)nb * K)) != cudaSuccess) break;
+            if ((e = ctx->d_mlam.reserve((size_t)nb * K)) != cudaSuccess) break;
+            if ((e = lg_build_chunk_queue(ctx, chunk, nchunks)) != cudaSuccess) break;
+            e = launch_stage<K, 1>(ctx, g, xb, axb, xa, axa, trans_out, w_out, chunk, nchunks, nsm);
+            if (e != cudaSuccess) break;
+            const int64_t runs = (b1 - b0 / R * R + R - 1) / R;
+            const int64_t eb = (runs + kT / 32 - 1) / (kT / 32);
+            const unsigned eblocks = (unsigned)(eb < nsm ? eb : nsm);
+            lg_count_launch();
+            k_eig_warp<K><<<eblocks, kT, ew, ctx->stream>>>(b0, b1, R, (double)(K - 1) / ctx->params.inflation,
+                                                          LG_MIXED_JACOBI_TOL, ctx->d_mA.p, ctx->d_mX.p,
+                                                          ctx->d_mlam.p, ctx->d_counters.p);
+            if ((e = cudaGetLastError()) != cudaSuccess) break;
+            e = launch_stage<K, 2>(ctx, g, xb, axb, xa, axa, trans_out, w_out, chunk, nchunks, nsm);
+        }
+        ctx->win0 = w0;
+        ctx->win1 = w1;
+        return e;
+    }
 }
 
 }  // namespace
