@@ -450,7 +450,9 @@ def run_ours(args, rank, world, local_rank):
         scale = 1e9 if pipe == "hbm" else 1e12
         achieved = work[pipe] / (core * 1e-3) / scale
         peak = peaks.get("hbm_gbs", 6800.0) if pipe == "hbm" else pk[pipe]
-        roof = {"bound": pipe, "kernel": f"k_core_mixed<{w.k}>",
+        kname = (f"k_core_mixed<{w.k},1> + k_eig_warp<{w.k}> + k_core_mixed<{w.k},2> (the staged core)"
+                 if w.k == 64 else f"k_core_mixed<{w.k},0>")
+        roof = {"bound": pipe, "kernel": kname,
                 "achieved": achieved, "peak": peak, "unit": unit, "frac": achieved / peak,
                 "traffic": traffic, "kernel_ms": core,
                 "work": "algorithmic work per pipe: tensor 2k^2(p+n) + 2kp, FP32 13k^3, FP64 "

@@ -2,6 +2,26 @@
 // core kernels: BF16 hi/lo splitting and cp.async row copies.
 #pragma once
 
+// float -> double without the FP64 pipe (which is narrow on this part): the
+// conversion is exact, so it is done on the integer pipe from the bits.
+// Zeros and subnormal floats become signed zeros; infinities and NaNs keep
+// their kind.
+__device__ __forceinline__ double lg_f2d_bits(float f)
+{
+    const unsigned u = __float_as_uint(f);
+    const unsigned sign = u & 0x80000000u, ex = (u >> 23) & 0xffu, man = u & 0x7fffffu;
+    unsigned hi, lo;
+    if (ex == 0u) {
+        hi = sign;
+        lo = 0u;
+    } else {
+        const unsigned e64 = (ex == 0xffu) ? 0x7ffu : ex + 896u;   // 1023 - 127
+        hi = sign | (e64 << 20) | (man >> 3);
+        lo = man << 29;
+    }
+    return __hiloint2double((int)hi, (int)lo);
+}
+
 #include <cuda_bf16.h>
 #include <stdint.h>
 

@@ -595,17 +595,24 @@ k_core_mixed_wide(LgGrid g, LgParams prm, const float *__restrict__ ys32, const 
                     if (warp < 4) {
                         const int r = warp * 32 + lane;
                         const uint32_t tl = tmem + ((uint32_t)(warp * 32) << 16);
-                        double sum = 0.0;
+                        // member mean and perturbations in FP32 (the products are
+                        // FP32 sums of BF16 hi/lo terms), written as FP64 with the
+                        // conversion on the integer pipe
+                        float part[8];
+#pragma unroll
+                        for (int q = 0; q < 8; q++) part[q] = 0.0f;
                         for (int c0 = 0; c0 < K; c0 += 16) {
                             float v[16];
                             lg_tmem_ld16(tl + (uint32_t)c0, v);
 #pragma unroll
-                            for (int e = 0; e < 16; e++) sum += (double)v[e];
+                            for (int e = 0; e < 16; e++) part[e & 7] += v[e];
                         }
-                        const double mean = sum / K;
+                        const float meanf =
+                            (((part[0] + part[1]) + (part[2] + part[3])) + ((part[4] + part[5]) + (part[6] + part[7]))) /
+                            (float)K;
                         if (r < R) {
                             const int64_t row = col * n + r0 + r;
-                            axa[row] = axb[row] + inc[r] + mean;
+                            axa[row] = axb[row] + inc[r] + lg_f2d_bits(meanf);
                         }
                         double *dst = xac + (int64_t)(r0 + r) * K;
                         for (int c0 = 0; c0 < K; c0 += 16) {
@@ -615,7 +622,7 @@ k_core_mixed_wide(LgGrid g, LgParams prm, const float *__restrict__ ys32, const 
 #pragma unroll
                                 for (int e = 0; e < 16; e += 2)
                                     *reinterpret_cast<double2 *>(dst + c0 + e) =
-                                        make_double2((double)v[e] - mean, (double)v[e + 1] - mean);
+                                        make_double2(lg_f2d_bits(v[e] - meanf), lg_f2d_bits(v[e + 1] - meanf));
                             }
                         }
                     }
