@@ -841,8 +841,8 @@ namespace {
 // warp per eigenproblem (the staged form of k_core_mixed): each lane owns a
 // column pair of the one-sided Jacobi in registers (lg_jacobi32w), so a step
 // needs no block barrier and moves columns by shuffles.  The cubes go in runs
-// of R consecutive cubes aligned to multiples of R in cube numbering (the
-// work-queue chunks); inside a run each cube starts from the previous one's
+// of R consecutive cubes aligned to multiples of R in cube numbering; inside a
+// run each cube starts from the previous one's
 // eigenvectors, W = A' V_prev, the first cold from W = A'.  Writes x_j
 // (columns, FP32, [j][r]) and lambda_j, and the sweep and conditioning
 // counters.
@@ -1010,7 +1010,10 @@ cudaError_t launch_mixed(letkf_ctx *ctx, const LgGrid &g, const double *xb, cons
         // staged: the A build (work queue), the eigenproblems one warp each,
         // the update (work queue), over blocks of at most kStagedCubes cubes
         const int64_t w0 = ctx->win0, w1 = ctx->win1;
-        const int R = lg_run_chunk(ctx);
+        // eigensolve runs of 8 cubes: short enough to spread evenly over the
+        // warps, aligned so that every window boundary (a multiple of the
+        // work-queue chunk, itself a multiple of 8) is a run boundary
+        const int R = 8;
         const size_t ew = (size_t)K * (K + 4) * sizeof(float) * (kT / 32);
         cudaError_t e = cudaFuncSetAttribute(k_eig_warp<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ew);
         for (int64_t b0 = w0; b0 < w1 && e == cudaSuccess; b0 += kStagedCubes) {
