@@ -50,6 +50,12 @@ __device__ __forceinline__ double ph_mid(const LgGrid &g, int i /* 0-based level
     return 0.5 * (ph_interface(g, i, ps) + ph_interface(g, i + 1, ps));
 }
 
+// One warp per group of 32 observations.  The per-observation scalar terms
+// (validity, grid cell, weights, geometry, bucket; FP64 trig and divides) run
+// one observation per lane, so a warp instruction serves 32 observations; the
+// warp then sweeps the group one observation at a time with the lanes over the
+// members, taking the cell from the owning lane by shuffles.  Arithmetic per
+// observation is the same as in the one-warp-per-observation form.
 __global__ void __launch_bounds__(256)
 k_obs_prepare(LgGrid g, LgParams prm, const double *__restrict__ xb, const double *__restrict__ axb,
               int64_t nobs, const double *__restrict__ olat, const double *__restrict__ olon,
@@ -65,130 +71,164 @@ k_obs_prepare(LgGrid g, LgParams prm, const double *__restrict__ xb, const doubl
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const int k = g.k, n = g.n;
+    // the mean as sum * 2^-m when k is a power of two (exact, equal to sum / k)
+    const bool kpow2 = (k & (k - 1)) == 0;
+    const double invk = 1.0 / (double)k;
 
-    for (int64_t o = warp; o < nobs; o += nwarps) {
-        const double lat = olat[o], lon = olon[o];
-        const int v = ovar[o];
-        const bool is3d = v >= g.nvar2d;
-        int lev = 1;
-        bool ok = (lat >= -90.0 && lat <= 90.0 && lon >= 0.0 && lon <= 360.0 &&
-                   v >= 0 && v < g.nvar2d + g.nvar3d);
-        if (ok && is3d && prm.h_mode == 1) {
-            lev = olev[o];
-            ok = lev >= 1 && lev <= g.nz;
-        }
-        if (ok && is3d && prm.h_mode == 0) ok = oph[o] > 0.0;
-        if (!ok) {
-            for (int e = lane; e < k; e += 32) {
-                yb[o * k + e] = 0.0;
-                if (ys32) ys32[o * k + e] = 0.0f;
+    for (int64_t base = warp * 32; base < nobs; base += nwarps * 32) {
+        // ---- per-observation terms, observation base + lane on this lane
+        const int64_t o = base + lane;
+        Corners q{0, 0, 0, 0, 0.0, 0.0};
+        int row = 0;             // state row, or the variable's first level (pressure search)
+        bool ok = false, psearch = false;
+        double sr = 0.0, p_obs = 0.0;
+        if (o < nobs) {
+            const double lat = olat[o], lon = olon[o];
+            const int v = ovar[o];
+            const bool is3d = v >= g.nvar2d;
+            int lev = 1;
+            ok = (lat >= -90.0 && lat <= 90.0 && lon >= 0.0 && lon <= 360.0 &&
+                  v >= 0 && v < g.nvar2d + g.nvar3d);
+            if (ok && is3d && prm.h_mode == 1) {
+                lev = olev[o];
+                ok = lev >= 1 && lev <= g.nz;
             }
-            if (lane == 0) {
+            if (ok && is3d && prm.h_mode == 0) ok = oph[o] > 0.0;
+            if (!ok) {
                 dep[o] = 0.0;
                 rinvf[o] = 0.0f;
                 if (oef) oef[o] = 0.0f;
                 obucket[o] = -1;
                 atomicOr(status, LG_ST_BAD_OBS);
-            }
-            continue;
-        }
-        // find_obs_grid (letkf_obs.F90:199-241); the spacing is a float difference
-        const int tx = first_ge(g.glat, g.nlat + 1, lat);
-        const int ty = first_ge(g.glon, g.nlon + 1, lon);
-        double ax = 0.0, ay = 0.0;
-        if (tx > 1) {
-            const double dlat = (double)(g.glat[tx - 1] - g.glat[tx - 2]);
-            ax = (dlat - lat + (double)g.glat[tx - 2]) / dlat;
-        }
-        if (ty > 1) {
-            const double dlon = (double)(g.glon[ty - 1] - g.glon[ty - 2]);
-            ay = (dlon - lon + (double)g.glon[ty - 2]) / dlon;
-        }
-        Corners q;
-        {
-            // rows beyond the poles clamp, columns wrap around the circle
-            const int la0 = min(max(tx - 2, 0), g.nlat - 1), la1 = min(max(tx - 1, 0), g.nlat - 1);
-            const int lo0 = ((ty - 2) % g.nlon + g.nlon) % g.nlon, lo1 = (ty - 1) % g.nlon;
-            q.c11 = la0 + (int64_t)g.nlat * lo0;
-            q.c21 = la1 + (int64_t)g.nlat * lo0;
-            q.c12 = la0 + (int64_t)g.nlat * lo1;
-            q.c22 = la1 + (int64_t)g.nlat * lo1;
-            q.t1 = ax;
-            q.t2 = ay;
-        }
-        const int start = is3d ? g.nvar2d + (v - g.nvar2d) * g.nz : v;
-        double sum = 0.0;
-        double yv[LG_MAX_ENS / 32];
-#pragma unroll
-        for (int j = 0; j < LG_MAX_ENS / 32; j++) {
-            const int e = lane + 32 * j;
-            double y = 0.0;
-            if (e < k) {
-                if (!is3d) {
-                    y = bilin(xb, axb, n, k, q, start, e);
-                } else if (prm.h_mode == 1) {
-                    y = bilin(xb, axb, n, k, q, start + lev - 1, e);
-                } else {
-                    // member's pressure profile, level search, log-p interpolation
-                    const double ps = bilin(xb, axb, n, k, q, g.ps_row, e);
-                    const double p_obs = oph[o];
-                    int jl = 1;
-                    while (jl <= g.nz && p_obs > ph_mid(g, jl - 1, ps)) jl++;
-                    const int pos = jl - 1;
-                    if (pos >= 1 && pos < g.nz) {
-                        const int tl = start + pos - 1;
-                        const double pa = ph_mid(g, pos, ps), pb = ph_mid(g, pos - 1, ps);
-                        const double t3 = (log(pa) - log(p_obs)) / (log(pa) - log(pb));
-                        const double r1 = bilin(xb, axb, n, k, q, tl, e);
-                        const double r3 = bilin(xb, axb, n, k, q, tl + 1, e);
-                        y = r1 * t3 + r3 * (1.0 - t3);
-                    } else {
-                        const int tl = (pos == 0) ? start : start + g.nz - 1;
-                        y = bilin(xb, axb, n, k, q, tl, e);
-                    }
+            } else {
+                // find_obs_grid (letkf_obs.F90:199-241); the spacing is a float difference
+                const int tx = first_ge(g.glat, g.nlat + 1, lat);
+                const int ty = first_ge(g.glon, g.nlon + 1, lon);
+                double ax = 0.0, ay = 0.0;
+                if (tx > 1) {
+                    const double dlat = (double)(g.glat[tx - 1] - g.glat[tx - 2]);
+                    ax = (dlat - lat + (double)g.glat[tx - 2]) / dlat;
                 }
-                sum += y;
+                if (ty > 1) {
+                    const double dlon = (double)(g.glon[ty - 1] - g.glon[ty - 2]);
+                    ay = (dlon - lon + (double)g.glon[ty - 2]) / dlon;
+                }
+                // rows beyond the poles clamp, columns wrap around the circle
+                const int la0 = min(max(tx - 2, 0), g.nlat - 1), la1 = min(max(tx - 1, 0), g.nlat - 1);
+                const int lo0 = ((ty - 2) % g.nlon + g.nlon) % g.nlon, lo1 = (ty - 1) % g.nlon;
+                q.c11 = la0 + (int64_t)g.nlat * lo0;
+                q.c21 = la1 + (int64_t)g.nlat * lo0;
+                q.c12 = la0 + (int64_t)g.nlat * lo1;
+                q.c22 = la1 + (int64_t)g.nlat * lo1;
+                q.t1 = ax;
+                q.t2 = ay;
+                const int start = is3d ? g.nvar2d + (v - g.nvar2d) * g.nz : v;
+                psearch = is3d && prm.h_mode == 0;
+                row = (is3d && prm.h_mode == 1) ? start + lev - 1 : start;
+                if (psearch) p_obs = oph[o];
+                const float rf = (float)orinv[o];
+                rinvf[o] = rf;
+                // scaled perturbations for the tensor-core products: y sqrt(rdiaginv)
+                sr = sqrt((double)rf);
+                const double xr = lg_rad(lat), yr = lg_rad(lon);
+                const double s = sin(xr), c = cos(xr);
+                os[o] = s;
+                oc[o] = c;
+                oyr[o] = yr;
+                oxyz[o] = make_float4((float)(c * cos(yr)), (float)(c * sin(yr)), (float)s,
+                                      __int_as_float((int)o));
+                int b = -1;
+                if (fabs(lat) <= prm.obs_polar) {
+                    int bl = (int)floor((lat + 90.0) / cell_lat);
+                    int bn = (int)floor(lon / cell_lon);
+                    bl = min(max(bl, 0), nblat - 1);
+                    bn = min(max(bn, 0), nblon - 1);
+                    b = bl * nblon + bn;
+                }
+                obucket[o] = b;
             }
-            yv[j] = y;
         }
+        const unsigned okmask = __ballot_sync(0xffffffffu, ok);
+        const unsigned psmask = __ballot_sync(0xffffffffu, psearch);
+
+        // ---- members of each observation of the group, lanes over the members
+        double mymean = 0.0;
+        const int gn = (int)min((int64_t)32, nobs - base);
+        for (int j = 0; j < gn; j++) {
+            const int64_t oj = base + j;
+            if (!((okmask >> j) & 1u)) {
+                for (int e = lane; e < k; e += 32) {
+                    yb[oj * k + e] = 0.0;
+                    if (ys32) ys32[oj * k + e] = 0.0f;
+                }
+                continue;
+            }
+            Corners qj;
+            qj.c11 = __shfl_sync(0xffffffffu, (long long)q.c11, j);
+            qj.c21 = __shfl_sync(0xffffffffu, (long long)q.c21, j);
+            qj.c12 = __shfl_sync(0xffffffffu, (long long)q.c12, j);
+            qj.c22 = __shfl_sync(0xffffffffu, (long long)q.c22, j);
+            qj.t1 = __shfl_sync(0xffffffffu, q.t1, j);
+            qj.t2 = __shfl_sync(0xffffffffu, q.t2, j);
+            const int rj = __shfl_sync(0xffffffffu, row, j);
+            const bool psj = (psmask >> j) & 1u;
+            const double pj = psj ? __shfl_sync(0xffffffffu, p_obs, j) : 0.0;
+            double sum = 0.0;
+            double yv[LG_MAX_ENS / 32];
 #pragma unroll
-        for (int s = 16; s > 0; s >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, s);
-        const double mean = sum / (double)k;
+            for (int i = 0; i < LG_MAX_ENS / 32; i++) {
+                const int e = lane + 32 * i;
+                double y = 0.0;
+                if (e < k) {
+                    if (!psj) {
+                        y = bilin(xb, axb, n, k, qj, rj, e);
+                    } else {
+                        // member's pressure profile, level search, log-p interpolation
+                        const double ps = bilin(xb, axb, n, k, qj, g.ps_row, e);
+                        int jl = 1;
+                        while (jl <= g.nz && pj > ph_mid(g, jl - 1, ps)) jl++;
+                        const int pos = jl - 1;
+                        if (pos >= 1 && pos < g.nz) {
+                            const int tl = rj + pos - 1;
+                            const double pa = ph_mid(g, pos, ps), pb = ph_mid(g, pos - 1, ps);
+                            const double t3 = (log(pa) - log(pj)) / (log(pa) - log(pb));
+                            const double r1 = bilin(xb, axb, n, k, qj, tl, e);
+                            const double r3 = bilin(xb, axb, n, k, qj, tl + 1, e);
+                            y = r1 * t3 + r3 * (1.0 - t3);
+                        } else {
+                            const int tl = (pos == 0) ? rj : rj + g.nz - 1;
+                            y = bilin(xb, axb, n, k, qj, tl, e);
+                        }
+                    }
+                    sum += y;
+                }
+                yv[i] = y;
+            }
 #pragma unroll
-        for (int j = 0; j < LG_MAX_ENS / 32; j++) {
-            const int e = lane + 32 * j;
-            if (e < k) yb[o * k + e] = yv[j] - mean;
-        }
-        if (ys32) {
-            // scaled perturbations for the tensor-core products: y sqrt(rdiaginv)
-            const double sr = sqrt((double)(float)orinv[o]);
+            for (int s = 16; s > 0; s >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, s);
+            const double mean = kpow2 ? sum * invk : sum / (double)k;
+            if (lane == j) mymean = mean;
 #pragma unroll
-            for (int j = 0; j < LG_MAX_ENS / 32; j++) {
-                const int e = lane + 32 * j;
-                if (e < k) ys32[o * k + e] = (float)((yv[j] - mean) * sr);
+            for (int i = 0; i < LG_MAX_ENS / 32; i++) {
+                const int e = lane + 32 * i;
+                if (e < k) yb[oj * k + e] = yv[i] - mean;
+            }
+            if (ys32) {
+                const double srj = __shfl_sync(0xffffffffu, sr, j);
+#pragma unroll
+                for (int i = 0; i < LG_MAX_ENS / 32; i++) {
+                    const int e = lane + 32 * i;
+                    if (e < k) ys32[oj * k + e] = (float)((yv[i] - mean) * srj);
+                }
             }
         }
-        if (lane == 0) {
-            dep[o] = oyo[o] - mean;
-            rinvf[o] = (float)orinv[o];
+
+        // ---- departures, observation base + lane on this lane
+        if (ok) {
+            const double d = oyo[o] - mymean;
+            dep[o] = d;
             // the mixed form's departure factor: e = sqrt(rloc) sqrt(rdiaginv) dep
-            if (oef) oef[o] = sqrtf(rinvf[o]) * (float)dep[o];
-            const double xr = lg_rad(lat), yr = lg_rad(lon);
-            const double s = sin(xr), c = cos(xr);
-            os[o] = s;
-            oc[o] = c;
-            oyr[o] = yr;
-            oxyz[o] = make_float4((float)(c * cos(yr)), (float)(c * sin(yr)), (float)s,
-                                  __int_as_float((int)o));
-            int b = -1;
-            if (fabs(lat) <= prm.obs_polar) {
-                int bl = (int)floor((lat + 90.0) / cell_lat);
-                int bn = (int)floor(lon / cell_lon);
-                bl = min(max(bl, 0), nblat - 1);
-                bn = min(max(bn, 0), nblon - 1);
-                b = bl * nblon + bn;
-            }
-            obucket[o] = b;
+            if (oef) oef[o] = sqrtf(rinvf[o]) * (float)d;
         }
     }
 }
@@ -258,7 +298,7 @@ cudaError_t lg_launch_obs_prepare(letkf_ctx *ctx, const LgGrid &g, const double 
 {
     if (nobs == 0) return cudaSuccess;
     const LgParams prm = lg_params(ctx);
-    const int blocks = grid_for(nobs * 32, 256, 152 * 64);
+    const int blocks = grid_for(nobs, 256, 152 * 64);
     lg_count_launch();
     k_obs_prepare<<<blocks, 256, 0, ctx->stream>>>(
         g, prm, xb, axb, nobs, olat, olon, oph, olev, ovar, oyo, orinv, ctx->d_yb.p, ctx->d_dep.p,
