@@ -398,9 +398,8 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
         for (int idx = tid; idx < K * K; idx += kT) {
             const int i = idx / K, j = idx % K;
             const float a32 = 0.5f * (Dhh[i * LDD + j] + Dhh[j * LDD + i]) + (Dlh[i * LDD + j] + Dlh[j * LDD + i]);
-            const double a = (double)a32 + (i == j ? cdiag : 0.0);
-            B1[idx] = a;
             if (ST == 1) mA[ci * K * K + idx] = a32;
+            else B1[idx] = (double)a32 + (i == j ? cdiag : 0.0);
         }
         __syncthreads();                                   // Dhh/Dlh are dead
         }
@@ -408,10 +407,6 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
         if (ST == 2) {
             // this cube's g, A' and eigenpairs from the build and eigensolve launches
             if (tid < K) gv[tid] = mgv[ci * K + tid];
-            for (int idx = tid; idx < K * K; idx += kT) {
-                const int i = idx / K, j = idx % K;
-                B1[idx] = (double)mA[ci * K * K + idx] + (i == j ? cdiag : 0.0);
-            }
             for (int idx = tid; idx < K * K / 4; idx += kT)
                 reinterpret_cast<float4 *>(X32)[idx] = reinterpret_cast<const float4 *>(mX + ci * K * K)[idx];
             if (tid < K) {
@@ -547,12 +542,35 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
             }
             __syncthreads();
             if (it == 0) {
-                for (int i = warp; i < K; i += kT / 32) {      // one warp per row of A'
+                // four threads per row of A', each over K/4 columns; the FP64
+                // A' is (double)A + (k-1)/rho on the diagonal, from the FP32 A
+                // of the build launch (ST 2, converted on the integer pipe) or
+                // from B1
+                constexpr int Q = K / 4;
+                for (int t0 = 0; t0 < 4 * K; t0 += kT) {
+                    const int t = t0 + tid, i = t >> 2, q = t & 3;
                     double d = 0.0;
-                    for (int l = lane; l < K; l += 32) d += B1[i * K + l] * wbar[l];
+                    if (t < 4 * K) {
+                        if (ST == 2) {
+                            const float4 *arow = reinterpret_cast<const float4 *>(mA + ci * K * K + i * K + q * Q);
 #pragma unroll
-                    for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
-                    if (lane == 0) r32[i] = (float)(gv[i] - d);
+                            for (int l4 = 0; l4 < Q / 4; l4++) {
+                                const float4 a = arow[l4];
+                                const int l = q * Q + 4 * l4;
+                                d = fma(lg_f2d_bits(a.x), wbar[l], d);
+                                d = fma(lg_f2d_bits(a.y), wbar[l + 1], d);
+                                d = fma(lg_f2d_bits(a.z), wbar[l + 2], d);
+                                d = fma(lg_f2d_bits(a.w), wbar[l + 3], d);
+                            }
+                            if (i / Q == q) d = fma(cdiag, wbar[i], d);
+                        } else {
+#pragma unroll 4
+                            for (int l = q * Q; l < q * Q + Q; l++) d = fma(B1[i * K + l], wbar[l], d);
+                        }
+                    }
+                    d += __shfl_xor_sync(0xffffffffu, d, 1);
+                    d += __shfl_xor_sync(0xffffffffu, d, 2);
+                    if (t < 4 * K && q == 0) r32[i] = (float)(gv[i] - d);
                 }
                 __syncthreads();
             }
@@ -641,6 +659,10 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
             *reinterpret_cast<uint4 *>(tb_lo + lg_sw128_offset(e, c)) = lo;
         }
         const int n = g.n;
+        // FP64 mean increment xb^T wbar: partial sums over 8 members, [c][row],
+        // after T in the space of A' (free in this phase)
+        double *incp = reinterpret_cast<double *>(T32 + K * K);
+        static_assert(128 * K <= 4 * K * K, "mean-increment partials must fit beside T");
         const int bjc = (int)(cube % prm.nbj), bic = (int)(cube / prm.nbj);
         const int sj = bjc * prm.cube_n, ej = min(sj + prm.cube_n - 1, g.nlat - 1);
         const int si = bic * prm.cube_n, ei = min(si + prm.cube_n - 1, g.nlon - 1);
@@ -657,12 +679,16 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
                         if (r < R) {
                             const double2 *src =
                                 reinterpret_cast<const double2 *>(xbc + (int64_t)(r0 + r) * K + 8 * c);
+                            double s = 0.0;
 #pragma unroll
                             for (int j = 0; j < 4; j++) {
                                 const double2 q = src[j];
                                 v[2 * j] = (float)q.x;
                                 v[2 * j + 1] = (float)q.y;
+                                s = fma(q.x, wbar[8 * c + 2 * j], s);
+                                s = fma(q.y, wbar[8 * c + 2 * j + 1], s);
                             }
+                            incp[c * 128 + r] = s;
                         } else {
 #pragma unroll
                             for (int j = 0; j < 8; j++) v[j] = 0.0f;
@@ -671,15 +697,6 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
                         split8(v, hi, lo);
                         *reinterpret_cast<uint4 *>(xa_hi + lg_sw128_offset(r, c)) = hi;
                         *reinterpret_cast<uint4 *>(xa_lo + lg_sw128_offset(r, c)) = lo;
-                    }
-                    // FP64 mean increment xb^T wbar, one row per thread
-                    for (int r = warp; r < R; r += kT / 32) {    // one warp per state row
-                        const double *src = xbc + (int64_t)(r0 + r) * K;
-                        double s = 0.0;
-                        for (int i = lane; i < K; i += 32) s += src[i] * wbar[i];
-#pragma unroll
-                        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-                        if (lane == 0) inc[r] = s;
                     }
                     lg_fence_async_smem();
                     __syncthreads();
@@ -720,8 +737,11 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
                             const float meanf =
                                 (((part[0] + part[1]) + (part[2] + part[3])) + ((part[4] + part[5]) + (part[6] + part[7]))) /
                                 (float)K;
+                            double incr = incp[r];
+#pragma unroll
+                            for (int c = 1; c < K / 8; c++) incr += incp[c * 128 + r];
                             const int64_t row = col * n + r0 + r;
-                            axa[row] = axb[row] + inc[r] + lg_f2d_bits(meanf);
+                            axa[row] = axb[row] + incr + lg_f2d_bits(meanf);
                             double *dst = xac + (int64_t)(r0 + r) * K;
 #pragma unroll
                             for (int e = 0; e < K; e += 2)
