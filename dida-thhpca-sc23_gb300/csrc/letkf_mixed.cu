@@ -91,20 +91,6 @@ struct MCfg {
     static_assert(STAGE <= B1 && (STAGE1_IN_B1 || 2 * TILE + STAGE <= 49152), "gather stages must fit");
 };
 
-__device__ __forceinline__ double block_sum(double v, double *red)
-{
-#pragma unroll
-    for (int s = 16; s > 0; s >>= 1) v += __shfl_xor_sync(0xffffffffu, v, s);
-    __syncthreads();
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
-    __syncthreads();
-    double t = 0.0;
-#pragma unroll
-    for (int w = 0; w < kT / 32; w++) t += red[w];
-    __syncthreads();
-    return t;
-}
-
 // ST selects the stages a launch runs: 0 all of them; 1 the A build only
 // (A without the diagonal shift and g to mA, mgv); 2 from the eigenpairs on
 // (X and lambda from mX, mlam, written by k_eig_warp).  The intermediates
@@ -139,7 +125,6 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
     __shared__ uint64_t mbar[3];
     __shared__ uint32_t s_tmem;
     __shared__ int s_rot, s_ok;
-    __shared__ double red[kT / 32];
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     if (warp == 0) lg_tmem_alloc(lg_smem_u32(&s_tmem), C::TMEM_COLS);
@@ -189,7 +174,7 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
     }
 
 #ifdef LG_PHASE_CLOCKS
-    long long ph_cyc[7] = {0, 0, 0, 0, 0, 0, 0};
+    long long ph_cyc[11] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     long long ph_last = clock64();
 #endif
     // Work queue: chunks of `chunk` consecutive cubes (neighbours along
@@ -298,27 +283,41 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
             const float *sq = msq + (ch % 3) * CH, *ev = me + (ch % 3) * CH;
             cp_async_wait<1>();              // this chunk's rows (the next chunk's may be in flight)
             __syncthreads();
+            LG_PHASE(7);
             unsigned char *tile = area + b * C::TILE;
             if (!wait_bar(b)) {
                 failed = true;
                 break;
             }
+            LG_PHASE(8);
             const int cnt = min(CH, p - ch * CH);
-            for (int t = tid; t < K * 8 + 8; t += kT) {
-                float v[8];
-                uint4 hi, lo;
-                if (t < K * 8) {
-                    const int m = t % K, c = t / K;
+            // one task: columns m, m + 1 of 8 observations (8-byte shared loads,
+            // packed scaling and split)
+            for (int t = tid; t < 4 * K + 8; t += kT) {
+                if (t < 4 * K) {
+                    const int m = 2 * (t % (K / 2)), c = t / (K / 2);
+                    unsigned long long x[8];
 #pragma unroll
                     for (int j = 0; j < 8; j++) {
                         const int o = 8 * c + j;
-                        v[j] = (o < cnt) ? st[o * K + m] * sq[o] : 0.0f;
+                        if (o < cnt) {
+                            const float2 y = *reinterpret_cast<const float2 *>(st + o * K + m);
+                            const float f = sq[o];
+                            x[j] = lg_fmul2(lg_pk2(y.x, y.y), lg_pk2(f, f));
+                        } else {
+                            x[j] = 0ull;
+                        }
                     }
-                    split8(v, hi, lo);
-                    *reinterpret_cast<uint4 *>(tile + lg_sw128_offset(K + m, c)) = hi;
-                    *reinterpret_cast<uint4 *>(tile + lg_sw128_offset(m, c)) = lo;
+                    uint4 h0, l0, h1, l1;
+                    split8x2(x, h0, l0, h1, l1);
+                    *reinterpret_cast<uint4 *>(tile + lg_sw128_offset(K + m, c)) = h0;
+                    *reinterpret_cast<uint4 *>(tile + lg_sw128_offset(m, c)) = l0;
+                    *reinterpret_cast<uint4 *>(tile + lg_sw128_offset(K + m + 1, c)) = h1;
+                    *reinterpret_cast<uint4 *>(tile + lg_sw128_offset(m + 1, c)) = l1;
                 } else {
-                    const int c = t - K * 8;
+                    const int c = t - 4 * K;
+                    float v[8];
+                    uint4 hi, lo;
 #pragma unroll
                     for (int j = 0; j < 8; j++) v[j] = ev[8 * c + j];
                     split8(v, hi, lo);
@@ -328,6 +327,7 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
             }
             lg_fence_async_smem();
             __syncthreads();
+            LG_PHASE(9);
             if (tid == 0) {
                 lg_tc_fence_after();
                 const uint64_t da = lg_desc_sw128(lg_smem_u32(tile));
@@ -346,6 +346,7 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
             }
             __syncthreads();
             issue_rows(ch + 2);
+            LG_PHASE(10);
         }
         cp_async_wait<0>();
         if (failed) break;
@@ -761,9 +762,10 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
     }
 #ifdef LG_PHASE_CLOCKS
     if (blockIdx.x == 0 && tid == 0)
-        printf("phase cycles cta0: A-build %lld, A'-form %lld, jacobi32 %lld, X/wbar %lld, T %lld, "
-               "update %lld, loop %lld\n",
-               ph_cyc[0], ph_cyc[1], ph_cyc[2], ph_cyc[3], ph_cyc[4], ph_cyc[5], ph_cyc[6]);
+        printf("phase cycles cta0 (K %d, stage %d): A-build %lld (gather wait %lld, MMA wait %lld, "
+               "convert %lld, issue %lld), A'-form %lld, jacobi32 %lld, X/wbar %lld, T %lld, update %lld, loop %lld\n",
+               K, ST, ph_cyc[0] + ph_cyc[7] + ph_cyc[8] + ph_cyc[9] + ph_cyc[10], ph_cyc[7], ph_cyc[8], ph_cyc[9],
+               ph_cyc[10], ph_cyc[1], ph_cyc[2], ph_cyc[3], ph_cyc[4], ph_cyc[5], ph_cyc[6]);
 #endif
     if (failed && tid == 0) atomicOr(status, LG_ST_TIMEOUT);
     cp_async_wait<0>();
@@ -880,18 +882,31 @@ k_eig_warp(int64_t cube0, int64_t cube_end, int R, double cdiag, float tol, cons
     const int64_t nruns = (cube_end - base + R - 1) / R;
     const int64_t nw = (int64_t)gridDim.x * (kT / 32);
     const float cd = (float)cdiag;
+#ifdef LG_PHASE_CLOCKS
+    long long ec[3] = {0, 0, 0}, et = clock64();
+#define LG_EPHASE(i)                                   \
+    do {                                               \
+        const long long n_ = clock64();                \
+        ec[i] += n_ - et;                              \
+        et = n_;                                       \
+    } while (0)
+#else
+#define LG_EPHASE(i) \
+    do {             \
+    } while (0)
+#endif
     for (int64_t run = blockIdx.x * (int64_t)(kT / 32) + warp; run < nruns; run += nw) {
         const int64_t c0 = max(cube0, base + run * R), c1 = min(cube_end, base + (run + 1) * R);
         for (int64_t c = c0; c < c1; c++) {
             const float *Ac = mA + (c - cube0) * K * K;
             // W columns lane and lane + NS into Wp (each lane reads and writes
             // only its own two columns)
+            if (c == c0) {
 #pragma unroll
-            for (int h = 0; h < 2; h++) {
-                const int j = lane + h * NS;
-                float4 *dst = reinterpret_cast<float4 *>(Wp + j * LDW);
-                if (c == c0) {
+                for (int h = 0; h < 2; h++) {
                     // cold: column j of A' is row j (A' symmetric)
+                    const int j = lane + h * NS;
+                    float4 *dst = reinterpret_cast<float4 *>(Wp + j * LDW);
                     const float4 *row = reinterpret_cast<const float4 *>(Ac + j * K);
 #pragma unroll
                     for (int q = 0; q < K / 4; q++) {
@@ -902,40 +917,59 @@ k_eig_warp(int64_t cube0, int64_t cube_end, int R, double cdiag, float tol, cons
                         }
                         dst[q] = x;
                     }
-                } else {
-                    // warm: w_j = A' v_j = sum_l A[l][:] v_j[l] + cd v_j (A symmetric;
-                    // all lanes read the same row of A at once, each its own v_j[l])
-                    const float *vj = Wp + j * LDW;
-                    unsigned long long acc[K / 2];
+                }
+            } else {
+                // warm: w_j = A' v_j = sum_l A[l][:] v_j[l] + cd v_j for both columns
+                // in one pass over A (A symmetric; all lanes read the same row of
+                // A at once, each its own v_j[l])
+                const float *v0 = Wp + lane * LDW, *v1 = Wp + (lane + NS) * LDW;
+                unsigned long long acc0[K / 2], acc1[K / 2];
 #pragma unroll
-                    for (int q = 0; q < K / 4; q++) {
-                        const float4 x = reinterpret_cast<const float4 *>(vj)[q];
-                        acc[2 * q] = lg_pk2(cd * x.x, cd * x.y);
-                        acc[2 * q + 1] = lg_pk2(cd * x.z, cd * x.w);
-                    }
+                for (int q = 0; q < K / 4; q++) {
+                    const float4 x = reinterpret_cast<const float4 *>(v0)[q];
+                    const float4 y = reinterpret_cast<const float4 *>(v1)[q];
+                    acc0[2 * q] = lg_pk2(cd * x.x, cd * x.y);
+                    acc0[2 * q + 1] = lg_pk2(cd * x.z, cd * x.w);
+                    acc1[2 * q] = lg_pk2(cd * y.x, cd * y.y);
+                    acc1[2 * q + 1] = lg_pk2(cd * y.z, cd * y.w);
+                }
 #pragma unroll 1
-                    for (int l = 0; l < K; l++) {
-                        const float4 *row = reinterpret_cast<const float4 *>(Ac + l * K);
-                        const float vl = vj[l];
-                        const unsigned long long v2 = lg_pk2(vl, vl);
-#pragma unroll
-                        for (int q = 0; q < K / 4; q++) {
-                            const float4 x = row[q];
-                            acc[2 * q] = lg_ffma2(lg_pk2(x.x, x.y), v2, acc[2 * q]);
-                            acc[2 * q + 1] = lg_ffma2(lg_pk2(x.z, x.w), v2, acc[2 * q + 1]);
-                        }
-                    }
+                for (int l = 0; l < K; l++) {
+                    const float4 *row = reinterpret_cast<const float4 *>(Ac + l * K);
+                    const float a0 = v0[l], a1 = v1[l];
+                    const unsigned long long p0 = lg_pk2(a0, a0), p1 = lg_pk2(a1, a1);
 #pragma unroll
                     for (int q = 0; q < K / 4; q++) {
-                        float a, b, cc, d;
-                        lg_upk2(acc[2 * q], a, b);
-                        lg_upk2(acc[2 * q + 1], cc, d);
-                        dst[q] = make_float4(a, b, cc, d);
+                        const float4 x = row[q];
+                        const unsigned long long xl = lg_pk2(x.x, x.y), xh = lg_pk2(x.z, x.w);
+                        acc0[2 * q] = lg_ffma2(xl, p0, acc0[2 * q]);
+                        acc0[2 * q + 1] = lg_ffma2(xh, p0, acc0[2 * q + 1]);
+                        acc1[2 * q] = lg_ffma2(xl, p1, acc1[2 * q]);
+                        acc1[2 * q + 1] = lg_ffma2(xh, p1, acc1[2 * q + 1]);
                     }
                 }
+                __syncwarp();                  // every lane has read its v_j before W replaces them
+#pragma unroll
+                for (int q = 0; q < K / 4; q++) {
+                    float a, b, cc, d;
+                    lg_upk2(acc0[2 * q], a, b);
+                    lg_upk2(acc0[2 * q + 1], cc, d);
+                    reinterpret_cast<float4 *>(Wp + lane * LDW)[q] = make_float4(a, b, cc, d);
+                    lg_upk2(acc1[2 * q], a, b);
+                    lg_upk2(acc1[2 * q + 1], cc, d);
+                    reinterpret_cast<float4 *>(Wp + (lane + NS) * LDW)[q] = make_float4(a, b, cc, d);
+                }
+            }
+            // the next cube's A into L2 while this one is solved (16 KB, 128 lines)
+            if (c + 1 < c1) {
+                const char *nxt = reinterpret_cast<const char *>(Ac + K * K);
+                for (int l = lane; l < K * K * 4 / 128; l += 32)
+                    asm volatile("prefetch.global.L2 [%0];" ::"l"(nxt + l * 128));
             }
             __syncwarp();
+            LG_EPHASE(0);
             const int sw = lg_jacobi32w<K, LDW>(Wp, tol, 24);
+            LG_EPHASE(1);
             // lambda_j = |w_j|, x_j = w_j / lambda_j (kept in Wp for the next cube)
             float lo = 3.0e38f, hi = 0.0f;
 #pragma unroll
@@ -973,8 +1007,14 @@ k_eig_warp(int64_t cube0, int64_t cube_end, int R, double cdiag, float tol, cons
                 if (hi > 1.0e4f * lo) atomicAdd(&counters[LG_CNT_ILLCOND], 1ull);
             }
             __syncwarp();
+            LG_EPHASE(2);
         }
     }
+#ifdef LG_PHASE_CLOCKS
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        printf("eig cycles warp 0 of cta 0: W build %lld, jacobi %lld, outputs %lld\n", ec[0], ec[1], ec[2]);
+#endif
+#undef LG_EPHASE
 }
 
 // Most cubes one staged launch sequence holds intermediates for (A, X: 2 k^2

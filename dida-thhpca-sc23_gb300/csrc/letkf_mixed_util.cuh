@@ -25,6 +25,40 @@ __device__ __forceinline__ double lg_f2d_bits(float f)
 #include <cuda_bf16.h>
 #include <stdint.h>
 
+// hi/lo BF16 split of two columns m, m + 1 over 8 observations: x[j] holds the
+// FP32 pair (column m, column m + 1) of observation j.  Gives the same bits as
+// split8 on each column (hi = bf16(v), lo = bf16(v - hi), observation 2i in
+// the low half of word i) with the residuals as packed f32x2 differences.
+__device__ __forceinline__ void split8x2(const unsigned long long *x, uint4 &hi0, uint4 &lo0, uint4 &hi1,
+                                         uint4 &lo1)
+{
+    uint32_t h0[4], l0[4], h1[4], l1[4];
+#pragma unroll
+    for (int i = 0; i < 4; i++) {
+        float a0, a1, b0, b1;                       // a: observation 2i, b: 2i + 1
+        asm("mov.b64 {%0, %1}, %2;" : "=f"(a0), "=f"(a1) : "l"(x[2 * i]));
+        asm("mov.b64 {%0, %1}, %2;" : "=f"(b0), "=f"(b1) : "l"(x[2 * i + 1]));
+        __nv_bfloat162 p0 = __floats2bfloat162_rn(a0, b0), p1 = __floats2bfloat162_rn(a1, b1);
+        h0[i] = *reinterpret_cast<uint32_t *>(&p0);
+        h1[i] = *reinterpret_cast<uint32_t *>(&p1);
+        unsigned long long ha, hb, ra, rb;
+        asm("mov.b64 %0, {%1, %2};" : "=l"(ha) : "r"(h0[i] << 16), "r"(h1[i] << 16));
+        asm("mov.b64 %0, {%1, %2};" : "=l"(hb) : "r"(h0[i] & 0xffff0000u), "r"(h1[i] & 0xffff0000u));
+        asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(ra) : "l"(x[2 * i]), "l"(ha));
+        asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(rb) : "l"(x[2 * i + 1]), "l"(hb));
+        asm("mov.b64 {%0, %1}, %2;" : "=f"(a0), "=f"(a1) : "l"(ra));
+        asm("mov.b64 {%0, %1}, %2;" : "=f"(b0), "=f"(b1) : "l"(rb));
+        p0 = __floats2bfloat162_rn(a0, b0);
+        p1 = __floats2bfloat162_rn(a1, b1);
+        l0[i] = *reinterpret_cast<uint32_t *>(&p0);
+        l1[i] = *reinterpret_cast<uint32_t *>(&p1);
+    }
+    hi0 = make_uint4(h0[0], h0[1], h0[2], h0[3]);
+    lo0 = make_uint4(l0[0], l0[1], l0[2], l0[3]);
+    hi1 = make_uint4(h1[0], h1[1], h1[2], h1[3]);
+    lo1 = make_uint4(l1[0], l1[1], l1[2], l1[3]);
+}
+
 // 16-byte global -> shared copies that bypass the registers (cp.async, L2 only).
 __device__ __forceinline__ void cp_async16(uint32_t dst, const void *src)
 {
