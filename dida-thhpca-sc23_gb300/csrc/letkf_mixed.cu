@@ -124,11 +124,12 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
     float *stage1 = C::STAGE1_IN_B1 ? stage0 + CH * K : reinterpret_cast<float *>(area + 2 * C::TILE);
     __shared__ uint64_t mbar[3];
     __shared__ uint32_t s_tmem;
-    __shared__ int s_rot, s_ok;
+    __shared__ int s_rot, s_ok, s_fail;
 
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     if (warp == 0) lg_tmem_alloc(lg_smem_u32(&s_tmem), C::TMEM_COLS);
     if (tid == 0) {
+        s_fail = 0;
         lg_mbar_init(&mbar[0], 1);
         lg_mbar_init(&mbar[1], 1);
         lg_mbar_init(&mbar[2], 1);
@@ -163,6 +164,14 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
         lok[m] = b < C::NLOW;
         lg_decode_block(lok[m] ? b : 0, lbi[m], lbj[m]);
     }
+    // A-build conversion task of this thread: columns tm, tm + 1 of the
+    // observations 8 tc .. 8 tc + 7 of a chunk (tile offsets fixed for the
+    // whole launch); thread te_base + c converts e of the observations 8 c ..
+    const bool has_task = tid < 4 * K;
+    const int tm = 2 * (tid % (K / 2)), tc = tid / (K / 2);
+    const uint32_t o_h0 = lg_sw128_offset(K + tm, tc), o_l0 = lg_sw128_offset(tm, tc);
+    const uint32_t o_h1 = lg_sw128_offset(K + tm + 1, tc), o_l1 = lg_sw128_offset(tm + 1, tc);
+    const int te = (4 * K + 8 <= kT) ? tid - 4 * K : tid;
     int fbi[C::MF], fbj[C::MF];
     bool fok[C::MF];
 #pragma unroll
@@ -231,8 +240,9 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
         }
         // Chunk x's observation rows are gathered by cp.async into stage x & 1,
         // two chunks ahead of the conversion; its list entries (index and the
-        // factors sqrt(rloc), e) sit in ring slot x % 3 and are read into
-        // registers one more chunk ahead.
+        // factors sqrt(rloc), e) sit in ring slot x % 3, written before the
+        // barrier after which the rows of x are requested, and are read into
+        // registers one chunk before that.  Two block barriers per chunk.
         const int nch = (p + CH - 1) / CH;
         auto load_meta = [&](int x, int &gi, float2 &mf) {      // tid < CH
             const int o = x * CH + tid;
@@ -282,48 +292,61 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
             const float *st = b ? stage1 : stage0;
             const float *sq = msq + (ch % 3) * CH, *ev = me + (ch % 3) * CH;
             cp_async_wait<1>();              // this chunk's rows (the next chunk's may be in flight)
+            // tile b is free once the products of chunk ch - 2 are done
+            if (tid == 0 && pending[b] && !lg_mbar_wait(&mbar[b], (ncommit[b] - 1u) & 1u)) s_fail = 1;
+            pending[b] = false;
             __syncthreads();
             LG_PHASE(7);
-            unsigned char *tile = area + b * C::TILE;
-            if (!wait_bar(b)) {
+            if (s_fail) {
                 failed = true;
                 break;
             }
-            LG_PHASE(8);
+            // slot (ch + 2) % 3 last served chunk ch - 1, converted before the barrier
+            if (tid < CH) {
+                put_meta(ch + 2, pf_g, pf_m);
+                load_meta(ch + 3, pf_g, pf_m);
+            }
+            unsigned char *tile = area + b * C::TILE;
             const int cnt = min(CH, p - ch * CH);
-            // one task: columns m, m + 1 of 8 observations (8-byte shared loads,
-            // packed scaling and split)
-            for (int t = tid; t < 4 * K + 8; t += kT) {
-                if (t < 4 * K) {
-                    const int m = 2 * (t % (K / 2)), c = t / (K / 2);
-                    unsigned long long x[8];
+            if (has_task) {
+                // columns tm, tm + 1 of 8 observations: 8-byte shared loads,
+                // packed scaling and split
+                const float *src = st + (8 * tc) * K + tm;
+                unsigned long long x[8];
+                if (cnt == CH) {
 #pragma unroll
                     for (int j = 0; j < 8; j++) {
-                        const int o = 8 * c + j;
-                        if (o < cnt) {
-                            const float2 y = *reinterpret_cast<const float2 *>(st + o * K + m);
-                            const float f = sq[o];
+                        const float2 y = *reinterpret_cast<const float2 *>(src + j * K);
+                        const float f = sq[8 * tc + j];
+                        x[j] = lg_fmul2(lg_pk2(y.x, y.y), lg_pk2(f, f));
+                    }
+                } else {
+#pragma unroll
+                    for (int j = 0; j < 8; j++) {
+                        if (8 * tc + j < cnt) {
+                            const float2 y = *reinterpret_cast<const float2 *>(src + j * K);
+                            const float f = sq[8 * tc + j];
                             x[j] = lg_fmul2(lg_pk2(y.x, y.y), lg_pk2(f, f));
                         } else {
                             x[j] = 0ull;
                         }
                     }
-                    uint4 h0, l0, h1, l1;
-                    split8x2(x, h0, l0, h1, l1);
-                    *reinterpret_cast<uint4 *>(tile + lg_sw128_offset(K + m, c)) = h0;
-                    *reinterpret_cast<uint4 *>(tile + lg_sw128_offset(m, c)) = l0;
-                    *reinterpret_cast<uint4 *>(tile + lg_sw128_offset(K + m + 1, c)) = h1;
-                    *reinterpret_cast<uint4 *>(tile + lg_sw128_offset(m + 1, c)) = l1;
-                } else {
-                    const int c = t - 4 * K;
-                    float v[8];
-                    uint4 hi, lo;
-#pragma unroll
-                    for (int j = 0; j < 8; j++) v[j] = ev[8 * c + j];
-                    split8(v, hi, lo);
-                    *reinterpret_cast<uint4 *>(tile + lg_sw128_offset(2 * K, c)) = hi;
-                    *reinterpret_cast<uint4 *>(tile + lg_sw128_offset(2 * K + 1, c)) = lo;
                 }
+                uint4 h0, l0, h1, l1;
+                split8x2(x, h0, l0, h1, l1);
+                *reinterpret_cast<uint4 *>(tile + o_h0) = h0;
+                *reinterpret_cast<uint4 *>(tile + o_l0) = l0;
+                *reinterpret_cast<uint4 *>(tile + o_h1) = h1;
+                *reinterpret_cast<uint4 *>(tile + o_l1) = l1;
+            }
+            if (te >= 0 && te < 8) {
+                float v[8];
+                uint4 hi, lo;
+#pragma unroll
+                for (int j = 0; j < 8; j++) v[j] = ev[8 * te + j];
+                split8(v, hi, lo);
+                *reinterpret_cast<uint4 *>(tile + lg_sw128_offset(2 * K, te)) = hi;
+                *reinterpret_cast<uint4 *>(tile + lg_sw128_offset(2 * K + 1, te)) = lo;
             }
             lg_fence_async_smem();
             __syncthreads();
@@ -339,12 +362,7 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
             }
             ncommit[b]++;
             pending[b] = true;
-            // refill this stage with chunk ch + 2 (its rows were read before the barrier)
-            if (tid < CH) {
-                put_meta(ch + 2, pf_g, pf_m);
-                load_meta(ch + 3, pf_g, pf_m);
-            }
-            __syncthreads();
+            // stage b was read before the barrier, slot (ch + 2) % 3 written before it
             issue_rows(ch + 2);
             LG_PHASE(10);
         }
@@ -762,7 +780,7 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
     }
 #ifdef LG_PHASE_CLOCKS
     if (blockIdx.x == 0 && tid == 0)
-        printf("phase cycles cta0 (K %d, stage %d): A-build %lld (gather wait %lld, MMA wait %lld, "
+        printf("phase cycles cta0 (K %d, stage %d): A-build %lld (rows and tile wait %lld, unused %lld, "
                "convert %lld, issue %lld), A'-form %lld, jacobi32 %lld, X/wbar %lld, T %lld, update %lld, loop %lld\n",
                K, ST, ph_cyc[0] + ph_cyc[7] + ph_cyc[8] + ph_cyc[9] + ph_cyc[10], ph_cyc[7], ph_cyc[8], ph_cyc[9],
                ph_cyc[10], ph_cyc[1], ph_cyc[2], ph_cyc[3], ph_cyc[4], ph_cyc[5], ph_cyc[6]);
