@@ -368,6 +368,19 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
         }
         cp_async_wait<0>();
         if (failed) break;
+        // the first list entries of the next cube into L2 (its first three chunks)
+        if (warp == 0 && cube + 1 < cube_end) {
+            const int64_t o2 = loff[cube + 1];
+            const int n2 = min(lcnt[cube + 1], 3 * CH);
+            const char *li = reinterpret_cast<const char *>(lidx + o2);
+            const char *lm = reinterpret_cast<const char *>(lmeta + o2);
+            // addresses inside the entries only: the last line by the last byte
+            const int nl = (n2 * 4 + 127) / 128 + 1, nm = (n2 * 8 + 127) / 128 + 1;
+            for (int l = lane; l < nl + nm; l += 32) {
+                const char *a = (l < nl) ? li + min(l * 128, n2 * 4 - 1) : lm + min((l - nl) * 128, n2 * 8 - 1);
+                if (n2 > 0) asm volatile("prefetch.global.L2 [%0];" ::"l"(a));
+            }
+        }
         if (!wait_bar(0) || !wait_bar(1)) {
             failed = true;
             break;
@@ -424,6 +437,19 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
         }
         if (ST == 1) continue;
         if (ST == 2) {
+            // the next cube's A, X, g and lambda into L2 while this one is done
+            if (cube + 1 < cube_end) {
+                // 128-byte lines of A and of X, of g, of lambda
+                constexpr int LA = K * K * 4 / 128, LG = (K * 8 + 127) / 128, LL = (K * 4 + 127) / 128;
+                for (int l = tid; l < 2 * LA + LG + LL; l += kT) {
+                    const char *a;
+                    if (l < LA) a = reinterpret_cast<const char *>(mA + (ci + 1) * K * K) + l * 128;
+                    else if (l < 2 * LA) a = reinterpret_cast<const char *>(mX + (ci + 1) * K * K) + (l - LA) * 128;
+                    else if (l < 2 * LA + LG) a = reinterpret_cast<const char *>(mgv + (ci + 1) * K) + (l - 2 * LA) * 128;
+                    else a = reinterpret_cast<const char *>(mlam + (ci + 1) * K) + (l - 2 * LA - LG) * 128;
+                    asm volatile("prefetch.global.L2 [%0];" ::"l"(a));
+                }
+            }
             // this cube's g, A' and eigenpairs from the build and eigensolve launches
             if (tid < K) gv[tid] = mgv[ci * K + tid];
             for (int idx = tid; idx < K * K / 4; idx += kT)
