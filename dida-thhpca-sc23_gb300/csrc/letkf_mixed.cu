@@ -912,8 +912,13 @@ namespace {
 // eigenvectors, W = A' V_prev, the first cold from W = A'.  Writes x_j
 // (columns, FP32, [j][r]) and lambda_j, and the sweep and conditioning
 // counters.
+#ifndef LG_EIG_THREADS
+#define LG_EIG_THREADS 384
+#endif
+constexpr int kTE = LG_EIG_THREADS;     // threads of an eigensolve block (one problem per warp)
+
 template <int K>
-__global__ void __launch_bounds__(kT, 1)
+__global__ void __launch_bounds__(kTE, 1)
 k_eig_warp(int64_t cube0, int64_t cube_end, int R, double cdiag, float tol, const float *__restrict__ mA,
            float *__restrict__ mX, float *__restrict__ mlam, unsigned long long *__restrict__ counters)
 {
@@ -924,7 +929,7 @@ k_eig_warp(int64_t cube0, int64_t cube_end, int R, double cdiag, float tol, cons
     float *Wp = smw + (size_t)warp * K * LDW;           // this warp's columns
     const int64_t base = cube0 / R * R;
     const int64_t nruns = (cube_end - base + R - 1) / R;
-    const int64_t nw = (int64_t)gridDim.x * (kT / 32);
+    const int64_t nw = (int64_t)gridDim.x * (kTE / 32);
     const float cd = (float)cdiag;
 #ifdef LG_PHASE_CLOCKS
     long long ec[3] = {0, 0, 0}, et = clock64();
@@ -939,7 +944,7 @@ k_eig_warp(int64_t cube0, int64_t cube_end, int R, double cdiag, float tol, cons
     do {             \
     } while (0)
 #endif
-    for (int64_t run = blockIdx.x * (int64_t)(kT / 32) + warp; run < nruns; run += nw) {
+    for (int64_t run = blockIdx.x * (int64_t)(kTE / 32) + warp; run < nruns; run += nw) {
         const int64_t c0 = max(cube0, base + run * R), c1 = min(cube_end, base + (run + 1) * R);
         for (int64_t c = c0; c < c1; c++) {
             const float *Ac = mA + (c - cube0) * K * K;
@@ -1118,7 +1123,7 @@ cudaError_t launch_mixed(letkf_ctx *ctx, const LgGrid &g, const double *xb, cons
         // warps, aligned so that every window boundary (a multiple of the
         // work-queue chunk, itself a multiple of 8) is a run boundary
         const int R = 8;
-        const size_t ew = (size_t)K * (K + 4) * sizeof(float) * (kT / 32);
+        const size_t ew = (size_t)K * (K + 4) * sizeof(float) * (kTE / 32);
         cudaError_t e = cudaFuncSetAttribute(k_eig_warp<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ew);
         for (int64_t b0 = w0; b0 < w1 && e == cudaSuccess; b0 += kStagedCubes) {
             const int64_t b1 = min(w1, b0 + kStagedCubes), nb = b1 - b0;
@@ -1132,10 +1137,10 @@ cudaError_t launch_mixed(letkf_ctx *ctx, const LgGrid &g, const double *xb, cons
             e = launch_stage<K, 1>(ctx, g, xb, axb, xa, axa, trans_out, w_out, chunk, nchunks, nsm);
             if (e != cudaSuccess) break;
             const int64_t runs = (b1 - b0 / R * R + R - 1) / R;
-            const int64_t eb = (runs + kT / 32 - 1) / (kT / 32);
+            const int64_t eb = (runs + kTE / 32 - 1) / (kTE / 32);
             const unsigned eblocks = (unsigned)(eb < nsm ? eb : nsm);
             lg_count_launch();
-            k_eig_warp<K><<<eblocks, kT, ew, ctx->stream>>>(b0, b1, R, (double)(K - 1) / ctx->params.inflation,
+            k_eig_warp<K><<<eblocks, kTE, ew, ctx->stream>>>(b0, b1, R, (double)(K - 1) / ctx->params.inflation,
                                                           LG_MIXED_JACOBI_TOL, ctx->d_mA.p, ctx->d_mX.p,
                                                           ctx->d_mlam.p, ctx->d_counters.p);
             if ((e = cudaGetLastError()) != cudaSuccess) break;
