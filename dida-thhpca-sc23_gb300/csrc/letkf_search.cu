@@ -47,30 +47,38 @@ struct CubeGeo {
     float lo2, hi2;          // chord^2 thresholds: below lo2 keep, above hi2 drop
 };
 
-__device__ __forceinline__ void add_lon_range(Seg *seg, int &ns, const LgBuckets &bk, int band,
-                                              float lon0, float lon1, int exact)
+// The buckets of band `band` between longitudes lon0 and lon1 (degrees,
+// wrapping around the circle) as up to two [b, e) ranges of bucket order.
+__device__ __forceinline__ int band_segments(const LgBuckets &bk, int band, float lon0, float lon1, int exact,
+                                             Seg &s0, Seg &s1)
 {
     const int nbl = bk.nblon;
     const int base = band * nbl;
     const float cl = (float)bk.cell_lon;
-    int j0 = (int)floorf(lon0 / cl), j1 = (int)floorf(lon1 / cl);
+    const int j0 = (int)floorf(lon0 / cl), j1 = (int)floorf(lon1 / cl);
+    int a0 = 0, e0 = -1, a1 = 0, e1 = -1;       // bucket column ranges [a, e]
     if (j1 - j0 + 1 >= nbl) {
-        if (ns < kMaxSeg) seg[ns++] = {bk.start[base], bk.start[base + nbl], exact};
-        return;
-    }
-    auto add = [&](int a, int b) {
-        if (a > b) return;
-        if (ns < kMaxSeg) seg[ns++] = {bk.start[base + a], bk.start[base + b + 1], exact};
-    };
-    if (j0 < 0) {
-        add(j0 + nbl, nbl - 1);
-        add(0, j1);
+        e0 = nbl - 1;
+    } else if (j0 < 0) {
+        a0 = j0 + nbl; e0 = nbl - 1;
+        e1 = j1;
     } else if (j1 >= nbl) {
-        add(j0, nbl - 1);
-        add(0, j1 - nbl);
+        a0 = j0; e0 = nbl - 1;
+        e1 = j1 - nbl;
     } else {
-        add(j0, j1);
+        a0 = j0; e0 = j1;
     }
+    int n = 0;
+    if (a0 <= e0) {
+        s0 = {bk.start[base + a0], bk.start[base + e0 + 1], exact};
+        n = 1;
+    }
+    if (a1 <= e1) {
+        const Seg t = {bk.start[base + a1], bk.start[base + e1 + 1], exact};
+        if (n == 0) s0 = t; else s1 = t;
+        n++;
+    }
+    return n;
 }
 
 // Classify one candidate; returns true if kept.  Counts borderline pairs.
@@ -92,30 +100,58 @@ __device__ __forceinline__ bool keep_candidate(const float4 &p, int exact, const
     return gc > 0.0;
 }
 
+// Visit every candidate of the segments once, four per thread at a time with
+// their loads in flight together: f(p, exact) for the candidate's float4
+// (unit vector, index in w).
+template <typename Fn>
+__device__ __forceinline__ void each_candidate(const Seg *seg, const int *soff, int ns, const LgBuckets &bk, Fn &&f)
+{
+    const int total = soff[ns];
+    int si = 0;
+    for (int k0 = 0; k0 < total; k0 += 4 * kThreads) {
+        int idx[4], ex[4];
+        bool v[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            const int k = k0 + u * kThreads + (int)threadIdx.x;
+            v[u] = k < total;
+            idx[u] = 0;
+            ex[u] = 0;
+            if (v[u]) {
+                while (soff[si + 1] <= k) si++;
+                idx[u] = seg[si].b + (k - soff[si]);
+                ex[u] = seg[si].exact;
+            }
+        }
+        float4 p[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) p[u] = v[u] ? bk.xyz[idx[u]] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+            if (v[u]) f(p[u], ex[u]);
+    }
+}
+
 // One pass over all candidate segments.
 //   mode 0: append every kept index (up to cap), count them and, with hist,
 //           count them by bin o >> shift
 //   mode 1: count kept indices below `thr`
 //   mode 2: append kept indices below `thr`
-__device__ int scan_pass(int mode, int thr, const Seg *seg, int ns, const LgBuckets &bk,
+__device__ int scan_pass(int mode, int thr, const Seg *seg, const int *soff, int ns, const LgBuckets &bk,
                          const CubeGeo &cg, const LgObsGeo &geo, const LgParams &prm,
                          int32_t *keys, int cap, int *s_count, unsigned long long *border,
                          int *hist = nullptr, int shift = 0)
 {
     if (threadIdx.x == 0) *s_count = 0;
     __syncthreads();
-    for (int si = 0; si < ns; si++) {
-        const Seg s = seg[si];
-        for (int i = s.b + threadIdx.x; i < s.e; i += kThreads) {
-            const float4 p = bk.xyz[i];
-            const int o = __float_as_int(p.w);
-            if (mode != 0 && o >= thr) continue;
-            if (!keep_candidate(p, s.exact, cg, geo, prm, mode == 0 ? border : nullptr)) continue;
-            const int pos = atomicAdd(s_count, 1);
-            if (mode != 1 && pos < cap) keys[pos] = o;
-            if (hist) atomicAdd(&hist[o >> shift], 1);
-        }
-    }
+    each_candidate(seg, soff, ns, bk, [&](const float4 &p, int exact) {
+        const int o = __float_as_int(p.w);
+        if (mode != 0 && o >= thr) return;
+        if (!keep_candidate(p, exact, cg, geo, prm, mode == 0 ? border : nullptr)) return;
+        const int pos = atomicAdd(s_count, 1);
+        if (mode != 1 && pos < cap) keys[pos] = o;
+        if (hist) atomicAdd(&hist[o >> shift], 1);
+    });
     __syncthreads();
     const int c = *s_count;
     __syncthreads();
@@ -211,6 +247,40 @@ __device__ __forceinline__ void write_entry(int o, long long at, const CubeGeo &
     }
 }
 
+// Entries at .. at + 3 for the indices o4[u] >= 0 (a prefix of the four),
+// their gathers issued together.
+__device__ __forceinline__ void write_entries4(const int *o4, long long at, const CubeGeo &cg, const LgObsGeo &geo,
+                                               const LgParams &prm, const LgListMeta &lm,
+                                               int32_t *__restrict__ lidx, double *__restrict__ lrloc)
+{
+    if (prm.precision == LETKF_PREC_MIXED) {
+        const float scale = (float)(LG_EARTH_A / prm.local_dist);
+        float4 q[4];
+        float ef[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            q[u] = o4[u] >= 0 ? geo.xyz[o4[u]] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            ef[u] = o4[u] >= 0 ? lm.ef[o4[u]] : 0.0f;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+            if (o4[u] < 0) continue;
+            const float dx = q[u].x - cg.cx, dy = q[u].y - cg.cy, dz = q[u].z - cg.cz;
+            const float half = fminf(1.0f, 0.5f * sqrtf(dx * dx + dy * dy + dz * dz));
+            const float ri = 2.0f * asinf(half) * scale;
+            const float rl = prm.gc_filter ? lg_schr2f(ri) : (ri > 2.0f ? 0.0f : 1.0f);
+            lidx[at + u] = o4[u];
+            lrloc[at + u] = (double)rl;
+            const float sr = sqrtf(rl);
+            lm.meta[at + u] = make_float2(sr, sr * ef[u]);
+        }
+    } else {
+#pragma unroll
+        for (int u = 0; u < 4; u++)
+            if (o4[u] >= 0) write_entry(o4[u], at + u, cg, geo, prm, lm, lidx, lrloc);
+    }
+}
+
 // Reserve the cube's slot in the list pool with one atomic add (thread 0;
 // the caller synchronizes before reading *s_off).
 __device__ __forceinline__ void reserve_list(int nout, bool truncated, int64_t cube, int64_t list_cap,
@@ -277,9 +347,13 @@ __device__ CubeGeo cube_geo(const LgGrid &g, const LgParams &prm, const LgSearch
 // buckets within 1e-6 rad of the antipode (exact test there).  FP32 with
 // margins of 1e-4 degrees (and the full circle of longitudes whenever the cap
 // comes within 1e-4 rad of a pole): the segments are a superset of the cap.
-__device__ int cap_segments(Seg *seg, const LgBuckets &bk, float clat, float clon, float theta)
+// Built by one warp, one latitude band per lane; writes seg[0..ns) and the
+// exclusive prefix of their lengths soff[0..ns] and returns ns (at most
+// kMaxSeg; *overflow set when the cap needed kMaxSeg or more).
+__device__ int cap_segments_warp(Seg *seg, int *soff, const LgBuckets &bk, float clat, float clon, float theta,
+                                 bool *overflow)
 {
-    int ns = 0;
+    const int lane = threadIdx.x & 31;
     const float deg = 57.295779513f, cla = (float)bk.cell_lat;
     const float band = (theta + 1e-6f) * deg + 1e-4f;
     const int b0 = max(0, (int)floorf((clat - band + 90.0f) / cla));
@@ -294,22 +368,61 @@ __device__ int cap_segments(Seg *seg, const LgBuckets &bk, float clat, float clo
             dlon = (asinf(sv) + 1e-6f) * deg + 1e-4f;
         }
     }
-    for (int b = b0; b <= b1; b++) {
-        if (full) add_lon_range(seg, ns, bk, b, 0.0f, 720.0f, 0);
-        else add_lon_range(seg, ns, bk, b, clon - dlon, clon + dlon, 0);
-    }
     // buckets within 1e-6 rad of the antipode
-    {
-        const float alat = -clat, alon = fmodf(clon + 180.0f, 360.0f);
-        const float ad = 1e-6f * deg + 1e-4f;
-        const int a0 = max(0, (int)floorf((alat - ad + 90.0f) / cla));
-        const int a1 = min(bk.nblat - 1, (int)floorf((alat + ad + 90.0f) / cla));
-        const float ca = cosf(alat / deg);
-        for (int b = a0; b <= a1; b++) {
-            if (ca < 1e-3f) add_lon_range(seg, ns, bk, b, 0.0f, 720.0f, 1);
-            else add_lon_range(seg, ns, bk, b, alon - ad / ca, alon + ad / ca, 1);
+    const float alat = -clat, alon = fmodf(clon + 180.0f, 360.0f);
+    const float ad = 1e-6f * deg + 1e-4f;
+    const int a0 = max(0, (int)floorf((alat - ad + 90.0f) / cla));
+    const int a1 = min(bk.nblat - 1, (int)floorf((alat + ad + 90.0f) / cla));
+    const float ca = cosf(alat / deg);
+    const int nmain = max(0, b1 - b0 + 1), nanti = max(0, a1 - a0 + 1);
+    int ns = 0;
+    for (int t0 = 0; t0 < nmain + nanti; t0 += 32) {
+        const int t = t0 + lane;
+        Seg s0{0, 0, 0}, s1{0, 0, 0};
+        int n = 0;
+        if (t < nmain) {
+            if (full) n = band_segments(bk, b0 + t, 0.0f, 720.0f, 0, s0, s1);
+            else n = band_segments(bk, b0 + t, clon - dlon, clon + dlon, 0, s0, s1);
+        } else if (t < nmain + nanti) {
+            if (ca < 1e-3f) n = band_segments(bk, a0 + t - nmain, 0.0f, 720.0f, 1, s0, s1);
+            else n = band_segments(bk, a0 + t - nmain, alon - ad / ca, alon + ad / ca, 1, s0, s1);
         }
+        int incl = n;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += v;
+        }
+        const int pos = ns + incl - n;
+        if (n > 0 && pos < kMaxSeg) seg[pos] = s0;
+        if (n > 1 && pos + 1 < kMaxSeg) seg[pos + 1] = s1;
+        ns += __shfl_sync(0xffffffffu, incl, 31);
     }
+    *overflow = ns >= kMaxSeg;
+    ns = min(ns, kMaxSeg);
+    __syncwarp();
+    // exclusive prefix of the segment lengths, four segments per lane
+    int len[4], sum = 0;
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        const int i = lane * 4 + q;
+        len[q] = (i < ns) ? seg[i].e - seg[i].b : 0;
+        sum += len[q];
+    }
+    int incl = sum;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+    }
+    int run = incl - sum;
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+        const int i = lane * 4 + q;
+        if (i <= ns) soff[i] = run;
+        run += len[q];
+    }
+    static_assert(kMaxSeg == 128, "four segments per lane");
     return ns;
 }
 
@@ -323,6 +436,7 @@ k_search(LgGrid g, LgParams prm, LgSearchGeo sgeo, LgBuckets bk, LgObsGeo geo, L
     extern __shared__ int32_t keys[];   // cap_sort keys, then kHistBins bins
     int *hist = keys + cap_sort;
     __shared__ Seg seg[kMaxSeg];
+    __shared__ int soff[kMaxSeg + 1];
     __shared__ int s_ns, s_count, s_bin, s_through;
     __shared__ int s_warp[kThreads / 32];
     __shared__ CubeGeo s_cg;
@@ -332,19 +446,22 @@ k_search(LgGrid g, LgParams prm, LgSearchGeo sgeo, LgBuckets bk, LgObsGeo geo, L
 
     for (int64_t cube = prm.cube0 + blockIdx.x; cube < ncubes; cube += gridDim.x) {
         for (int i = threadIdx.x; i < kHistBins; i += kThreads) hist[i] = 0;
-        if (threadIdx.x == 0) {
+        if (threadIdx.x < 32) {
             float clat, clon;
             const CubeGeo cg = cube_geo(g, prm, sgeo, cube, clat, clon);
-            s_cg = cg;
-            int ns = cap_segments(seg, bk, clat, clon, sgeo.theta);
-            if (ns >= kMaxSeg) atomicOr(status, LG_ST_SEGMENTS);
-            s_ns = ns;
+            bool over;
+            const int ns = cap_segments_warp(seg, soff, bk, clat, clon, sgeo.theta, &over);
+            if (threadIdx.x == 0) {
+                s_cg = cg;
+                if (over) atomicOr(status, LG_ST_SEGMENTS);
+                s_ns = ns;
+            }
         }
         __syncthreads();
         const int ns = s_ns;
         const CubeGeo cg = s_cg;
 
-        int nk = scan_pass(0, 0, seg, ns, bk, cg, geo, prm, keys, cap_sort, &s_count,
+        int nk = scan_pass(0, 0, seg, soff, ns, bk, cg, geo, prm, keys, cap_sort, &s_count,
                            &counters[LG_CNT_BORDER], hist, shift);
         if (prm.count_only) {
             if (threadIdx.x == 0) lm.need[cube] = min(nk, prm.max_obs);
@@ -372,11 +489,11 @@ k_search(LgGrid g, LgParams prm, LgSearchGeo sgeo, LgBuckets bk, LgObsGeo geo, L
             }
             while (lo < hi) {
                 const int mid = lo + (hi - lo) / 2;
-                const int c = scan_pass(1, mid, seg, ns, bk, cg, geo, prm, keys, cap_sort, &s_count,
+                const int c = scan_pass(1, mid, seg, soff, ns, bk, cg, geo, prm, keys, cap_sort, &s_count,
                                         nullptr);
                 if (c >= prm.max_obs) hi = mid; else lo = mid + 1;
             }
-            const int c = scan_pass(2, lo, seg, ns, bk, cg, geo, prm, keys, cap_sort, &s_count,
+            const int c = scan_pass(2, lo, seg, soff, ns, bk, cg, geo, prm, keys, cap_sort, &s_count,
                                     nullptr);
             int np2 = 1;
             while (np2 < c) np2 <<= 1;
@@ -395,7 +512,7 @@ k_search(LgGrid g, LgParams prm, LgSearchGeo sgeo, LgBuckets bk, LgObsGeo geo, L
 // (when nobs/8 bytes fit in shared memory): each kept candidate sets its bit,
 // and one ordered pass over the bitmap yields the list in canonical (index)
 // order, so no sort is needed and no list length is limited by shared memory.
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, 4)
 k_search_bitmap(LgGrid g, LgParams prm, LgSearchGeo sgeo, LgBuckets bk, LgObsGeo geo, LgListMeta lm,
                 int64_t nobs,
                 int32_t *__restrict__ lidx, double *__restrict__ lrloc, int64_t list_cap,
@@ -404,6 +521,7 @@ k_search_bitmap(LgGrid g, LgParams prm, LgSearchGeo sgeo, LgBuckets bk, LgObsGeo
 {
     extern __shared__ uint32_t bits[];
     __shared__ Seg seg[kMaxSeg];
+    __shared__ int soff[kMaxSeg + 1];
     __shared__ int s_ns;
     __shared__ CubeGeo s_cg;
     __shared__ long long s_off;
@@ -415,27 +533,26 @@ k_search_bitmap(LgGrid g, LgParams prm, LgSearchGeo sgeo, LgBuckets bk, LgObsGeo
 
     for (int64_t cube = prm.cube0 + blockIdx.x; cube < ncubes; cube += gridDim.x) {
         for (int w = threadIdx.x; w < nw; w += kThreads) bits[w] = 0u;
-        if (threadIdx.x == 0) {
+        if (threadIdx.x < 32) {
             float clat, clon;
             const CubeGeo cg = cube_geo(g, prm, sgeo, cube, clat, clon);
-            s_cg = cg;
-            const int ns = cap_segments(seg, bk, clat, clon, sgeo.theta);
-            if (ns >= kMaxSeg) atomicOr(status, LG_ST_SEGMENTS);
-            s_ns = ns;
+            bool over;
+            const int ns = cap_segments_warp(seg, soff, bk, clat, clon, sgeo.theta, &over);
+            if (threadIdx.x == 0) {
+                s_cg = cg;
+                if (over) atomicOr(status, LG_ST_SEGMENTS);
+                s_ns = ns;
+            }
         }
         __syncthreads();
         const int ns = s_ns;
         const CubeGeo cg = s_cg;
-        for (int si = 0; si < ns; si++) {
-            const Seg sg = seg[si];
-            for (int i = sg.b + threadIdx.x; i < sg.e; i += kThreads) {
-                const float4 p = bk.xyz[i];
-                if (keep_candidate(p, sg.exact, cg, geo, prm, &counters[LG_CNT_BORDER])) {
-                    const int o = __float_as_int(p.w);
-                    atomicOr(&bits[o >> 5], 1u << (o & 31));
-                }
+        each_candidate(seg, soff, ns, bk, [&](const float4 &p, int exact) {
+            if (keep_candidate(p, exact, cg, geo, prm, &counters[LG_CNT_BORDER])) {
+                const int o = __float_as_int(p.w);
+                atomicOr(&bits[o >> 5], 1u << (o & 31));
             }
-        }
+        });
         __syncthreads();
         // exclusive prefix of the kept counts of each thread's word range
         int cnt = 0;
@@ -465,16 +582,27 @@ k_search_bitmap(LgGrid g, LgParams prm, LgSearchGeo sgeo, LgBuckets bk, LgObsGeo
                          &s_off);
         __syncthreads();
         const long long off = s_off;
-        if (off >= 0) {
-            int pos = before;
-            for (int w = w0; w < w1 && pos < nout; w++) {
-                uint32_t m = bits[w];
-                while (m && pos < nout) {
-                    const int b = __ffs(m) - 1;
-                    m &= m - 1u;
-                    write_entry(w * 32 + b, off + pos, cg, geo, prm, lm, lidx, lrloc);
-                    pos++;
+        if (off >= 0 && w0 < w1) {
+            // this thread's kept indices in order, four entries at a time
+            // (their gathers in flight together)
+            int pos = before, w = w0;
+            uint32_t m = bits[w];
+            while (pos < nout) {
+                int o4[4];
+                int nv = 0;
+#pragma unroll
+                for (int u = 0; u < 4; u++) {
+                    while (m == 0u && w + 1 < w1) m = bits[++w];
+                    o4[u] = -1;
+                    if (m != 0u && pos + u < nout) {
+                        o4[u] = w * 32 + __ffs(m) - 1;
+                        m &= m - 1u;
+                        nv++;
+                    }
                 }
+                write_entries4(o4, off + pos, cg, geo, prm, lm, lidx, lrloc);
+                pos += nv;
+                if (nv < 4) break;
             }
         }
         __syncthreads();
