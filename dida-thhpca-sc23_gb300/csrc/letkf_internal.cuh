@@ -151,6 +151,10 @@ struct LgSearchGeo {
     const double *row_s, *row_c;
     const double *col_yr, *col_cos, *col_sin;
     float theta, lo2, hi2;
+    // the cap stays far from the antipode's buckets: there only obs within a
+    // chord of 1e-5 of the antipode (where the double acos can give NaN)
+    // need the double test, the rest are out
+    int anti_far;
 };
 
 struct LgObsGeo {

@@ -368,6 +368,9 @@ LgSearchGeo lg_search_geo(letkf_ctx *ctx)
         sg.lo2 = -1.0f;           // every candidate takes the double test
         sg.hi2 = 1.0e30f;
     }
+    // antipode buckets reach at most two bucket sizes from the antipode
+    const double ext = 2.0 * (ctx->cell_lat + ctx->cell_lon) * (M_PI / 180.0);
+    sg.anti_far = (theta + ext + 0.01 < M_PI) ? 1 : 0;
     return sg;
 }
 

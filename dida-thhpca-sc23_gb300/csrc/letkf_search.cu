@@ -45,6 +45,7 @@ struct CubeGeo {
     double s2, c2, y2r;      // centre sin/cos latitude, longitude (rad)
     float cx, cy, cz;        // centre unit vector
     float lo2, hi2;          // chord^2 thresholds: below lo2 keep, above hi2 drop
+    int anti_far;            // exact candidates beyond a 1e-5 chord of the antipode are out
 };
 
 // The buckets of band `band` between longitudes lon0 and lon1 (degrees,
@@ -91,6 +92,12 @@ __device__ __forceinline__ bool keep_candidate(const float4 &p, int exact, const
         const float d2 = dx * dx + dy * dy + dz * dz;
         if (d2 > cg.hi2) return false;
         if (d2 < cg.lo2) return true;
+    } else if (cg.anti_far) {
+        // near the antipode the double distance is about pi (out) unless the
+        // acos argument rounds below -1 (NaN, kept), which needs a chord to
+        // the antipode far below 1e-5
+        const float ax = p.x + cg.cx, ay = p.y + cg.cy, az = p.z + cg.cz;
+        if (ax * ax + ay * ay + az * az > 1e-10f) return false;
     }
     const int o = __float_as_int(p.w);
     const double dist = lg_dist(geo.s[o], geo.c[o], geo.yr[o], cg.s2, cg.c2, cg.y2r);
@@ -340,6 +347,7 @@ __device__ CubeGeo cube_geo(const LgGrid &g, const LgParams &prm, const LgSearch
     cg.cz = (float)cg.s2;
     cg.lo2 = sg.lo2;
     cg.hi2 = sg.hi2;
+    cg.anti_far = sg.anti_far;
     return cg;
 }
 
