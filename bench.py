@@ -182,6 +182,16 @@ def measured_peaks():
         return {}
 
 
+def workload_label(cfg, w):
+    """The workload of configurations 0-2 in words, from the generated instance."""
+    res = 180.0 / w.nlat
+    c = w.loc_dist_km
+    dens = " (4x box 0-60E 10S-30N)" if cfg in (1, 2) else " uniform"
+    return (f"config{cfg}{'/2' if cfg == 1 else ''}: {res:g}deg {w.nlon}x{w.nlat}x{w.nz}, k={w.k}, "
+            f"{w.obs['lat'].size} obs{dens}, GC c={c:g} km (cut-off {2 * c:g} km), rho={w.inflation:g}, "
+            f"{'level-select' if w.h_mode == 1 else 'log-p'} H")
+
+
 def cpu_baseline(w, seconds_target, label):
     """The CPU oracle on a bounded sample of the workload's columns."""
     from oracle import oracle as O
@@ -478,13 +488,13 @@ def run_ours(args, rank, world, local_rank):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "bf16 hi/lo tensor products + f64 eigen/mean" if head == "mixed" else "f64",
         "data": "synthetic (seeded; no public dataset for this path)",
-        "config": {"workload": "config1/2: 1deg 360x180x32, k=64, 200k obs (4x box 0-60E 10S-30N), "
-                               "GC c=400 km (cut-off 800 km), rho=1.08, level-select H",
+        "config": {"workload": workload_label(args.config, w),
                    "form": "mixed precision (precision 1)" if head == "mixed" else "plain FP64",
                    "columns": w.ncol, "ensemble": w.k, "obs": int(w.obs["lat"].size),
                    "sum_p": st["sum_p"], "max_p": st["max_p"],
                    "jacobi_max_sweeps": st["max_sweeps"], "jacobi_sweep_cap_hits": st["n_not_converged"],
-                   "l2": "inputs larger than L2 (xb 3.2 GB)", "parallelism": f"replicas x{world}"},
+                   "l2": f"inputs larger than L2 (xb {w.xb.nbytes / 1e9:.1f} GB)",
+                   "parallelism": f"replicas x{world}"},
         "e2e": {"value": whole_job_columns_per_s(world, w.ncol, ms_e2e), "unit": "columns/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "max_abs_diff_vs_device_run": e2e_vs_device},
@@ -511,7 +521,7 @@ def run_ours(args, rank, world, local_rank):
         line["mixed_error_vs_fp64"] = errs
         line["mixed_error_max"] = max(max(v.values()) for v in errs.values())
     if world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(w, args.cpu_seconds, "config1")
+        line["cpu_baseline"] = cpu_baseline(w, args.cpu_seconds, f"config{args.config}")
         line["cpu_baseline"]["cpu"] = cpu_model()
     print(json.dumps(line), flush=True)
 
