@@ -44,6 +44,41 @@ cudaError_t h2d(DevBuf<T> &buf, const T *src, size_t count, cudaStream_t s)
     return cudaMemcpyAsync(buf.p, src, sizeof(T) * count, cudaMemcpyHostToDevice, s);
 }
 
+// The copy streams and their events (created on first use).
+cudaError_t copy_streams(letkf_ctx *ctx)
+{
+    for (int i = 0; i < letkf_ctx::kCopyStreams; i++) {
+        if (ctx->cstream[i]) continue;
+        cudaError_t e = cudaStreamCreateWithFlags(&ctx->cstream[i], cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->cev[i], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->sev[i], cudaEventDisableTiming);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+// Host -> device copy of count elements in equal parts on the copy streams,
+// joined back into the main stream.
+template <typename T>
+cudaError_t h2d_parts(letkf_ctx *ctx, DevBuf<T> &buf, const T *src, size_t count)
+{
+    cudaError_t e = buf.reserve(count);
+    if (e != cudaSuccess || count == 0) return e;
+    constexpr int NS = letkf_ctx::kCopyStreams;
+    if ((e = cudaEventRecord(ctx->sev[0], ctx->stream)) != cudaSuccess) return e;
+    const size_t part = (count + NS - 1) / NS;
+    for (int i = 0; i < NS; i++) {
+        const size_t a = std::min(count, i * part), b = std::min(count, a + part);
+        if ((e = cudaStreamWaitEvent(ctx->cstream[i], ctx->sev[0], 0)) != cudaSuccess) return e;
+        if (b > a && (e = cudaMemcpyAsync(buf.p + a, src + a, sizeof(T) * (b - a), cudaMemcpyHostToDevice,
+                                          ctx->cstream[i])) != cudaSuccess)
+            return e;
+        if ((e = cudaEventRecord(ctx->cev[i], ctx->cstream[i])) != cudaSuccess) return e;
+        if ((e = cudaStreamWaitEvent(ctx->stream, ctx->cev[i], 0)) != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
 float elapsed(cudaEvent_t a, cudaEvent_t b)
 {
     float ms = 0.f;
@@ -599,6 +634,23 @@ int letkf_gpu_set_cube_range(letkf_ctx *ctx, int64_t first, int64_t count)
 }  // extern "C"
 
 int lg_set_err(letkf_ctx *ctx, int code, const char *msg) { return set_err(ctx, code, msg); }
+
+cudaError_t lg_sink_columns(letkf_ctx *ctx, int64_t c0, int64_t c1)
+{
+    if (!ctx->sink_xa || c1 <= c0) return cudaSuccess;
+    const int i = ctx->sink_next++ % letkf_ctx::kCopyStreams;
+    cudaError_t e = cudaEventRecord(ctx->sev[i], ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->cstream[i], ctx->sev[i], 0);
+    const size_t per_s = (size_t)ctx->n * ctx->k, per_m = (size_t)ctx->n;
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(ctx->sink_xa + c0 * per_s, ctx->sink_dxa + c0 * per_s,
+                            sizeof(double) * (c1 - c0) * per_s, cudaMemcpyDeviceToHost, ctx->cstream[i]);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(ctx->sink_axa + c0 * per_m, ctx->sink_daxa + c0 * per_m,
+                            sizeof(double) * (c1 - c0) * per_m, cudaMemcpyDeviceToHost, ctx->cstream[i]);
+    if (e == cudaSuccess) ctx->sink_cols += c1 - c0;
+    return e;
+}
 int lg_reset_status(letkf_ctx *ctx) { return reset_status(ctx); }
 int lg_read_status(letkf_ctx *ctx, unsigned &status, unsigned long long *cnt)
 {
@@ -678,7 +730,8 @@ int letkf_gpu_run(letkf_ctx *ctx, const double *xb, const double *axb, const let
     const double *dxb = xb, *daxb = axb;
     double *dxa = xa, *daxa = axa;
     if (host) {
-        LG_CUDA(h2d(ctx->d_xb, xb, nstate, ctx->stream));
+        LG_CUDA(copy_streams(ctx));
+        LG_CUDA(h2d_parts(ctx, ctx->d_xb, xb, nstate));
         LG_CUDA(h2d(ctx->d_axb, axb, nmean, ctx->stream));
         LG_CUDA(ctx->d_xa.reserve(nstate));
         LG_CUDA(ctx->d_axa.reserve(nmean));
@@ -686,11 +739,29 @@ int letkf_gpu_run(letkf_ctx *ctx, const double *xb, const double *axb, const let
         daxb = ctx->d_axb.p;
         dxa = ctx->d_xa.p;
         daxa = ctx->d_axa.p;
+        // one column per cube and no averaging over cubes: the core can hand
+        // out finished columns (the staged k = 64 core does)
+        if (ctx->params.cube_n == 1 && ctx->params.overlap == 0) {
+            ctx->sink_xa = xa;
+            ctx->sink_axa = axa;
+            ctx->sink_dxa = dxa;
+            ctx->sink_daxa = daxa;
+        }
+        ctx->sink_cols = 0;
     }
     unsigned long long cnt[LG_CNT_N] = {};
     rc = lg_run_analysis(ctx, obs, host, dxb, daxb, dxa, daxa, cnt);
+    ctx->sink_xa = nullptr;
+    ctx->sink_axa = nullptr;
     if (rc) return rc;
-    if (host) {
+    if (host && ctx->sink_cols > 0) {
+        // the copies on the copy streams, before the status read
+        for (int i = 0; i < letkf_ctx::kCopyStreams; i++) {
+            LG_CUDA(cudaEventRecord(ctx->cev[i], ctx->cstream[i]));
+            LG_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->cev[i], 0));
+        }
+    }
+    if (host && ctx->sink_cols != ctx->range1 - ctx->range0) {
         // the columns of the analysed cubes: with cube_n 1 the cubes
         // themselves, else whole longitude strips of them
         int64_t col0 = ctx->range0, col1 = ctx->range1;
@@ -893,6 +964,11 @@ int letkf_gpu_destroy(letkf_ctx *ctx)
     ctx->d_counters.release();
     for (int i = 0; i < 8; i++)
         if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
+    for (int i = 0; i < letkf_ctx::kCopyStreams; i++) {
+        if (ctx->cev[i]) cudaEventDestroy(ctx->cev[i]);
+        if (ctx->sev[i]) cudaEventDestroy(ctx->sev[i]);
+        if (ctx->cstream[i]) cudaStreamDestroy(ctx->cstream[i]);
+    }
     if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
     delete ctx;
     return LETKF_OK;

@@ -268,6 +268,19 @@ struct letkf_ctx {
     cudaEvent_t ev[8] = {};
     letkf_stats stats{};
     std::string last_error;
+
+    // Host copies beside the analysis (letkf_gpu_run with host pointers): the
+    // state goes in on the copy streams in parts, and the staged k = 64 core
+    // hands each finished block of cubes to lg_sink_columns, which copies its
+    // analysis columns out on a copy stream while the next block runs.
+    static constexpr int kCopyStreams = 2;
+    cudaStream_t cstream[kCopyStreams] = {};
+    cudaEvent_t cev[kCopyStreams] = {};      // a copy stream's work so far
+    cudaEvent_t sev[kCopyStreams] = {};      // the main stream's work before a copy
+    double *sink_xa = nullptr, *sink_axa = nullptr;          // host outputs, or null
+    const double *sink_dxa = nullptr, *sink_daxa = nullptr;  // device outputs
+    int sink_next = 0;
+    int64_t sink_cols = 0;                   // columns handed to the copy streams
 };
 
 // ---------------------------------------------------------------------------
@@ -295,6 +308,10 @@ cudaError_t lg_launch_search_dec(letkf_ctx *ctx, const LgGrid &g, const double *
 cudaError_t lg_launch_overlap_update(letkf_ctx *ctx, const LgGrid &g, const double *xb, const double *axb,
                                      double *xa, double *axa);
 cudaError_t lg_launch_obs_lnp(letkf_ctx *ctx, int64_t nobs, const double *oph);
+// Copy the analysis columns of cubes [c0, c1) (one column per cube) to the
+// host outputs of a letkf_gpu_run on a copy stream, after the main stream's
+// work so far; no-op without host outputs.
+cudaError_t lg_sink_columns(letkf_ctx *ctx, int64_t c0, int64_t c1);
 
 // The analysis of letkf_gpu_run on device state: observations staged (host or
 // device pointers), H, search and core (cube windows), overlapped-cube

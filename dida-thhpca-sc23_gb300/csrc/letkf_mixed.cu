@@ -929,7 +929,6 @@ k_eig_warp(int64_t cube0, int64_t cube_end, int R, double cdiag, float tol, cons
     float *Wp = smw + (size_t)warp * K * LDW;           // this warp's columns
     const int64_t base = cube0 / R * R;
     const int64_t nruns = (cube_end - base + R - 1) / R;
-    const int64_t nw = (int64_t)gridDim.x * (kTE / 32);
     const float cd = (float)cdiag;
 #ifdef LG_PHASE_CLOCKS
     long long ec[3] = {0, 0, 0}, et = clock64();
@@ -944,7 +943,13 @@ k_eig_warp(int64_t cube0, int64_t cube_end, int R, double cdiag, float tol, cons
     do {             \
     } while (0)
 #endif
-    for (int64_t run = blockIdx.x * (int64_t)(kTE / 32) + warp; run < nruns; run += nw) {
+    for (;;) {
+        // the next run from the queue cursor (runs cost different numbers of
+        // sweeps, so a fixed deal leaves some warps with the longest tail)
+        int64_t run = 0;
+        if (lane == 0) run = (int64_t)atomicAdd(&counters[LG_CNT_QUEUE], 1ull);
+        run = __shfl_sync(0xffffffffu, run, 0);
+        if (run >= nruns) break;
         const int64_t c0 = max(cube0, base + run * R), c1 = min(cube_end, base + (run + 1) * R);
         for (int64_t c = c0; c < c1; c++) {
             const float *Ac = mA + (c - cube0) * K * K;
@@ -1068,7 +1073,7 @@ k_eig_warp(int64_t cube0, int64_t cube_end, int R, double cdiag, float tol, cons
 
 // Most cubes one staged launch sequence holds intermediates for (A, X: 2 k^2
 // floats, g: k doubles, lambda: k floats per cube); a multiple of every
-// work-queue chunk size.
+// work-queue chunk size and of the eigensolve run.
 constexpr int64_t kStagedCubes = 1 << 17;
 
 template <int K, int ST>
@@ -1125,8 +1130,21 @@ cudaError_t launch_mixed(letkf_ctx *ctx, const LgGrid &g, const double *xb, cons
         const int R = 8;
         const size_t ew = (size_t)K * (K + 4) * sizeof(float) * (kTE / 32);
         cudaError_t e = cudaFuncSetAttribute(k_eig_warp<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ew);
-        for (int64_t b0 = w0; b0 < w1 && e == cudaSuccess; b0 += kStagedCubes) {
-            const int64_t b1 = min(w1, b0 + kStagedCubes), nb = b1 - b0;
+        // blocks end at multiples of `sub` in cube numbering (so the runs and
+        // chunks, and the results, do not depend on the blocking); when the
+        // analysis goes back to host memory, two blocks, the first (3/5 of the
+        // cubes) copied out while the second runs: the copy of 3/5 of the
+        // state takes about as long as the analysis of 2/5 (smaller blocks
+        // leave the eigensolve's warps short of runs)
+        int64_t sub = kStagedCubes;
+        if (ctx->sink_xa) {
+            const int64_t step = max((int64_t)4096, (int64_t)lg_run_chunk(ctx));
+            sub = min(kStagedCubes, max(step, ((w1 - w0) * 3 / 5 + step - 1) / step * step));
+        }
+        int64_t b1 = w0;
+        for (int64_t b0 = w0; b0 < w1 && e == cudaSuccess; b0 = b1) {
+            b1 = min(w1, (b0 / sub + 1) * sub);
+            const int64_t nb = b1 - b0;
             ctx->win0 = b0;
             ctx->win1 = b1;
             if ((e = ctx->d_mA.reserve((size_t)nb * K * K)) != cudaSuccess) break;
@@ -1139,12 +1157,16 @@ cudaError_t launch_mixed(letkf_ctx *ctx, const LgGrid &g, const double *xb, cons
             const int64_t runs = (b1 - b0 / R * R + R - 1) / R;
             const int64_t eb = (runs + kTE / 32 - 1) / (kTE / 32);
             const unsigned eblocks = (unsigned)(eb < nsm ? eb : nsm);
+            if ((e = cudaMemsetAsync(ctx->d_counters.p + LG_CNT_QUEUE, 0, sizeof(unsigned long long),
+                                     ctx->stream)) != cudaSuccess)
+                break;
             lg_count_launch();
             k_eig_warp<K><<<eblocks, kTE, ew, ctx->stream>>>(b0, b1, R, (double)(K - 1) / ctx->params.inflation,
                                                           LG_MIXED_JACOBI_TOL, ctx->d_mA.p, ctx->d_mX.p,
                                                           ctx->d_mlam.p, ctx->d_counters.p);
             if ((e = cudaGetLastError()) != cudaSuccess) break;
             e = launch_stage<K, 2>(ctx, g, xb, axb, xa, axa, trans_out, w_out, chunk, nchunks, nsm);
+            if (e == cudaSuccess) e = lg_sink_columns(ctx, b0, b1);
         }
         ctx->win0 = w0;
         ctx->win1 = w1;
