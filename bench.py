@@ -426,7 +426,7 @@ def run_ours(args, rank, world, local_rank):
     # each step timed on its own (the call returns when its outputs are in
     # host memory); the median over the steps, since the host link is shared
     # with other work on the machine and single steps can stall
-    e2e_steps = max(3, min(args.steps, 5))
+    e2e_steps = 5
     e2e_ms_steps = []
     for _ in range(e2e_steps):
         f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)

@@ -58,9 +58,9 @@ cudaError_t copy_streams(letkf_ctx *ctx)
 }
 
 // Host -> device copy of count elements in equal parts on the copy streams,
-// joined back into the main stream.
+// joined back into the main stream (else the caller joins the events cev).
 template <typename T>
-cudaError_t h2d_parts(letkf_ctx *ctx, DevBuf<T> &buf, const T *src, size_t count)
+cudaError_t h2d_parts(letkf_ctx *ctx, DevBuf<T> &buf, const T *src, size_t count, bool join = true)
 {
     cudaError_t e = buf.reserve(count);
     if (e != cudaSuccess || count == 0) return e;
@@ -74,7 +74,7 @@ cudaError_t h2d_parts(letkf_ctx *ctx, DevBuf<T> &buf, const T *src, size_t count
                                           ctx->cstream[i])) != cudaSuccess)
             return e;
         if ((e = cudaEventRecord(ctx->cev[i], ctx->cstream[i])) != cudaSuccess) return e;
-        if ((e = cudaStreamWaitEvent(ctx->stream, ctx->cev[i], 0)) != cudaSuccess) return e;
+        if (join && (e = cudaStreamWaitEvent(ctx->stream, ctx->cev[i], 0)) != cudaSuccess) return e;
     }
     return cudaSuccess;
 }
@@ -169,13 +169,30 @@ int reset_status(letkf_ctx *ctx)
 }
 
 // H and the observation buckets for the staged observations.
-int obs_prepare(letkf_ctx *ctx, const double *xb, const double *axb, const ObsDev &od, int64_t no)
+// H, the buckets and the per-observation terms of the search.  With
+// defer_members the state is still being copied in: only the geometry pass
+// runs now, and the members pass waits for the copy in lg_members_if_pending.
+int obs_prepare(letkf_ctx *ctx, const double *xb, const double *axb, const ObsDev &od, int64_t no,
+                bool defer_members = false)
 {
     const LgGrid g = lg_grid(ctx);
     int rc = reserve_obs_work(ctx, no);
     if (rc) return rc;
     LG_CUDA(lg_launch_obs_prepare(ctx, g, xb, axb, no, od.lat, od.lon, od.ph, od.lev, od.var, od.yo,
-                                  od.rinv));
+                                  od.rinv, defer_members ? 1 : 0));
+    if (defer_members) {
+        ctx->members_pending = true;
+        ctx->pend_xb = xb;
+        ctx->pend_axb = axb;
+        ctx->pend_lat = od.lat;
+        ctx->pend_lon = od.lon;
+        ctx->pend_ph = od.ph;
+        ctx->pend_lev = od.lev;
+        ctx->pend_var = od.var;
+        ctx->pend_yo = od.yo;
+        ctx->pend_rinv = od.rinv;
+        ctx->pend_no = no;
+    }
     LG_CUDA(lg_launch_buckets(ctx, no));
     if (ctx->dec_nx > 0) LG_CUDA(lg_launch_block_members(ctx, no, od.lat, od.lon));
     if (ctx->params.overlap == 0 && ctx->params.vert_dist > 0.0) {
@@ -227,11 +244,17 @@ int size_pool(letkf_ctx *ctx, int64_t cap)
 cudaError_t launch_search(letkf_ctx *ctx, const ObsDev &od, int64_t no)
 {
     const LgGrid g = lg_grid(ctx);
+    // before the departures (H's members pass deferred) the entries get
+    // their second factor at the core launch
+    ctx->lists_need_ef = ctx->members_pending && ctx->params.precision == LETKF_PREC_MIXED;
     return ctx->dec_nx > 0 ? lg_launch_search_dec(ctx, g, od.lat) : lg_launch_search(ctx, g, no);
 }
 
 cudaError_t launch_core(letkf_ctx *ctx, const double *xb, const double *axb, double *xa, double *axa)
 {
+    cudaError_t e = lg_members_if_pending(ctx);
+    if (e != cudaSuccess) return e;
+    if (ctx->lists_need_ef && (e = lg_launch_list_efactor(ctx)) != cudaSuccess) return e;
     const LgGrid g = lg_grid(ctx);
     // overlapped cubes: each cube's trans now, the columns' averages after
     // the last window (lg_launch_overlap_update)
@@ -635,6 +658,20 @@ int letkf_gpu_set_cube_range(letkf_ctx *ctx, int64_t first, int64_t count)
 
 int lg_set_err(letkf_ctx *ctx, int code, const char *msg) { return set_err(ctx, code, msg); }
 
+cudaError_t lg_members_if_pending(letkf_ctx *ctx)
+{
+    if (!ctx->members_pending) return cudaSuccess;
+    ctx->members_pending = false;
+    // the state copy on the copy streams
+    for (int i = 0; i < letkf_ctx::kCopyStreams; i++) {
+        cudaError_t e = cudaStreamWaitEvent(ctx->stream, ctx->cev[i], 0);
+        if (e != cudaSuccess) return e;
+    }
+    return lg_launch_obs_prepare(ctx, lg_grid(ctx), ctx->pend_xb, ctx->pend_axb, ctx->pend_no, ctx->pend_lat,
+                                 ctx->pend_lon, ctx->pend_ph, ctx->pend_lev, ctx->pend_var, ctx->pend_yo,
+                                 ctx->pend_rinv, 2);
+}
+
 cudaError_t lg_sink_columns(letkf_ctx *ctx, int64_t c0, int64_t c1)
 {
     if (!ctx->sink_xa || c1 <= c0) return cudaSuccess;
@@ -667,13 +704,13 @@ int lg_check_run(letkf_ctx *ctx, const letkf_obs *obs)
 }
 
 int lg_run_analysis(letkf_ctx *ctx, const letkf_obs *obs, bool host_obs, const double *dxb,
-                    const double *daxb, double *dxa, double *daxa, unsigned long long *cnt)
+                    const double *daxb, double *dxa, double *daxa, unsigned long long *cnt, bool state_in_flight)
 {
     ObsDev od;
     int rc = stage_obs(ctx, obs, host_obs, od);
     if (rc) return rc;
     LG_CUDA(cudaEventRecord(ctx->ev[1], ctx->stream));
-    rc = obs_prepare(ctx, dxb, daxb, od, obs->nobs);
+    rc = obs_prepare(ctx, dxb, daxb, od, obs->nobs, state_in_flight);
     if (rc) return rc;
     LG_CUDA(cudaEventRecord(ctx->ev[2], ctx->stream));
     if (ctx->params.overlap > 0) {
@@ -731,7 +768,7 @@ int letkf_gpu_run(letkf_ctx *ctx, const double *xb, const double *axb, const let
     double *dxa = xa, *daxa = axa;
     if (host) {
         LG_CUDA(copy_streams(ctx));
-        LG_CUDA(h2d_parts(ctx, ctx->d_xb, xb, nstate));
+        LG_CUDA(h2d_parts(ctx, ctx->d_xb, xb, nstate, false));
         LG_CUDA(h2d(ctx->d_axb, axb, nmean, ctx->stream));
         LG_CUDA(ctx->d_xa.reserve(nstate));
         LG_CUDA(ctx->d_axa.reserve(nmean));
@@ -750,9 +787,16 @@ int letkf_gpu_run(letkf_ctx *ctx, const double *xb, const double *axb, const let
         ctx->sink_cols = 0;
     }
     unsigned long long cnt[LG_CNT_N] = {};
-    rc = lg_run_analysis(ctx, obs, host, dxb, daxb, dxa, daxa, cnt);
+    // with host buffers the state is still on the copy streams: the H
+    // geometry, the buckets and the search run meanwhile
+    rc = lg_run_analysis(ctx, obs, host, dxb, daxb, dxa, daxa, cnt, host);
     ctx->sink_xa = nullptr;
     ctx->sink_axa = nullptr;
+    if (host) {
+        // the copy is joined even when the analysis stopped early
+        for (int i = 0; i < letkf_ctx::kCopyStreams; i++) LG_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->cev[i], 0));
+        ctx->members_pending = false;
+    }
     if (rc) return rc;
     if (host && ctx->sink_cols > 0) {
         // the copies on the copy streams, before the status read

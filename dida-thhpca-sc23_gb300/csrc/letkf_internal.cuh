@@ -281,6 +281,18 @@ struct letkf_ctx {
     const double *sink_dxa = nullptr, *sink_daxa = nullptr;  // device outputs
     int sink_next = 0;
     int64_t sink_cols = 0;                   // columns handed to the copy streams
+    // H on the members waits for the state copy: the geometry, buckets and
+    // search run while it is on the way, and the first core launch runs the
+    // members pass first (lg_members_if_pending)
+    bool members_pending = false;
+    const double *pend_xb = nullptr, *pend_axb = nullptr;
+    const double *pend_lat = nullptr, *pend_lon = nullptr, *pend_ph = nullptr, *pend_yo = nullptr,
+                 *pend_rinv = nullptr;
+    const int32_t *pend_lev = nullptr, *pend_var = nullptr;
+    int64_t pend_no = 0;
+    // the search ran before the departures: its list entries hold sqrt(rloc)
+    // only, and each core launch first completes them (lg_launch_list_efactor)
+    bool lists_need_ef = false;
 };
 
 // ---------------------------------------------------------------------------
@@ -288,15 +300,22 @@ struct letkf_ctx {
 void lg_count_launch();
 
 // Kernel launchers (letkf_prep.cu, letkf_search.cu, letkf_core.cu).
+// H: mode 0 everything; 1 the per-observation geometry, weights and bucket
+// (no state read); 2 the members, the means and the departures.
 cudaError_t lg_launch_obs_prepare(letkf_ctx *ctx, const LgGrid &g, const double *xb,
                                   const double *axb, int64_t nobs, const double *olat,
                                   const double *olon, const double *oph, const int32_t *olev,
-                                  const int32_t *ovar, const double *oyo, const double *orinv);
+                                  const int32_t *ovar, const double *oyo, const double *orinv, int mode = 0);
+// The members pass of H when a run deferred it behind the state copy.
+cudaError_t lg_members_if_pending(letkf_ctx *ctx);
 cudaError_t lg_launch_buckets(letkf_ctx *ctx, int64_t nobs);
 void lg_launch_scan_exclusive(const int *in, int *out, int n, cudaStream_t stream);
 cudaError_t lg_launch_geo_tables(letkf_ctx *ctx);
 LgSearchGeo lg_search_geo(letkf_ctx *ctx);
 cudaError_t lg_launch_search(letkf_ctx *ctx, const LgGrid &g, int64_t nobs);
+// The second factor of the mixed form's list entries of the last search,
+// sqrt(rloc) sqrt(rdiaginv) dep, once the departures exist.
+cudaError_t lg_launch_list_efactor(letkf_ctx *ctx);
 // decomposed observation sets (letkf_decomp.cu, letkf_search.cu)
 int lg_decomp_dims(int nranks, int &lat_blocks, int &lon_blocks);
 cudaError_t lg_decomp_setup(letkf_ctx *ctx, const std::vector<float> &glat_ext,
@@ -315,10 +334,13 @@ cudaError_t lg_sink_columns(letkf_ctx *ctx, int64_t c0, int64_t c1);
 
 // The analysis of letkf_gpu_run on device state: observations staged (host or
 // device pointers), H, search and core (cube windows), overlapped-cube
-// averaging; events 1-4 recorded.  lg_finish_run records event 5, reads the
-// status and counters, fills the stats and maps the status to a return code.
+// averaging; events 1-4 recorded.  state_in_flight: dxb is still being
+// copied in on the copy streams (H on the members waits for it).
+// lg_finish_run records event 5, reads the status and counters, fills the
+// stats and maps the status to a return code.
 int lg_run_analysis(letkf_ctx *ctx, const letkf_obs *obs, bool host_obs, const double *dxb,
-                    const double *daxb, double *dxa, double *daxa, unsigned long long *cnt);
+                    const double *daxb, double *dxa, double *daxa, unsigned long long *cnt,
+                    bool state_in_flight = false);
 int lg_finish_run(letkf_ctx *ctx, const letkf_obs *obs, unsigned long long *cnt);
 int lg_check_run(letkf_ctx *ctx, const letkf_obs *obs);
 int lg_reset_status(letkf_ctx *ctx);

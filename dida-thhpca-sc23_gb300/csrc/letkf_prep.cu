@@ -65,7 +65,7 @@ k_obs_prepare(LgGrid g, LgParams prm, const double *__restrict__ xb, const doubl
               float *__restrict__ rinvf, double *__restrict__ os, double *__restrict__ oc,
               double *__restrict__ oyr, float4 *__restrict__ oxyz, int *__restrict__ obucket,
               float *__restrict__ ys32, float *__restrict__ oef,
-              int nblat, int nblon, double cell_lat, double cell_lon, unsigned *status)
+              int nblat, int nblon, double cell_lat, double cell_lon, unsigned *status, int mode)
 {
     const int lane = threadIdx.x & 31;
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -95,11 +95,15 @@ k_obs_prepare(LgGrid g, LgParams prm, const double *__restrict__ xb, const doubl
             }
             if (ok && is3d && prm.h_mode == 0) ok = oph[o] > 0.0;
             if (!ok) {
-                dep[o] = 0.0;
-                rinvf[o] = 0.0f;
-                if (oef) oef[o] = 0.0f;
-                obucket[o] = -1;
-                atomicOr(status, LG_ST_BAD_OBS);
+                if (mode != 1) {
+                    dep[o] = 0.0;
+                    if (oef) oef[o] = 0.0f;
+                }
+                if (mode != 2) {
+                    rinvf[o] = 0.0f;
+                    obucket[o] = -1;
+                    atomicOr(status, LG_ST_BAD_OBS);
+                }
             } else {
                 // find_obs_grid (letkf_obs.F90:199-241); the spacing is a float difference
                 const int tx = first_ge(g.glat, g.nlat + 1, lat);
@@ -127,9 +131,11 @@ k_obs_prepare(LgGrid g, LgParams prm, const double *__restrict__ xb, const doubl
                 row = (is3d && prm.h_mode == 1) ? start + lev - 1 : start;
                 if (psearch) p_obs = oph[o];
                 const float rf = (float)orinv[o];
-                rinvf[o] = rf;
                 // scaled perturbations for the tensor-core products: y sqrt(rdiaginv)
                 sr = sqrt((double)rf);
+            }
+            if (ok && mode != 2) {
+                rinvf[o] = (float)orinv[o];
                 const double xr = lg_rad(lat), yr = lg_rad(lon);
                 const double s = sin(xr), c = cos(xr);
                 os[o] = s;
@@ -150,6 +156,7 @@ k_obs_prepare(LgGrid g, LgParams prm, const double *__restrict__ xb, const doubl
         }
         const unsigned okmask = __ballot_sync(0xffffffffu, ok);
         const unsigned psmask = __ballot_sync(0xffffffffu, psearch);
+        if (mode == 1) continue;
 
         // ---- members of each observation of the group, lanes over the members
         double mymean = 0.0;
@@ -294,7 +301,7 @@ int grid_for(int64_t work, int threads, int cap)
 cudaError_t lg_launch_obs_prepare(letkf_ctx *ctx, const LgGrid &g, const double *xb,
                                   const double *axb, int64_t nobs, const double *olat,
                                   const double *olon, const double *oph, const int32_t *olev,
-                                  const int32_t *ovar, const double *oyo, const double *orinv)
+                                  const int32_t *ovar, const double *oyo, const double *orinv, int mode)
 {
     if (nobs == 0) return cudaSuccess;
     const LgParams prm = lg_params(ctx);
@@ -305,7 +312,7 @@ cudaError_t lg_launch_obs_prepare(letkf_ctx *ctx, const LgGrid &g, const double 
         ctx->d_rinvf.p, ctx->d_os.p, ctx->d_oc.p, ctx->d_oyr.p, ctx->d_oxyz.p, ctx->d_obucket.p,
         ctx->params.precision == LETKF_PREC_MIXED ? ctx->d_ys32.p : nullptr,
         ctx->params.precision == LETKF_PREC_MIXED ? ctx->d_oef.p : nullptr,
-        ctx->nblat, ctx->nblon, ctx->cell_lat, ctx->cell_lon, ctx->d_status.p);
+        ctx->nblat, ctx->nblon, ctx->cell_lat, ctx->cell_lon, ctx->d_status.p, mode);
     return cudaGetLastError();
 }
 

@@ -220,7 +220,7 @@ __device__ void bitonic_sort(int32_t *keys, int n_pow2)
 
 // Observation terms the mixed form's list entries carry.
 struct LgListMeta {
-    const float *ef;          // sqrt(rdiaginv) dep per obs (mixed form)
+    const float *ef;          // sqrt(rdiaginv) dep per obs, or null before the departures exist
     float2 *meta;             // out, mixed form only
     int32_t *need;            // out: each cube's list length, written even when the pool is full
 };
@@ -243,9 +243,10 @@ __device__ __forceinline__ void write_entry(int o, long long at, const CubeGeo &
         lidx[at] = o;
         lrloc[at] = (double)rl;
         // the mixed core's per-entry factors: Yhat = y sqrt(rdiaginv) sqrt(rloc)
-        // and e = sqrt(rdiaginv rloc) dep (g = Yhat e)
+        // and e = sqrt(rdiaginv rloc) dep (g = Yhat e); the second waits for
+        // the departures when the search runs first (k_list_efactor)
         const float sr = sqrtf(rl);
-        lm.meta[at] = make_float2(sr, sr * lm.ef[o]);
+        lm.meta[at] = make_float2(sr, lm.ef ? sr * lm.ef[o] : 0.0f);
     } else {
         const double dist = lg_dist(geo.s[o], geo.c[o], geo.yr[o], cg.s2, cg.c2, cg.y2r);
         const double ri = lg_ri(dist, prm.local_dist);
@@ -267,7 +268,7 @@ __device__ __forceinline__ void write_entries4(const int *o4, long long at, cons
 #pragma unroll
         for (int u = 0; u < 4; u++) {
             q[u] = o4[u] >= 0 ? geo.xyz[o4[u]] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            ef[u] = o4[u] >= 0 ? lm.ef[o4[u]] : 0.0f;
+            ef[u] = (o4[u] >= 0 && lm.ef) ? lm.ef[o4[u]] : 0.0f;
         }
 #pragma unroll
         for (int u = 0; u < 4; u++) {
@@ -705,6 +706,32 @@ int lg_search_cap(int max_obs)
     return c;
 }
 
+namespace {
+
+// meta[i].y = meta[i].x * ef[lidx[i]] for the entries of the last search
+// (the first *cursor of the pool).
+__global__ void k_list_efactor(const int32_t *__restrict__ lidx, float2 *__restrict__ meta,
+                               const float *__restrict__ ef, const unsigned long long *__restrict__ cursor,
+                               int64_t cap)
+{
+    const int64_t n = min((int64_t)*cursor, cap);
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        float2 m = meta[i];
+        m.y = m.x * ef[lidx[i]];
+        meta[i] = m;
+    }
+}
+
+}  // namespace
+
+cudaError_t lg_launch_list_efactor(letkf_ctx *ctx)
+{
+    lg_count_launch();
+    k_list_efactor<<<152 * 8, 256, 0, ctx->stream>>>(ctx->d_lidx.p, ctx->d_lmeta.p, ctx->d_oef.p,
+                                                     ctx->d_counters.p + LG_CNT_CURSOR, ctx->list_cap);
+    return cudaGetLastError();
+}
+
 cudaError_t lg_launch_search(letkf_ctx *ctx, const LgGrid &g, int64_t nobs)
 {
     const LgParams prm = lg_params(ctx);
@@ -726,7 +753,7 @@ cudaError_t lg_launch_search(letkf_ctx *ctx, const LgGrid &g, int64_t nobs)
         if (e != cudaSuccess) return e;
         lg_count_launch();
         k_search_bitmap<<<(unsigned)(blocks > 0 ? blocks : 1), kThreads, bitmap_bytes, ctx->stream>>>(
-            g, prm, lg_search_geo(ctx), bk, geo, LgListMeta{ctx->d_oef.p, ctx->d_lmeta.p, ctx->d_lneed.p}, nobs, ctx->d_lidx.p,
+            g, prm, lg_search_geo(ctx), bk, geo, LgListMeta{ctx->lists_need_ef ? nullptr : ctx->d_oef.p, ctx->d_lmeta.p, ctx->d_lneed.p}, nobs, ctx->d_lidx.p,
             ctx->d_lrloc.p, ctx->list_cap, ctx->d_loff.p, ctx->d_lcnt.p, ctx->d_counters.p, ctx->d_status.p,
             ctx->win1);
         return cudaGetLastError();
@@ -737,7 +764,7 @@ cudaError_t lg_launch_search(letkf_ctx *ctx, const LgGrid &g, int64_t nobs)
     if (e != cudaSuccess) return e;
     lg_count_launch();
     k_search<<<(unsigned)(blocks > 0 ? blocks : 1), kThreads, smem, ctx->stream>>>(
-        g, prm, lg_search_geo(ctx), bk, geo, LgListMeta{ctx->d_oef.p, ctx->d_lmeta.p, ctx->d_lneed.p}, nobs, cap, ctx->d_lidx.p, ctx->d_lrloc.p, ctx->list_cap, ctx->d_loff.p,
+        g, prm, lg_search_geo(ctx), bk, geo, LgListMeta{ctx->lists_need_ef ? nullptr : ctx->d_oef.p, ctx->d_lmeta.p, ctx->d_lneed.p}, nobs, cap, ctx->d_lidx.p, ctx->d_lrloc.p, ctx->list_cap, ctx->d_loff.p,
         ctx->d_lcnt.p, ctx->d_counters.p, ctx->d_status.p, ctx->win1);
     return cudaGetLastError();
 }
@@ -754,7 +781,7 @@ cudaError_t lg_launch_search_dec(letkf_ctx *ctx, const LgGrid &g, const double *
     const int64_t blocks = nwin < (1 << 30) ? nwin : (1 << 30);
     lg_count_launch();
     k_search_dec<<<(unsigned)(blocks > 0 ? blocks : 1), kThreads, smem, ctx->stream>>>(
-        g, prm, lg_search_geo(ctx), geo, LgListMeta{ctx->d_oef.p, ctx->d_lmeta.p, ctx->d_lneed.p}, olat, ctx->dec_ny, ctx->dec_nchunk, ctx->d_dec_row_blk.p, ctx->d_dec_col_blk.p,
+        g, prm, lg_search_geo(ctx), geo, LgListMeta{ctx->lists_need_ef ? nullptr : ctx->d_oef.p, ctx->d_lmeta.p, ctx->d_lneed.p}, olat, ctx->dec_ny, ctx->dec_nchunk, ctx->d_dec_row_blk.p, ctx->d_dec_col_blk.p,
         ctx->d_dec_slot_off.p, ctx->d_dec_slot_blk.p, ctx->d_dec_pos.p, ctx->d_dec_obs.p, ctx->d_lidx.p,
         ctx->d_lrloc.p, ctx->list_cap, ctx->d_loff.p, ctx->d_lcnt.p, ctx->d_counters.p, ctx->d_status.p,
         ctx->win1);

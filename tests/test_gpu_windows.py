@@ -142,3 +142,28 @@ def test_cube_range_with_cubes_of_several_columns(letkf):
     cols = slice(2 * 2 * w.nlat, 5 * 2 * w.nlat)   # lon strips 2..4 of two columns each
     assert np.array_equal(xa[cols], xa0[cols]) and np.array_equal(axa[cols], axa0[cols])
     assert np.isnan(xa[:cols.start]).all() and np.isnan(xa[cols.stop:]).all()
+
+
+def test_host_run_in_blocks_matches_the_device_run(letkf):
+    """A run with host buffers analyses the k = 64 mixed core in two blocks of
+    cubes and copies the first block out while the second runs; the blocks end
+    on multiples of the work-queue chunk and of the eigensolve run, so the
+    analysis is bitwise the one of a run on device buffers (one block)."""
+    torch = pytest.importorskip("torch")
+    w = pkg("synthetic").small_case(nlat=90, nlon=180, nz=3, k=64, nobs=8000, loc_dist_km=600.0, seed=71)
+    ctx = letkf.LetkfGPU.from_workload(w, precision=letkf.LETKF_PREC_MIXED)
+    assert ctx.ncubes >= 2 * 4096 * 5 // 3          # two blocks of a host run
+    xa_h, axa_h = ctx.run(w.xb, w.axb, w.obs)
+    dev = torch.device("cuda", 0)
+    xb, axb = torch.from_numpy(w.xb).to(dev), torch.from_numpy(w.axb).to(dev)
+    obs = letkf.ObsArrays({k: torch.from_numpy(np.ascontiguousarray(w.obs[k])).to(dev)
+                           for k in ("lat", "lon", "ph", "lev", "var", "yo", "rinv")}, device=True)
+    xa, axa = torch.empty_like(xb), torch.empty_like(axb)
+    ctx.run_device(xb, axb, obs, xa, axa)
+    torch.cuda.synchronize()
+    assert np.array_equal(xa.cpu().numpy(), xa_h)
+    assert np.array_equal(axa.cpu().numpy(), axa_h)
+    # and again with host buffers (the copy streams are reused)
+    xa2, axa2 = ctx.run(w.xb, w.axb, w.obs)
+    assert np.array_equal(xa2, xa_h) and np.array_equal(axa2, axa_h)
+    ctx.close()
