@@ -1130,20 +1130,24 @@ cudaError_t launch_mixed(letkf_ctx *ctx, const LgGrid &g, const double *xb, cons
         const int R = 8;
         const size_t ew = (size_t)K * (K + 4) * sizeof(float) * (kTE / 32);
         cudaError_t e = cudaFuncSetAttribute(k_eig_warp<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ew);
-        // blocks end at multiples of `sub` in cube numbering (so the runs and
-        // chunks, and the results, do not depend on the blocking); when the
-        // analysis goes back to host memory, two blocks, the first (3/5 of the
-        // cubes) copied out while the second runs: the copy of 3/5 of the
-        // state takes about as long as the analysis of 2/5 (smaller blocks
-        // leave the eigensolve's warps short of runs)
-        int64_t sub = kStagedCubes;
+        // blocks end at multiples of `step` in cube numbering (so the runs and
+        // chunks, and the results, do not depend on the blocking), at most
+        // kStagedCubes each; when the analysis goes back to host memory, three
+        // blocks of 1/2, 3/10 and 1/5 of the cubes, each copied out while the
+        // next ones run (copying a block takes about 0.64 of its analysis
+        // time; smaller blocks leave the eigensolve's warps short of runs)
+        const int64_t step = max((int64_t)4096, (int64_t)lg_run_chunk(ctx));
+        auto align_up = [&](int64_t c) { return min(w1, (c + step - 1) / step * step); };
+        int64_t cut[2] = {w1, w1};
         if (ctx->sink_xa) {
-            const int64_t step = max((int64_t)4096, (int64_t)lg_run_chunk(ctx));
-            sub = min(kStagedCubes, max(step, ((w1 - w0) * 3 / 5 + step - 1) / step * step));
+            cut[0] = align_up(w0 + (w1 - w0) / 2);
+            cut[1] = align_up(w0 + (w1 - w0) * 4 / 5);
         }
         int64_t b1 = w0;
         for (int64_t b0 = w0; b0 < w1 && e == cudaSuccess; b0 = b1) {
-            b1 = min(w1, (b0 / sub + 1) * sub);
+            b1 = min(w1, (b0 / kStagedCubes + 1) * kStagedCubes);
+            for (int i = 0; i < 2; i++)
+                if (cut[i] > b0 && cut[i] < b1) b1 = cut[i];
             const int64_t nb = b1 - b0;
             ctx->win0 = b0;
             ctx->win1 = b1;
