@@ -272,9 +272,11 @@ def run_reference(args, rank, world):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": 1e3 * t, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"config{args.config} ({w.name}): {w.nlon}x{w.nlat}x{w.nz}, k={w.k}, "
-                               f"{w.obs['lat'].size} obs, c={w.loc_dist_km:g} km, rho={w.inflation:g} "
-                               f"(sample of {ns} columns per step)"},
+        "config": {"workload": (workload_label(args.config, w) if args.config in (0, 1, 2) else
+                                f"config{args.config} ({w.name}): {w.nlon}x{w.nlat}x{w.nz}, k={w.k}, "
+                                f"{w.obs['lat'].size} obs, c={w.loc_dist_km:g} km, rho={w.inflation:g}"),
+                   "columns": nc, "sample_columns_per_step": ns,
+                   "form": "the oracle (C restatement of the reference's CPU LETKF), FP64"},
         "cpu_baseline": {"value": value, "unit": "columns/s", "cores": O.num_threads(),
                          "kind": "port",
                          "sample": f"{ns} of {nc} columns per step; H over all obs pro rata; "
