@@ -167,3 +167,36 @@ def test_host_run_in_blocks_matches_the_device_run(letkf):
     xa2, axa2 = ctx.run(w.xb, w.axb, w.obs)
     assert np.array_equal(xa2, xa_h) and np.array_equal(axa2, axa_h)
     ctx.close()
+
+
+@pytest.mark.parametrize("k,prec,decomp,windows", [(64, "MIXED", (0, 0), False), (64, "MIXED", (0, 0), True),
+                                                   (32, "MIXED", (2, 3), True), (96, "MIXED", (0, 0), False),
+                                                   (16, "FP64", (0, 0), True)])
+def test_host_run_equals_device_run(letkf, k, prec, decomp, windows):
+    """With host buffers the search runs while the state copies in (H's
+    member pass after it; the mixed form completes its list entries' second
+    factor then), and the analysis is copied out in blocks: bitwise the run on
+    device buffers, also in cube windows and with the decomposed sets."""
+    torch = pytest.importorskip("torch")
+    w = _case(k, seed=90 + k)
+    precision = getattr(letkf, f"LETKF_PREC_{prec}")
+    ctx = letkf.LetkfGPU.from_workload(w, precision=precision, decomp=decomp)
+    if windows:
+        xa0, axa0 = ctx.run(w.xb, w.axb, w.obs)
+        st0 = ctx.stats()
+        ctx.set_list_limit(max(st0["sum_p"] // 5, st0["max_p"]))
+    xa_h, axa_h = ctx.run(w.xb, w.axb, w.obs)
+    if windows:
+        assert ctx.stats()["n_windows"] >= 3
+    dev = torch.device("cuda", 0)
+    xb, axb = torch.from_numpy(w.xb).to(dev), torch.from_numpy(w.axb).to(dev)
+    obs = letkf.ObsArrays({key: torch.from_numpy(np.ascontiguousarray(w.obs[key])).to(dev)
+                           for key in ("lat", "lon", "ph", "lev", "var", "yo", "rinv")}, device=True)
+    xa, axa = torch.empty_like(xb), torch.empty_like(axb)
+    ctx.run_device(xb, axb, obs, xa, axa)
+    torch.cuda.synchronize()
+    assert np.array_equal(xa.cpu().numpy(), xa_h)
+    assert np.array_equal(axa.cpu().numpy(), axa_h)
+    if windows:
+        assert np.array_equal(xa_h, xa0) and np.array_equal(axa_h, axa0)
+    ctx.close()
