@@ -451,6 +451,17 @@ __device__ int lg_jacobi32h(float *W, int *s_rot, float tol, int max_sweeps, flo
     return sweep;
 }
 
+// Stop level of the early exit of the FP32 Jacobis (lg_jacobi32b2 and
+// lg_jacobi32w): a sweep whose rotations all had |cos| below it ends the solve
+// (Jacobi converges quadratically, so the next sweep would find every pair
+// below tol).  On the 1 deg, k = 64 workload
+// 3e-4 gives the same analysis as sweeping until no pair is above tol, with
+// 5.3 instead of 6.1 sweeps per cube; 3e-3 raised the spread error to 2.6e-4.
+// 0 turns it off.
+#ifndef LG_JACOBI32W_QSTOP
+#define LG_JACOBI32W_QSTOP 3e-4f
+#endif
+
 // FP32 one-sided Jacobi with the hierarchical ordering over blocks of two
 // columns (K = 64 or 128, 256 threads): the K/4 slots each hold a fixed block
 // (F1, F2) and a moving block (M1, M2), G = 1024/K lanes per slot and K/G rows
@@ -516,8 +527,10 @@ __device__ int lg_jacobi32b2(float *W, float *extra, int *s_rot, float tol, int 
             b += __shfl_xor_sync(0xffffffffu, b, o);
         }
     };
-    bool rotated_any = false;
+    bool rotated_any = false, big_any = false;
     auto apply = [&](float *X, float *Y, float &nx, float &ny, float gam) {
+        if (LG_JACOBI32W_QSTOP > 0.0f && gam * gam > LG_JACOBI32W_QSTOP * LG_JACOBI32W_QSTOP * (nx * ny))
+            big_any = true;
         if (gam * gam > tol2 * (nx * ny)) {
             float c, s, tt;
             lg_rotation(nx, ny, gam, c, s, tt);
@@ -544,6 +557,7 @@ __device__ int lg_jacobi32b2(float *W, float *extra, int *s_rot, float tol, int 
     for (sweep = 1; sweep <= max_sweeps; sweep++) {
         if (tid == 0) *s_rot = 0;
         rotated_any = false;
+        big_any = false;
         for (int B = NB; B >= 2; B >>= 1) {            // B blocks per group
             const int half = B / 2, u = slot / half, i = slot % half;
             const int fb = u * B + i;
@@ -605,24 +619,18 @@ __device__ int lg_jacobi32b2(float *W, float *extra, int *s_rot, float tol, int 
             st(W + (2 * mbk) * LD, M1);
             st(W + (2 * mbk + 1) * LD, M2);
         }
-        if (rotated_any && lane == 0) *s_rot = 1;
+        if (lane == 0 && (rotated_any || big_any)) atomicOr(s_rot, (rotated_any ? 1 : 0) | (big_any ? 2 : 0));
         __syncthreads();
         const int rotated = *s_rot;
         __syncthreads();
-        if (!rotated) break;
+        if (!(rotated & 1)) break;
+        // the early exit of lg_jacobi32w: a sweep of rotations all below the
+        // stop level ends the solve
+        if (LG_JACOBI32W_QSTOP > 0.0f && !(rotated & 2)) break;
     }
     return sweep;
 }
 
-// Stop level of the warp Jacobi's early exit: a sweep whose rotations all had
-// |cos| below it ends the solve (Jacobi converges quadratically, so the next
-// sweep would find every pair below tol).  On the 1 deg, k = 64 workload
-// 3e-4 gives the same analysis as sweeping until no pair is above tol, with
-// 5.3 instead of 6.1 sweeps per cube; 3e-3 raised the spread error to 2.6e-4.
-// 0 turns it off.
-#ifndef LG_JACOBI32W_QSTOP
-#define LG_JACOBI32W_QSTOP 3e-4f
-#endif
 
 // FP32 one-sided Jacobi of one K x K problem by one warp (K = 64): lane l
 // owns a column pair in registers, so the inner products need no reduction
