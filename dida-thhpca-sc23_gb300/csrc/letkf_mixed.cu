@@ -502,7 +502,8 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
         if constexpr (K == 64)
             sw = lg_jacobi32b2<K, C::LDW, K>(W32, W32 + 2 * (K / 4) * 2 * K, &s_rot, LG_MIXED_JACOBI_TOL, 24);
         else if constexpr ((K & (K - 1)) == 0) sw = lg_jacobi32h<K, C::G, C::LDW>(W32, &s_rot, LG_MIXED_JACOBI_TOL, 24);
-        else sw = lg_jacobi32<K, C::G, C::LDW>(W32, nrm32, &s_rot, LG_MIXED_JACOBI_TOL, LG_MIXED_JACOBI_TOL, 24);
+        else sw = lg_jacobi32<K, C::G, C::LDW>(W32, nrm32, &s_rot, LG_MIXED_JACOBI_TOL,
+                                          LG_JACOBI32W_QSTOP > 0.0f ? LG_JACOBI32W_QSTOP : LG_MIXED_JACOBI_TOL, 24);
         if (tid == 0) {
             atomicMax(&counters[LG_CNT_MAXSWEEP], (unsigned long long)sw);
             atomicAdd(&counters[LG_CNT_SUMSWEEP], (unsigned long long)sw);

@@ -355,7 +355,8 @@ k_core_mixed_wide(LgGrid g, LgParams prm, const float *__restrict__ ys32, const 
         int sw;
         if constexpr (K == 128)
             sw = lg_jacobi32b2<K, C::LDW, C::LDW>(W32, W32 + K * C::LDW, &s_rot, LG_MIXED_JACOBI_TOL, 24);
-        else sw = lg_jacobi32<K, C::G, C::LDW>(W32, nrm32, &s_rot, LG_MIXED_JACOBI_TOL, LG_MIXED_JACOBI_TOL, 24);
+        else sw = lg_jacobi32<K, C::G, C::LDW>(W32, nrm32, &s_rot, LG_MIXED_JACOBI_TOL,
+                                          LG_JACOBI32W_QSTOP > 0.0f ? LG_JACOBI32W_QSTOP : LG_MIXED_JACOBI_TOL, 24);
         if (tid == 0) {
             atomicMax(&counters[LG_CNT_MAXSWEEP], (unsigned long long)sw);
             atomicAdd(&counters[LG_CNT_SUMSWEEP], (unsigned long long)sw);
