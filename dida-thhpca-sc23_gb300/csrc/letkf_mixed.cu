@@ -17,14 +17,21 @@
 //   2. A' = A + (k-1)/rho I in FP64.
 //   3. FP32 one-sided Jacobi of A' (warm-started from the neighbouring
 //      cube's eigenvectors) gives the eigenpairs: lambda_j = |w_j|, x_j = w_j/lambda_j.
-//   4. wbar = X diag(1/lambda) X^T g in FP64, then one step of iterative
+//   4. wbar = X diag(1/lambda) X^T g in FP32, then one step of iterative
 //      refinement: wbar += X diag(1/lambda) X^T (g - A' wbar) with the
-//      residual against the FP64 A'.  A' has condition numbers below ~1e3 at
-//      these sizes, so one step takes wbar from ~1e-7 to ~1e-13 relative.
+//      residual in FP64 against the FP64 A'.  A' has condition numbers below
+//      ~1e3 at these sizes, so one step takes wbar from ~1e-7 to ~1e-13
+//      relative; wbar is accumulated in FP64.
 //   5. T = X diag(sqrt((k-1)/lambda)) X^T in FP32: it only feeds the BF16
 //      hi/lo update, and FP32 eigenpairs give it to ~1e-7 relative.
 //   6. xa = xb^T T on tcgen05 (hi/lo BF16 of both operands, three products in
 //      one accumulator); the mean increment xb^T wbar is FP64.
+//
+// k = 32 and 48 run all steps in one persistent launch (k_core_mixed<k, 0>).
+// k = 64 runs them in three launches per block of cubes: the A and g build
+// (k_core_mixed<64, 1>), the eigensolves one warp each (k_eig_warp<64>, runs
+// of 8 cubes warm-started inside a run, taken from a queue) and steps 4-6
+// (k_core_mixed<64, 2>), with A, g, X and lambda in HBM between them.
 #include <cuda_bf16.h>
 
 #include "letkf_internal.cuh"

@@ -3,9 +3,12 @@
 //
 // Reference: gen_obs_struct (code/x86/TradDA/DA/LETKF/src/letkf_obs.F90:16-182)
 // with find_obs_grid (:187-243), ps2ph_3d_interp and obs_interpolation_3d_2
-// (obs_make.F90:233-381).  One warp per observation; lanes stride over the
-// members, so every state read is a contiguous run of the member-fastest
-// state (coalesced), and the ensemble mean is a warp-shuffle reduction.
+// (obs_make.F90:233-381).  One warp per 32 observations: the scalar terms of
+// an observation on one lane, then for each observation the lanes stride over
+// the members, so every state read is a contiguous run of the member-fastest
+// state (coalesced), and the ensemble mean is a warp-shuffle reduction.  A
+// run whose state is still being copied in runs the geometry pass (mode 1)
+// first and the members pass (mode 2) after the copy.
 #include "letkf_internal.cuh"
 
 namespace {
