@@ -796,6 +796,7 @@ int letkf_gpu_run(letkf_ctx *ctx, const double *xb, const double *axb, const let
         // the copy is joined even when the analysis stopped early
         for (int i = 0; i < letkf_ctx::kCopyStreams; i++) LG_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->cev[i], 0));
         ctx->members_pending = false;
+        ctx->lists_need_ef = false;
     }
     if (rc) return rc;
     if (host && ctx->sink_cols > 0) {

@@ -145,14 +145,14 @@ def test_cube_range_with_cubes_of_several_columns(letkf):
 
 
 def test_host_run_in_blocks_matches_the_device_run(letkf):
-    """A run with host buffers analyses the k = 64 mixed core in two blocks of
-    cubes and copies the first block out while the second runs; the blocks end
-    on multiples of the work-queue chunk and of the eigensolve run, so the
-    analysis is bitwise the one of a run on device buffers (one block)."""
+    """A run with host buffers analyses the k = 64 mixed core in blocks of
+    cubes (up to three) and copies each block out while the next runs; the
+    blocks end on multiples of the work-queue chunk and of the eigensolve run,
+    so the analysis is bitwise the one of a run on device buffers (one block)."""
     torch = pytest.importorskip("torch")
     w = pkg("synthetic").small_case(nlat=90, nlon=180, nz=3, k=64, nobs=8000, loc_dist_km=600.0, seed=71)
     ctx = letkf.LetkfGPU.from_workload(w, precision=letkf.LETKF_PREC_MIXED)
-    assert ctx.ncubes >= 2 * 4096 * 5 // 3          # two blocks of a host run
+    assert ctx.ncubes > 2 * 4096                     # at least two blocks of a host run
     xa_h, axa_h = ctx.run(w.xb, w.axb, w.obs)
     dev = torch.device("cuda", 0)
     xb, axb = torch.from_numpy(w.xb).to(dev), torch.from_numpy(w.axb).to(dev)
