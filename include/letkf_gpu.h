@@ -148,8 +148,11 @@ int letkf_gpu_set_stream(letkf_ctx *ctx, void *stream);
  * mean, as run_da_parallel hands them over (module_da_parallel.F90:184-211);
  * xa/axa receive the analysis perturbations and mean.  With
  * LETKF_HOST_PTRS the call copies in and out and returns when xa/axa are
- * written; with LETKF_DEVICE_PTRS it returns with the work queued on the
- * stream (call letkf_gpu_synchronize before reading the outputs).           */
+ * written (with page-locked buffers the state copies overlap the search and
+ * the analysis: the copy-in runs beside H's geometry pass and the search, and
+ * finished blocks of columns are copied out while later ones are analysed);
+ * with LETKF_DEVICE_PTRS it returns with the work queued on the stream (call
+ * letkf_gpu_synchronize before reading the outputs).                        */
 int letkf_gpu_run(letkf_ctx *ctx, const double *xb, const double *axb, const letkf_obs *obs,
                   double *xa, double *axa, int flags);
 
