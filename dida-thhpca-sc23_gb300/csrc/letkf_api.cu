@@ -793,19 +793,18 @@ int letkf_gpu_run(letkf_ctx *ctx, const double *xb, const double *axb, const let
     ctx->sink_xa = nullptr;
     ctx->sink_axa = nullptr;
     if (host) {
-        // the copy is joined even when the analysis stopped early
-        for (int i = 0; i < letkf_ctx::kCopyStreams; i++) LG_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->cev[i], 0));
+        // every copy of the copy streams (the state in, finished blocks out)
+        // before the main stream goes on, also when the analysis stopped
+        // early; then nothing is left writing into the caller's buffers
         ctx->members_pending = false;
         ctx->lists_need_ef = false;
-    }
-    if (rc) return rc;
-    if (host && ctx->sink_cols > 0) {
-        // the copies on the copy streams, before the status read
         for (int i = 0; i < letkf_ctx::kCopyStreams; i++) {
             LG_CUDA(cudaEventRecord(ctx->cev[i], ctx->cstream[i]));
             LG_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->cev[i], 0));
         }
+        if (rc) cudaStreamSynchronize(ctx->stream);
     }
+    if (rc) return rc;
     if (host && ctx->sink_cols != ctx->range1 - ctx->range0) {
         // the columns of the analysed cubes: with cube_n 1 the cubes
         // themselves, else whole longitude strips of them
