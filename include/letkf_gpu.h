@@ -118,7 +118,11 @@ typedef struct letkf_stats {
     int64_t n_not_converged;   /* eigensolves that hit the sweep limit              */
     int32_t max_sweeps;        /* most Jacobi sweeps any cube needed                */
     int32_t precision;
-    double ms_h2d, ms_obs, ms_search, ms_core, ms_d2h, ms_total;  /* device-event times */
+    /* Device-event times between the stages of the last run.  In a run with
+     * host buffers the state copies overlap the stages: ms_h2d then holds the
+     * observations' copy only, ms_core includes waiting for the state copy,
+     * and ms_d2h is the copy left after the analysis; ms_total is the whole. */
+    double ms_h2d, ms_obs, ms_search, ms_core, ms_d2h, ms_total;
     int64_t sum_sweeps;        /* Jacobi sweeps summed over all cubes               */
     int64_t n_ill_conditioned; /* mixed form: cubes whose A' has lambda_max/lambda_min
                                   above 1e4, where the FP32 eigenpairs lose digits    */
