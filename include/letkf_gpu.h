@@ -120,7 +120,8 @@ typedef struct letkf_stats {
     int32_t precision;
     /* Device-event times between the stages of the last run.  In a run with
      * host buffers the state copies overlap the stages: ms_h2d then holds the
-     * observations' copy only, ms_core includes waiting for the state copy,
+     * mean's and the observations' copies only, ms_core includes waiting for
+     * the perturbations' copy,
      * and ms_d2h is the copy left after the analysis; ms_total is the whole. */
     double ms_h2d, ms_obs, ms_search, ms_core, ms_d2h, ms_total;
     int64_t sum_sweeps;        /* Jacobi sweeps summed over all cubes               */
