@@ -29,11 +29,11 @@ def sources():
     return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
 
 
-def _compile(src: str, extra: list[str], out: str = OUT) -> str:
+def _compile(src: str, extra: list[str], out: str = OUT, force: bool = False) -> str:
     obj = os.path.join(out, os.path.basename(src)[:-3] + ".o")
     deps = [src] + [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".cuh", ".h"))]
     deps.append(os.path.join(REPO, "include", "letkf_gpu.h"))
-    if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(d) for d in deps):
+    if not force and os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(d) for d in deps):
         return obj
     cmd = [nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
            "-I", os.path.join(REPO, "include"), "-I", CSRC, "-c", src, "-o", obj, *extra]
@@ -51,14 +51,21 @@ def build(verbose: bool = False, extra: list[str] | None = None, out_dir: str | 
     os.makedirs(out, exist_ok=True)
     extra = list(extra or [])
     srcs = sources()
+    # objects built with other flags are rebuilt (the flags of the last build
+    # are kept beside the library)
+    stamp = os.path.join(out, "build_flags.txt")
+    flags = " ".join(extra)
+    force = not os.path.exists(stamp) or open(stamp).read() != flags
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
-        objs = list(ex.map(lambda s: _compile(s, extra, out), srcs))
-    if not os.path.exists(lib) or os.path.getmtime(lib) < max(os.path.getmtime(o) for o in objs):
+        objs = list(ex.map(lambda s: _compile(s, extra, out, force), srcs))
+    if force or not os.path.exists(lib) or os.path.getmtime(lib) < max(os.path.getmtime(o) for o in objs):
         cmd = [nvcc(), *ARCH, "-shared", "-o", lib, *objs, "-cudart", "shared",
                "-Xlinker", f"-rpath,{os.path.join(CUDA_HOME, 'lib64')}"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    with open(stamp, "w") as f:
+        f.write(flags)
     if verbose:
         print(lib)
     return lib
