@@ -56,6 +56,10 @@ def build(verbose: bool = False, extra: list[str] | None = None, out_dir: str | 
     stamp = os.path.join(out, "build_flags.txt")
     flags = " ".join(extra)
     force = not os.path.exists(stamp) or open(stamp).read() != flags
+    if force and os.path.exists(stamp):
+        # a build with new flags that fails part way leaves no stamp, so the
+        # next build recompiles every object instead of reusing some by mtime
+        os.remove(stamp)
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         objs = list(ex.map(lambda s: _compile(s, extra, out, force), srcs))
     if force or not os.path.exists(lib) or os.path.getmtime(lib) < max(os.path.getmtime(o) for o in objs):

@@ -440,6 +440,22 @@ void fill_stats(letkf_ctx *ctx, const unsigned long long *cnt)
 
 void lg_count_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
+void lg_stage_mark(letkf_ctx *ctx, int s, bool end)
+{
+    if (s < 0 || s >= letkf_ctx::kStages) return;
+    const int i = ctx->stg_n[s];
+    if (i >= letkf_ctx::kStageMarks) return;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(ctx->stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) return;
+    cudaEvent_t &e = ctx->stg_ev[s][end ? 1 : 0][i];
+    if (!e && cudaEventCreate(&e) != cudaSuccess) {
+        e = nullptr;
+        return;
+    }
+    if (cudaEventRecord(e, ctx->stream) != cudaSuccess) return;
+    if (end) ctx->stg_n[s] = i + 1;
+}
+
 LgGrid lg_grid(letkf_ctx *ctx)
 {
     LgGrid g;
@@ -481,6 +497,9 @@ LgParams lg_params(letkf_ctx *ctx)
     p.cube_step = q.cube_n - q.overlap;
     p.cube0 = ctx->win0;
     p.count_only = ctx->count_pass ? 1 : 0;
+    p.spin_limit = ctx->wait_limit < 0 ? LG_MBAR_SPIN_LIMIT
+                   : (uint32_t)(ctx->wait_limit < (int64_t)LG_MBAR_SPIN_LIMIT ? ctx->wait_limit
+                                                                              : (int64_t)LG_MBAR_SPIN_LIMIT);
     return p;
 }
 
@@ -611,6 +630,13 @@ int letkf_gpu_set_stream(letkf_ctx *ctx, void *stream)
 {
     if (!ctx) return LETKF_ERR_INVALID;
     ctx->stream = stream ? (cudaStream_t)stream : ctx->own_stream;
+    return LETKF_OK;
+}
+
+int letkf_gpu_set_wait_limit(letkf_ctx *ctx, int64_t polls)
+{
+    if (!ctx) return LETKF_ERR_INVALID;
+    ctx->wait_limit = polls < 0 ? -1 : polls;
     return LETKF_OK;
 }
 

@@ -95,6 +95,9 @@ k_core_fp64(LgGrid g, LgParams prm, RowSrc src, const int64_t *__restrict__ loff
         lg_decode_block(bok[m] ? b : 0, bi[m], bj[m]);
     }
 
+    // batched core: offsets flagged as bad by the counts pass before this
+    // launch (same stream) stop every CTA before it reads a row
+    if (src.batch && status && (*reinterpret_cast<volatile const unsigned *>(status) & LG_ST_BAD_OBS)) return;
     const bool vertical = !src.batch && src.olnp != nullptr;
     const int nvb = vertical ? (g.nz + prm.cube_nz - 1) / prm.cube_nz : 1;
     for (int64_t cube = prm.cube0 + blockIdx.x; cube < ncubes; cube += gridDim.x) {

@@ -21,6 +21,9 @@
 #define LG_GC_C2 0.666666686534881591796875
 
 #define LG_THREADS 256          // threads of the per-cube kernels
+#ifndef LG_MBAR_SPIN_LIMIT
+#define LG_MBAR_SPIN_LIMIT (1u << 22)   // polls of a bounded tensor-core wait
+#endif
 #define LG_MAX_ENS 128          // largest ensemble the kernels are built for
 
 // Status bits written by kernels into ctx->d_status.
@@ -132,6 +135,7 @@ struct LgParams {
     int cube_step;        // grid points between cube starts (cube_n - overlap)
     int64_t cube0;        // first cube of the launch's window
     int count_only;       // search: only each cube's list length (LgListMeta::need)
+    uint32_t spin_limit;  // polls of each bounded mbarrier wait of the mixed cores
 };
 
 // Lat-lon bucket grid of the observations.
@@ -252,6 +256,8 @@ struct letkf_ctx {
     DevBuf<int> d_dec_cnt, d_dec_pos, d_dec_obs; // per (block, chunk) counts, offsets; obs of blocks
     // mixed core schedule (0: defaults) and its work queue
     int sched_chunk = 0, sched_p0 = 0;
+    // polls of each bounded tensor-core wait (letkf_gpu_set_wait_limit; < 0: the default)
+    int64_t wait_limit = -1;
     DevBuf<int> d_queue;
     // per-cube results
     DevBuf<double> d_trans, d_w;
@@ -266,6 +272,12 @@ struct letkf_ctx {
     bool have_run = false;
 
     cudaEvent_t ev[8] = {};
+    // device-event marks around each launch of the staged core's stages (A
+    // build, eigensolve, update; letkf_stats.ms_stage), at most kStageMarks
+    // launches per stage and run
+    static constexpr int kStages = 3, kStageMarks = 32;
+    cudaEvent_t stg_ev[kStages][2][kStageMarks] = {};
+    int stg_n[kStages] = {};
     letkf_stats stats{};
     std::string last_error;
 
@@ -298,6 +310,10 @@ struct letkf_ctx {
 // ---------------------------------------------------------------------------
 // Launch counting (every kernel launch of this library goes through it).
 void lg_count_launch();
+// Device-event mark before (end = false) or after a launch of stage s of the
+// staged core (0 A build, 1 eigensolve, 2 update); skipped while the stream
+// is being captured into a graph.
+void lg_stage_mark(letkf_ctx *ctx, int s, bool end);
 
 // Kernel launchers (letkf_prep.cu, letkf_search.cu, letkf_core.cu).
 // H: mode 0 everything; 1 the per-observation geometry, weights and bucket

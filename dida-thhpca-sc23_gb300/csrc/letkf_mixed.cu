@@ -151,14 +151,18 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
     bool pending[3] = {false, false, false};
     bool failed = false;
 
-    // Wait (thread 0 polls, bounded) for the last commit on barrier b.
-    auto wait_bar = [&](int b) -> bool {
+    // Wait (thread 0 polls, at most `limit` times) for the last commit on
+    // barrier b.  A wait that runs out leaves the commit pending: the drain
+    // before the TMEM is freed waits for it again.  Each barrier has at most one
+    // commit outstanding (a tile is waited for before it is refilled), so its
+    // phase parity names that commit.
+    auto wait_bar = [&](int b, uint32_t limit) -> bool {
         if (!pending[b]) return true;
-        if (tid == 0) s_ok = lg_mbar_wait(&mbar[b], (ncommit[b] - 1u) & 1u) ? 1 : 0;
+        if (tid == 0) s_ok = lg_mbar_wait(&mbar[b], (ncommit[b] - 1u) & 1u, limit) ? 1 : 0;
         __syncthreads();
         const int ok = s_ok;
         __syncthreads();
-        pending[b] = false;
+        if (ok) pending[b] = false;
         return ok != 0;
     };
 
@@ -300,14 +304,15 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
             const float *sq = msq + (ch % 3) * CH, *ev = me + (ch % 3) * CH;
             cp_async_wait<1>();              // this chunk's rows (the next chunk's may be in flight)
             // tile b is free once the products of chunk ch - 2 are done
-            if (tid == 0 && pending[b] && !lg_mbar_wait(&mbar[b], (ncommit[b] - 1u) & 1u)) s_fail = 1;
-            pending[b] = false;
+            if (tid == 0 && pending[b] && !lg_mbar_wait(&mbar[b], (ncommit[b] - 1u) & 1u, prm.spin_limit))
+                s_fail = 1;
             __syncthreads();
             LG_PHASE(7);
             if (s_fail) {
-                failed = true;
+                failed = true;         // pending[b] stays set for the drain
                 break;
             }
+            pending[b] = false;
             // slot (ch + 2) % 3 last served chunk ch - 1, converted before the barrier
             if (tid < CH) {
                 put_meta(ch + 2, pf_g, pf_m);
@@ -388,7 +393,7 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
                 if (n2 > 0) asm volatile("prefetch.global.L2 [%0];" ::"l"(a));
             }
         }
-        if (!wait_bar(0) || !wait_bar(1)) {
+        if (!wait_bar(0, prm.spin_limit) || !wait_bar(1, prm.spin_limit)) {
             failed = true;
             break;
         }
@@ -767,7 +772,7 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
                     }
                     ncommit[2]++;
                     pending[2] = true;
-                    if (!wait_bar(2)) {
+                    if (!wait_bar(2, prm.spin_limit)) {
                         failed = true;
                         break;
                     }
@@ -821,8 +826,12 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
 #endif
     if (failed && tid == 0) atomicOr(status, LG_ST_TIMEOUT);
     cp_async_wait<0>();
-    // let any MMA still in flight finish before the TMEM is freed
-    for (int b = 0; b < 3; b++) wait_bar(b);
+    // let every committed MMA finish before the TMEM is freed: a wait that ran
+    // out left its commit pending, and the drain waits for it at the normal
+    // limit whatever limit the run's waits had
+    bool drained = true;
+    for (int b = 0; b < 3; b++) drained = wait_bar(b, LG_MBAR_SPIN_LIMIT) && drained;
+    if (!drained && tid == 0) atomicOr(status, LG_ST_TIMEOUT);
     lg_tc_fence_before();
     __syncthreads();
     lg_tc_fence_after();

@@ -123,13 +123,16 @@ k_core_mixed_wide(LgGrid g, LgParams prm, const float *__restrict__ ys32, const 
     bool pending[3] = {false, false, false};
     bool failed = false;
 
-    auto wait_bar = [&](int b) -> bool {
+    // Bounded wait for the last commit on barrier b; one that runs out leaves
+    // the commit pending for the drain (at most one commit per barrier is
+    // outstanding, so the phase parity names it).
+    auto wait_bar = [&](int b, uint32_t limit) -> bool {
         if (!pending[b]) return true;
-        if (tid == 0) s_ok = lg_mbar_wait(&mbar[b], (ncommit[b] - 1u) & 1u) ? 1 : 0;
+        if (tid == 0) s_ok = lg_mbar_wait(&mbar[b], (ncommit[b] - 1u) & 1u, limit) ? 1 : 0;
         __syncthreads();
         const int ok = s_ok;
         __syncthreads();
-        pending[b] = false;
+        if (ok) pending[b] = false;
         return ok != 0;
     };
 
@@ -216,7 +219,7 @@ k_core_mixed_wide(LgGrid g, LgParams prm, const float *__restrict__ ys32, const 
             cp_async_wait<1>();
             __syncthreads();
             unsigned char *tile = RA + b * C::TILE;
-            if (!wait_bar(b)) {
+            if (!wait_bar(b, prm.spin_limit)) {
                 failed = true;
                 break;
             }
@@ -268,7 +271,7 @@ k_core_mixed_wide(LgGrid g, LgParams prm, const float *__restrict__ ys32, const 
         }
         cp_async_wait<0>();
         if (failed) break;
-        if (!wait_bar(0) || !wait_bar(1)) {
+        if (!wait_bar(0, prm.spin_limit) || !wait_bar(1, prm.spin_limit)) {
             failed = true;
             break;
         }
@@ -588,7 +591,7 @@ k_core_mixed_wide(LgGrid g, LgParams prm, const float *__restrict__ ys32, const 
                     }
                     ncommit[2]++;
                     pending[2] = true;
-                    if (!wait_bar(2)) {
+                    if (!wait_bar(2, prm.spin_limit)) {
                         failed = true;
                         break;
                     }
@@ -645,7 +648,11 @@ k_core_mixed_wide(LgGrid g, LgParams prm, const float *__restrict__ ys32, const 
 #endif
     if (failed && tid == 0) atomicOr(status, LG_ST_TIMEOUT);
     cp_async_wait<0>();
-    for (int b = 0; b < 3; b++) wait_bar(b);
+    // every committed MMA finishes before the TMEM is freed (at the normal
+    // limit, whatever limit the run's waits had)
+    bool drained = true;
+    for (int b = 0; b < 3; b++) drained = wait_bar(b, LG_MBAR_SPIN_LIMIT) && drained;
+    if (!drained && tid == 0) atomicOr(status, LG_ST_TIMEOUT);
     lg_tc_fence_before();
     __syncthreads();
     lg_tc_fence_after();

@@ -50,14 +50,17 @@ int scratch_address(int dev, unsigned char **out)
 }
 
 // counts[b] = offsets[b+1] - offsets[b]; flags offsets that do not start at 0,
-// go backwards or give a problem more than 2^31-1 rows.
+// are negative, go backwards or give a problem more than 2^31-1 rows.  A
+// flagged problem gets count 0 (no row of it is read), and the core launched
+// after this kernel returns at once when anything was flagged.
 __global__ void k_noalloc_counts(int64_t nb, const int64_t *__restrict__ offsets,
                                  int32_t *__restrict__ counts, unsigned *__restrict__ status)
 {
     for (int64_t b = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; b < nb;
          b += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t c = offsets[b + 1] - offsets[b];
-        const bool bad = c < 0 || c > 0x7fffffffLL || (b == 0 && offsets[0] != 0);
+        const int64_t o0 = offsets[b], o1 = offsets[b + 1];
+        const int64_t c = o1 - o0;
+        const bool bad = o0 < 0 || o1 < 0 || c < 0 || c > 0x7fffffffLL || (b == 0 && o0 != 0);
         counts[b] = bad ? 0 : (int32_t)c;
         if (bad) atomicOr(status, LG_ST_BAD_OBS);
     }

@@ -14,7 +14,9 @@
 
 #include <stdint.h>
 
+#ifndef LG_MBAR_SPIN_LIMIT
 #define LG_MBAR_SPIN_LIMIT (1u << 22)
+#endif
 
 __device__ __forceinline__ uint32_t lg_smem_u32(const void *p)
 {
@@ -72,12 +74,13 @@ __device__ __forceinline__ void lg_mbar_init(uint64_t *mbar, uint32_t count)
     asm volatile("fence.mbarrier_init.release.cluster;");
 }
 
-// Wait for phase `parity` of the mbarrier, at most LG_MBAR_SPIN_LIMIT polls.
-// Returns false if the wait ran out.
-__device__ __forceinline__ bool lg_mbar_wait(uint64_t *mbar, uint32_t parity)
+// Wait for phase `parity` of the mbarrier, at most `limit` polls (the
+// kernels pass LG_MBAR_SPIN_LIMIT unless a context set another limit; 0 gives
+// up at once).  Returns false if the wait ran out.
+__device__ __forceinline__ bool lg_mbar_wait(uint64_t *mbar, uint32_t parity, uint32_t limit = LG_MBAR_SPIN_LIMIT)
 {
     const uint32_t addr = lg_smem_u32(mbar);
-    for (uint32_t i = 0; i < LG_MBAR_SPIN_LIMIT; i++) {
+    for (uint32_t i = 0; i < limit; i++) {
         uint32_t done;
         asm volatile(
             "{\n .reg .pred P;\n mbarrier.try_wait.parity.shared::cta.b64 P, [%1], %2;\n"

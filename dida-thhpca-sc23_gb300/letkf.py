@@ -46,7 +46,7 @@ EXPORTED = [
     "letkf_batch_create", "letkf_batch_launch", "letkf_batch_sync", "letkf_batch_launches",
     "letkf_batch_destroy", "letkf_gpu_set_list_limit", "letkf_gpu_set_cube_range", "letkf_gpu_run_members",
     "letkf_struct_atm2endnn", "letkf_struct_endnn2atm", "letkf_struct_atm2endnn_a", "letkf_struct_endnn2atm_a",
-    "letkf_gpu_obs_from_records", "letkf_gpu_obs_regular",
+    "letkf_gpu_obs_from_records", "letkf_gpu_obs_regular", "letkf_gpu_set_wait_limit",
     "letkf_init_gpu_", "letkf_set_obs_gpu_", "letkf_run_gpu_", "letkf_final_gpu_",
 ]
 
@@ -118,6 +118,7 @@ def load_library(path: str = LIB_PATH):
     L.letkf_gpu_create.argtypes = [C.POINTER(vp), C.POINTER(Grid), C.POINTER(Params), i32]
     L.letkf_gpu_set_stream.argtypes = [vp, vp]
     L.letkf_gpu_set_keep_trans.argtypes = [vp, i32]
+    L.letkf_gpu_set_wait_limit.argtypes = [vp, i64]
     L.letkf_gpu_run.argtypes = [vp, vp, vp, C.POINTER(Obs), vp, vp, i32]
     L.letkf_gpu_synchronize.argtypes = [vp]
     L.letkf_gpu_obs_operator.argtypes = [vp, vp, vp, C.POINTER(Obs), vp, vp]
@@ -346,6 +347,11 @@ class LetkfGPU:
         """Most local-list entries held at once (0: from free memory); runs
         whose lists exceed it go through consecutive cube windows."""
         self._check(self.L.letkf_gpu_set_list_limit(self.h, int(max_entries)), "set_list_limit")
+
+    def set_wait_limit(self, polls: int = -1):
+        """Most polls of each bounded tensor-core wait (< 0: the default; 0:
+        every wait gives up at once, which exercises the timeout path)."""
+        self._check(self.L.letkf_gpu_set_wait_limit(self.h, int(polls)), "set_wait_limit")
 
     def set_cube_range(self, first: int = 0, count: int = -1):
         """Analyse only cubes first .. first+count-1 (count < 0: all)."""

@@ -253,6 +253,14 @@ int letkf_gpu_set_list_limit(letkf_ctx *ctx, int64_t max_entries);
  * precision); windows never cut a chunk.                                     */
 int letkf_gpu_set_cube_range(letkf_ctx *ctx, int64_t first, int64_t count);
 
+/* Most polls of each bounded wait of the mixed cores on their own
+ * tensor-core work (polls < 0: the default, 2^22; 0: every wait gives up at
+ * once).  A wait that runs out makes the run return LETKF_ERR_TIMEOUT after
+ * the kernel has let its committed products finish and freed its tensor
+ * memory, so the context stays usable.  For tests of that path; no
+ * counterpart in the reference.                                             */
+int letkf_gpu_set_wait_limit(letkf_ctx *ctx, int64_t polls);
+
 /* Keep (1) or drop (0) every cube's trans and w of the following runs in
  * device memory (ncubes * ens * (ens+1) doubles) for letkf_gpu_last_trans. */
 int letkf_gpu_set_keep_trans(letkf_ctx *ctx, int keep);
@@ -296,7 +304,12 @@ int letkf_gpu_core_batch(letkf_ctx *ctx, int64_t nb, const int64_t *offsets,
  * fixed array inside the library that every GPU which loads the library holds
  * until the process exits, sized for at most LETKF_NOALLOC_MAX_PROBLEMS
  * problems; larger nb returns LETKF_ERR_INVALID.  The first call on a device
- * looks up that array's device address (make it before any stream capture).
+ * looks up that array's device address (make it before any stream capture);
+ * with CUDA's lazy module loading (the default) that first call also loads
+ * the library's kernels and the array onto the device, which takes device
+ * memory, so make it before a memory pool reserves the rest of the GPU.  The
+ * address is kept for the life of the process: do not use the call across a
+ * cudaDeviceReset of that device.
  * All calls share the one array, so calls that overlap on the GPU (different
  * streams or host threads at once) race; issue them one after another.  The
  * call waits for `stream` (a cudaStream_t, NULL = the default stream) before it

@@ -1,5 +1,8 @@
-"""Mixed-precision form (BF16 hi/lo tensor-core products, FP64 eigensolve
-refinement and mean increment) against the FP64 oracle and the FP64 GPU form.
+"""Mixed-precision form against the FP64 oracle and the FP64 GPU form.
+
+The form (LETKF_PREC_MIXED): BF16 hi/lo tensor-core products for A, g and the
+update, an FP32 Jacobi eigensolve and FP32 T, w-bar solved in FP32 with one
+FP64-residual refinement step, and the mean increment in FP64.
 
 Bar: relative error of the analysis mean and of the analysis spread of every
 state variable (ps, u, v, T) within 1e-4 of the FP64 result; local observation
@@ -108,3 +111,26 @@ def test_mixed_config1_vs_fp64(letkf, synthetic):
     # A' stays well conditioned at this size (lambda_max / lambda_min < 1e4)
     assert st["n_ill_conditioned"] == 0 and st["n_not_converged"] == 0
     print("config1 mixed vs fp64:", errs)
+
+
+@pytest.mark.parametrize("k", [32, 64, 128])
+def test_mixed_wait_timeout_leaves_context_usable(letkf, synthetic, k):
+    # Every bounded wait of the mixed cores on their own tensor-core products
+    # gives up at once (0 polls): the run reports LETKF_ERR_TIMEOUT, each CTA
+    # lets its committed products finish before it frees its tensor memory,
+    # and the next run on the same context with the default limit is bitwise
+    # the run of a fresh context.  Covers the single-launch core (k = 32), the
+    # staged k = 64 core and the wide core (k = 128).
+    w = synthetic.small_case(nlat=10, nlon=20, nz=3, k=k, nobs=1200, loc_dist_km=900.0, seed=70 + k)
+    ref = letkf.LetkfGPU.from_workload(w, precision=letkf.LETKF_PREC_MIXED)
+    xa_ref, axa_ref = ref.run(w.xb, w.axb, w.obs)
+    ref.close()
+    ctx = letkf.LetkfGPU.from_workload(w, precision=letkf.LETKF_PREC_MIXED)
+    ctx.set_wait_limit(0)
+    with pytest.raises(letkf.LetkfError) as ei:
+        ctx.run(w.xb, w.axb, w.obs)
+    assert ei.value.code == letkf.LETKF_ERR_TIMEOUT
+    ctx.set_wait_limit(-1)
+    xa, axa = ctx.run(w.xb, w.axb, w.obs)
+    assert np.array_equal(xa, xa_ref) and np.array_equal(axa, axa_ref)
+    ctx.close()

@@ -81,3 +81,23 @@ def test_noalloc_rejects_sizes_beyond_its_scratch(lib):
     rc = L.letkf_gpu_core_batch_noalloc(32, C.c_double(1.1), C.c_int64(nmax + 1), None, None,
                                         None, None, None, None, None, None)
     assert rc == letkf.LETKF_ERR_INVALID
+
+
+def test_noalloc_rejects_offsets_that_go_backwards(lib):
+    # offsets start at 0 and step back once (problem 1 would have -25 rows):
+    # the call returns LETKF_ERR_INVALID and no row is read (every row index
+    # the offsets name lies inside the 100-row arrays anyway); a following
+    # call with good offsets is unaffected by the flag the bad one left.
+    import torch
+    letkf, L = lib
+    k, infl = 16, 1.1
+    offs, hx, rdi, dep, rloc = _problems(5, k, [40, 35, 25])
+    bad = np.array([0, 40, 15, 100], dtype=np.int64)
+    dev = {name: torch.from_numpy(np.ascontiguousarray(a)).cuda()
+           for name, a in (("offs", bad), ("hx", hx), ("rdi", rdi), ("dep", dep), ("rloc", rloc))}
+    tr = torch.zeros((3, k, k), dtype=torch.float64, device="cuda")
+    wb = torch.zeros((3, k), dtype=torch.float64, device="cuda")
+    assert _call(L, k, infl, 3, dev, tr, wb) == letkf.LETKF_ERR_INVALID
+    dev["offs"] = torch.from_numpy(offs).cuda()
+    assert _call(L, k, infl, 3, dev, tr, wb) == letkf.LETKF_OK
+    assert np.isfinite(tr.cpu().numpy()).all()
