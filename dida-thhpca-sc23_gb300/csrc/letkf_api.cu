@@ -135,7 +135,7 @@ int reserve_obs_work(letkf_ctx *ctx, int64_t no)
 {
     const size_t n = (size_t)std::max<int64_t>(no, 1);
     LG_CUDA(ctx->d_yb.reserve(n * ctx->k));
-    if (ctx->params.precision == LETKF_PREC_MIXED) {
+    if (lg_is_mixed(ctx->params.precision)) {
         LG_CUDA(ctx->d_ys32.reserve((n > 0 ? n : 1) * ctx->k));
         LG_CUDA(ctx->d_oef.reserve(n));
     }
@@ -204,7 +204,7 @@ int obs_prepare(letkf_ctx *ctx, const double *xb, const double *axb, const ObsDe
 
 size_t list_entry_bytes(const letkf_ctx *ctx)
 {
-    return sizeof(int32_t) + sizeof(double) + (ctx->params.precision == LETKF_PREC_MIXED ? sizeof(float2) : 0);
+    return sizeof(int32_t) + sizeof(double) + (lg_is_mixed(ctx->params.precision) ? sizeof(float2) : 0);
 }
 
 // Entries the list pool may hold: the caller's limit, else the device's free
@@ -236,7 +236,7 @@ int size_pool(letkf_ctx *ctx, int64_t cap)
     release_pool(ctx);
     LG_CUDA(ctx->d_lidx.reserve((size_t)cap));
     LG_CUDA(ctx->d_lrloc.reserve((size_t)cap));
-    if (ctx->params.precision == LETKF_PREC_MIXED) LG_CUDA(ctx->d_lmeta.reserve((size_t)cap));
+    if (lg_is_mixed(ctx->params.precision)) LG_CUDA(ctx->d_lmeta.reserve((size_t)cap));
     ctx->list_cap = cap;
     return LETKF_OK;
 }
@@ -246,7 +246,7 @@ cudaError_t launch_search(letkf_ctx *ctx, const ObsDev &od, int64_t no)
     const LgGrid g = lg_grid(ctx);
     // before the departures (H's members pass deferred) the entries get
     // their second factor at the core launch
-    ctx->lists_need_ef = ctx->members_pending && ctx->params.precision == LETKF_PREC_MIXED;
+    ctx->lists_need_ef = ctx->members_pending && lg_is_mixed(ctx->params.precision);
     return ctx->dec_nx > 0 ? lg_launch_search_dec(ctx, g, od.lat) : lg_launch_search(ctx, g, no);
 }
 
@@ -260,7 +260,7 @@ cudaError_t launch_core(letkf_ctx *ctx, const double *xb, const double *axb, dou
     // the last window (lg_launch_overlap_update)
     if (ctx->params.overlap > 0) return lg_launch_core_fp64(ctx, g, nullptr, nullptr, nullptr, nullptr, true);
     const bool keep = ctx->d_trans.p != nullptr;
-    return ctx->params.precision == LETKF_PREC_MIXED ? lg_launch_core_mixed(ctx, g, xb, axb, xa, axa, keep)
+    return lg_is_mixed(ctx->params.precision) ? lg_launch_core_mixed(ctx, g, xb, axb, xa, axa, keep)
                                                      : lg_launch_core_fp64(ctx, g, xb, axb, xa, axa, keep);
 }
 
@@ -355,7 +355,7 @@ int search_and_core(letkf_ctx *ctx, const double *xb, const double *axb, double 
     }
     // windows end on multiples of the mixed core's chunk size (so that every
     // cube keeps its chunk); the pool holds at least the heaviest chunk
-    const int64_t align = ctx->params.precision == LETKF_PREC_MIXED ? lg_run_chunk(ctx) : 1;
+    const int64_t align = lg_is_mixed(ctx->params.precision) ? lg_run_chunk(ctx) : 1;
     std::vector<int64_t> unit;   // list entries of each aligned group of cubes
     for (int64_t c = c0; c < c1;) {
         const int64_t e = std::min(c1, (c / align + 1) * align);
@@ -538,7 +538,7 @@ int letkf_gpu_create(letkf_ctx **out, const letkf_grid *grid, const letkf_params
     if (!(P.loc_dist_km > 0.0 && P.loc_dist_km <= 4000.0) || !(P.inflation > 0.0) ||
         P.max_obs < 1 || P.cube_n < 1 || P.cube_nz < 1 || P.overlap < 0 ||
         P.overlap >= P.cube_n || (P.h_mode != 0 && P.h_mode != 1) ||
-        (P.precision != LETKF_PREC_FP64 && P.precision != LETKF_PREC_MIXED) ||
+        (P.precision != LETKF_PREC_FP64 && !lg_is_mixed(P.precision)) ||
         !(P.obs_polar_deg >= 0.0))
         return LETKF_ERR_INVALID;
     const bool need_hybrid = P.h_mode == 0 || P.vert_dist > 0.0;
@@ -553,6 +553,8 @@ int letkf_gpu_create(letkf_ctx **out, const letkf_grid *grid, const letkf_params
     // the overlapped-cube and vertical-localization modes run in the FP64 form
     if ((P.overlap != 0 || P.vert_dist > 0.0) && P.precision != LETKF_PREC_FP64) return LETKF_ERR_UNSUPPORTED;
     if (P.precision == LETKF_PREC_MIXED && !lg_mixed_supports(G.ens)) return LETKF_ERR_UNSUPPORTED;
+    // the FP64 eigenpair refinement is a stage of the staged (k = 64) core
+    if (P.precision == LETKF_PREC_MIXED_F64EIG && G.ens != 64) return LETKF_ERR_UNSUPPORTED;
 
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) return LETKF_ERR_CUDA;
@@ -733,6 +735,7 @@ int lg_run_analysis(letkf_ctx *ctx, const letkf_obs *obs, bool host_obs, const d
                     const double *daxb, double *dxa, double *daxa, unsigned long long *cnt, bool state_in_flight)
 {
     ObsDev od;
+    for (int s = 0; s < letkf_ctx::kStages; s++) ctx->stg_n[s] = 0;
     int rc = stage_obs(ctx, obs, host_obs, od);
     if (rc) return rc;
     LG_CUDA(cudaEventRecord(ctx->ev[1], ctx->stream));
@@ -764,6 +767,11 @@ int lg_finish_run(letkf_ctx *ctx, const letkf_obs *obs, unsigned long long *cnt)
     ctx->stats.ms_core = elapsed(ctx->ev[3], ctx->ev[4]);
     ctx->stats.ms_d2h = elapsed(ctx->ev[4], ctx->ev[5]);
     ctx->stats.ms_total = elapsed(ctx->ev[0], ctx->ev[5]);
+    for (int s = 0; s < letkf_ctx::kStages; s++) {
+        double t = 0.0;
+        for (int i = 0; i < ctx->stg_n[s]; i++) t += elapsed(ctx->stg_ev[s][0][i], ctx->stg_ev[s][1][i]);
+        ctx->stats.ms_stage[s] = t;
+    }
     ctx->have_run = true;
     ctx->last_nobs = obs->nobs;
     if (st & LG_ST_TIMEOUT)
@@ -888,6 +896,37 @@ int letkf_gpu_obs_operator(letkf_ctx *ctx, const double *xb, const double *axb,
     if (st & LG_ST_BAD_OBS)
         return set_err(ctx, LETKF_ERR_INVALID,
                        "observation outside the grid or with a bad variable/level/pressure");
+    return LETKF_OK;
+}
+
+int letkf_gpu_local_obs_cubes(letkf_ctx *ctx, const int64_t *cubes, int64_t n, int64_t *offsets,
+                              int32_t *idx, double *rloc)
+{
+    if (!ctx || n < 0 || (n > 0 && !cubes) || !offsets) return LETKF_ERR_INVALID;
+    if (!ctx->have_run) return set_err(ctx, LETKF_ERR_STATE, "no run yet");
+    if (!ctx->lists_whole)
+        return set_err(ctx, LETKF_ERR_STATE, "the last run kept no complete lists (cube windows or a cube range)");
+    for (int64_t i = 0; i < n; i++)
+        if (cubes[i] < 0 || cubes[i] >= ctx->ncubes) return set_err(ctx, LETKF_ERR_INVALID, "cube out of range");
+    LG_CUDA(cudaSetDevice(ctx->device));
+    LG_CUDA(cudaStreamSynchronize(ctx->stream));
+    std::vector<int64_t> off((size_t)n);
+    std::vector<int32_t> cnt((size_t)n);
+    for (int64_t i = 0; i < n; i++) {
+        LG_CUDA(cudaMemcpy(&off[i], ctx->d_loff.p + cubes[i], sizeof(int64_t), cudaMemcpyDeviceToHost));
+        LG_CUDA(cudaMemcpy(&cnt[i], ctx->d_lcnt.p + cubes[i], sizeof(int32_t), cudaMemcpyDeviceToHost));
+    }
+    offsets[0] = 0;
+    for (int64_t i = 0; i < n; i++) offsets[i + 1] = offsets[i] + cnt[i];
+    for (int64_t i = 0; i < n; i++) {
+        if (cnt[i] == 0) continue;
+        if (idx)
+            LG_CUDA(cudaMemcpy(idx + offsets[i], ctx->d_lidx.p + off[i], sizeof(int32_t) * cnt[i],
+                               cudaMemcpyDeviceToHost));
+        if (rloc)
+            LG_CUDA(cudaMemcpy(rloc + offsets[i], ctx->d_lrloc.p + off[i], sizeof(double) * cnt[i],
+                               cudaMemcpyDeviceToHost));
+    }
     return LETKF_OK;
 }
 
@@ -1034,6 +1073,10 @@ int letkf_gpu_destroy(letkf_ctx *ctx)
     ctx->d_counters.release();
     for (int i = 0; i < 8; i++)
         if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
+    for (int s = 0; s < letkf_ctx::kStages; s++)
+        for (int h = 0; h < 2; h++)
+            for (int i = 0; i < letkf_ctx::kStageMarks; i++)
+                if (ctx->stg_ev[s][h][i]) cudaEventDestroy(ctx->stg_ev[s][h][i]);
     for (int i = 0; i < letkf_ctx::kCopyStreams; i++) {
         if (ctx->cev[i]) cudaEventDestroy(ctx->cev[i]);
         if (ctx->sev[i]) cudaEventDestroy(ctx->sev[i]);
@@ -1169,7 +1212,7 @@ int letkf_gpu_autotune(letkf_ctx *ctx, const double *xb, const double *axb, cons
                        double *xa, double *axa, int flags)
 {
     if (!ctx) return LETKF_ERR_INVALID;
-    if (ctx->params.precision != LETKF_PREC_MIXED)
+    if (!lg_is_mixed(ctx->params.precision))
         return letkf_gpu_run(ctx, xb, axb, obs, xa, axa, flags);
     // chunk sizes of the mixed core's work queue: small chunks balance the
     // load, large ones keep more cubes warm-started; the fastest core wins

@@ -26,6 +26,12 @@
 #endif
 #define LG_MAX_ENS 128          // largest ensemble the kernels are built for
 
+// The precision forms whose products run on the tensor cores.
+__host__ __device__ __forceinline__ bool lg_is_mixed(int precision)
+{
+    return precision == LETKF_PREC_MIXED || precision == LETKF_PREC_MIXED_F64EIG;
+}
+
 // Status bits written by kernels into ctx->d_status.
 #define LG_ST_BAD_OBS      1u   // obs outside the grid / bad variable or level
 #define LG_ST_LIST_FULL    2u   // local-list storage too small
@@ -273,9 +279,9 @@ struct letkf_ctx {
 
     cudaEvent_t ev[8] = {};
     // device-event marks around each launch of the staged core's stages (A
-    // build, eigensolve, update; letkf_stats.ms_stage), at most kStageMarks
-    // launches per stage and run
-    static constexpr int kStages = 3, kStageMarks = 32;
+    // build, eigensolve, update, FP64 refinement; letkf_stats.ms_stage), at
+    // most kStageMarks launches per stage and run
+    static constexpr int kStages = 4, kStageMarks = 32;
     cudaEvent_t stg_ev[kStages][2][kStageMarks] = {};
     int stg_n[kStages] = {};
     letkf_stats stats{};
@@ -311,7 +317,8 @@ struct letkf_ctx {
 // Launch counting (every kernel launch of this library goes through it).
 void lg_count_launch();
 // Device-event mark before (end = false) or after a launch of stage s of the
-// staged core (0 A build, 1 eigensolve, 2 update); skipped while the stream
+// staged core (0 A build, 1 eigensolve, 2 update, 3 FP64 refinement of the
+// eigenpairs); skipped while the stream
 // is being captured into a graph.
 void lg_stage_mark(letkf_ctx *ctx, int s, bool end);
 

@@ -29,9 +29,12 @@
 //
 // k = 32 and 48 run all steps in one persistent launch (k_core_mixed<k, 0>).
 // k = 64 runs them in three launches per block of cubes: the A and g build
-// (k_core_mixed<64, 1>), the eigensolves one warp each (k_eig_warp<64>, runs
-// of 8 cubes warm-started inside a run, taken from a queue) and steps 4-6
-// (k_core_mixed<64, 2>), with A, g, X and lambda in HBM between them.
+// (k_core_mixed<64, 1>), steps 3-5 one warp per cube (k_eig_warp<64>, runs of
+// 8 cubes warm-started inside a run, taken from a queue) and step 6
+// (k_core_mixed<64, 3>), with A and g, then T and wbar, in HBM between them.
+// LETKF_PREC_MIXED_F64EIG adds a fourth launch between the eigensolve and
+// the update (k_eig_refine<64>): the FP32 eigenpairs refined in FP64, then
+// T and wbar in FP64.
 #include <cuda_bf16.h>
 
 #include "letkf_internal.cuh"
@@ -99,9 +102,10 @@ struct MCfg {
 };
 
 // ST selects the stages a launch runs: 0 all of them; 1 the A build only
-// (A without the diagonal shift and g to mA, mgv); 2 from the eigenpairs on
-// (X and lambda from mX, mlam, written by k_eig_warp).  The intermediates
-// are indexed by cube - prm.cube0.
+// (A without the diagonal shift and g to mA, mgv); 3 the update only, from T
+// (FP32, row-major, in the slot of X) and wbar (FP64, in the slot of g),
+// written by the eigensolve launch (k_eig_warp) or by the FP64 refinement
+// (k_eig_refine).  The intermediates are indexed by cube - prm.cube0.
 template <int K, int ST>
 __global__ void __launch_bounds__(kT, 2)
 k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32_t *__restrict__ lidx,
@@ -110,8 +114,7 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
              const double *__restrict__ xb, const double *__restrict__ axb, double *__restrict__ xa,
              double *__restrict__ axa, double *__restrict__ trans_out, double *__restrict__ w_out,
              unsigned long long *__restrict__ counters, unsigned *__restrict__ status,
-             float *__restrict__ mA, double *__restrict__ mgv, const float *__restrict__ mX,
-             const float *__restrict__ mlam)
+             float *__restrict__ mA, double *__restrict__ mgv, const float *__restrict__ mX)
 {
     using C = MCfg<K>;
     constexpr int CH = C::CH;
@@ -234,7 +237,7 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
         (void)w32;
         (void)ci;
 
-        if (ST != 2) {
+        if (ST == 0 || ST == 1) {
         // ---------------- phase 1: A and g on the tensor cores ----------------------
         // Tile rows: Yhat_lo (0..K-1), Yhat_hi (K..2K-1), e_hi (2K), e_lo (2K+1),
         // zeros to TROWS.  The A operand is rows 0..127, the B operand rows
@@ -448,29 +451,22 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
         __syncthreads();                                   // Dhh/Dlh are dead
         }
         if (ST == 1) continue;
-        if (ST == 2) {
-            // the next cube's A, X, g and lambda into L2 while this one is done
+        if (ST == 3) {
+            // T (row-major, FP32) and wbar (FP64) from the eigensolve or the
+            // FP64 refinement launch, in the slots of X and g; the next cube's
+            // into L2
             if (cube + 1 < cube_end) {
-                // 128-byte lines of A and of X, of g, of lambda
-                constexpr int LA = K * K * 4 / 128, LG = (K * 8 + 127) / 128, LL = (K * 4 + 127) / 128;
-                for (int l = tid; l < 2 * LA + LG + LL; l += kT) {
-                    const char *a;
-                    if (l < LA) a = reinterpret_cast<const char *>(mA + (ci + 1) * K * K) + l * 128;
-                    else if (l < 2 * LA) a = reinterpret_cast<const char *>(mX + (ci + 1) * K * K) + (l - LA) * 128;
-                    else if (l < 2 * LA + LG) a = reinterpret_cast<const char *>(mgv + (ci + 1) * K) + (l - 2 * LA) * 128;
-                    else a = reinterpret_cast<const char *>(mlam + (ci + 1) * K) + (l - 2 * LA - LG) * 128;
+                constexpr int LA = K * K * 4 / 128, LG = (K * 8 + 127) / 128;
+                for (int l = tid; l < LA + LG; l += kT) {
+                    const char *a = (l < LA) ? reinterpret_cast<const char *>(mX + (ci + 1) * K * K) + l * 128
+                                             : reinterpret_cast<const char *>(mgv + (ci + 1) * K) + (l - LA) * 128;
                     asm volatile("prefetch.global.L2 [%0];" ::"l"(a));
                 }
             }
-            // this cube's g, A' and eigenpairs from the build and eigensolve launches
-            if (tid < K) gv[tid] = mgv[ci * K + tid];
+            float *T32s = reinterpret_cast<float *>(B1);
             for (int idx = tid; idx < K * K / 4; idx += kT)
-                reinterpret_cast<float4 *>(X32)[idx] = reinterpret_cast<const float4 *>(mX + ci * K * K)[idx];
-            if (tid < K) {
-                const float lamf = mlam[ci * K + tid];
-                ilam32[tid] = 1.0f / lamf;
-                hc32[tid] = sqrtf((float)(K - 1) / lamf);
-            }
+                reinterpret_cast<float4 *>(T32s)[idx] = reinterpret_cast<const float4 *>(mX + ci * K * K)[idx];
+            if (tid < K) wbar[tid] = mgv[ci * K + tid];
             __syncthreads();
         }
         if (ST == 0) {
@@ -571,6 +567,7 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
             }
         }
         }
+        if constexpr (ST != 3) {
         if (tid < K) {
             nrm32[tid] = hc32[tid];                    // f for T
             r32[tid] = (float)gv[tid];                 // right-hand side of the first solve
@@ -600,31 +597,14 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
             }
             __syncthreads();
             if (it == 0) {
-                // four threads per row of A', each over K/4 columns; the FP64
-                // A' is (double)A + (k-1)/rho on the diagonal, from the FP32 A
-                // of the build launch (ST 2, converted on the integer pipe) or
-                // from B1
+                // four threads per row of A' (FP64, in B1), each over K/4 columns
                 constexpr int Q = K / 4;
                 for (int t0 = 0; t0 < 4 * K; t0 += kT) {
                     const int t = t0 + tid, i = t >> 2, q = t & 3;
                     double d = 0.0;
                     if (t < 4 * K) {
-                        if (ST == 2) {
-                            const float4 *arow = reinterpret_cast<const float4 *>(mA + ci * K * K + i * K + q * Q);
-#pragma unroll
-                            for (int l4 = 0; l4 < Q / 4; l4++) {
-                                const float4 a = arow[l4];
-                                const int l = q * Q + 4 * l4;
-                                d = fma(lg_f2d_bits(a.x), wbar[l], d);
-                                d = fma(lg_f2d_bits(a.y), wbar[l + 1], d);
-                                d = fma(lg_f2d_bits(a.z), wbar[l + 2], d);
-                                d = fma(lg_f2d_bits(a.w), wbar[l + 3], d);
-                            }
-                            if (i / Q == q) d = fma(cdiag, wbar[i], d);
-                        } else {
 #pragma unroll 4
-                            for (int l = q * Q; l < q * Q + Q; l++) d = fma(B1[i * K + l], wbar[l], d);
-                        }
+                        for (int l = q * Q; l < q * Q + Q; l++) d = fma(B1[i * K + l], wbar[l], d);
                     }
                     d += __shfl_xor_sync(0xffffffffu, d, 1);
                     d += __shfl_xor_sync(0xffffffffu, d, 2);
@@ -633,6 +613,7 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
                 __syncthreads();
             }
         }
+        }   // ST != 3
         LG_PHASE(3);
 
         // ---------------- phase 5: T in FP32 ------------------------------------------------
@@ -653,7 +634,7 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
         // T = X diag(f) X^T only feeds the BF16 hi/lo tensor-core update (16
         // significant bits); FP32 eigenpairs give it to ~1e-7 relative.
         float *T32 = reinterpret_cast<float *>(B1);               // T, FP32, row-major
-        {
+        if constexpr (ST != 3) {
             float tacc[C::ML][16];
 #pragma unroll
             for (int m = 0; m < C::ML; m++) {
@@ -937,13 +918,18 @@ constexpr int kTE = LG_EIG_THREADS;     // threads of an eigensolve block (one p
 template <int K>
 __global__ void __launch_bounds__(kTE, 1)
 k_eig_warp(int64_t cube0, int64_t cube_end, int R, double cdiag, float tol, const float *__restrict__ mA,
-           float *__restrict__ mX, float *__restrict__ mlam, unsigned long long *__restrict__ counters)
+           float *__restrict__ mX, float *__restrict__ mlam, double *__restrict__ mgv, int emit_tw,
+           unsigned long long *__restrict__ counters)
 {
     constexpr int LDW = K + 4, NS = K / 2;
     static_assert(NS == 32, "one lane per column pair");
     extern __shared__ float smw[];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     float *Wp = smw + (size_t)warp * K * LDW;           // this warp's columns
+    // this warp's vectors (emit_tw): wbar (FP64), then g or the residual,
+    // X^T g / lambda, f = sqrt((k-1)/lambda) and 1/lambda (FP32)
+    double *wv = reinterpret_cast<double *>(smw + (size_t)(kTE / 32) * K * LDW) + (size_t)warp * 3 * K;
+    float *gs = reinterpret_cast<float *>(wv + K), *cs = gs + K, *fs = cs + K, *ils = fs + K;
     const int64_t base = cube0 / R * R;
     const int64_t nruns = (cube_end - base + R - 1) / R;
     const float cd = (float)cdiag;
@@ -1060,9 +1046,14 @@ k_eig_warp(int64_t cube0, int64_t cube_end, int R, double cdiag, float tol, cons
                     float4 x = col[q];
                     x.x *= il; x.y *= il; x.z *= il; x.w *= il;
                     col[q] = x;
-                    out[q] = x;
+                    if (!emit_tw) out[q] = x;
                 }
-                mlam[(c - cube0) * K + j] = lamf;
+                if (!emit_tw) {
+                    mlam[(c - cube0) * K + j] = lamf;
+                } else {
+                    fs[j] = sqrtf((float)(K - 1) / lamf);
+                    ils[j] = il;
+                }
                 lo = fminf(lo, lamf);
                 hi = fmaxf(hi, lamf);
             }
@@ -1078,6 +1069,103 @@ k_eig_warp(int64_t cube0, int64_t cube_end, int R, double cdiag, float tol, cons
                 if (hi > 1.0e4f * lo) atomicAdd(&counters[LG_CNT_ILLCOND], 1ull);
             }
             __syncwarp();
+            if (emit_tw) {
+                // wbar = X diag(1/lambda) X^T g in FP32, then one refinement
+                // step wbar += X diag(1/lambda) X^T (g - A' wbar) with the
+                // residual in FP64 against A' = (double)A + (k-1)/rho I; the
+                // FP32 solve has a relative error of about eps32 kappa, the step
+                // leaves that times the FP32 eigenpairs' error.  Then T = X
+                // diag(sqrt((k-1)/lambda)) X^T in FP32 (it feeds the BF16 hi/lo
+                // update).  wbar goes over g in mgv, T (row-major) over X's slot.
+                const int64_t ci = c - cube0;
+                const double g0 = mgv[ci * K + lane], g1 = mgv[ci * K + lane + NS];
+                gs[lane] = (float)g0;
+                gs[lane + NS] = (float)g1;
+                double w0 = 0.0, w1 = 0.0;
+                for (int it = 0; it < 2; it++) {
+                    __syncwarp();
+                    // c_j = x_j . rhs / lambda_j for this lane's two columns
+#pragma unroll
+                    for (int h = 0; h < 2; h++) {
+                        const int j = lane + h * NS;
+                        const float4 *col = reinterpret_cast<const float4 *>(Wp + j * LDW);
+                        const float4 *rv = reinterpret_cast<const float4 *>(gs);
+                        float d0 = 0.0f, d1 = 0.0f;
+#pragma unroll
+                        for (int q = 0; q < K / 4; q++) {
+                            const float4 x = col[q], y = rv[q];
+                            d0 = fmaf(x.x, y.x, fmaf(x.y, y.y, d0));
+                            d1 = fmaf(x.z, y.z, fmaf(x.w, y.w, d1));
+                        }
+                        cs[j] = (d0 + d1) * ils[j];
+                    }
+                    __syncwarp();
+                    // rows lane and lane + NS of X c
+                    float a0 = 0.0f, a1 = 0.0f;
+#pragma unroll 8
+                    for (int j = 0; j < K; j++) {
+                        const float cj = cs[j];
+                        a0 = fmaf(Wp[j * LDW + lane], cj, a0);
+                        a1 = fmaf(Wp[j * LDW + lane + NS], cj, a1);
+                    }
+                    w0 += (double)a0;
+                    w1 += (double)a1;
+                    if (it == 1) break;
+                    wv[lane] = w0;
+                    wv[lane + NS] = w1;
+                    __syncwarp();
+                    // residual rows lane and lane + NS in FP64 (A symmetric:
+                    // row r of A from the build launch, FP32 values converted
+                    // exactly on the integer pipe)
+#pragma unroll
+                    for (int h = 0; h < 2; h++) {
+                        const int r = lane + h * NS;
+                        const float4 *arow = reinterpret_cast<const float4 *>(mA + ci * K * K + r * K);
+                        double d = 0.0;
+#pragma unroll 4
+                        for (int q = 0; q < K / 4; q++) {
+                            const float4 a = arow[q];
+                            d = fma(lg_f2d_bits(a.x), wv[4 * q], d);
+                            d = fma(lg_f2d_bits(a.y), wv[4 * q + 1], d);
+                            d = fma(lg_f2d_bits(a.z), wv[4 * q + 2], d);
+                            d = fma(lg_f2d_bits(a.w), wv[4 * q + 3], d);
+                        }
+                        d = fma(cdiag, wv[r], d);
+                        gs[r] = (float)((h ? g1 : g0) - d);
+                    }
+                }
+                mgv[ci * K + lane] = w0;
+                mgv[ci * K + lane + NS] = w1;
+                // T rows lane and lane + NS, one at a time: sum_j f_j x_j[r] x_j
+#pragma unroll 1
+                for (int h = 0; h < 2; h++) {
+                    const int r = lane + h * NS;
+                    unsigned long long t0[K / 2];
+#pragma unroll
+                    for (int q = 0; q < K / 2; q++) t0[q] = 0ull;
+#pragma unroll 2
+                    for (int j = 0; j < K; j++) {
+                        const float b0 = fs[j] * Wp[j * LDW + r];
+                        const unsigned long long p0 = lg_pk2(b0, b0);
+                        const float4 *col = reinterpret_cast<const float4 *>(Wp + j * LDW);
+#pragma unroll
+                        for (int q = 0; q < K / 4; q++) {
+                            const float4 x = col[q];
+                            t0[2 * q] = lg_ffma2(lg_pk2(x.x, x.y), p0, t0[2 * q]);
+                            t0[2 * q + 1] = lg_ffma2(lg_pk2(x.z, x.w), p0, t0[2 * q + 1]);
+                        }
+                    }
+                    float4 *o0 = reinterpret_cast<float4 *>(mX + ci * K * K + (int64_t)r * K);
+#pragma unroll
+                    for (int q = 0; q < K / 4; q++) {
+                        float a, b, cc, d;
+                        lg_upk2(t0[2 * q], a, b);
+                        lg_upk2(t0[2 * q + 1], cc, d);
+                        o0[q] = make_float4(a, b, cc, d);
+                    }
+                }
+                __syncwarp();
+            }
             LG_EPHASE(2);
         }
     }
@@ -1086,6 +1174,293 @@ k_eig_warp(int64_t cube0, int64_t cube_end, int R, double cdiag, float tol, cons
         printf("eig cycles warp 0 of cta 0: W build %lld, jacobi %lld, outputs %lld\n", ec[0], ec[1], ec[2]);
 #endif
 #undef LG_EPHASE
+}
+
+// FP64 refinement of the eigenpairs of A' = A + cdiag I (LETKF_PREC_MIXED_F64EIG)
+// for the cubes cube0 .. cube_end - 1, one cube per CTA at a time: one step
+// of the iterative refinement of Ogita and Aishima (Japan J. Indust. Appl.
+// Math. 35 (2018) 1007-1035, Algorithm 1) on the FP32 Jacobi eigenvectors
+// X^ (columns of mX):
+//     R = I - X^T X^,  S = X^T A' X^                          (FP64)
+//     lambda_i = S_ii / (1 - R_ii)
+//     E_ij = (S_ij + lambda_j R_ij) / (lambda_j - lambda_i)   if |lambda_i - lambda_j| > delta
+//          = R_ij / 2                                          otherwise, and for i = j
+//     delta = 2 (||S - diag(lambda)||_F + max|lambda| ||R||_F)
+//     X = X^ + X^ E
+// The step squares the eigenvectors' error (about 1e-6 from the FP32 Jacobi,
+// so about 1e-12 after it).  E is of that size, so the product X^ E is taken
+// in FP32 (its rounding is ~1e-13 of X) and added in FP64.  Then, in FP64,
+// f_j = sqrt((k-1)/lambda_j), T = X diag(f) X^T (letkf_core.F90:98-160) and
+// wbar = X diag(1/lambda) X^T g (:162-195).  T goes as FP32 row-major into
+// the cube's slot of mX (it only feeds the BF16 hi/lo update) and wbar into
+// the cube's slot of g in mgv.  Every product of the step runs on the FP64
+// pipe: about 0.69 M DFMA per cube at k = 64.
+constexpr int kTR = 256;
+// Largest first-order correction the step applies to a pair of eigenvectors
+// (above it the pair is treated as a cluster): the step's second-order
+// remainder, ~kRefineMaxRot^2 of non-orthogonality, stays near 1e-8.  On
+// k = 64 test matrices (a CPU replica of the FP32 warp Jacobi and of this
+// step) T comes out within 6e-7 of an FP64 eigendecomposition of the same A'
+// (FP32 eigenpairs alone: 5e-6); the rest is the pairs kept as clusters, whose
+// FP32 rotation changes T by their angle times the difference of their f.
+constexpr double kRefineMaxRot = 1e-4;
+
+template <int K>
+__global__ void __launch_bounds__(kTR, 2)
+k_eig_refine(int64_t cube0, int64_t cube_end, double cdiag, const float *mA, float *mX, double *mgv)
+{
+    static_assert(K == 64, "one 4x4 tile of the k x k products per thread");
+    constexpr int KB = K / 4, NLOW = KB * (KB + 1) / 2;
+    extern __shared__ double smr[];
+    double *Xd = smr;                 // X^ by rows: Xd[r*K + j] = x^_j[r]
+    double *Bd = Xd + K * K;          // B = A' X^ by rows; then E (FP32, [i*K + j])
+    double *RS = Bd + K * K;          // R below the diagonal ([i*K + j], i > j), S above ([j*K + i]); then X^T
+    double *rdg = RS + K * K;         // R_ii
+    double *sdg = rdg + K;            // S_ii
+    double *lam = sdg + K;            // refined eigenvalues
+    double *fv = lam + K;             // sqrt((k-1)/lambda)
+    double *ilv = fv + K;             // 1/lambda
+    double *gvv = ilv + K;            // g
+    double *cv = gvv + K;             // X^T g / lambda
+    double *red = cv + K;             // 3 x 8 warp partial sums
+    float *Ef = reinterpret_cast<float *>(Bd);
+    double *Xt = RS;                  // refined X by eigenvector: Xt[j*K + r]
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    // this thread's full tile and (threads < NLOW) lower tile
+    const int fi = tid / KB, fj = tid % KB;
+    int li = 0, lj = 0;
+    const bool has_low = tid < NLOW;
+    lg_decode_block(has_low ? tid : 0, li, lj);
+
+    for (int64_t c = cube0 + blockIdx.x; c < cube_end; c += gridDim.x) {
+        const int64_t ci = c - cube0;
+        const float *Ac = mA + ci * K * K;
+        float *Xc = mX + ci * K * K;
+        for (int idx = tid; idx < K * K; idx += kTR) {
+            const int j = idx / K, r = idx % K;
+            Xd[r * K + j] = (double)Xc[idx];
+        }
+        if (tid < K) gvv[tid] = mgv[ci * K + tid];
+        __syncthreads();
+
+        // R (lower tiles) and B = A X^ + cdiag X^ (all tiles)
+        if (has_low) {
+            double acc[16];
+#pragma unroll
+            for (int q = 0; q < 16; q++) acc[q] = 0.0;
+            for (int r = 0; r < K; r++) {
+                const double *row = Xd + r * K;
+                double a[4], b[4];
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    a[q] = row[4 * li + q];
+                    b[q] = row[4 * lj + q];
+                }
+#pragma unroll
+                for (int p = 0; p < 4; p++)
+#pragma unroll
+                    for (int q = 0; q < 4; q++) acc[p * 4 + q] = fma(a[p], b[q], acc[p * 4 + q]);
+            }
+#pragma unroll
+            for (int p = 0; p < 4; p++)
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const int i = 4 * li + p, j = 4 * lj + q;
+                    if (i > j) RS[i * K + j] = -acc[p * 4 + q];
+                    else if (i == j) rdg[i] = 1.0 - acc[p * 4 + q];
+                }
+        }
+        {
+            double acc[16];
+#pragma unroll
+            for (int q = 0; q < 16; q++) acc[q] = 0.0;
+            for (int l = 0; l < K; l++) {
+                // A symmetric: rows 4 fi .. of column l = row l at 4 fi ..
+                const float4 av = *reinterpret_cast<const float4 *>(Ac + l * K + 4 * fi);
+                const double a[4] = {(double)av.x, (double)av.y, (double)av.z, (double)av.w};
+                const double *xr = Xd + l * K + 4 * fj;
+                const double b[4] = {xr[0], xr[1], xr[2], xr[3]};
+#pragma unroll
+                for (int p = 0; p < 4; p++)
+#pragma unroll
+                    for (int q = 0; q < 4; q++) acc[p * 4 + q] = fma(a[p], b[q], acc[p * 4 + q]);
+            }
+#pragma unroll
+            for (int p = 0; p < 4; p++)
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const int r = 4 * fi + p, j = 4 * fj + q;
+                    Bd[r * K + j] = fma(cdiag, Xd[r * K + j], acc[p * 4 + q]);
+                }
+        }
+        __syncthreads();
+
+        // S = X^T B (lower tiles)
+        if (has_low) {
+            double acc[16];
+#pragma unroll
+            for (int q = 0; q < 16; q++) acc[q] = 0.0;
+            for (int r = 0; r < K; r++) {
+                double a[4], b[4];
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    a[q] = Xd[r * K + 4 * li + q];
+                    b[q] = Bd[r * K + 4 * lj + q];
+                }
+#pragma unroll
+                for (int p = 0; p < 4; p++)
+#pragma unroll
+                    for (int q = 0; q < 4; q++) acc[p * 4 + q] = fma(a[p], b[q], acc[p * 4 + q]);
+            }
+#pragma unroll
+            for (int p = 0; p < 4; p++)
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const int i = 4 * li + p, j = 4 * lj + q;
+                    if (i > j) RS[j * K + i] = acc[p * 4 + q];
+                    else if (i == j) sdg[i] = acc[p * 4 + q];
+                }
+        }
+        __syncthreads();
+
+        // lambda_i and the cluster threshold delta
+        if (tid < K) lam[tid] = sdg[tid] / (1.0 - rdg[tid]);
+        __syncthreads();
+        {
+            double so = 0.0, ro = 0.0, lm = 0.0;
+            for (int idx = tid; idx < K * K; idx += kTR) {
+                const int i = idx / K, j = idx % K;
+                if (i > j) {
+                    const double s = RS[j * K + i], r = RS[i * K + j];
+                    so += 2.0 * s * s;
+                    ro += 2.0 * r * r;
+                } else if (i == j) {
+                    const double s = sdg[i] - lam[i], r = rdg[i];
+                    so += s * s;
+                    ro += r * r;
+                    lm = fmax(lm, fabs(lam[i]));
+                }
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                so += __shfl_xor_sync(0xffffffffu, so, o);
+                ro += __shfl_xor_sync(0xffffffffu, ro, o);
+                lm = fmax(lm, __shfl_xor_sync(0xffffffffu, lm, o));
+            }
+            if (lane == 0) {
+                red[warp] = so;
+                red[8 + warp] = ro;
+                red[16 + warp] = lm;
+            }
+        }
+        __syncthreads();
+        double so = 0.0, ro = 0.0, lm = 0.0;
+#pragma unroll
+        for (int w8 = 0; w8 < kTR / 32; w8++) {
+            so += red[w8];
+            ro += red[8 + w8];
+            lm = fmax(lm, red[16 + w8]);
+        }
+        const double delta = 2.0 * (sqrt(so) + lm * sqrt(ro));
+        // E (FP32) over B, which is dead after S
+        for (int idx = tid; idx < K * K; idx += kTR) {
+            const int i = idx / K, j = idx % K;
+            double e;
+            if (i == j) {
+                e = 0.5 * rdg[i];
+            } else {
+                const int hi = i > j ? i : j, lo = i > j ? j : i;
+                const double s = RS[lo * K + hi], r = RS[hi * K + lo];
+                const double gap = lam[j] - lam[i];
+                e = 0.5 * r;
+                if (fabs(gap) > delta) {
+                    // the pair is rotated only when both first-order terms are
+                    // small: the step leaves O(e^2) of non-orthogonality in X,
+                    // and a pair whose FP32 vectors are far off (eigenvalues
+                    // close at FP32 resolution) is kept as a cluster instead,
+                    // where its rotation changes T by less than its gap does
+                    const double eij = (s + lam[j] * r) / gap, eji = -(s + lam[i] * r) / gap;
+                    if (fmax(fabs(eij), fabs(eji)) <= kRefineMaxRot) e = eij;
+                }
+            }
+            Ef[idx] = (float)e;
+        }
+        __syncthreads();
+
+        // X = X^ + X^ E: the correction in FP32 from X^ (mX) and E, added in
+        // FP64; written by eigenvector (Xt over R and S, dead now)
+        {
+            float acc[16];
+#pragma unroll
+            for (int q = 0; q < 16; q++) acc[q] = 0.0f;
+            for (int i = 0; i < K; i++) {
+                // X^ rows 4 fi .. of column i, E row i at 4 fj ..
+                const float4 xv = *reinterpret_cast<const float4 *>(Xc + i * K + 4 * fi);
+                const float4 ev = *reinterpret_cast<const float4 *>(Ef + i * K + 4 * fj);
+                const float a[4] = {xv.x, xv.y, xv.z, xv.w}, b[4] = {ev.x, ev.y, ev.z, ev.w};
+#pragma unroll
+                for (int p = 0; p < 4; p++)
+#pragma unroll
+                    for (int q = 0; q < 4; q++) acc[p * 4 + q] = fmaf(a[p], b[q], acc[p * 4 + q]);
+            }
+            __syncthreads();               // every thread is done with R and S
+#pragma unroll
+            for (int p = 0; p < 4; p++)
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const int r = 4 * fi + p, j = 4 * fj + q;
+                    Xt[j * K + r] = Xd[r * K + j] + (double)acc[p * 4 + q];
+                }
+        }
+        if (tid < K) {
+            fv[tid] = sqrt((double)(K - 1) / lam[tid]);
+            ilv[tid] = 1.0 / lam[tid];
+        }
+        __syncthreads();
+
+        // T = X diag(f) X^T (lower tiles), FP32 row-major into the slot of X^
+        if (has_low) {
+            double acc[16];
+#pragma unroll
+            for (int q = 0; q < 16; q++) acc[q] = 0.0;
+            for (int j = 0; j < K; j++) {
+                const double f = fv[j];
+                const double *xj = Xt + j * K;
+                double a[4], b[4];
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    a[q] = xj[4 * li + q];
+                    b[q] = xj[4 * lj + q] * f;
+                }
+#pragma unroll
+                for (int p = 0; p < 4; p++)
+#pragma unroll
+                    for (int q = 0; q < 4; q++) acc[p * 4 + q] = fma(a[p], b[q], acc[p * 4 + q]);
+            }
+#pragma unroll
+            for (int p = 0; p < 4; p++)
+#pragma unroll
+                for (int q = 0; q < 4; q++) {
+                    const int r = 4 * li + p, s = 4 * lj + q;
+                    const float t = (float)acc[p * 4 + q];
+                    Xc[r * K + s] = t;
+                    Xc[s * K + r] = t;
+                }
+        }
+        // wbar = X diag(1/lambda) X^T g
+        if (tid < K) {
+            double d = 0.0;
+            for (int r = 0; r < K; r++) d = fma(Xt[tid * K + r], gvv[r], d);
+            cv[tid] = d * ilv[tid];
+        }
+        __syncthreads();
+        if (tid < K) {
+            double d = 0.0;
+            for (int j = 0; j < K; j++) d = fma(Xt[j * K + tid], cv[j], d);
+            mgv[ci * K + tid] = d;
+        }
+        __syncthreads();
+    }
 }
 
 // Most cubes one staged launch sequence holds intermediates for (A, X: 2 k^2
@@ -1119,7 +1494,7 @@ cudaError_t launch_stage(letkf_ctx *ctx, const LgGrid &g, const double *xb, cons
     k_core_mixed<K, ST><<<blocks, kT, smem, ctx->stream>>>(
         g, lg_params(ctx), ctx->d_ys32.p, ctx->d_lidx.p, ctx->d_lmeta.p, ctx->d_queue.p, nchunks, chunk,
         ctx->d_loff.p, ctx->d_lcnt.p, ctx->win1, xb, axb, xa, axa, trans_out, w_out, ctx->d_counters.p,
-        ctx->d_status.p, ctx->d_mA.p, ctx->d_mg.p, ctx->d_mX.p, ctx->d_mlam.p);
+        ctx->d_status.p, ctx->d_mA.p, ctx->d_mg.p, ctx->d_mX.p);
     return cudaGetLastError();
 }
 
@@ -1145,7 +1520,8 @@ cudaError_t launch_mixed(letkf_ctx *ctx, const LgGrid &g, const double *xb, cons
         // warps, aligned so that every window boundary (a multiple of the
         // work-queue chunk, itself a multiple of 8) is a run boundary
         const int R = 8;
-        const size_t ew = (size_t)K * (K + 4) * sizeof(float) * (kTE / 32);
+        // each warp: its K x (K+4) columns, then 3K doubles of vectors
+        const size_t ew = ((size_t)K * (K + 4) * sizeof(float) + 3 * K * sizeof(double)) * (kTE / 32);
         cudaError_t e = cudaFuncSetAttribute(k_eig_warp<K>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ew);
         // blocks end at multiples of `step` in cube numbering (so the runs and
         // chunks, and the results, do not depend on the blocking), at most
@@ -1173,7 +1549,9 @@ cudaError_t launch_mixed(letkf_ctx *ctx, const LgGrid &g, const double *xb, cons
             if ((e = ctx->d_mg.reserve((size_t)nb * K)) != cudaSuccess) break;
             if ((e = ctx->d_mlam.reserve((size_t)nb * K)) != cudaSuccess) break;
             if ((e = lg_build_chunk_queue(ctx, chunk, nchunks)) != cudaSuccess) break;
+            lg_stage_mark(ctx, 0, false);
             e = launch_stage<K, 1>(ctx, g, xb, axb, xa, axa, trans_out, w_out, chunk, nchunks, nsm);
+            lg_stage_mark(ctx, 0, true);
             if (e != cudaSuccess) break;
             const int64_t runs = (b1 - b0 / R * R + R - 1) / R;
             const int64_t eb = (runs + kTE / 32 - 1) / (kTE / 32);
@@ -1182,11 +1560,35 @@ cudaError_t launch_mixed(letkf_ctx *ctx, const LgGrid &g, const double *xb, cons
                                      ctx->stream)) != cudaSuccess)
                 break;
             lg_count_launch();
+            lg_stage_mark(ctx, 1, false);
+            // LETKF_PREC_MIXED: the warps also form wbar and T (for the update
+            // launch); LETKF_PREC_MIXED_F64EIG: they write X and lambda for the
+            // FP64 refinement
+            const bool f64eig = ctx->params.precision == LETKF_PREC_MIXED_F64EIG;
             k_eig_warp<K><<<eblocks, kTE, ew, ctx->stream>>>(b0, b1, R, (double)(K - 1) / ctx->params.inflation,
                                                           LG_MIXED_JACOBI_TOL, ctx->d_mA.p, ctx->d_mX.p,
-                                                          ctx->d_mlam.p, ctx->d_counters.p);
+                                                          ctx->d_mlam.p, ctx->d_mg.p, f64eig ? 0 : 1,
+                                                          ctx->d_counters.p);
+            lg_stage_mark(ctx, 1, true);
             if ((e = cudaGetLastError()) != cudaSuccess) break;
-            e = launch_stage<K, 2>(ctx, g, xb, axb, xa, axa, trans_out, w_out, chunk, nchunks, nsm);
+            if (f64eig) {
+                // FP64 eigenpairs, T and wbar, then the update from them
+                constexpr size_t rs = sizeof(double) * (3 * K * K + 7 * K + 32);
+                if ((e = cudaFuncSetAttribute(k_eig_refine<K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                              (int)rs)) != cudaSuccess)
+                    break;
+                const int64_t rb = std::min<int64_t>(b1 - b0, (int64_t)nsm * 2);
+                lg_count_launch();
+                lg_stage_mark(ctx, 3, false);
+                k_eig_refine<K><<<(unsigned)rb, kTR, rs, ctx->stream>>>(b0, b1, (double)(K - 1) / ctx->params.inflation,
+                                                                         ctx->d_mA.p, ctx->d_mX.p, ctx->d_mg.p);
+                lg_stage_mark(ctx, 3, true);
+                if ((e = cudaGetLastError()) != cudaSuccess) break;
+            }
+            // the update from T and wbar
+            lg_stage_mark(ctx, 2, false);
+            e = launch_stage<K, 3>(ctx, g, xb, axb, xa, axa, trans_out, w_out, chunk, nchunks, nsm);
+            lg_stage_mark(ctx, 2, true);
             if (e == cudaSuccess) e = lg_sink_columns(ctx, b0, b1);
         }
         ctx->win0 = w0;

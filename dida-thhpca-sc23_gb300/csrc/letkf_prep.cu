@@ -313,8 +313,8 @@ cudaError_t lg_launch_obs_prepare(letkf_ctx *ctx, const LgGrid &g, const double 
     k_obs_prepare<<<blocks, 256, 0, ctx->stream>>>(
         g, prm, xb, axb, nobs, olat, olon, oph, olev, ovar, oyo, orinv, ctx->d_yb.p, ctx->d_dep.p,
         ctx->d_rinvf.p, ctx->d_os.p, ctx->d_oc.p, ctx->d_oyr.p, ctx->d_oxyz.p, ctx->d_obucket.p,
-        ctx->params.precision == LETKF_PREC_MIXED ? ctx->d_ys32.p : nullptr,
-        ctx->params.precision == LETKF_PREC_MIXED ? ctx->d_oef.p : nullptr,
+        lg_is_mixed(ctx->params.precision) ? ctx->d_ys32.p : nullptr,
+        lg_is_mixed(ctx->params.precision) ? ctx->d_oef.p : nullptr,
         ctx->nblat, ctx->nblon, ctx->cell_lat, ctx->cell_lon, ctx->d_status.p, mode);
     return cudaGetLastError();
 }

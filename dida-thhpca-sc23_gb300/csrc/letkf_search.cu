@@ -232,7 +232,7 @@ __device__ __forceinline__ void write_entry(int o, long long at, const CubeGeo &
                                             const LgParams &prm, const LgListMeta &lm,
                                             int32_t *__restrict__ lidx, double *__restrict__ lrloc)
 {
-    if (prm.precision == LETKF_PREC_MIXED) {
+    if (lg_is_mixed(prm.precision)) {
         // the selection used the reference's double formula where it mattered
         const float scale = (float)(LG_EARTH_A / prm.local_dist);
         const float4 q = geo.xyz[o];
@@ -261,7 +261,7 @@ __device__ __forceinline__ void write_entries4(const int *o4, long long at, cons
                                                const LgParams &prm, const LgListMeta &lm,
                                                int32_t *__restrict__ lidx, double *__restrict__ lrloc)
 {
-    if (prm.precision == LETKF_PREC_MIXED) {
+    if (lg_is_mixed(prm.precision)) {
         const float scale = (float)(LG_EARTH_A / prm.local_dist);
         float4 q[4];
         float ef[4];

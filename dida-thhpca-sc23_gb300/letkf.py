@@ -29,6 +29,7 @@ LETKF_HOST_PTRS = 0
 LETKF_DEVICE_PTRS = 1
 LETKF_PREC_FP64 = 0
 LETKF_PREC_MIXED = 1
+LETKF_PREC_MIXED_F64EIG = 2
 
 ERROR_NAMES = {
     LETKF_ERR_INVALID: "LETKF_ERR_INVALID", LETKF_ERR_CUDA: "LETKF_ERR_CUDA",
@@ -47,7 +48,7 @@ EXPORTED = [
     "letkf_batch_destroy", "letkf_gpu_set_list_limit", "letkf_gpu_set_cube_range", "letkf_gpu_run_members",
     "letkf_struct_atm2endnn", "letkf_struct_endnn2atm", "letkf_struct_atm2endnn_a", "letkf_struct_endnn2atm_a",
     "letkf_gpu_obs_from_records", "letkf_gpu_obs_regular", "letkf_gpu_set_wait_limit",
-    "letkf_init_gpu_", "letkf_set_obs_gpu_", "letkf_run_gpu_", "letkf_final_gpu_",
+    "letkf_gpu_local_obs_cubes", "letkf_init_gpu_", "letkf_set_obs_gpu_", "letkf_run_gpu_", "letkf_final_gpu_",
 ]
 
 
@@ -97,10 +98,13 @@ class Stats(C.Structure):
         ("ms_core", C.c_double), ("ms_d2h", C.c_double), ("ms_total", C.c_double),
         ("sum_sweeps", C.c_int64), ("n_ill_conditioned", C.c_int64),
         ("sched_chunk", C.c_int32), ("n_windows", C.c_int32),
+        ("ms_stage", C.c_double * 4),
     ]
 
     def as_dict(self):
-        return {f: getattr(self, f) for f, _ in self._fields_}
+        d = {f: getattr(self, f) for f, _ in self._fields_}
+        d["ms_stage"] = list(self.ms_stage)
+        return d
 
 
 _lib = None
@@ -123,6 +127,7 @@ def load_library(path: str = LIB_PATH):
     L.letkf_gpu_synchronize.argtypes = [vp]
     L.letkf_gpu_obs_operator.argtypes = [vp, vp, vp, C.POINTER(Obs), vp, vp]
     L.letkf_gpu_local_obs.argtypes = [vp, vp, vp, vp]
+    L.letkf_gpu_local_obs_cubes.argtypes = [vp, vp, i64, vp, vp, vp]
     L.letkf_gpu_last_trans.argtypes = [vp, vp, i64, vp, vp]
     L.letkf_gpu_core_batch.argtypes = [vp, i64, vp, vp, vp, vp, vp, vp, vp]
     L.letkf_gpu_get_stats.argtypes = [vp, C.POINTER(Stats)]
@@ -441,6 +446,18 @@ class LetkfGPU:
         idx = np.empty(max(int(off[-1]), 1), dtype=np.int32)
         rloc = np.empty(max(int(off[-1]), 1))
         self._check(self.L.letkf_gpu_local_obs(self.h, _ptr(off), _ptr(idx), _ptr(rloc)), "local_obs")
+        return off, idx[:off[-1]], rloc[:off[-1]]
+
+    def local_obs_cubes(self, cubes):
+        """(offsets, idx, rloc) of the listed cubes only, packed in their order."""
+        cubes = np.ascontiguousarray(cubes, dtype=np.int64)
+        off = np.zeros(cubes.size + 1, dtype=np.int64)
+        self._check(self.L.letkf_gpu_local_obs_cubes(self.h, _ptr(cubes), cubes.size, _ptr(off), None, None),
+                    "local_obs_cubes")
+        idx = np.empty(max(int(off[-1]), 1), dtype=np.int32)
+        rloc = np.empty(max(int(off[-1]), 1))
+        self._check(self.L.letkf_gpu_local_obs_cubes(self.h, _ptr(cubes), cubes.size, _ptr(off), _ptr(idx),
+                                                     _ptr(rloc)), "local_obs_cubes")
         return off, idx[:off[-1]], rloc[:off[-1]]
 
     def last_trans(self, cubes):

@@ -296,11 +296,13 @@ def _members_on_device(basis, coef2d, device, chunk_cols=1 << 16):
 
 
 def generate(name, res_deg, nz, k, nobs, loc_dist_km, inflation, seed,
-             boxes=(), box_factor=1.0, lmax_noise=12, noise_len_km=2000.0, device=None):
+             boxes=(), box_factor=1.0, lmax_noise=12, noise_len_km=2000.0, device=None, members=True):
     """Build one analysis instance (see the module docstring for the recipe).
     With a torch `device` the members xb are built there (a torch float64
     tensor [ncol][n][k]) from the same random draws, for ensembles larger than
-    host memory; everything else stays on the host."""
+    host memory; everything else stays on the host.  members=False draws the
+    same random numbers but leaves xb None (the grid, mean and observations
+    are those of the full instance: for checks of the observation lists)."""
     rng = np.random.Generator(np.random.PCG64(seed))
     glat, glon = make_grid(res_deg)
     hyai, hybi = hybrid_coefficients(nz)
@@ -318,7 +320,9 @@ def generate(name, res_deg, nz, k, nobs, loc_dist_km, inflation, seed,
     coef = rng.standard_normal((basis_t.shape[0], n, k))
     coef -= coef.mean(axis=2, keepdims=True)      # sample mean removed (linear)
     coef *= spec[:, None, None] * std[None, :, None]
-    if device is None:
+    if not members:
+        xb = None
+    elif device is None:
         xb = (basis_t.T @ coef.reshape(basis_t.shape[0], n * k)).reshape(ncol, n, k)
     else:
         xb = _members_on_device(basis, coef.reshape(basis_t.shape[0], n * k), device).view(ncol, n, k)
@@ -342,17 +346,18 @@ INSTANCES_3 = [  # (res_deg, k, nobs, radius_km, inflation)
 
 
 def config(cfg: int, instance: int = 0, nobs: int | None = None, res_deg: float | None = None,
-           device=None):
+           device=None, members: bool = True):
     """Workload of a benchmark configuration (0, 1, 2, the instances of 3, and
     4).  nobs overrides the observation count and res_deg the grid spacing
     (smaller cases with the same observation density when both are scaled,
     e.g. for profiling).  device: build the members on this torch device
-    (configuration 4's ensemble, 103 GB in float64, is built only there)."""
+    (configuration 4's ensemble, 103 GB in float64, is built only there).
+    members=False: the same instance without its members (see generate)."""
     if cfg == 4:
         res = res_deg or 0.25
         no = nobs if nobs is not None else int(round(4_000_000 * (0.25 / res) ** 2))
         return generate("cfg4", res, 32, 128, no, 250.0, 1.05, 4000, boxes=CLUSTERS_4,
-                        box_factor=10.0, device=device)
+                        box_factor=10.0, device=device, members=members)
     seed = 1000 * cfg + instance
     if cfg == 0:
         return generate("cfg0", res_deg or 2.0, 32, 32, nobs or 20_000, 500.0, 1.1, seed)

@@ -51,7 +51,16 @@ extern "C" {
 /* letkf_params.precision (the reference's computing_precision knob,
  * da_namelist_mod.F90:49, selects the core's arithmetic the same way)       */
 #define LETKF_PREC_FP64    0   /* FP64 throughout                                  */
-#define LETKF_PREC_MIXED   1   /* BF16 hi/lo tensor-core products, FP64 eigensolve */
+#define LETKF_PREC_MIXED   1   /* BF16 hi/lo tensor-core products for A, g and the
+                                  update (FP32 accumulation); FP32 Jacobi
+                                  eigenpairs and FP32 T; wbar in FP32 with one
+                                  FP64-residual refinement step; FP64 mean
+                                  increment                                        */
+#define LETKF_PREC_MIXED_F64EIG 2 /* the same tensor-core products, with the FP32
+                                  Jacobi eigenpairs refined to FP64 (one
+                                  Ogita-Aishima step on FP64 residuals), FP64
+                                  eigenvalues, 1/sqrt(lambda), T and wbar, and
+                                  the FP64 mean increment; ensembles of 64      */
 
 typedef struct letkf_ctx letkf_ctx;
 
@@ -130,6 +139,11 @@ typedef struct letkf_stats {
     int32_t sched_chunk;       /* mixed form: cubes per work-queue chunk (0: default 16) */
     int32_t n_windows;         /* consecutive cube windows the run was split into
                                   (1 when every local list fit the list pool)        */
+    double ms_stage[4];        /* mixed forms, k = 64 (the staged core): device-event
+                                  times of the A-build, eigensolve, update and
+                                  (LETKF_PREC_MIXED_F64EIG) FP64 refinement
+                                  launches, each summed over the run's blocks of
+                                  cubes (0 for other forms and inside a graph)       */
 } letkf_stats;
 
 /* The lat x lon blocks of a DA group of nranks MPI ranks: MPI_Dims_create(
@@ -279,6 +293,13 @@ int letkf_gpu_obs_operator(letkf_ctx *ctx, const double *xb, const double *axb,
  * canonical order and their localization weights, packed by cube
  * (offsets[cube] = start; ncubes+1 entries).  Host pointers.                */
 int letkf_gpu_local_obs(letkf_ctx *ctx, int64_t *offsets, int32_t *idx, double *rloc);
+
+/* The same lists for the n cubes listed in `cubes` only, packed in that
+ * order (offsets has n+1 entries; idx and rloc may be NULL): for checking a
+ * sample of a large grid's lists without copying every list to the host.
+ * Host pointers.  No counterpart in the reference.                          */
+int letkf_gpu_local_obs_cubes(letkf_ctx *ctx, const int64_t *cubes, int64_t n, int64_t *offsets,
+                              int32_t *idx, double *rloc);
 
 /* Transform matrices of the last run for the listed cubes: trans (ens x ens,
  * column-major, trans(i,j) + w(i) as letkf_core returns it) and w.          */

@@ -751,6 +751,53 @@ int64_t orc_local_obs(const orc_config *cfg, const orc_obs *obs,
     return total;
 }
 
+/* The lists of the selected cubes only (same selection and order as
+ * orc_local_obs, letkf_yb.F90:3-133), packed in the order of `cubes`:
+ * offsets[n + 1]; idx/rloc may be NULL for counts only.  The observation
+ * index is built once for all of them.  Returns the total, or -1 when it
+ * exceeds cap.                                                              */
+int64_t orc_local_obs_cubes(const orc_config *cfg, const orc_obs *obs, int64_t n, const int64_t *cubes,
+                            int64_t *offsets, int32_t *idx, double *rloc, int64_t cap)
+{
+    int64_t i, total;
+    obs_index ix;
+    obs_index_build(cfg, obs, &ix);
+#pragma omp parallel
+    {
+        int32_t *buf = (int32_t *)malloc(sizeof(int32_t) * (obs->nobs + 1));
+#pragma omp for schedule(dynamic, 4)
+        for (i = 0; i < n; i++) {
+            int sj, ej, si, ei;
+            orc_cube_bounds(cfg, cubes[i], &sj, &ej, &si, &ei);
+            offsets[i + 1] = cube_list(cfg, obs, &ix, sj, ej, si, ei, NULL, NULL, buf);
+        }
+        free(buf);
+    }
+    offsets[0] = 0;
+    for (i = 0; i < n; i++) offsets[i + 1] += offsets[i];
+    total = offsets[n];
+    if (idx != NULL) {
+        if (total > cap) {
+            obs_index_free(&ix);
+            return -1;
+        }
+#pragma omp parallel
+        {
+            int32_t *buf = (int32_t *)malloc(sizeof(int32_t) * (obs->nobs + 1));
+#pragma omp for schedule(dynamic, 4)
+            for (i = 0; i < n; i++) {
+                int sj, ej, si, ei;
+                orc_cube_bounds(cfg, cubes[i], &sj, &ej, &si, &ei);
+                cube_list(cfg, obs, &ix, sj, ej, si, ei, idx + offsets[i], rloc ? rloc + offsets[i] : NULL,
+                          buf);
+            }
+            free(buf);
+        }
+    }
+    obs_index_free(&ix);
+    return total;
+}
+
 /* ---- eigensolver --------------------------------------------------------- */
 
 /* Cyclic Jacobi for a symmetric matrix (Golub & Van Loan, Alg. 8.5.3, with

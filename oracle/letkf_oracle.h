@@ -104,6 +104,12 @@ void orc_cube_center(const orc_config *cfg, int sj, int ej, int si, int ei,
 int64_t orc_local_obs(const orc_config *cfg, const orc_obs *obs,
                       int64_t *offsets, int32_t *idx, double *rloc, int64_t cap);
 
+/* Local lists of the n cubes listed in `cubes`, packed in that order
+ * (offsets has n+1 entries; idx == NULL: offsets only).  Returns the total,
+ * or a negative value if it exceeds cap.                                    */
+int64_t orc_local_obs_cubes(const orc_config *cfg, const orc_obs *obs, int64_t n, const int64_t *cubes,
+                            int64_t *offsets, int32_t *idx, double *rloc, int64_t cap);
+
 /* Local list for one point.  Returns nobsl. */
 int orc_local_obs_point(const orc_config *cfg, const orc_obs *obs, double clat, double clon,
                         int32_t *idx, double *rloc);

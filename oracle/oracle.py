@@ -140,6 +140,22 @@ class Oracle:
         assert total2 == total
         return off, idx[:total], rloc[:total]
 
+    def local_obs_cubes(self, cubes):
+        """(offsets, idx, rloc) of the listed cubes only, packed in their order."""
+        cubes = np.ascontiguousarray(cubes, dtype=np.int64)
+        L = lib()
+        L.orc_local_obs_cubes.restype = C.c_int64
+        off = np.zeros(cubes.size + 1, dtype=np.int64)
+        total = L.orc_local_obs_cubes(C.byref(self.cfg), C.byref(self.obs), C.c_int64(cubes.size),
+                                      _p(cubes, C.c_int64), _p(off, C.c_int64), None, None, C.c_int64(0))
+        idx = np.empty(max(total, 1), dtype=np.int32)
+        rloc = np.empty(max(total, 1))
+        total2 = L.orc_local_obs_cubes(C.byref(self.cfg), C.byref(self.obs), C.c_int64(cubes.size),
+                                       _p(cubes, C.c_int64), _p(off, C.c_int64), _p(idx, C.c_int32),
+                                       _p(rloc, C.c_double), C.c_int64(idx.size))
+        assert total2 == total
+        return off, idx[:total], rloc[:total]
+
     def run(self):
         xa = np.empty_like(self.xb)
         axa = np.empty_like(self.axb)

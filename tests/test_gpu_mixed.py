@@ -134,3 +134,61 @@ def test_mixed_wait_timeout_leaves_context_usable(letkf, synthetic, k):
     xa, axa = ctx.run(w.xb, w.axb, w.obs)
     assert np.array_equal(xa, xa_ref) and np.array_equal(axa, axa_ref)
     ctx.close()
+
+
+def test_f64eig_small_case_vs_oracle(letkf, synthetic):
+    # LETKF_PREC_MIXED_F64EIG: the FP32 Jacobi eigenpairs refined to FP64 (one
+    # Ogita-Aishima step), FP64 T and wbar, on a small k = 64 case
+    w = synthetic.small_case(nlat=12, nlon=24, nz=4, k=64, nobs=900, loc_dist_km=900.0, seed=164)
+    ctx = letkf.LetkfGPU.from_workload(w, precision=letkf.LETKF_PREC_MIXED_F64EIG)
+    xa, axa = ctx.run(w.xb, w.axb, w.obs)
+    orc = O.Oracle(w)
+    off_g, idx_g, _ = ctx.local_obs()
+    off_o, idx_o, _ = orc.local_obs()
+    assert np.array_equal(off_g, off_o) and np.array_equal(idx_g, idx_o)
+    xa_o, axa_o = orc.run()
+    assert_mixed(xa, axa, xa_o, axa_o, w)
+    st = ctx.stats()
+    assert st["precision"] == letkf.LETKF_PREC_MIXED_F64EIG and st["ms_stage"][3] > 0.0
+
+
+def test_f64eig_transforms_vs_fp64(letkf, synthetic):
+    # T and wbar of the F64EIG form against the FP64 form: the remaining
+    # difference is the BF16 hi/lo representation of A and g, so both forms
+    # meet the same bound, and the F64EIG form's T is no farther from FP64 than
+    # the FP32-eigensolve form's by more than FP32 rounding of T
+    w = synthetic.small_case(nlat=10, nlon=20, nz=3, k=64, nobs=1500, loc_dist_km=1000.0, seed=31)
+    out = {}
+    for nm, prec in (("fp64", letkf.LETKF_PREC_FP64), ("mixed", letkf.LETKF_PREC_MIXED),
+                     ("f64eig", letkf.LETKF_PREC_MIXED_F64EIG)):
+        c = letkf.LetkfGPU.from_workload(w, precision=prec)
+        c.keep_trans(True)
+        c.run(w.xb, w.axb, w.obs)
+        out[nm] = c.last_trans(np.arange(c.ncubes))
+        c.close()
+    t64, w64 = out["fp64"]
+    for nm in ("mixed", "f64eig"):
+        t, wv = out[nm]
+        assert np.max(np.abs(t - t64)) <= 1e-4 * np.abs(t64).max(), nm
+        assert np.max(np.abs(wv - w64)) <= 1e-3 * np.abs(w64).max(), nm
+    d_mixed = np.max(np.abs(out["mixed"][0] - t64))
+    d_f64 = np.max(np.abs(out["f64eig"][0] - t64))
+    assert d_f64 <= 1.1 * d_mixed + 1e-6 * np.abs(t64).max(), (d_f64, d_mixed)
+
+
+def test_f64eig_config1_vs_fp64(letkf, synthetic):
+    w = synthetic.config(1)
+    fp = letkf.LetkfGPU.from_workload(w)
+    mx = letkf.LetkfGPU.from_workload(w, precision=letkf.LETKF_PREC_MIXED_F64EIG)
+    xa64, axa64 = fp.run(w.xb, w.axb, w.obs)
+    xa16, axa16 = mx.run(w.xb, w.axb, w.obs)
+    errs = assert_mixed(xa16, axa16, xa64, axa64, w)
+    assert mx.stats()["n_not_converged"] == 0
+    print("config1 mixed (FP64 eigenpairs) vs fp64:", errs)
+
+
+def test_f64eig_needs_ensemble_64(letkf, synthetic):
+    w = synthetic.small_case(nlat=8, nlon=16, nz=2, k=32, nobs=50, seed=3)
+    with pytest.raises(letkf.LetkfError) as ei:
+        letkf.LetkfGPU.from_workload(w, precision=letkf.LETKF_PREC_MIXED_F64EIG)
+    assert ei.value.code == letkf.LETKF_ERR_UNSUPPORTED

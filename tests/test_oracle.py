@@ -215,6 +215,34 @@ def test_local_search_equals_brute_force_scan():
         assert np.array_equal(rloc[off[cube]:off[cube + 1]], e_gc), cube
 
 
+def test_local_obs_cubes_equals_whole_grid_lists():
+    # the selected-cubes search (used to check samples of large grids) packs
+    # the same lists as the whole-grid search, in the order asked for
+    synthetic = pkg("synthetic")
+    w = synthetic.small_case(nlat=12, nlon=24, nz=2, k=4, nobs=900, loc_dist_km=800.0, seed=9)
+    w.max_obs = 40
+    orc = O.Oracle(w)
+    off, idx, rloc = orc.local_obs()
+    cubes = np.array([5, 0, 287, 5, 131, 17], dtype=np.int64)
+    off_s, idx_s, rloc_s = orc.local_obs_cubes(cubes)
+    for n, c in enumerate(cubes):
+        assert np.array_equal(idx_s[off_s[n]:off_s[n + 1]], idx[off[c]:off[c + 1]])
+        assert np.array_equal(rloc_s[off_s[n]:off_s[n + 1]], rloc[off[c]:off[c + 1]])
+
+
+def test_instance_without_members_keeps_the_draws():
+    # members=False draws the same random numbers: same grid, mean and
+    # observations as the full instance (configuration 4's recipe on a
+    # 2-degree grid with its observation density)
+    synthetic = pkg("synthetic")
+    full = synthetic.config(4, res_deg=2.0)
+    bare = synthetic.config(4, res_deg=2.0, members=False)
+    assert bare.xb is None and full.xb is not None
+    assert np.array_equal(full.axb, bare.axb)
+    for key in full.obs:
+        assert np.array_equal(full.obs[key], bare.obs[key]), key
+
+
 # ---- oracle vs the golden fixtures ---------------------------------------------------
 @pytest.mark.parametrize("name", GOLDEN_CASES)
 def test_oracle_matches_golden(name):
