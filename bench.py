@@ -53,6 +53,8 @@ def parse_args():
                     help="observation count override (configuration 4)")
     ap.add_argument("--grid-res", type=float, default=None,
                     help="grid spacing override (same obs density; profiling cases)")
+    ap.add_argument("--no-extra-configs", action="store_true",
+                    help="leave out the configuration 3 and 4 records of the default run")
     return ap.parse_args()
 
 
@@ -538,6 +540,26 @@ def run_ours(args, rank, world, local_rank):
     h2d = sum(a.nbytes for a in (xbn, axbn)) + sum(a.nbytes for a in obs_h.values())
     d2h = xan.nbytes + axan.nbytes
     e2e_vs_device = float(np.abs(xan - outs[head][0].cpu().numpy()).max())
+    # the same call with ordinary (pageable) host arrays, as a Fortran caller
+    # of the drop-in passes them
+    xb_p, axb_p = np.array(w.xb, copy=True), np.array(w.axb, copy=True)
+    xa_p, axa_p = np.empty_like(xb_p), np.empty_like(axb_p)
+    obs_p = letkf.ObsArrays({key: np.array(o[key], copy=True) for key in obs_h})
+    ctx.run(xb_p, axb_p, obs_p, xa_p, axa_p)
+    torch.cuda.synchronize()
+    pg_ms_steps = []
+    for _ in range(e2e_steps):
+        f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        f0.record(stream)
+        ctx.run(xb_p, axb_p, obs_p, xa_p, axa_p)
+        f1.record(stream)
+        torch.cuda.synchronize()
+        pg_ms_steps.append(f0.elapsed_time(f1))
+    ms_pg = statistics.median(pg_ms_steps)
+    if dist:
+        ms_pg = _max_over_ranks(torch, tdist, dev, ms_pg)
+    pg_vs_device = float(np.abs(xa_p - outs[head][0].cpu().numpy()).max())
+    del xb_p, xa_p
 
     if rank != 0:
         return
@@ -604,6 +626,11 @@ def run_ours(args, rank, world, local_rank):
                 "ms_per_step_median": ms_e2e, "ms_steps": e2e_ms_steps,
                 "host_memory": "page-locked (pinned) host buffers",
                 "max_abs_diff_vs_device_run": e2e_vs_device},
+        "e2e_pageable": {"value": whole_job_columns_per_s(world, w.ncol, ms_pg), "unit": "columns/s",
+                         "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                         "ms_per_step_median": ms_pg, "ms_steps": pg_ms_steps,
+                         "host_memory": "ordinary pageable host arrays (numpy), as the Fortran drop-in passes",
+                         "max_abs_diff_vs_device_run": pg_vs_device},
         "gpu_launches": res[head][3],
         "roofline": roof,
         "stages_ms": {"obs_H_buckets": statistics.mean(s[0] for s in stages),
@@ -640,7 +667,9 @@ def run_ours(args, rank, world, local_rank):
     if world == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(w, args.cpu_seconds, f"config{args.config}")
         line["cpu_baseline"]["cpu"] = cpu_model()
-    print(json.dumps(line), flush=True)
+    for ctx in forms.values():
+        ctx.close()
+    return line
 
 
 # ---------------------------------------------------------------------------
@@ -778,7 +807,7 @@ def run_ours_c4(args, rank, world, local_rank):
         "cpu_baseline_note": "the oracle needs the ensemble on the host (103 GB); the CPU figure "
                              "is the 1-degree configuration's",
     }
-    print(json.dumps(line), flush=True)
+    return line
 
 # ---------------------------------------------------------------------------
 def run_ours_batch(args, rank, world, local_rank):
@@ -859,9 +888,11 @@ def run_ours_batch(args, rank, world, local_rank):
     ncol = sum(w.ncol for w in ws)
     value = whole_job_columns_per_s(world, ncol, ms)
     # end to end: each step copies every instance's inputs in from pinned host
-    # memory, replays the graph and copies every analysis out
+    # memory, replays the graph and copies every analysis out (left out of
+    # the companion record of the default run: 47 GB of pinned host memory)
+    sub = getattr(args, "sub_record", False)
     host_in, host_out = [], []
-    for w, b in zip(ws, bufs):
+    for w, b in zip(ws, bufs if not sub else []):
         pin = lambda a: torch.from_numpy(np.ascontiguousarray(a)).pin_memory()
         host_in.append([pin(w.xb), pin(w.axb)] + [pin(w.obs[k]) for k in keys])
         host_out.append([torch.empty(b[3].shape, dtype=torch.float64, pin_memory=True),
@@ -870,23 +901,25 @@ def run_ours_batch(args, rank, world, local_rank):
     h2d = sum(t.numel() * t.element_size() for hs in host_in for t in hs)
     d2h = sum(t.numel() * t.element_size() for hs in host_out for t in hs)
     e2e_steps = max(1, min(args.steps, 3))
-    torch.cuda.synchronize()
-    e0.record(stream)
-    with torch.cuda.stream(stream):
-        for _ in range(e2e_steps):
-            for hs, ds in zip(host_in, dev_in):
-                for h, d in zip(hs, ds):
-                    d.copy_(h, non_blocking=True)
-            batch.launch(sh)
-            for hs, b in zip(host_out, bufs):
-                hs[0].copy_(b[3], non_blocking=True)
-                hs[1].copy_(b[4], non_blocking=True)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    batch.sync(sh)
-    ms_e2e = e0.elapsed_time(e1) / e2e_steps
-    if world > 1:
-        ms_e2e = _max_over_ranks(torch, tdist, dev, ms_e2e)
+    ms_e2e = None
+    if not sub:
+        torch.cuda.synchronize()
+        e0.record(stream)
+        with torch.cuda.stream(stream):
+            for _ in range(e2e_steps):
+                for hs, ds in zip(host_in, dev_in):
+                    for h, d in zip(hs, ds):
+                        d.copy_(h, non_blocking=True)
+                batch.launch(sh)
+                for hs, b in zip(host_out, bufs):
+                    hs[0].copy_(b[3], non_blocking=True)
+                    hs[1].copy_(b[4], non_blocking=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        batch.sync(sh)
+        ms_e2e = e0.elapsed_time(e1) / e2e_steps
+        if world > 1:
+            ms_e2e = _max_over_ranks(torch, tdist, dev, ms_e2e)
     if rank != 0:
         return
     peaks = measured_peaks()
@@ -926,8 +959,9 @@ def run_ours_batch(args, rank, world, local_rank):
                    "l2": "inputs larger than L2", "parallelism": f"replicas x{world}"},
         "sequential_ms": ms_seq,
         "graph_speedup_vs_sequential": ms_seq / ms,
-        "e2e": {"value": whole_job_columns_per_s(world, ncol, ms_e2e), "unit": "columns/s",
-                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "e2e": (None if ms_e2e is None else
+                {"value": whole_job_columns_per_s(world, ncol, ms_e2e), "unit": "columns/s",
+                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}),
         "gpu_launches": launches,
         "roofline": roof,
         "clocks": clk,
@@ -936,8 +970,36 @@ def run_ours_batch(args, rank, world, local_rank):
     if not args.no_cpu_baseline and world == 1:
         line["cpu_baseline"] = cpu_baseline(ws[4], args.cpu_seconds, "config3 instance 4 (1 deg, k=64)")
         line["cpu_baseline"]["cpu"] = cpu_model()
-    print(json.dumps(line), flush=True)
     batch.close()
+    for ctx in ctxs:
+        ctx.close()
+    return line
+
+
+def extra_configs(args, rank, world, local_rank):
+    """Records of the batching form (configuration 3) and of the largest
+    configuration (4) beside the 1-degree headline, with fewer steps: each is
+    its own workload, so these are companion records, not part of `value`."""
+    import gc
+    import torch
+    out = {}
+    for cfg, steps, warmup in ((3, min(args.steps, 5), min(args.warmup, 2)), (4, 2, 1)):
+        gc.collect()
+        torch.cuda.empty_cache()
+        sub = argparse.Namespace(**vars(args))
+        sub.config, sub.steps, sub.warmup, sub.no_cpu_baseline, sub.sub_record = cfg, steps, warmup, True, True
+        t0 = time.perf_counter()
+        try:
+            rec = run_ours_batch(sub, rank, world, local_rank) if cfg == 3 else run_ours_c4(sub, rank, world,
+                                                                                             local_rank)
+        except Exception as ex:            # the headline stands without the companion record
+            rec = {"error": f"{type(ex).__name__}: {ex}"}
+        if rec is not None:
+            rec["wall_s"] = time.perf_counter() - t0
+            out[f"config{cfg}"] = rec
+    gc.collect()
+    torch.cuda.empty_cache()
+    return out
 
 
 def main():
@@ -955,11 +1017,16 @@ def main():
         tdist.init_process_group("nccl")
     try:
         if args.config == 3:
-            run_ours_batch(args, rank, world, local_rank)
+            line = run_ours_batch(args, rank, world, local_rank)
         elif args.config == 4:
-            run_ours_c4(args, rank, world, local_rank)
+            line = run_ours_c4(args, rank, world, local_rank)
         else:
-            run_ours(args, rank, world, local_rank)
+            line = run_ours(args, rank, world, local_rank)
+            if line is not None and world == 1 and args.config in (1, 2) and not args.no_extra_configs \
+                    and args.grid_res is None:
+                line.update(extra_configs(args, rank, world, local_rank))
+        if line is not None:
+            print(json.dumps(line), flush=True)
     finally:
         if world > 1:
             import torch.distributed as tdist

@@ -500,6 +500,12 @@ LgParams lg_params(letkf_ctx *ctx)
     p.spin_limit = ctx->wait_limit < 0 ? LG_MBAR_SPIN_LIMIT
                    : (uint32_t)(ctx->wait_limit < (int64_t)LG_MBAR_SPIN_LIMIT ? ctx->wait_limit
                                                                               : (int64_t)LG_MBAR_SPIN_LIMIT);
+    p.members = ctx->members_on ? 1 : 0;
+    p.gamma1 = ctx->members_g1;
+    p.gamma2 = ctx->members_g2;
+    p.polar = ctx->members_polar;
+    p.spb = ctx->members_spb;
+    p.spa = ctx->members_spa;
     return p;
 }
 
@@ -760,6 +766,8 @@ int lg_finish_run(letkf_ctx *ctx, const letkf_obs *obs, unsigned long long *cnt)
     int rc = read_status(ctx, st, cnt);
     if (rc) return rc;
     if (st & LG_ST_LIST_FULL) return set_err(ctx, LETKF_ERR_ALLOC, "local observation lists did not fit");
+    // a fused members run found a NaN background member
+    if (st & LG_ST_BAD_STATE) return set_err(ctx, LETKF_ERR_INVALID, "a background member is NaN");
     fill_stats(ctx, cnt);
     ctx->stats.ms_h2d = elapsed(ctx->ev[0], ctx->ev[1]);
     ctx->stats.ms_obs = elapsed(ctx->ev[1], ctx->ev[2]);

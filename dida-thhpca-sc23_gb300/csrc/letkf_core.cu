@@ -62,7 +62,9 @@ struct RowSrc {
     const float *brdi;
 };
 
-template <int K>
+// MEM: the fused members run (LgParams::members), a separate instantiation so
+// the plain analysis keeps its registers.
+template <int K, bool MEM = false>
 __global__ void __launch_bounds__(kT)
 k_core_fp64(LgGrid g, LgParams prm, RowSrc src, const int64_t *__restrict__ loff,
             const int32_t *__restrict__ lcnt, int64_t ncubes, const double *__restrict__ xb,
@@ -300,6 +302,32 @@ k_core_fp64(LgGrid g, LgParams prm, RowSrc src, const int64_t *__restrict__ loff
                     const int R = min(CH, re - r0 + 1);
                     for (int idx = tid; idx < R * K; idx += kT) S[idx] = xbc[(int64_t)r0 * K + idx];
                     __syncthreads();
+                    if constexpr (MEM) {
+                        // full members in: the row's mean (sum / real(ens),
+                        // module_da_parallel.F90:194-199) into scl, the sum of
+                        // squared perturbations into hco, perturbations into S
+                        if (tid < R) {
+                            const double fk = (double)(float)K;
+                            double s = 0.0;
+                            bool bad = false;
+                            for (int e = 0; e < K; e++) {
+                                s += S[tid * K + e];
+                                bad |= isnan(S[tid * K + e]);
+                            }
+                            if (bad) atomicOr(status, LG_ST_BAD_STATE);
+                            const double mb = s / fk;
+                            double q2 = 0.0;
+                            for (int e = 0; e < K; e++) {
+                                const double d = S[tid * K + e] - mb;
+                                q2 += d * d;
+                            }
+                            scl[tid] = mb;
+                            hco[tid] = q2;
+                        }
+                        __syncthreads();
+                        for (int idx = tid; idx < R * K; idx += kT) S[idx] -= scl[idx / K];
+                        __syncthreads();
+                    }
                     double out[C::NO];
 #pragma unroll
                     for (int q = 0; q < C::NO; q++) {
@@ -311,7 +339,7 @@ k_core_fp64(LgGrid g, LgParams prm, RowSrc src, const int64_t *__restrict__ loff
                             double a = 0.0;
 #pragma unroll 8
                             for (int i = 0; i < K; i++) a += W[i * K + e] * xr[i];
-                            out[q] = a + axb[c * n + r0 + rl];
+                            out[q] = a + (MEM ? scl[rl] : axb[c * n + r0 + rl]);
                         }
                     }
                     __syncthreads();
@@ -326,11 +354,40 @@ k_core_fp64(LgGrid g, LgParams prm, RowSrc src, const int64_t *__restrict__ loff
                         for (int e = 0; e < K; e++) m += S[tid * K + e];
                         m = m / K;
                         sd[tid] = m;
-                        axa[c * n + r0 + tid] = m;
+                        if (!MEM) axa[c * n + r0 + tid] = m;
                     }
                     __syncthreads();
-                    for (int idx = tid; idx < R * K; idx += kT)
-                        xac[(int64_t)r0 * K + idx] = S[idx] - sd[idx / K];
+                    if constexpr (!MEM) {
+                        for (int idx = tid; idx < R * K; idx += kT)
+                            xac[(int64_t)r0 * K + idx] = S[idx] - sd[idx / K];
+                    } else {
+                        // letkf2dnn (module_da_parallel.F90:214-258): the
+                        // blend, or the background where |lat| > polar, into
+                        // the member array; S keeps what the analysis spread sums
+                        const bool blend = fabs((double)g.glat[c % g.nlat]) <= prm.polar;
+                        for (int idx = tid; idx < R * K; idx += kT) {
+                            const int rl = idx / K;
+                            const double mb = scl[rl], ma = sd[rl];
+                            const double b = xbc[(int64_t)r0 * K + idx] - mb;
+                            double o;
+                            if (blend) {
+                                o = prm.gamma1 * (mb + b) + prm.gamma2 * (ma + (S[idx] - ma));
+                                S[idx] = o - ma;
+                            } else {
+                                o = b + mb;
+                                S[idx] = b;
+                            }
+                            xac[(int64_t)r0 * K + idx] = o;
+                        }
+                        __syncthreads();
+                        if (tid < R) {
+                            const double fk = (double)(float)K;
+                            double q2 = 0.0;
+                            for (int e = 0; e < K; e++) q2 += S[tid * K + e] * S[tid * K + e];
+                            prm.spb[c * n + r0 + tid] = sqrt(hco[tid] / fk);
+                            prm.spa[c * n + r0 + tid] = sqrt(q2 / fk);
+                        }
+                    }
                     __syncthreads();
                 }
                 }
@@ -434,18 +491,17 @@ cudaError_t launch_k(letkf_ctx *ctx, const LgGrid &g, const RowSrc &src, const i
                      double *xa, double *axa, double *trans_out, double *w_out)
 {
     const size_t smem = Cfg<K>::SMEM;
-    cudaError_t e = cudaFuncSetAttribute(k_core_fp64<K>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
+    LgParams prm = lg_params(ctx);
+    prm.cube0 = cube0;
+    auto kern = prm.members ? k_core_fp64<K, true> : k_core_fp64<K, false>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     if (ncubes <= cube0) return cudaSuccess;
     const int64_t nwin = ncubes - cube0;
     const unsigned blocks = (unsigned)(nwin < (1 << 30) ? nwin : (1 << 30));
-    LgParams prm = lg_params(ctx);
-    prm.cube0 = cube0;
     lg_count_launch();
-    k_core_fp64<K><<<blocks, kT, smem, ctx->stream>>>(g, prm, src, loff, lcnt, ncubes, xb,
-                                                      axb, xa, axa, trans_out, w_out,
-                                                      ctx->d_counters.p, ctx->d_status.p);
+    kern<<<blocks, kT, smem, ctx->stream>>>(g, prm, src, loff, lcnt, ncubes, xb, axb, xa, axa, trans_out, w_out,
+                                            ctx->d_counters.p, ctx->d_status.p);
     return cudaGetLastError();
 }
 

@@ -142,6 +142,17 @@ struct LgParams {
     int64_t cube0;        // first cube of the launch's window
     int count_only;       // search: only each cube's list length (LgListMeta::need)
     uint32_t spin_limit;  // polls of each bounded mbarrier wait of the mixed cores
+    // The caller's conversion around the analysis fused into it
+    // (letkf_gpu_run_members, run_da_parallel in module_da_parallel.F90:
+    // 163-261): the state input is the full members and there is no mean
+    // array; H reads the members as they are, the update forms each row's
+    // mean (sum / real(ens)) and perturbations as it reads the row, and writes
+    // the blended members gamma1 (axb + xb) + gamma2 (axa + xa) in place of the
+    // analysis perturbations (the background where |grid_lat| > polar) and the
+    // background and analysis spreads to spb, spa instead of the mean.
+    int members;
+    double gamma1, gamma2, polar;
+    double *spb, *spa;
 };
 
 // Lat-lon bucket grid of the observations.
@@ -311,6 +322,10 @@ struct letkf_ctx {
     // the search ran before the departures: its list entries hold sqrt(rloc)
     // only, and each core launch first completes them (lg_launch_list_efactor)
     bool lists_need_ef = false;
+    // a fused members run is in progress (LgParams::members and the blend)
+    bool members_on = false;
+    double members_g1 = 0.0, members_g2 = 1.0, members_polar = 90.0;
+    double *members_spb = nullptr, *members_spa = nullptr;
 };
 
 // ---------------------------------------------------------------------------

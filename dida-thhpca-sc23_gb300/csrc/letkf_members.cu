@@ -5,7 +5,12 @@
 // and turns the analysis back into full members with the relaxation-to-prior
 // blend and the background and analysis spreads (letkf2dnn, :214-258).
 // letkf_gpu_run_members runs the three steps on the GPU, so full members go in
-// and full members and spreads come out without a host pass over the state:
+// and full members and spreads come out without a host pass over the state.
+// With one column per cube, no overlap and no vertical blocks (and k <= 64 in
+// the mixed forms) the steps are fused into the analysis (LgParams::members):
+// H reads the members as they are, and the update kernels form each row's
+// mean and perturbations as they read the row and write the blended members
+// and both spreads, so no pass over the state is added.  Otherwise:
 //   k_members_split: per state row, the mean over members (sum / real(ens))
 //       and the perturbations; a NaN member stops the run (the reference
 //       prints and stops, :188-193);
@@ -125,6 +130,46 @@ extern "C" int letkf_gpu_run_members(letkf_ctx *ctx, const double *xb_in, const 
     LG_TRY(cudaEventRecord(ctx->ev[0], ctx->stream));
     rc = lg_reset_status(ctx);
     if (rc) return rc;
+    // The split and the blend fused into the analysis (H reads the members as
+    // they are, the update forms each row's mean and perturbations as it reads
+    // it and writes the blended members and both spreads): no state pass of
+    // its own.  Kept as separate passes where the update is not one pass over
+    // one column per cube (overlapped cubes, vertical blocks) and for the
+    // mixed form's wide core (k = 96, 128).
+    const bool fused = ctx->params.cube_n == 1 && ctx->params.overlap == 0 && !(ctx->params.vert_dist > 0.0) &&
+                       !(lg_is_mixed(ctx->params.precision) && k > 64);
+    if (fused) {
+        LG_TRY(ctx->d_spb.reserve(nmean));
+        LG_TRY(ctx->d_spa.reserve(nmean));
+        const double *din = xb_in;
+        double *dout = xa_out, *dsb = spread_b, *dsa = spread_a;
+        if (host) {
+            LG_TRY(ctx->d_xb.reserve(nstate));
+            LG_TRY(ctx->d_xa.reserve(nstate));
+            LG_TRY(cudaMemcpyAsync(ctx->d_xb.p, xb_in, sizeof(double) * nstate, cudaMemcpyHostToDevice, ctx->stream));
+            din = ctx->d_xb.p;
+            dout = ctx->d_xa.p;
+            dsb = ctx->d_spb.p;
+            dsa = ctx->d_spa.p;
+        }
+        ctx->members_on = true;
+        ctx->members_g1 = blend->gamma1;
+        ctx->members_g2 = blend->gamma2;
+        ctx->members_polar = blend->polar_lat_deg;
+        ctx->members_spb = dsb;
+        ctx->members_spa = dsa;
+        unsigned long long cnt[LG_CNT_N] = {};
+        rc = lg_run_analysis(ctx, obs, host, din, nullptr, dout, nullptr, cnt);
+        ctx->members_on = false;
+        ctx->members_spb = ctx->members_spa = nullptr;
+        if (rc) return rc;
+        if (host) {
+            LG_TRY(cudaMemcpyAsync(xa_out, dout, sizeof(double) * nstate, cudaMemcpyDeviceToHost, ctx->stream));
+            LG_TRY(cudaMemcpyAsync(spread_b, dsb, sizeof(double) * nmean, cudaMemcpyDeviceToHost, ctx->stream));
+            LG_TRY(cudaMemcpyAsync(spread_a, dsa, sizeof(double) * nmean, cudaMemcpyDeviceToHost, ctx->stream));
+        }
+        return lg_finish_run(ctx, obs, cnt);
+    }
     LG_TRY(ctx->d_xb.reserve(nstate));
     LG_TRY(ctx->d_axb.reserve(nmean));
     LG_TRY(ctx->d_xa.reserve(nstate));

@@ -90,6 +90,12 @@ struct MCfg {
     static constexpr size_t VEC = sizeof(double) * (4 * K + 128) + sizeof(float) * (2 * K) +
                                   3 * CH * (sizeof(int) + 2 * sizeof(float));
     static constexpr size_t SMEM = 1024 + AREA + B1 + VEC + 256;
+    // the A-build launch (ST 1) holds only the two tiles (then Dhh, Dlh) and
+    // the two gather stages: three CTAs per SM
+    static constexpr size_t AREA1 = 2 * (size_t)TILE;
+    static constexpr size_t SMEM1 = 1024 + AREA1 + B1 + VEC;
+    static_assert(2 * (size_t)K * (K + 1) * sizeof(float) <= AREA1, "Dhh and Dlh must fit over the tiles");
+    static_assert(AREA1 % 1024 == 0, "1024-byte aligned tiles");
     // gathered FP32 observation rows of one chunk; two stages: the first in B1
     // (free while A is built), the second after it in B1 or after the tiles
     static constexpr size_t STAGE = (size_t)CH * K * sizeof(float);
@@ -101,13 +107,66 @@ struct MCfg {
     static_assert(STAGE <= B1 && (STAGE1_IN_B1 || 2 * TILE + STAGE <= 49152), "gather stages must fit");
 };
 
+// The end of a fused members run for one state row (letkf2dnn,
+// module_da_parallel.F90:214-258), from the update's FP32 products v (member
+// mean meanf), the row's background mean mb and the FP64 mean increment:
+// axa = mb + incr + meanf; where |grid_lat| <= polar the members are
+// gamma1 (axb + xb) + gamma2 (axa + xa), taken as the FP64 row constant
+// gamma1 mb + gamma2 axa plus the FP32 perturbation part gamma1 xb + gamma2
+// xa (xb from the row's BF16 hi/lo tile, 2^-17 of xb), else the background
+// members themselves; spread_b = sqrt(sum xb^2 / ens) from the staging's
+// partial sums, spread_a = sqrt(sum (member - axa)^2 / ens).
+template <int K>
+__device__ __forceinline__ void members_epilogue(const LgParams &prm, const LgGrid &g, int64_t col, int r,
+                                                 const double *xin_row, const unsigned char *t_hi,
+                                                 const unsigned char *t_lo, double mb, double incr, float meanf,
+                                                 const float *v, const float *sqp, double *dst, int64_t row)
+{
+    const float fk = (float)K;
+    float sb = 0.0f;
+#pragma unroll
+    for (int c = 0; c < K / 8; c++) sb += sqp[c * 128 + r];
+    const double ma = mb + incr + lg_f2d_bits(meanf);
+    const bool blend = fabs((double)g.glat[col % g.nlat]) <= prm.polar;
+    if (!blend) {
+        for (int e = 0; e < K; e += 2)
+            *reinterpret_cast<double2 *>(dst + e) = *reinterpret_cast<const double2 *>(xin_row + e);
+        prm.spb[row] = sqrt((double)(sb / fk));
+        prm.spa[row] = sqrt((double)(sb / fk));
+        return;
+    }
+    const double cst = prm.gamma1 * mb + prm.gamma2 * ma;
+    const float df = (float)(cst - ma), g1 = (float)prm.gamma1, g2 = (float)prm.gamma2;
+    float sa = 0.0f;
+#pragma unroll
+    for (int c = 0; c < K / 8; c++) {
+        const uint4 h = *reinterpret_cast<const uint4 *>(t_hi + lg_sw128_offset(r, c));
+        const uint4 l = *reinterpret_cast<const uint4 *>(t_lo + lg_sw128_offset(r, c));
+        const uint32_t hw[4] = {h.x, h.y, h.z, h.w}, lw[4] = {l.x, l.y, l.z, l.w};
+#pragma unroll
+        for (int q = 0; q < 4; q++) {
+            // BF16 pairs: element 2q in the low half, 2q + 1 in the high half
+            const float b0 = __uint_as_float(hw[q] << 16) + __uint_as_float(lw[q] << 16);
+            const float b1 = __uint_as_float(hw[q] & 0xffff0000u) + __uint_as_float(lw[q] & 0xffff0000u);
+            const int e = 8 * c + 2 * q;
+            const float d0 = fmaf(g1, b0, g2 * (v[e] - meanf)), d1 = fmaf(g1, b1, g2 * (v[e + 1] - meanf));
+            sa = fmaf(df + d0, df + d0, fmaf(df + d1, df + d1, sa));
+            *reinterpret_cast<double2 *>(dst + e) = make_double2(cst + lg_f2d_bits(d0), cst + lg_f2d_bits(d1));
+        }
+    }
+    prm.spb[row] = sqrt((double)(sb / fk));
+    prm.spa[row] = sqrt((double)(sa / fk));
+}
+
 // ST selects the stages a launch runs: 0 all of them; 1 the A build only
 // (A without the diagonal shift and g to mA, mgv); 3 the update only, from T
 // (FP32, row-major, in the slot of X) and wbar (FP64, in the slot of g),
 // written by the eigensolve launch (k_eig_warp) or by the FP64 refinement
 // (k_eig_refine).  The intermediates are indexed by cube - prm.cube0.
-template <int K, int ST>
-__global__ void __launch_bounds__(kT, 2)
+// MEM: the fused members run (LgParams::members; stages 0 and 3), a separate
+// instantiation so the plain update keeps its registers.
+template <int K, int ST, bool MEM = false>
+__global__ void __launch_bounds__(kT, ST == 1 ? 3 : 2)
 k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32_t *__restrict__ lidx,
              const float2 *__restrict__ lmeta, const int *__restrict__ queue, int nchunks, int chunk,
              const int64_t *__restrict__ loff, const int32_t *__restrict__ lcnt, int64_t ncubes,
@@ -120,7 +179,7 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
     constexpr int CH = C::CH;
     extern __shared__ unsigned char smem_raw[];
     unsigned char *area = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    double *B1 = reinterpret_cast<double *>(area + C::AREA);
+    double *B1 = reinterpret_cast<double *>(area + (ST == 1 ? C::AREA1 : C::AREA));
     double *gv = B1 + K * K;
     double *wbar = gv + K;
     double *misc = wbar + K;       // 2K
@@ -200,6 +259,19 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
     long long ph_cyc[11] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
     long long ph_last = clock64();
 #endif
+    // 128-byte lines of the background state of cube cb's columns into L2
+    auto prefetch_state = [&](int64_t cb) {
+        const int bjc = (int)(cb % prm.nbj), bic = (int)(cb / prm.nbj);
+        const int sj = bjc * prm.cube_n, ej = min(sj + prm.cube_n - 1, g.nlat - 1);
+        const int si = bic * prm.cube_n, ei = min(si + prm.cube_n - 1, g.nlon - 1);
+        const int64_t lines = ((int64_t)g.n * K * (int64_t)sizeof(double) + 127) / 128;
+        for (int ii = si; ii <= ei; ii++)
+            for (int jj = sj; jj <= ej; jj++) {
+                const int64_t col = jj + (int64_t)g.nlat * ii;
+                const char *base = reinterpret_cast<const char *>(xb + col * g.n * K);
+                for (int64_t l = tid; l < lines; l += kT) asm volatile("prefetch.global.L2 [%0];" ::"l"(base + l * 128));
+            }
+    };
     // Work queue: chunks of `chunk` consecutive cubes (neighbours along
     // latitude, so a cube's eigenvectors are a good start for the next one),
     // taken heaviest first (queue order) by an atomic cursor.
@@ -454,8 +526,10 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
         if (ST == 3) {
             // T (row-major, FP32) and wbar (FP64) from the eigensolve or the
             // FP64 refinement launch, in the slots of X and g; the next cube's
-            // into L2
+            // T, wbar and state into L2 while this one is updated
+            if (!have_prev) prefetch_state(cube);
             if (cube + 1 < cube_end) {
+                prefetch_state(cube + 1);
                 constexpr int LA = K * K * 4 / 128, LG = (K * 8 + 127) / 128;
                 for (int l = tid; l < LA + LG; l += kT) {
                     const char *a = (l < LA) ? reinterpret_cast<const char *>(mX + (ci + 1) * K * K) + l * 128
@@ -618,19 +692,8 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
 
         // ---------------- phase 5: T in FP32 ------------------------------------------------
         // start moving this cube's background state into L2 for the update
-        {
-            const int bjc = (int)(cube % prm.nbj), bic = (int)(cube / prm.nbj);
-            const int sj = bjc * prm.cube_n, ej = min(sj + prm.cube_n - 1, g.nlat - 1);
-            const int si = bic * prm.cube_n, ei = min(si + prm.cube_n - 1, g.nlon - 1);
-            const int64_t lines = ((int64_t)g.n * K * (int64_t)sizeof(double) + 127) / 128;
-            for (int ii = si; ii <= ei; ii++)
-                for (int jj = sj; jj <= ej; jj++) {
-                    const int64_t col = jj + (int64_t)g.nlat * ii;
-                    const char *base = reinterpret_cast<const char *>(xb + col * g.n * K);
-                    for (int64_t l = tid; l < lines; l += kT)
-                        asm volatile("prefetch.global.L2 [%0];" ::"l"(base + l * 128));
-                }
-        }
+        // (stage 3 has no T to form first: it fetches a cube ahead instead)
+        if (ST != 3) prefetch_state(cube);
         // T = X diag(f) X^T only feeds the BF16 hi/lo tensor-core update (16
         // significant bits); FP32 eigenpairs give it to ~1e-7 relative.
         float *T32 = reinterpret_cast<float *>(B1);               // T, FP32, row-major
@@ -701,7 +764,14 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
         // FP64 mean increment xb^T wbar: partial sums over 8 members, [c][row],
         // after T in the space of A' (free in this phase)
         double *incp = reinterpret_cast<double *>(T32 + K * K);
+        // fused members run: squared perturbations summed over 8 members,
+        // [c][row], beside the mean-increment partials (k >= 48) or after the
+        // warm-start vectors (k = 32)
+        constexpr bool SQ_IN_B1 = 128 * K + 64 * K <= 4 * K * K;
+        float *sqp = SQ_IN_B1 ? reinterpret_cast<float *>(incp + 128 * (K / 8))
+                              : reinterpret_cast<float *>(area + 49152 + K * K * sizeof(float));
         static_assert(128 * K <= 4 * K * K, "mean-increment partials must fit beside T");
+        static_assert(SQ_IN_B1 || 49152 + (K * K + 16 * K) * sizeof(float) <= C::AREA, "members partials");
         const int bjc = (int)(cube % prm.nbj), bic = (int)(cube / prm.nbj);
         const int sj = bjc * prm.cube_n, ej = min(sj + prm.cube_n - 1, g.nlat - 1);
         const int si = bic * prm.cube_n, ei = min(si + prm.cube_n - 1, g.nlon - 1);
@@ -712,22 +782,63 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
                 double *xac = xa + col * n * K;
                 for (int r0 = 0; r0 < n; r0 += 128) {
                     const int R = min(128, n - r0);
-                    for (int t = tid; t < 128 * (K / 8); t += kT) {
-                        const int r = t / (K / 8), c = t % (K / 8);
-                        float v[8];
-                        if (r < R) {
+                    if constexpr (MEM) {
+                        // full members in: each row's mean (sum / real(ens),
+                        // module_da_parallel.F90:194-199) into inc, from
+                        // partial sums over 8 members.  A NaN member makes its
+                        // row's sum NaN; only such a row is checked member by
+                        // member (module_da_parallel.F90:188-193 tests isnan)
+                        for (int t = tid; t < 128 * (K / 8); t += kT) {
+                            const int r = t / (K / 8), c = t % (K / 8);
+                            if (r >= R) continue;
                             const double2 *src =
                                 reinterpret_cast<const double2 *>(xbc + (int64_t)(r0 + r) * K + 8 * c);
                             double s = 0.0;
 #pragma unroll
                             for (int j = 0; j < 4; j++) {
                                 const double2 q = src[j];
+                                s += q.x + q.y;
+                            }
+                            incp[c * 128 + r] = s;
+                        }
+                        __syncthreads();
+                        if (tid < R) {
+                            double s = 0.0;
+#pragma unroll
+                            for (int c = 0; c < K / 8; c++) s += incp[c * 128 + tid];
+                            inc[tid] = s / (double)(float)K;
+                            if (isnan(s)) {
+                                bool bad = false;
+                                for (int e = 0; e < K; e++) bad |= isnan(xbc[(int64_t)(r0 + tid) * K + e]);
+                                if (bad) atomicOr(status, LG_ST_BAD_STATE);
+                            }
+                        }
+                        __syncthreads();
+                    }
+                    for (int t = tid; t < 128 * (K / 8); t += kT) {
+                        const int r = t / (K / 8), c = t % (K / 8);
+                        float v[8];
+                        if (r < R) {
+                            const double2 *src =
+                                reinterpret_cast<const double2 *>(xbc + (int64_t)(r0 + r) * K + 8 * c);
+                            const double mb = MEM ? inc[r] : 0.0;
+                            double s = 0.0;
+                            float q2 = 0.0f;
+#pragma unroll
+                            for (int j = 0; j < 4; j++) {
+                                double2 q = src[j];
+                                if constexpr (MEM) {
+                                    q.x -= mb;
+                                    q.y -= mb;
+                                }
                                 v[2 * j] = (float)q.x;
                                 v[2 * j + 1] = (float)q.y;
+                                if constexpr (MEM) q2 = fmaf(v[2 * j], v[2 * j], fmaf(v[2 * j + 1], v[2 * j + 1], q2));
                                 s = fma(q.x, wbar[8 * c + 2 * j], s);
                                 s = fma(q.y, wbar[8 * c + 2 * j + 1], s);
                             }
                             incp[c * 128 + r] = s;
+                            if constexpr (MEM) sqp[c * 128 + r] = q2;
                         } else {
 #pragma unroll
                             for (int j = 0; j < 8; j++) v[j] = 0.0f;
@@ -780,12 +891,17 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
 #pragma unroll
                             for (int c = 1; c < K / 8; c++) incr += incp[c * 128 + r];
                             const int64_t row = col * n + r0 + r;
-                            axa[row] = axb[row] + incr + lg_f2d_bits(meanf);
                             double *dst = xac + (int64_t)(r0 + r) * K;
+                            if constexpr (!MEM) {
+                                axa[row] = axb[row] + incr + lg_f2d_bits(meanf);
 #pragma unroll
-                            for (int e = 0; e < K; e += 2)
-                                *reinterpret_cast<double2 *>(dst + e) =
-                                    make_double2(lg_f2d_bits(v[e] - meanf), lg_f2d_bits(v[e + 1] - meanf));
+                                for (int e = 0; e < K; e += 2)
+                                    *reinterpret_cast<double2 *>(dst + e) =
+                                        make_double2(lg_f2d_bits(v[e] - meanf), lg_f2d_bits(v[e + 1] - meanf));
+                            } else {
+                                members_epilogue<K>(prm, g, col, r, xbc + (int64_t)(r0 + r) * K, xa_hi, xa_lo,
+                                                    inc[r], incr, meanf, v, sqp, dst, row);
+                            }
                         }
                     }
                     lg_tc_fence_before();
@@ -1472,18 +1588,20 @@ template <int K, int ST>
 cudaError_t launch_stage(letkf_ctx *ctx, const LgGrid &g, const double *xb, const double *axb, double *xa,
                          double *axa, double *trans_out, double *w_out, int chunk, int nchunks, int nsm)
 {
-    const size_t smem = MCfg<K>::SMEM;
-    cudaError_t e = cudaFuncSetAttribute(k_core_mixed<K, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
+    const size_t smem = ST == 1 ? MCfg<K>::SMEM1 : MCfg<K>::SMEM;
+    auto kern = (ST != 1 && ctx->members_on) ? k_core_mixed<K, ST, ST != 1> : k_core_mixed<K, ST, false>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    e = cudaFuncSetAttribute(k_core_mixed<K, ST>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
     if (e != cudaSuccess) return e;
     int dev = 0, smem_sm = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
-    // two CTAs per SM when their shared memory fits (registers are capped at
-    // 128 per thread by the launch bounds, so two 256-thread CTAs fit)
-    const int per_sm = (2 * (smem + 1024) <= (size_t)smem_sm) ? 2 : 1;
+    // CTAs per SM: as many as the launch bounds give registers for (2; 3 for
+    // the A build) when their shared memory (plus the 1 KB the system keeps per
+    // CTA and the static barriers) fits
+    int per_sm = ST == 1 ? 3 : 2;
+    while (per_sm > 1 && (size_t)per_sm * (smem + 1024 + 64) > (size_t)smem_sm) per_sm--;
     // persistent grid: each CTA allocates its tensor memory once
     const int64_t want = (int64_t)nsm * per_sm;
     const unsigned blocks = (unsigned)(nchunks < want ? nchunks : want);
@@ -1491,7 +1609,7 @@ cudaError_t launch_stage(letkf_ctx *ctx, const LgGrid &g, const double *xb, cons
     e = cudaMemsetAsync(ctx->d_counters.p + LG_CNT_QUEUE, 0, sizeof(unsigned long long), ctx->stream);
     if (e != cudaSuccess) return e;
     lg_count_launch();
-    k_core_mixed<K, ST><<<blocks, kT, smem, ctx->stream>>>(
+    kern<<<blocks, kT, smem, ctx->stream>>>(
         g, lg_params(ctx), ctx->d_ys32.p, ctx->d_lidx.p, ctx->d_lmeta.p, ctx->d_queue.p, nchunks, chunk,
         ctx->d_loff.p, ctx->d_lcnt.p, ctx->win1, xb, axb, xa, axa, trans_out, w_out, ctx->d_counters.p,
         ctx->d_status.p, ctx->d_mA.p, ctx->d_mg.p, ctx->d_mX.p);

@@ -30,14 +30,17 @@ struct Corners {
     double t1, t2;
 };
 
-// Bilinear value of (xb + axb) for member e at row r (obs_make.F90:285-294).
+// Bilinear value of (xb + axb) for member e at row r (obs_make.F90:285-294);
+// with axb NULL, xb holds the full members (a fused members run).
 __device__ __forceinline__ double bilin(const double *__restrict__ xb, const double *__restrict__ axb,
                                         int n, int k, const Corners &q, int r, int e)
 {
-    const double v11 = xb[(q.c11 * n + r) * k + e] + axb[q.c11 * n + r];
-    const double v21 = xb[(q.c21 * n + r) * k + e] + axb[q.c21 * n + r];
-    const double v12 = xb[(q.c12 * n + r) * k + e] + axb[q.c12 * n + r];
-    const double v22 = xb[(q.c22 * n + r) * k + e] + axb[q.c22 * n + r];
+    const double a11 = axb ? axb[q.c11 * n + r] : 0.0, a21 = axb ? axb[q.c21 * n + r] : 0.0;
+    const double a12 = axb ? axb[q.c12 * n + r] : 0.0, a22 = axb ? axb[q.c22 * n + r] : 0.0;
+    const double v11 = xb[(q.c11 * n + r) * k + e] + a11;
+    const double v21 = xb[(q.c21 * n + r) * k + e] + a21;
+    const double v12 = xb[(q.c12 * n + r) * k + e] + a12;
+    const double v22 = xb[(q.c22 * n + r) * k + e] + a22;
     const double r1 = v11 * q.t1 + v21 * (1.0 - q.t1);
     const double r2 = v12 * q.t1 + v22 * (1.0 - q.t1);
     return r1 * q.t2 + r2 * (1.0 - q.t2);

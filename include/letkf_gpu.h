@@ -187,13 +187,19 @@ typedef struct letkf_blend {
 
 /* run_da_parallel's body on the device: full background members
  * xb_in [col][row][member] in; the mean and perturbations formed (dnn2letkf,
- * module_da_parallel.F90:184-204: mean = sum / real(ens); a NaN member returns
- * LETKF_ERR_INVALID before any analysis), the analysis of letkf_gpu_run, and
- * the blend and spreads (letkf2dnn, :214-258): xa_out [col][row][member] the
- * analysis members, spread_b and spread_a [col][row] the background and
- * analysis spreads sqrt(sum d^2 / ens).  Every cube is analysed (no cube
- * range).  With LETKF_HOST_PTRS all arrays, observations included, are host
- * memory; with LETKF_DEVICE_PTRS all are device memory.                     */
+ * module_da_parallel.F90:184-204: mean = sum / real(ens); a NaN member makes
+ * the call return LETKF_ERR_INVALID, and the outputs are then not meaningful),
+ * the analysis of letkf_gpu_run, and the blend and spreads (letkf2dnn,
+ * :214-258): xa_out [col][row][member] the analysis members, spread_b and
+ * spread_a [col][row] the background and analysis spreads sqrt(sum d^2 / ens).
+ * With one column per cube, no overlap and no vertical localization (and an
+ * ensemble of at most 64 in the mixed forms) the split and the blend are done
+ * inside the analysis (H reads the members, the update forms each row's mean
+ * and writes the blended members and both spreads), so the call makes no
+ * pass over the state beyond those of letkf_gpu_run; otherwise they are one
+ * pass each before and after it.  Every cube is analysed (no cube range).
+ * With LETKF_HOST_PTRS all arrays, observations included, are host memory;
+ * with LETKF_DEVICE_PTRS all are device memory.                             */
 int letkf_gpu_run_members(letkf_ctx *ctx, const double *xb_in, const letkf_obs *obs,
                           const letkf_blend *blend, double *xa_out, double *spread_b,
                           double *spread_a, int flags);
