@@ -18,6 +18,76 @@ bool lg_core_supports(int k);
 bool lg_mixed_supports(int k);
 int lg_search_cap(int max_obs);
 
+cudaError_t lg_issue_copy(const LgCopyJob &j)
+{
+    cudaError_t e = cudaSuccess;
+    if (j.after) e = cudaStreamWaitEvent(j.stream, j.after, 0);
+    for (const LgCopyJob::Part &p : j.part) {
+        if (e != cudaSuccess || !p.width || !p.height) continue;
+        e = p.height == 1 ? cudaMemcpyAsync(p.dst, p.src, p.width, j.kind, j.stream)
+                          : cudaMemcpy2DAsync(p.dst, p.dpitch, p.src, p.spitch, p.width, p.height, j.kind, j.stream);
+    }
+    if (e == cudaSuccess && j.done) e = cudaEventRecord(j.done, j.stream);
+    return e;
+}
+
+LgCopyAgent::LgCopyAgent(int device) : device_(device) { thread_ = std::thread(&LgCopyAgent::loop, this); }
+
+LgCopyAgent::~LgCopyAgent()
+{
+    {
+        std::lock_guard<std::mutex> lk(mu_);
+        stop_ = true;
+    }
+    work_.notify_all();
+    thread_.join();
+}
+
+void LgCopyAgent::push(const LgCopyJob &job)
+{
+    {
+        std::lock_guard<std::mutex> lk(mu_);
+        queue_.push_back(job);
+    }
+    work_.notify_one();
+}
+
+cudaError_t LgCopyAgent::drain()
+{
+    std::unique_lock<std::mutex> lk(mu_);
+    idle_.wait(lk, [this] { return queue_.empty() && !busy_; });
+    const cudaError_t e = err_;
+    err_ = cudaSuccess;
+    return e;
+}
+
+void LgCopyAgent::loop()
+{
+    const cudaError_t dev = cudaSetDevice(device_);
+    std::unique_lock<std::mutex> lk(mu_);
+    for (;;) {
+        work_.wait(lk, [this] { return stop_ || !queue_.empty(); });
+        if (queue_.empty()) return;
+        const LgCopyJob j = queue_.front();
+        queue_.pop_front();
+        busy_ = true;
+        lk.unlock();
+        // after a failed job the rest of the run's jobs are dropped: the run
+        // reports the error, and its outputs are not meaningful
+        cudaError_t e = dev;
+        if (e == cudaSuccess) {
+            lk.lock();
+            const bool failed = err_ != cudaSuccess;
+            lk.unlock();
+            if (!failed) e = lg_issue_copy(j);
+        }
+        lk.lock();
+        busy_ = false;
+        if (e != cudaSuccess && err_ == cudaSuccess) err_ = e;
+        if (queue_.empty()) idle_.notify_all();
+    }
+}
+
 namespace {
 
 std::atomic<int64_t> g_launches{0};
@@ -57,27 +127,117 @@ cudaError_t copy_streams(letkf_ctx *ctx)
     return cudaSuccess;
 }
 
-// Host -> device copy of count elements in equal parts on the copy streams,
-// joined back into the main stream (else the caller joins the events cev).
-template <typename T>
-cudaError_t h2d_parts(letkf_ctx *ctx, DevBuf<T> &buf, const T *src, size_t count, bool join = true)
+// True where p is ordinary pageable host memory (neither page-locked nor
+// registered with the runtime, nor device or managed memory).
+bool pageable(const void *p)
 {
-    cudaError_t e = buf.reserve(count);
-    if (e != cudaSuccess || count == 0) return e;
-    constexpr int NS = letkf_ctx::kCopyStreams;
-    if ((e = cudaEventRecord(ctx->sev[0], ctx->stream)) != cudaSuccess) return e;
-    const size_t part = (count + NS - 1) / NS;
-    for (int i = 0; i < NS; i++) {
-        const size_t a = std::min(count, i * part), b = std::min(count, a + part);
-        if ((e = cudaStreamWaitEvent(ctx->cstream[i], ctx->sev[0], 0)) != cudaSuccess) return e;
-        if (b > a && (e = cudaMemcpyAsync(buf.p + a, src + a, sizeof(T) * (b - a), cudaMemcpyHostToDevice,
-                                          ctx->cstream[i])) != cudaSuccess)
-            return e;
-        if ((e = cudaEventRecord(ctx->cev[i], ctx->cstream[i])) != cudaSuccess) return e;
-        if (join && (e = cudaStreamWaitEvent(ctx->stream, ctx->cev[i], 0)) != cudaSuccess) return e;
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return true;
     }
+    return a.type == cudaMemoryTypeUnregistered;
+}
+
+// A copy job of this run: issued here, or by the copy agent when a host
+// buffer is pageable.  `after` is an event the caller records on the main
+// stream next (copy_event hands out one per agent job, since the agent may
+// issue the wait after the main stream's next record of a shared event).
+cudaError_t copy_job(letkf_ctx *ctx, const LgCopyJob &j)
+{
+    if (!ctx->agent_on) return lg_issue_copy(j);
+    ctx->agent->push(j);
     return cudaSuccess;
 }
+
+cudaError_t copy_event(letkf_ctx *ctx, int stream, cudaEvent_t &ev)
+{
+    if (!ctx->agent_on) {
+        ev = ctx->sev[stream];
+        return cudaSuccess;
+    }
+    if (ctx->agent_ev_next == ctx->agent_ev.size()) {
+        cudaEvent_t e = nullptr;
+        cudaError_t r = cudaEventCreateWithFlags(&e, cudaEventDisableTiming);
+        if (r != cudaSuccess) return r;
+        ctx->agent_ev.push_back(e);
+    }
+    ev = ctx->agent_ev[ctx->agent_ev_next++];
+    return cudaSuccess;
+}
+
+// The copies of columns [c0, c1) of an array of `per` doubles per column
+// between the device (columns contiguous) and the host array in the run's
+// layout (ctx->host_ld, host_off): one copy without a halo, else the partial
+// longitude lines at either end as plain copies and the whole lines between
+// as one strided copy.
+void column_parts(const letkf_ctx *ctx, std::vector<LgCopyJob::Part> &out, bool to_host, const void *host,
+                  const void *dev, size_t per, int64_t c0, int64_t c1)
+{
+    const int64_t nlat = ctx->nlat, ld = ctx->host_ld, off = ctx->host_off;
+    const size_t cb = per * sizeof(double);
+    auto hp = [&](int64_t c) { return (char *)host + (size_t)(off + c % nlat + ld * (c / nlat)) * cb; };
+    auto dp = [&](int64_t c) { return (char *)dev + (size_t)c * cb; };
+    auto add = [&](int64_t c, size_t width, size_t lines) {
+        LgCopyJob::Part p;
+        p.width = width;
+        p.height = lines;
+        p.dst = to_host ? hp(c) : dp(c);
+        p.src = to_host ? (const void *)dp(c) : (const void *)hp(c);
+        p.dpitch = to_host ? (size_t)ld * cb : (size_t)nlat * cb;
+        p.spitch = to_host ? (size_t)nlat * cb : (size_t)ld * cb;
+        out.push_back(p);
+    };
+    if (ld == nlat && off == 0) {
+        if (c1 > c0) add(c0, (size_t)(c1 - c0) * cb, 1);
+        return;
+    }
+    // strided copies take pitches below 2^31 bytes; wider lines go one by one
+    const bool strided = (size_t)ld * cb < ((size_t)1 << 31);
+    for (int64_t c = c0; c < c1;) {
+        const int64_t line_end = (c / nlat + 1) * nlat;
+        if (c % nlat != 0 || c1 < line_end || !strided) {
+            const int64_t e = std::min(c1, line_end);
+            add(c, (size_t)(e - c) * cb, 1);
+            c = e;
+        } else {
+            const int64_t lines = (c1 - c) / nlat;
+            add(c, (size_t)nlat * cb, (size_t)lines);
+            c += lines * nlat;
+        }
+    }
+}
+
+// The state in for a run with host buffers: the members in equal column
+// ranges on the copy streams and the mean behind the last range, each copy
+// stream recording cev when its range is in.  The members pass of H and the
+// core wait for those events (lg_members_if_pending).
+cudaError_t state_in(letkf_ctx *ctx, const double *xb, const double *axb)
+{
+    const size_t per_s = (size_t)ctx->n * ctx->k, per_m = (size_t)ctx->n;
+    cudaError_t e = ctx->d_xb.reserve((size_t)ctx->ncol * per_s);
+    if (e == cudaSuccess) e = ctx->d_axb.reserve((size_t)ctx->ncol * per_m);
+    constexpr int NS = letkf_ctx::kCopyStreams;
+    cudaEvent_t start = nullptr;
+    if (e == cudaSuccess) e = copy_event(ctx, 0, start);
+    if (e == cudaSuccess) e = cudaEventRecord(start, ctx->stream);
+    const int64_t part = (ctx->ncol + NS - 1) / NS;
+    for (int i = 0; i < NS && e == cudaSuccess; i++) {
+        const int64_t a = std::min<int64_t>(ctx->ncol, i * part), b = std::min<int64_t>(ctx->ncol, a + part);
+        LgCopyJob j;
+        j.stream = ctx->cstream[i];
+        j.after = start;
+        j.done = ctx->cev[i];
+        j.kind = cudaMemcpyHostToDevice;
+        column_parts(ctx, j.part, false, xb, ctx->d_xb.p, per_s, a, b);
+        if (i == NS - 1) column_parts(ctx, j.part, false, axb, ctx->d_axb.p, per_m, 0, ctx->ncol);
+        e = copy_job(ctx, j);
+    }
+    return e;
+}
+
+// Wait for the copy agent's jobs (none without a pageable buffer).
+cudaError_t drain_copies(letkf_ctx *ctx) { return ctx->agent_on ? ctx->agent->drain() : cudaSuccess; }
 
 float elapsed(cudaEvent_t a, cudaEvent_t b)
 {
@@ -696,9 +856,12 @@ cudaError_t lg_members_if_pending(letkf_ctx *ctx)
 {
     if (!ctx->members_pending) return cudaSuccess;
     ctx->members_pending = false;
-    // the state copy on the copy streams
+    // the state copy on the copy streams (pageable: the agent has issued it
+    // and recorded the events once it drains)
+    cudaError_t e = drain_copies(ctx);
+    if (e != cudaSuccess) return e;
     for (int i = 0; i < letkf_ctx::kCopyStreams; i++) {
-        cudaError_t e = cudaStreamWaitEvent(ctx->stream, ctx->cev[i], 0);
+        e = cudaStreamWaitEvent(ctx->stream, ctx->cev[i], 0);
         if (e != cudaSuccess) return e;
     }
     return lg_launch_obs_prepare(ctx, lg_grid(ctx), ctx->pend_xb, ctx->pend_axb, ctx->pend_no, ctx->pend_lat,
@@ -710,15 +873,15 @@ cudaError_t lg_sink_columns(letkf_ctx *ctx, int64_t c0, int64_t c1)
 {
     if (!ctx->sink_xa || c1 <= c0) return cudaSuccess;
     const int i = ctx->sink_next++ % letkf_ctx::kCopyStreams;
-    cudaError_t e = cudaEventRecord(ctx->sev[i], ctx->stream);
-    if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->cstream[i], ctx->sev[i], 0);
+    LgCopyJob j;
+    cudaError_t e = copy_event(ctx, i, j.after);
+    if (e == cudaSuccess) e = cudaEventRecord(j.after, ctx->stream);
     const size_t per_s = (size_t)ctx->n * ctx->k, per_m = (size_t)ctx->n;
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(ctx->sink_xa + c0 * per_s, ctx->sink_dxa + c0 * per_s,
-                            sizeof(double) * (c1 - c0) * per_s, cudaMemcpyDeviceToHost, ctx->cstream[i]);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(ctx->sink_axa + c0 * per_m, ctx->sink_daxa + c0 * per_m,
-                            sizeof(double) * (c1 - c0) * per_m, cudaMemcpyDeviceToHost, ctx->cstream[i]);
+    j.stream = ctx->cstream[i];
+    j.kind = cudaMemcpyDeviceToHost;
+    column_parts(ctx, j.part, true, ctx->sink_xa, ctx->sink_dxa, per_s, c0, c1);
+    column_parts(ctx, j.part, true, ctx->sink_axa, ctx->sink_daxa, per_m, c0, c1);
+    if (e == cudaSuccess) e = copy_job(ctx, j);
     if (e == cudaSuccess) ctx->sink_cols += c1 - c0;
     return e;
 }
@@ -789,20 +952,21 @@ int lg_finish_run(letkf_ctx *ctx, const letkf_obs *obs, unsigned long long *cnt)
     return LETKF_OK;
 }
 
-extern "C" {
+namespace {
 
-int letkf_gpu_run(letkf_ctx *ctx, const double *xb, const double *axb, const letkf_obs *obs,
-                  double *xa, double *axa, int flags)
+// letkf_gpu_run and letkf_gpu_run_halo: with host buffers the state goes in
+// on the copy streams while the geometry, buckets and search run, and the
+// staged core's finished blocks go out while later blocks run; the host
+// arrays hold the columns in the layout of ctx->host_ld / host_off.
+int run_impl(letkf_ctx *ctx, const double *xb, const double *axb, const letkf_obs *obs, double *xa, double *axa,
+             bool host, int halo)
 {
-    if (!ctx) return LETKF_ERR_INVALID;
-    if (!xb || !axb || !xa || !axa) return set_err(ctx, LETKF_ERR_INVALID, "NULL state pointer");
-    if (flags != LETKF_HOST_PTRS && flags != LETKF_DEVICE_PTRS)
-        return set_err(ctx, LETKF_ERR_INVALID, "bad flags");
     int rc = lg_check_run(ctx, obs);
     if (rc) return rc;
     LG_CUDA(cudaSetDevice(ctx->device));
-    const bool host = flags == LETKF_HOST_PTRS;
     const size_t nstate = (size_t)ctx->ncol * ctx->n * ctx->k, nmean = (size_t)ctx->ncol * ctx->n;
+    ctx->host_ld = ctx->nlat + 2 * (int64_t)halo;
+    ctx->host_off = halo + ctx->host_ld * halo;
     LG_CUDA(cudaEventRecord(ctx->ev[0], ctx->stream));
     rc = reset_status(ctx);
     if (rc) return rc;
@@ -810,10 +974,27 @@ int letkf_gpu_run(letkf_ctx *ctx, const double *xb, const double *axb, const let
     double *dxa = xa, *daxa = axa;
     if (host) {
         LG_CUDA(copy_streams(ctx));
-        LG_CUDA(h2d_parts(ctx, ctx->d_xb, xb, nstate, false));
-        LG_CUDA(h2d(ctx->d_axb, axb, nmean, ctx->stream));
         LG_CUDA(ctx->d_xa.reserve(nstate));
         LG_CUDA(ctx->d_axa.reserve(nmean));
+        // from the state copy on, every return passes the join below: no
+        // copy may still use the caller's buffers after the call
+        ctx->agent_on = pageable(xb) || pageable(axb) || pageable(xa) || pageable(axa);
+        ctx->agent_ev_next = 0;
+        if (ctx->agent_on && !ctx->agent) {
+            try {
+                ctx->agent.reset(new LgCopyAgent(ctx->device));
+            } catch (const std::exception &) {
+                ctx->agent_on = false;
+                return set_err(ctx, LETKF_ERR_ALLOC, "cannot start the host copy thread");
+            }
+        }
+        cudaError_t e = state_in(ctx, xb, axb);
+        if (e != cudaSuccess) {
+            drain_copies(ctx);
+            ctx->agent_on = false;
+            cudaStreamSynchronize(ctx->stream);
+            return set_err(ctx, LETKF_ERR_CUDA, cudaGetErrorString(e));
+        }
         dxb = ctx->d_xb.p;
         daxb = ctx->d_axb.p;
         dxa = ctx->d_xa.p;
@@ -840,10 +1021,13 @@ int letkf_gpu_run(letkf_ctx *ctx, const double *xb, const double *axb, const let
         // early; then nothing is left writing into the caller's buffers
         ctx->members_pending = false;
         ctx->lists_need_ef = false;
+        const cudaError_t ae = drain_copies(ctx);
+        ctx->agent_on = false;
         for (int i = 0; i < letkf_ctx::kCopyStreams; i++) {
             LG_CUDA(cudaEventRecord(ctx->cev[i], ctx->cstream[i]));
             LG_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->cev[i], 0));
         }
+        if (!rc && ae != cudaSuccess) rc = set_err(ctx, LETKF_ERR_CUDA, cudaGetErrorString(ae));
         if (rc) cudaStreamSynchronize(ctx->stream);
     }
     if (rc) return rc;
@@ -855,13 +1039,37 @@ int letkf_gpu_run(letkf_ctx *ctx, const double *xb, const double *axb, const let
             col0 = ctx->range0 / ctx->nbj * ctx->params.cube_n * ctx->nlat;
             col1 = std::min<int64_t>(ctx->range1 / ctx->nbj * ctx->params.cube_n, ctx->nlon) * ctx->nlat;
         }
-        const size_t per_s = (size_t)ctx->n * ctx->k, per_m = (size_t)ctx->n;
-        LG_CUDA(cudaMemcpyAsync(xa + col0 * per_s, dxa + col0 * per_s, sizeof(double) * (col1 - col0) * per_s,
-                                cudaMemcpyDeviceToHost, ctx->stream));
-        LG_CUDA(cudaMemcpyAsync(axa + col0 * per_m, daxa + col0 * per_m, sizeof(double) * (col1 - col0) * per_m,
-                                cudaMemcpyDeviceToHost, ctx->stream));
+        LgCopyJob j;
+        j.stream = ctx->stream;
+        j.kind = cudaMemcpyDeviceToHost;
+        column_parts(ctx, j.part, true, xa, dxa, (size_t)ctx->n * ctx->k, col0, col1);
+        column_parts(ctx, j.part, true, axa, daxa, (size_t)ctx->n, col0, col1);
+        LG_CUDA(lg_issue_copy(j));
     }
     return lg_finish_run(ctx, obs, cnt);
+}
+
+}  // namespace
+
+extern "C" {
+
+int letkf_gpu_run(letkf_ctx *ctx, const double *xb, const double *axb, const letkf_obs *obs,
+                  double *xa, double *axa, int flags)
+{
+    if (!ctx) return LETKF_ERR_INVALID;
+    if (!xb || !axb || !xa || !axa) return set_err(ctx, LETKF_ERR_INVALID, "NULL state pointer");
+    if (flags != LETKF_HOST_PTRS && flags != LETKF_DEVICE_PTRS)
+        return set_err(ctx, LETKF_ERR_INVALID, "bad flags");
+    return run_impl(ctx, xb, axb, obs, xa, axa, flags == LETKF_HOST_PTRS, 0);
+}
+
+int letkf_gpu_run_halo(letkf_ctx *ctx, int halo, const double *xb, const double *axb, const letkf_obs *obs,
+                       double *xa, double *axa)
+{
+    if (!ctx) return LETKF_ERR_INVALID;
+    if (!xb || !axb || !xa || !axa) return set_err(ctx, LETKF_ERR_INVALID, "NULL state pointer");
+    if (halo < 0 || halo > 1 << 16) return set_err(ctx, LETKF_ERR_INVALID, "bad halo width");
+    return run_impl(ctx, xb, axb, obs, xa, axa, true, halo);
 }
 
 int letkf_gpu_synchronize(letkf_ctx *ctx)
@@ -1085,6 +1293,8 @@ int letkf_gpu_destroy(letkf_ctx *ctx)
         for (int h = 0; h < 2; h++)
             for (int i = 0; i < letkf_ctx::kStageMarks; i++)
                 if (ctx->stg_ev[s][h][i]) cudaEventDestroy(ctx->stg_ev[s][h][i]);
+    ctx->agent.reset();
+    for (cudaEvent_t e : ctx->agent_ev) cudaEventDestroy(e);
     for (int i = 0; i < letkf_ctx::kCopyStreams; i++) {
         if (ctx->cev[i]) cudaEventDestroy(ctx->cev[i]);
         if (ctx->sev[i]) cudaEventDestroy(ctx->sev[i]);
@@ -1101,7 +1311,6 @@ int letkf_gpu_destroy(letkf_ctx *ctx)
 static letkf_ctx *g_fctx = nullptr;
 static std::vector<double> g_olat, g_olon, g_oph, g_oyo, g_orinv;
 static std::vector<int32_t> g_olev, g_ovar;
-static std::vector<double> g_xb, g_axb, g_xa, g_axa;
 
 void letkf_init_gpu_(const int *nlat, const int *nlon, const int *nz, const int *nvar2d,
                      const int *nvar3d, const int *ens, const float *lat, const float *lon,
@@ -1174,21 +1383,6 @@ void letkf_run_gpu_(const int *ntimes, const int *halo, const double *xb, const 
         *ierr = LETKF_ERR_STATE;
         return;
     }
-    const int h = *halo, nlat = g_fctx->nlat, nlon = g_fctx->nlon, n = g_fctx->n, k = g_fctx->k;
-    const int64_t lath = nlat + 2 * h;
-    const size_t ncol = (size_t)nlat * nlon;
-    g_xb.resize(ncol * n * k);
-    g_axb.resize(ncol * n);
-    g_xa.resize(ncol * n * k);
-    g_axa.resize(ncol * n);
-    // strip the halo: xb(ens, n, 1-h:nlat+h, 1-h:nlon+h)
-    for (int i = 0; i < nlon; i++)
-        for (int j = 0; j < nlat; j++) {
-            const int64_t src = (int64_t)(j + h) + lath * (i + h);
-            const size_t dst = (size_t)j + (size_t)nlat * i;
-            std::memcpy(&g_xb[dst * n * k], xb + src * n * k, sizeof(double) * n * k);
-            std::memcpy(&g_axb[dst * n], axb + src * n, sizeof(double) * n);
-        }
     letkf_obs o{};
     o.nobs = (int64_t)g_olat.size();
     o.lat = g_olat.data();
@@ -1198,16 +1392,9 @@ void letkf_run_gpu_(const int *ntimes, const int *halo, const double *xb, const 
     o.var = g_ovar.data();
     o.yo = g_oyo.data();
     o.rinv = g_orinv.data();
-    *ierr = letkf_gpu_run(g_fctx, g_xb.data(), g_axb.data(), &o, g_xa.data(), g_axa.data(),
-                          LETKF_HOST_PTRS);
-    if (*ierr != LETKF_OK && *ierr != LETKF_ERR_NOT_CONVERGED) return;
-    for (int i = 0; i < nlon; i++)
-        for (int j = 0; j < nlat; j++) {
-            const int64_t dst = (int64_t)(j + h) + lath * (i + h);
-            const size_t src = (size_t)j + (size_t)nlat * i;
-            std::memcpy(xa + dst * n * k, &g_xa[src * n * k], sizeof(double) * n * k);
-            std::memcpy(axa + dst * n, &g_axa[src * n], sizeof(double) * n);
-        }
+    // xb(ens, n, 1-halo:nlat+halo, 1-halo:nlon+halo): the copies skip the
+    // halo, which xa and axa keep as they were
+    *ierr = letkf_gpu_run_halo(g_fctx, *halo, xb, axb, &o, xa, axa);
 }
 
 void letkf_final_gpu_(int *ierr)

@@ -4,7 +4,12 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <condition_variable>
+#include <deque>
+#include <memory>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "letkf_gpu.h"
@@ -212,6 +217,50 @@ struct DevBuf {
     ~DevBuf() { release(); }
 };
 
+// Copies on one stream: after the main-stream point `after` (if any), the
+// parts in one direction (height 1: a plain copy of width bytes; else width
+// bytes of each of height lines, pitches apart), then the event `done`.
+struct LgCopyJob {
+    cudaStream_t stream = nullptr;
+    cudaEvent_t after = nullptr, done = nullptr;
+    cudaMemcpyKind kind = cudaMemcpyDefault;
+    struct Part {
+        void *dst;
+        size_t dpitch;
+        const void *src;
+        size_t spitch;
+        size_t width, height;
+    };
+    std::vector<Part> part;
+};
+
+// A host thread that issues copy jobs in order.  A cudaMemcpyAsync between
+// the device and pageable host memory returns only when the runtime has moved
+// the bytes, so issued by the thread that enqueues the analysis it would hold
+// every later launch behind the copy; issued here, the launches go on and the
+// copies keep the host link busy beside them.
+class LgCopyAgent {
+  public:
+    explicit LgCopyAgent(int device);
+    ~LgCopyAgent();     // issues what is queued, then joins the thread
+    void push(const LgCopyJob &job);
+    // waits until every pushed job has been issued (pageable copies: done);
+    // returns and clears the first error of those jobs
+    cudaError_t drain();
+    LgCopyAgent(const LgCopyAgent &) = delete;
+    LgCopyAgent &operator=(const LgCopyAgent &) = delete;
+
+  private:
+    void loop();
+    int device_;
+    std::mutex mu_;
+    std::condition_variable work_, idle_;
+    std::deque<LgCopyJob> queue_;
+    bool busy_ = false, stop_ = false;
+    cudaError_t err_ = cudaSuccess;
+    std::thread thread_;
+};
+
 struct letkf_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -310,6 +359,16 @@ struct letkf_ctx {
     const double *sink_dxa = nullptr, *sink_daxa = nullptr;  // device outputs
     int sink_next = 0;
     int64_t sink_cols = 0;                   // columns handed to the copy streams
+    // a host buffer of the run is pageable: the copy-stream copies go
+    // through the copy agent, each job with its own main-stream event
+    bool agent_on = false;
+    // the host arrays' column layout: column c (c % nlat along latitude,
+    // c / nlat along longitude) sits at host column host_off + c % nlat +
+    // host_ld * (c / nlat); host_ld = nlat, host_off = 0 without a halo
+    int64_t host_ld = 0, host_off = 0;
+    std::unique_ptr<LgCopyAgent> agent;
+    std::vector<cudaEvent_t> agent_ev;
+    size_t agent_ev_next = 0;
     // H on the members waits for the state copy: the geometry, buckets and
     // search run while it is on the way, and the first core launch runs the
     // members pass first (lg_members_if_pending)
@@ -369,6 +428,8 @@ cudaError_t lg_launch_obs_lnp(letkf_ctx *ctx, int64_t nobs, const double *oph);
 // host outputs of a letkf_gpu_run on a copy stream, after the main stream's
 // work so far; no-op without host outputs.
 cudaError_t lg_sink_columns(letkf_ctx *ctx, int64_t c0, int64_t c1);
+// Issue one copy job on its stream (from the calling thread).
+cudaError_t lg_issue_copy(const LgCopyJob &j);
 
 // The analysis of letkf_gpu_run on device state: observations staged (host or
 // device pointers), H, search and core (cube windows), overlapped-cube

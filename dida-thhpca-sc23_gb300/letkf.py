@@ -40,6 +40,7 @@ ERROR_NAMES = {
 
 EXPORTED = [
     "letkf_gpu_create", "letkf_gpu_set_stream", "letkf_gpu_set_keep_trans", "letkf_gpu_run",
+    "letkf_gpu_run_halo",
     "letkf_gpu_synchronize", "letkf_gpu_obs_operator", "letkf_gpu_local_obs",
     "letkf_gpu_last_trans", "letkf_gpu_core_batch", "letkf_gpu_get_stats",
     "letkf_gpu_last_error", "letkf_gpu_destroy", "letkf_gpu_launch_count",
@@ -124,6 +125,7 @@ def load_library(path: str = LIB_PATH):
     L.letkf_gpu_set_keep_trans.argtypes = [vp, i32]
     L.letkf_gpu_set_wait_limit.argtypes = [vp, i64]
     L.letkf_gpu_run.argtypes = [vp, vp, vp, C.POINTER(Obs), vp, vp, i32]
+    L.letkf_gpu_run_halo.argtypes = [vp, i32, vp, vp, C.POINTER(Obs), vp, vp]
     L.letkf_gpu_synchronize.argtypes = [vp]
     L.letkf_gpu_obs_operator.argtypes = [vp, vp, vp, C.POINTER(Obs), vp, vp]
     L.letkf_gpu_local_obs.argtypes = [vp, vp, vp, vp]
@@ -373,6 +375,24 @@ class LetkfGPU:
                                   LETKF_HOST_PTRS)
         if not (allow_not_converged and rc == LETKF_ERR_NOT_CONVERGED):
             self._check(rc, "letkf_gpu_run")
+        return xa, axa
+
+    def run_halo(self, halo, xb, axb, obs, xa, axa, allow_not_converged=False):
+        """letkf_run on arrays in its own layout with a halo: xb of shape
+        (nlon + 2 halo, nlat + 2 halo, n, k) in C order (the Fortran
+        xb(ens, n, 1-halo:nlat+halo, 1-halo:nlon+halo)), axb of shape
+        (nlon + 2 halo, nlat + 2 halo, n); xa, axa alike, written in place
+        (their halo is left as it was)."""
+        for a in (xb, axb, xa, axa):
+            if not (isinstance(a, np.ndarray) and a.dtype == np.float64 and a.flags.c_contiguous):
+                raise TypeError("run_halo takes C-contiguous float64 arrays")
+        lay = (self.nlon + 2 * halo, self.nlat + 2 * halo, self.n)
+        if xb.shape != lay + (self.k,) or xa.shape != xb.shape or axb.shape != lay or axa.shape != lay:
+            raise ValueError(f"run_halo wants xb, xa of shape {lay + (self.k,)} and axb, axa of shape {lay}")
+        o = obs if isinstance(obs, ObsArrays) else ObsArrays(obs)
+        rc = self.L.letkf_gpu_run_halo(self.h, int(halo), _ptr(xb), _ptr(axb), C.byref(o.c), _ptr(xa), _ptr(axa))
+        if not (allow_not_converged and rc == LETKF_ERR_NOT_CONVERGED):
+            self._check(rc, "letkf_gpu_run_halo")
         return xa, axa
 
     def run_members(self, xb_in, obs, gamma1=0.0, gamma2=1.0, polar_lat_deg=90.0):

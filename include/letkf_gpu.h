@@ -169,11 +169,22 @@ int letkf_gpu_set_stream(letkf_ctx *ctx, void *stream);
  * LETKF_HOST_PTRS the call copies in and out and returns when xa/axa are
  * written (with page-locked buffers the state copies overlap the search and
  * the analysis: the copy-in runs beside H's geometry pass and the search, and
- * finished blocks of columns are copied out while later ones are analysed);
- * with LETKF_DEVICE_PTRS it returns with the work queued on the stream (call
+ * finished blocks of columns are copied out while later ones are analysed;
+ * ordinary pageable buffers get the same overlap: a host thread of the
+ * context issues their copies, since a copy from or to pageable memory holds
+ * the thread that issues it until the bytes have moved); with
+ * LETKF_DEVICE_PTRS it returns with the work queued on the stream (call
  * letkf_gpu_synchronize before reading the outputs).                        */
 int letkf_gpu_run(letkf_ctx *ctx, const double *xb, const double *axb, const letkf_obs *obs,
                   double *xa, double *axa, int flags);
+
+/* letkf_gpu_run on host arrays in letkf_run's own layout with a halo
+ * (letkf.F90:157-257; xb(ens, n, 1-halo:nlat+halo, 1-halo:nlon+halo), axb,
+ * xa, axa alike): the copies read and write the interior columns in place
+ * (strided copies of whole longitude lines), and the halo of xa/axa is left
+ * as it was.  halo = 0 is letkf_gpu_run with LETKF_HOST_PTRS.               */
+int letkf_gpu_run_halo(letkf_ctx *ctx, int halo, const double *xb, const double *axb,
+                       const letkf_obs *obs, double *xa, double *axa);
 
 /* The caller's conversion around letkf_run (run_da_parallel,
  * EnDNN/src/module_da_parallel.F90:163-261), for letkf_gpu_run_members.     */
@@ -405,7 +416,8 @@ void letkf_set_obs_gpu_(const int64_t *nobs, const double *lat, const double *lo
                         const double *ph, const int *lev, const int *var, const double *yo,
                         const double *rinv, int *ierr);
 /* letkf_run with the reference's halo layout: xb(ens, n, 1-halo:nlat+halo,
- * 1-halo:nlon+halo); only the interior is read and written.                */
+ * 1-halo:nlon+halo); only the interior is read and written, straight from
+ * and to the caller's arrays (letkf_gpu_run_halo).                          */
 void letkf_run_gpu_(const int *ntimes, const int *halo, const double *xb, const double *axb,
                     double *xa, double *axa, int *ierr);
 void letkf_final_gpu_(int *ierr);
