@@ -1403,6 +1403,15 @@ void letkf_final_gpu_(int *ierr)
     g_fctx = nullptr;
 }
 
+int letkf_gpu_set_schedule(letkf_ctx *ctx, int chunk)
+{
+    if (!ctx) return LETKF_ERR_INVALID;
+    if (chunk != 0 && (chunk < 8 || chunk > 1024 || (chunk & (chunk - 1)) != 0))
+        return set_err(ctx, LETKF_ERR_INVALID, "the chunk must be 0 or a power of two from 8 to 1024");
+    ctx->sched_chunk = chunk;
+    return LETKF_OK;
+}
+
 int letkf_gpu_autotune(letkf_ctx *ctx, const double *xb, const double *axb, const letkf_obs *obs,
                        double *xa, double *axa, int flags)
 {
@@ -1410,11 +1419,12 @@ int letkf_gpu_autotune(letkf_ctx *ctx, const double *xb, const double *axb, cons
     if (!lg_is_mixed(ctx->params.precision))
         return letkf_gpu_run(ctx, xb, axb, obs, xa, axa, flags);
     // chunk sizes of the mixed core's work queue: small chunks balance the
-    // load, large ones keep more cubes warm-started; the fastest core wins
-    static const int cand[] = {8, 16, 32, 64};
+    // load, large ones cost fewer queue fetches; the fastest core wins (the
+    // one-launch cores take chunks of whole warm-start runs)
+    static const int cand64[] = {8, 16, 32, 64}, cand[] = {16, 32, 64, 128};
     int best = 0;
     double best_ms = 1e300;
-    for (int c : cand) {
+    for (int c : (ctx->k == 64 ? cand64 : cand)) {
         ctx->sched_chunk = c;
         const int rc = letkf_gpu_run(ctx, xb, axb, obs, xa, axa, flags);
         if (rc != LETKF_OK && rc != LETKF_ERR_NOT_CONVERGED) return rc;

@@ -30,6 +30,11 @@
 #define LG_MBAR_SPIN_LIMIT (1u << 22)   // polls of a bounded tensor-core wait
 #endif
 #define LG_MAX_ENS 128          // largest ensemble the kernels are built for
+// The one-launch mixed cores (k != 64) warm-start each cube's eigensolve from
+// the cube before it only inside aligned runs of this many cubes, and their
+// work-queue chunks are multiples of it: a cube's result does not depend on
+// the chunk size.  (The staged k = 64 core's eigensolve runs are 8 cubes.)
+#define LG_WARM_RUN 16
 
 // The precision forms whose products run on the tensor cores.
 __host__ __device__ __forceinline__ bool lg_is_mixed(int precision)

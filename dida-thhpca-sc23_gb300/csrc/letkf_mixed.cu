@@ -16,7 +16,9 @@
 //      e's hi and lo parts are two more rows of the B operand (N = k + 16).
 //   2. A' = A + (k-1)/rho I in FP64.
 //   3. FP32 one-sided Jacobi of A' (warm-started from the neighbouring
-//      cube's eigenvectors) gives the eigenpairs: lambda_j = |w_j|, x_j = w_j/lambda_j.
+//      cube's eigenvectors inside aligned runs of cubes, so that results do
+//      not depend on the schedule) gives the eigenpairs: lambda_j = |w_j|,
+//      x_j = w_j/lambda_j.
 //   4. wbar = X diag(1/lambda) X^T g in FP32, then one step of iterative
 //      refinement: wbar += X diag(1/lambda) X^T (g - A' wbar) with the
 //      residual in FP64 against the FP64 A'.  A' has condition numbers below
@@ -27,7 +29,8 @@
 //   6. xa = xb^T T on tcgen05 (hi/lo BF16 of both operands, three products in
 //      one accumulator); the mean increment xb^T wbar is FP64.
 //
-// k = 32 and 48 run all steps in one persistent launch (k_core_mixed<k, 0>).
+// k = 32 and 48 run all steps in one persistent launch (k_core_mixed<k, 0>;
+// warm-start runs of LG_WARM_RUN cubes).
 // k = 64 runs them in three launches per block of cubes: the A and g build
 // (k_core_mixed<64, 1>), steps 3-5 one warp per cube (k_eig_warp<64>, runs of
 // 8 cubes warm-started inside a run, taken from a queue) and step 6
@@ -292,6 +295,7 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
     const int cube_end = (int)min(ncubes, chunk_at + chunk);
     bool have_prev = false;
     for (int cube = cube_begin; cube < cube_end; cube++) {
+        if (ST == 0 && cube % LG_WARM_RUN == 0) have_prev = false;
         const int64_t off = loff[cube];
         const int p = lcnt[cube];
         LG_PHASE(6);
@@ -981,14 +985,14 @@ k_chunk_queue(const int32_t *__restrict__ lcnt, int64_t win0, int64_t win1, int 
 }  // namespace
 
 // Cubes per work-queue chunk for the run's cube range: the context's
-// schedule (16 by default), grown until any window of the range takes at most
-// kQueueMax chunks.  One size for every window of a run keeps each cube's
-// chunk (and so its eigenvector warm start) the same however the range is
-// windowed.
+// schedule (16 by default; at least LG_WARM_RUN for the one-launch cores, so
+// that chunks hold whole warm-start runs), grown until any window of the
+// range takes at most kQueueMax chunks.  Windows end on chunk boundaries.
 int lg_run_chunk(const letkf_ctx *ctx)
 {
     const int64_t n = ctx->range1 - ctx->range0;
     int chunk = ctx->sched_chunk > 0 ? ctx->sched_chunk : 16;
+    if (ctx->k != 64 && chunk < LG_WARM_RUN) chunk = LG_WARM_RUN;
     while ((n + chunk - 1) / chunk + 1 > kQueueMax) chunk *= 2;
     return chunk;
 }

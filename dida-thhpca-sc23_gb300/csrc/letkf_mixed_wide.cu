@@ -156,6 +156,7 @@ k_core_mixed_wide(LgGrid g, LgParams prm, const float *__restrict__ ys32, const 
     const int cube_end = (int)min(ncubes, chunk_at + chunk);
     bool have_prev = false;
     for (int cube = cube_begin; cube < cube_end; cube++) {
+        if (cube % LG_WARM_RUN == 0) have_prev = false;
         const int64_t off = loff[cube];
         const int p = lcnt[cube];
         LGW_PHASE(6);

@@ -278,10 +278,11 @@ int letkf_gpu_set_list_limit(letkf_ctx *ctx, int64_t max_entries);
  * pointers: not copied back).  With cube_n > 1, first and count must be
  * multiples of the number of lat blocks (whole longitude strips).  The local
  * lists of a range run are not kept for letkf_gpu_local_obs.  The mixed form
- * warm-starts each cube's eigensolve from the cube before it in the same
- * work-queue chunk, so a range that cuts a chunk starts that chunk's first
- * cube cold (results then agree with a whole run to FP32 eigensolve
- * precision); windows never cut a chunk.                                     */
+ * warm-starts each cube's eigensolve from the cube before it inside aligned
+ * runs of cubes (8 cubes for k = 64, 16 otherwise), so a range whose first
+ * cube is inside a run starts that cube cold (results then agree with a whole
+ * run to FP32 eigensolve precision); ranges starting at multiples of 16,
+ * windows and the work-queue schedule leave every result unchanged.          */
 int letkf_gpu_set_cube_range(letkf_ctx *ctx, int64_t first, int64_t count);
 
 /* Most polls of each bounded wait of the mixed cores on their own
@@ -360,13 +361,21 @@ int letkf_gpu_core_batch_noalloc(int ens, double inflation, int64_t nb, const in
 
 /* Autotuner of the mixed form's schedule: runs the analysis (as
  * letkf_gpu_run) once per candidate chunk size of the core's work queue
- * (8, 16, 32, 64 consecutive cubes per chunk; chunks are taken heaviest
- * first) and keeps the one with the fastest core for the context's later
- * runs (letkf_stats.sched_chunk).  xa/axa hold the last run's analysis.
- * For the FP64 form it is one letkf_gpu_run.  No counterpart in the
- * reference.                                                                 */
+ * (consecutive cubes per chunk, chunks taken heaviest first: 8, 16, 32, 64
+ * for k = 64; 16, 32, 64, 128 otherwise) and keeps the one with the fastest
+ * core for the context's later runs (letkf_stats.sched_chunk).  The chunk
+ * size changes the speed only: every candidate gives the same analysis bit
+ * for bit.  xa/axa hold the last run's analysis.  For the FP64 form it is one
+ * letkf_gpu_run.  No counterpart in the reference.                           */
 int letkf_gpu_autotune(letkf_ctx *ctx, const double *xb, const double *axb, const letkf_obs *obs,
                        double *xa, double *axa, int flags);
+
+/* Set the mixed form's work-queue chunk (cubes per chunk, a power of two
+ * from 8 to 1024; 0: the default, 16) instead of autotuning it.  Chunks of
+ * the one-launch cores (k != 64) are at least 16 cubes; a run whose range
+ * would need more than 8191 chunks doubles the size.  LETKF_ERR_INVALID for
+ * other values.  No counterpart in the reference.                            */
+int letkf_gpu_set_schedule(letkf_ctx *ctx, int chunk);
 
 /* One CUDA graph over the analyses of several contexts (the batching form:
  * instances of different grids and ensemble sizes, each on its own stream
