@@ -7,6 +7,7 @@ from __future__ import annotations
 
 import concurrent.futures as cf
 import os
+import shlex
 import shutil
 import subprocess
 import sys
@@ -49,7 +50,9 @@ def build(verbose: bool = False, extra: list[str] | None = None, out_dir: str | 
     out = out_dir or OUT
     lib = os.path.join(out, "libletkf_gpu.so")
     os.makedirs(out, exist_ok=True)
-    extra = list(extra or [])
+    # LETKF_NVCC_FLAGS adds flags to every build (e.g. a kernel variant for
+    # a timing comparison, kept through the builds that scripts run first)
+    extra = list(extra or []) + shlex.split(os.environ.get("LETKF_NVCC_FLAGS", ""))
     srcs = sources()
     # objects built with other flags are rebuilt (the flags of the last build
     # are kept beside the library)

@@ -43,19 +43,28 @@ LgCopyAgent::~LgCopyAgent()
     thread_.join();
 }
 
-void LgCopyAgent::push(const LgCopyJob &job)
+uint64_t LgCopyAgent::push(const LgCopyJob &job)
 {
+    uint64_t seq;
     {
         std::lock_guard<std::mutex> lk(mu_);
         queue_.push_back(job);
+        seq = ++pushed_;
     }
     work_.notify_one();
+    return seq;
+}
+
+void LgCopyAgent::wait_issued(uint64_t seq)
+{
+    std::unique_lock<std::mutex> lk(mu_);
+    idle_.wait(lk, [&] { return issued_ >= seq; });
 }
 
 cudaError_t LgCopyAgent::drain()
 {
     std::unique_lock<std::mutex> lk(mu_);
-    idle_.wait(lk, [this] { return queue_.empty() && !busy_; });
+    idle_.wait(lk, [this] { return issued_ == pushed_; });
     const cudaError_t e = err_;
     err_ = cudaSuccess;
     return e;
@@ -70,7 +79,6 @@ void LgCopyAgent::loop()
         if (queue_.empty()) return;
         const LgCopyJob j = queue_.front();
         queue_.pop_front();
-        busy_ = true;
         lk.unlock();
         // after a failed job the rest of the run's jobs are dropped: the run
         // reports the error, and its outputs are not meaningful
@@ -82,9 +90,9 @@ void LgCopyAgent::loop()
             if (!failed) e = lg_issue_copy(j);
         }
         lk.lock();
-        busy_ = false;
+        issued_++;
         if (e != cudaSuccess && err_ == cudaSuccess) err_ = e;
-        if (queue_.empty()) idle_.notify_all();
+        idle_.notify_all();
     }
 }
 
@@ -124,6 +132,11 @@ cudaError_t copy_streams(letkf_ctx *ctx)
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->sev[i], cudaEventDisableTiming);
         if (e != cudaSuccess) return e;
     }
+    for (int i = 0; i < letkf_ctx::kPieces; i++) {
+        if (ctx->pev[i]) continue;
+        cudaError_t e = cudaEventCreateWithFlags(&ctx->pev[i], cudaEventDisableTiming);
+        if (e != cudaSuccess) return e;
+    }
     return cudaSuccess;
 }
 
@@ -143,10 +156,12 @@ bool pageable(const void *p)
 // buffer is pageable.  `after` is an event the caller records on the main
 // stream next (copy_event hands out one per agent job, since the agent may
 // issue the wait after the main stream's next record of a shared event).
-cudaError_t copy_job(letkf_ctx *ctx, const LgCopyJob &j)
+cudaError_t copy_job(letkf_ctx *ctx, const LgCopyJob &j, uint64_t *seq = nullptr)
 {
+    if (seq) *seq = 0;
     if (!ctx->agent_on) return lg_issue_copy(j);
-    ctx->agent->push(j);
+    const uint64_t q = ctx->agent->push(j);
+    if (seq) *seq = q;
     return cudaSuccess;
 }
 
@@ -208,32 +223,59 @@ void column_parts(const letkf_ctx *ctx, std::vector<LgCopyJob::Part> &out, bool 
     }
 }
 
-// The state in for a run with host buffers: the members in equal column
-// ranges on the copy streams and the mean behind the last range, each copy
-// stream recording cev when its range is in.  The members pass of H and the
-// core wait for those events (lg_members_if_pending).
-cudaError_t state_in(letkf_ctx *ctx, const double *xb, const double *axb)
+// The state in for a run with host buffers: kPieces equal column ranges of
+// the members and the mean, in column order, dealt in turn to the copy
+// streams; each piece's stream records its event pev[i] when it is in.  The
+// launches that read the state wait for the pieces they need (lg_state_wait).
+cudaError_t state_in(letkf_ctx *ctx, const double *xb, const double *axb, cudaEvent_t after = nullptr)
 {
     const size_t per_s = (size_t)ctx->n * ctx->k, per_m = (size_t)ctx->n;
     cudaError_t e = ctx->d_xb.reserve((size_t)ctx->ncol * per_s);
     if (e == cudaSuccess) e = ctx->d_axb.reserve((size_t)ctx->ncol * per_m);
-    constexpr int NS = letkf_ctx::kCopyStreams;
-    cudaEvent_t start = nullptr;
-    if (e == cudaSuccess) e = copy_event(ctx, 0, start);
-    if (e == cudaSuccess) e = cudaEventRecord(start, ctx->stream);
-    const int64_t part = (ctx->ncol + NS - 1) / NS;
-    for (int i = 0; i < NS && e == cudaSuccess; i++) {
+    constexpr int NS = letkf_ctx::kCopyStreams, P = letkf_ctx::kPieces;
+    // the pieces start after the main stream's work so far, or after `after`
+    cudaEvent_t start = after;
+    if (!start && e == cudaSuccess) e = copy_event(ctx, 0, start);
+    if (!after && e == cudaSuccess) e = cudaEventRecord(start, ctx->stream);
+    const int64_t part = (ctx->ncol + P - 1) / P;
+    ctx->npieces = 0;
+    for (int i = 0; i < P && e == cudaSuccess; i++) {
         const int64_t a = std::min<int64_t>(ctx->ncol, i * part), b = std::min<int64_t>(ctx->ncol, a + part);
+        if (b <= a) break;
         LgCopyJob j;
-        j.stream = ctx->cstream[i];
-        j.after = start;
-        j.done = ctx->cev[i];
+        j.stream = ctx->cstream[i % NS];
+        j.after = i < NS ? start : nullptr;
+        j.done = ctx->pev[i];
         j.kind = cudaMemcpyHostToDevice;
         column_parts(ctx, j.part, false, xb, ctx->d_xb.p, per_s, a, b);
-        if (i == NS - 1) column_parts(ctx, j.part, false, axb, ctx->d_axb.p, per_m, 0, ctx->ncol);
-        e = copy_job(ctx, j);
+        column_parts(ctx, j.part, false, axb, ctx->d_axb.p, per_m, a, b);
+        ctx->piece_c0[i] = a;
+        ctx->piece_c1[i] = b;
+        ctx->piece_waited[i] = false;
+        e = copy_job(ctx, j, &ctx->piece_seq[i]);
+        if (e == cudaSuccess) ctx->npieces = i + 1;
     }
     return e;
+}
+
+// A device address of host array p for the kernels (mapped page-locked
+// memory, or pageable memory on a device that uses the host's page tables);
+// null where the device cannot read it.
+const void *host_view(letkf_ctx *ctx, const void *p)
+{
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type == cudaMemoryTypeHost) return a.devicePointer;
+    if (a.type != cudaMemoryTypeUnregistered) return nullptr;
+    int pma = 0;
+    if (cudaDeviceGetAttribute(&pma, cudaDevAttrPageableMemoryAccess, ctx->device) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return pma ? p : nullptr;
 }
 
 // Wait for the copy agent's jobs (none without a pageable buffer).
@@ -415,6 +457,10 @@ cudaError_t launch_core(letkf_ctx *ctx, const double *xb, const double *axb, dou
     cudaError_t e = lg_members_if_pending(ctx);
     if (e != cudaSuccess) return e;
     if (ctx->lists_need_ef && (e = lg_launch_list_efactor(ctx)) != cudaSuccess) return e;
+    // the cores read the state: its copy first (the staged k = 64 core waits
+    // before each block's update for the block's columns)
+    const bool staged = lg_is_mixed(ctx->params.precision) && ctx->k == 64 && ctx->params.overlap == 0;
+    if (!staged && (e = lg_state_wait(ctx, 0, ctx->ncol)) != cudaSuccess) return e;
     const LgGrid g = lg_grid(ctx);
     // overlapped cubes: each cube's trans now, the columns' averages after
     // the last window (lg_launch_overlap_update)
@@ -856,17 +902,25 @@ cudaError_t lg_members_if_pending(letkf_ctx *ctx)
 {
     if (!ctx->members_pending) return cudaSuccess;
     ctx->members_pending = false;
-    // the state copy on the copy streams (pageable: the agent has issued it
-    // and recorded the events once it drains)
-    cudaError_t e = drain_copies(ctx);
+    // H's rows: gathered from the host arrays, else the whole state copy
+    cudaError_t e = ctx->gathered ? cudaStreamWaitEvent(ctx->stream, ctx->gev, 0) : lg_state_wait(ctx, 0, ctx->ncol);
     if (e != cudaSuccess) return e;
-    for (int i = 0; i < letkf_ctx::kCopyStreams; i++) {
-        e = cudaStreamWaitEvent(ctx->stream, ctx->cev[i], 0);
-        if (e != cudaSuccess) return e;
-    }
     return lg_launch_obs_prepare(ctx, lg_grid(ctx), ctx->pend_xb, ctx->pend_axb, ctx->pend_no, ctx->pend_lat,
                                  ctx->pend_lon, ctx->pend_ph, ctx->pend_lev, ctx->pend_var, ctx->pend_yo,
                                  ctx->pend_rinv, 2);
+}
+
+cudaError_t lg_state_wait(letkf_ctx *ctx, int64_t c0, int64_t c1)
+{
+    for (int i = 0; i < ctx->npieces; i++) {
+        if (ctx->piece_waited[i] || ctx->piece_c1[i] <= c0 || ctx->piece_c0[i] >= c1) continue;
+        // a piece of the copy thread: its event is recorded once the job is issued
+        if (ctx->piece_seq[i]) ctx->agent->wait_issued(ctx->piece_seq[i]);
+        const cudaError_t e = cudaStreamWaitEvent(ctx->stream, ctx->pev[i], 0);
+        if (e != cudaSuccess) return e;
+        ctx->piece_waited[i] = true;
+    }
+    return cudaSuccess;
 }
 
 cudaError_t lg_sink_columns(letkf_ctx *ctx, int64_t c0, int64_t c1)
@@ -908,6 +962,29 @@ int lg_run_analysis(letkf_ctx *ctx, const letkf_obs *obs, bool host_obs, const d
     int rc = stage_obs(ctx, obs, host_obs, od);
     if (rc) return rc;
     LG_CUDA(cudaEventRecord(ctx->ev[1], ctx->stream));
+    ctx->gathered = false;
+    if (ctx->copy_xb) {
+        // The state copy, behind the observations (small copies that would
+        // wait behind it on the copy engines).  Where the device can read the
+        // host arrays, the rows H reads go first, by a kernel on the first
+        // copy stream, and the bulk copy follows: H's members pass then waits
+        // for those rows only, the geometry and the search run meanwhile.
+        cudaEvent_t after = nullptr;
+        if (ctx->gather_xb && dxb == ctx->d_xb.p && daxb == ctx->d_axb.p) {
+            if (!ctx->gev) LG_CUDA(cudaEventCreateWithFlags(&ctx->gev, cudaEventDisableTiming));
+            LG_CUDA(cudaEventRecord(ctx->sev[0], ctx->stream));
+            LG_CUDA(cudaStreamWaitEvent(ctx->cstream[0], ctx->sev[0], 0));
+            LG_CUDA(lg_launch_gather_rows(ctx, ctx->cstream[0], lg_grid(ctx), obs->nobs, od.lat, od.lon, od.ph,
+                                          od.lev, od.var, ctx->gather_xb, ctx->gather_axb, ctx->d_xb.p,
+                                          ctx->d_axb.p));
+            LG_CUDA(cudaEventRecord(ctx->gev, ctx->cstream[0]));
+            after = ctx->gev;
+            ctx->gathered = true;
+        }
+        const cudaError_t e = state_in(ctx, ctx->copy_xb, ctx->copy_axb, after);
+        ctx->copy_xb = ctx->copy_axb = nullptr;
+        if (e != cudaSuccess) return set_err(ctx, LETKF_ERR_CUDA, cudaGetErrorString(e));
+    }
     rc = obs_prepare(ctx, dxb, daxb, od, obs->nobs, state_in_flight);
     if (rc) return rc;
     LG_CUDA(cudaEventRecord(ctx->ev[2], ctx->stream));
@@ -976,6 +1053,15 @@ int run_impl(letkf_ctx *ctx, const double *xb, const double *axb, const letkf_ob
         LG_CUDA(copy_streams(ctx));
         LG_CUDA(ctx->d_xa.reserve(nstate));
         LG_CUDA(ctx->d_axa.reserve(nmean));
+        // device views of the input arrays for H's rows (null: H waits)
+        ctx->gather_xb = ctx->gather_axb = nullptr;
+        if (ctx->host_read) {
+            const void *vx = host_view(ctx, xb), *va = host_view(ctx, axb);
+            if (vx && va) {
+                ctx->gather_xb = static_cast<const double *>(vx);
+                ctx->gather_axb = static_cast<const double *>(va);
+            }
+        }
         // from the state copy on, every return passes the join below: no
         // copy may still use the caller's buffers after the call
         ctx->agent_on = pageable(xb) || pageable(axb) || pageable(xa) || pageable(axa);
@@ -988,13 +1074,11 @@ int run_impl(letkf_ctx *ctx, const double *xb, const double *axb, const letkf_ob
                 return set_err(ctx, LETKF_ERR_ALLOC, "cannot start the host copy thread");
             }
         }
-        cudaError_t e = state_in(ctx, xb, axb);
-        if (e != cudaSuccess) {
-            drain_copies(ctx);
-            ctx->agent_on = false;
-            cudaStreamSynchronize(ctx->stream);
-            return set_err(ctx, LETKF_ERR_CUDA, cudaGetErrorString(e));
-        }
+        // the state goes in once the observations are staged (lg_run_analysis)
+        LG_CUDA(ctx->d_xb.reserve(nstate));
+        LG_CUDA(ctx->d_axb.reserve(nmean));
+        ctx->copy_xb = xb;
+        ctx->copy_axb = axb;
         dxb = ctx->d_xb.p;
         daxb = ctx->d_axb.p;
         dxa = ctx->d_xa.p;
@@ -1023,6 +1107,10 @@ int run_impl(letkf_ctx *ctx, const double *xb, const double *axb, const letkf_ob
         ctx->lists_need_ef = false;
         const cudaError_t ae = drain_copies(ctx);
         ctx->agent_on = false;
+        ctx->npieces = 0;
+        ctx->gather_xb = ctx->gather_axb = nullptr;
+        ctx->gathered = false;
+        ctx->copy_xb = ctx->copy_axb = nullptr;
         for (int i = 0; i < letkf_ctx::kCopyStreams; i++) {
             LG_CUDA(cudaEventRecord(ctx->cev[i], ctx->cstream[i]));
             LG_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->cev[i], 0));
@@ -1295,6 +1383,9 @@ int letkf_gpu_destroy(letkf_ctx *ctx)
                 if (ctx->stg_ev[s][h][i]) cudaEventDestroy(ctx->stg_ev[s][h][i]);
     ctx->agent.reset();
     for (cudaEvent_t e : ctx->agent_ev) cudaEventDestroy(e);
+    for (int i = 0; i < letkf_ctx::kPieces; i++)
+        if (ctx->pev[i]) cudaEventDestroy(ctx->pev[i]);
+    if (ctx->gev) cudaEventDestroy(ctx->gev);
     for (int i = 0; i < letkf_ctx::kCopyStreams; i++) {
         if (ctx->cev[i]) cudaEventDestroy(ctx->cev[i]);
         if (ctx->sev[i]) cudaEventDestroy(ctx->sev[i]);
@@ -1401,6 +1492,13 @@ void letkf_final_gpu_(int *ierr)
 {
     *ierr = letkf_gpu_destroy(g_fctx);
     g_fctx = nullptr;
+}
+
+int letkf_gpu_set_host_read(letkf_ctx *ctx, int on)
+{
+    if (!ctx) return LETKF_ERR_INVALID;
+    ctx->host_read = on ? 1 : 0;
+    return LETKF_OK;
 }
 
 int letkf_gpu_set_schedule(letkf_ctx *ctx, int chunk)

@@ -248,7 +248,10 @@ class LgCopyAgent {
   public:
     explicit LgCopyAgent(int device);
     ~LgCopyAgent();     // issues what is queued, then joins the thread
-    void push(const LgCopyJob &job);
+    // queues a job; returns its number (1, 2, ... over the agent's life)
+    uint64_t push(const LgCopyJob &job);
+    // waits until job `seq` and those before it have been issued
+    void wait_issued(uint64_t seq);
     // waits until every pushed job has been issued (pageable copies: done);
     // returns and clears the first error of those jobs
     cudaError_t drain();
@@ -261,7 +264,8 @@ class LgCopyAgent {
     std::mutex mu_;
     std::condition_variable work_, idle_;
     std::deque<LgCopyJob> queue_;
-    bool busy_ = false, stop_ = false;
+    bool stop_ = false;
+    uint64_t pushed_ = 0, issued_ = 0;
     cudaError_t err_ = cudaSuccess;
     std::thread thread_;
 };
@@ -367,6 +371,29 @@ struct letkf_ctx {
     // a host buffer of the run is pageable: the copy-stream copies go
     // through the copy agent, each job with its own main-stream event
     bool agent_on = false;
+    // The state copy of a run with host buffers, in pieces of columns: piece
+    // i holds columns [piece_c0[i], piece_c1[i]) (xb and axb), its copy
+    // stream records pev[i] once they are in, and piece_seq[i] is its copy
+    // agent job (0: issued by the calling thread).  lg_state_wait makes the
+    // main stream wait for the pieces a launch reads.
+    static constexpr int kPieces = 8;
+    cudaEvent_t pev[kPieces] = {};
+    int64_t piece_c0[kPieces] = {}, piece_c1[kPieces] = {};
+    uint64_t piece_seq[kPieces] = {};
+    bool piece_waited[kPieces] = {};
+    int npieces = 0;
+    // H reads the state rows it needs straight from the host arrays through
+    // these device views (null: H waits for the whole state), while the bulk
+    // copy runs; d_rowmark marks the (column, row) pairs already read
+    const double *gather_xb = nullptr, *gather_axb = nullptr;
+    bool gathered = false;                   // this run's H rows come from the gather
+    cudaEvent_t gev = nullptr;               // the gather done (first copy stream)
+    // the host arrays of a state copy that lg_run_analysis starts once the
+    // observations are staged (small copies that would otherwise queue
+    // behind the bulk copy on the copy engines)
+    const double *copy_xb = nullptr, *copy_axb = nullptr;
+    int host_read = 1;                       // letkf_gpu_set_host_read
+    DevBuf<unsigned> d_rowmark;
     // the host arrays' column layout: column c (c % nlat along latitude,
     // c / nlat along longitude) sits at host column host_off + c % nlat +
     // host_ld * (c / nlat); host_ld = nlat, host_off = 0 without a halo
@@ -404,6 +431,15 @@ void lg_stage_mark(letkf_ctx *ctx, int s, bool end);
 // Kernel launchers (letkf_prep.cu, letkf_search.cu, letkf_core.cu).
 // H: mode 0 everything; 1 the per-observation geometry, weights and bucket
 // (no state read); 2 the members, the means and the departures.
+// Copy the state rows the observation operator reads from the host arrays
+// (device views hxb, haxb in the run's host layout) into dxb, daxb.
+cudaError_t lg_launch_gather_rows(letkf_ctx *ctx, cudaStream_t stream, const LgGrid &g, int64_t nobs,
+                                  const double *olat, const double *olon, const double *oph,
+                                  const int32_t *olev, const int32_t *ovar, const double *hxb,
+                                  const double *haxb, double *dxb, double *daxb);
+// Make the main stream wait for the pieces of the state copy that hold
+// columns [c0, c1) (no-op when the state is not being copied in).
+cudaError_t lg_state_wait(letkf_ctx *ctx, int64_t c0, int64_t c1);
 cudaError_t lg_launch_obs_prepare(letkf_ctx *ctx, const LgGrid &g, const double *xb,
                                   const double *axb, int64_t nobs, const double *olat,
                                   const double *olon, const double *oph, const int32_t *olev,

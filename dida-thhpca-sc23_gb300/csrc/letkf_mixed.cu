@@ -1707,7 +1707,11 @@ cudaError_t launch_mixed(letkf_ctx *ctx, const LgGrid &g, const double *xb, cons
                 lg_stage_mark(ctx, 3, true);
                 if ((e = cudaGetLastError()) != cudaSuccess) break;
             }
-            // the update from T and wbar
+            // the update from T and wbar, once the block's columns of the state
+            // are in (a run from host buffers copies them in meanwhile)
+            if (ctx->params.cube_n == 1) e = lg_state_wait(ctx, b0, b1);
+            else e = lg_state_wait(ctx, 0, ctx->ncol);
+            if (e != cudaSuccess) break;
             lg_stage_mark(ctx, 2, false);
             e = launch_stage<K, 3>(ctx, g, xb, axb, xa, axa, trans_out, w_out, chunk, nchunks, nsm);
             lg_stage_mark(ctx, 2, true);

@@ -46,6 +46,111 @@ __device__ __forceinline__ double bilin(const double *__restrict__ xb, const dou
     return r1 * q.t2 + r2 * (1.0 - q.t2);
 }
 
+// The grid cell of a valid observation (find_obs_grid, letkf_obs.F90:199-241;
+// the spacing is a float difference) and its state row: the level's row for
+// level select (h_mode 1), else the variable's first row with psearch set for
+// a 3-D variable (the pressure search of obs_interpolation_3d_2).
+__device__ __forceinline__ void obs_stencil(const LgGrid &g, const LgParams &prm, double lat, double lon, int v,
+                                            int lev, Corners &q, int &row, bool &psearch)
+{
+    const bool is3d = v >= g.nvar2d;
+    const int tx = first_ge(g.glat, g.nlat + 1, lat);
+    const int ty = first_ge(g.glon, g.nlon + 1, lon);
+    double ax = 0.0, ay = 0.0;
+    if (tx > 1) {
+        const double dlat = (double)(g.glat[tx - 1] - g.glat[tx - 2]);
+        ax = (dlat - lat + (double)g.glat[tx - 2]) / dlat;
+    }
+    if (ty > 1) {
+        const double dlon = (double)(g.glon[ty - 1] - g.glon[ty - 2]);
+        ay = (dlon - lon + (double)g.glon[ty - 2]) / dlon;
+    }
+    // rows beyond the poles clamp, columns wrap around the circle
+    const int la0 = min(max(tx - 2, 0), g.nlat - 1), la1 = min(max(tx - 1, 0), g.nlat - 1);
+    const int lo0 = ((ty - 2) % g.nlon + g.nlon) % g.nlon, lo1 = (ty - 1) % g.nlon;
+    q.c11 = la0 + (int64_t)g.nlat * lo0;
+    q.c21 = la1 + (int64_t)g.nlat * lo0;
+    q.c12 = la0 + (int64_t)g.nlat * lo1;
+    q.c22 = la1 + (int64_t)g.nlat * lo1;
+    q.t1 = ax;
+    q.t2 = ay;
+    const int start = is3d ? g.nvar2d + (v - g.nvar2d) * g.nz : v;
+    psearch = is3d && prm.h_mode == 0;
+    row = (is3d && prm.h_mode == 1) ? start + lev - 1 : start;
+}
+
+// Validity of an observation as k_obs_prepare tests it, with its level.
+__device__ __forceinline__ bool obs_valid(const LgGrid &g, const LgParams &prm, double lat, double lon, int v,
+                                          const int32_t *olev, const double *oph, int64_t o, int &lev)
+{
+    const bool is3d = v >= g.nvar2d;
+    lev = 1;
+    bool ok = (lat >= -90.0 && lat <= 90.0 && lon >= 0.0 && lon <= 360.0 && v >= 0 && v < g.nvar2d + g.nvar3d);
+    if (ok && is3d && prm.h_mode == 1) {
+        lev = olev[o];
+        ok = lev >= 1 && lev <= g.nz;
+    }
+    if (ok && is3d && prm.h_mode == 0) ok = oph[o] > 0.0;
+    return ok;
+}
+
+// The state rows the observation operator reads, copied from the caller's
+// host arrays (a device-accessible view: mapped page-locked memory, or
+// pageable memory where the device shares the host's page tables) into the
+// device state, so that H can run while the bulk copy of the state is still
+// under way.  One warp per observation: the rows of its four stencil columns
+// (the level's row; with the pressure search the surface-pressure row and
+// every level of the variable), each (column, row) once per run (a bit in
+// `mark` decides which warp copies it), k doubles of xb and one of axb.  The
+// host arrays hold column c at host column off + c % nlat + ld * (c / nlat).
+__global__ void __launch_bounds__(256)
+k_gather_rows(LgGrid g, LgParams prm, int64_t nobs, const double *__restrict__ olat,
+              const double *__restrict__ olon, const double *__restrict__ oph, const int32_t *__restrict__ olev,
+              const int32_t *__restrict__ ovar, const double *__restrict__ hxb, const double *__restrict__ haxb,
+              int64_t ld, int64_t off, double *__restrict__ dxb, double *__restrict__ daxb,
+              unsigned *__restrict__ mark, int vec2)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int k = g.k, n = g.n;
+    for (int64_t o = warp; o < nobs; o += nwarps) {
+        const double lat = olat[o], lon = olon[o];
+        const int v = ovar[o];
+        int lev = 1;
+        if (!obs_valid(g, prm, lat, lon, v, olev, oph, o, lev)) continue;
+        Corners q;
+        int row = 0;
+        bool psearch = false;
+        obs_stencil(g, prm, lat, lon, v, lev, q, row, psearch);
+        const int nrows = psearch ? g.nz + 1 : 1;
+        const int64_t cols[4] = {q.c11, q.c21, q.c12, q.c22};
+        for (int ci = 0; ci < 4; ci++) {
+            const int64_t c = cols[ci];
+            const int64_t hc = off + c % g.nlat + ld * (c / g.nlat);
+            for (int ri = 0; ri < nrows; ri++) {
+                const int r = ri == g.nz ? g.ps_row : row + ri;
+                const int64_t bit = c * n + r;
+                unsigned fresh = 0;
+                if (lane == 0) {
+                    const unsigned m = 1u << (bit & 31);
+                    fresh = (atomicOr(mark + (bit >> 5), m) & m) == 0;
+                }
+                if (!__shfl_sync(0xffffffffu, fresh, 0)) continue;
+                const double *src = hxb + (hc * n + r) * k;
+                double *dst = dxb + bit * k;
+                if (vec2) {
+                    for (int e = lane; e < k / 2; e += 32)
+                        reinterpret_cast<double2 *>(dst)[e] = reinterpret_cast<const double2 *>(src)[e];
+                } else {
+                    for (int e = lane; e < k; e += 32) dst[e] = src[e];
+                }
+                if (lane == 0) daxb[bit] = haxb[hc * n + r];
+            }
+        }
+    }
+}
+
 __device__ __forceinline__ double ph_interface(const LgGrid &g, int i, double ps)
 {
     return g.hyai[i] * (g.p0 - g.ptop) + g.hybi[i] * (ps - g.ptop) + g.ptop;
@@ -91,15 +196,8 @@ k_obs_prepare(LgGrid g, LgParams prm, const double *__restrict__ xb, const doubl
         if (o < nobs) {
             const double lat = olat[o], lon = olon[o];
             const int v = ovar[o];
-            const bool is3d = v >= g.nvar2d;
             int lev = 1;
-            ok = (lat >= -90.0 && lat <= 90.0 && lon >= 0.0 && lon <= 360.0 &&
-                  v >= 0 && v < g.nvar2d + g.nvar3d);
-            if (ok && is3d && prm.h_mode == 1) {
-                lev = olev[o];
-                ok = lev >= 1 && lev <= g.nz;
-            }
-            if (ok && is3d && prm.h_mode == 0) ok = oph[o] > 0.0;
+            ok = obs_valid(g, prm, lat, lon, v, olev, oph, o, lev);
             if (!ok) {
                 if (mode != 1) {
                     dep[o] = 0.0;
@@ -111,30 +209,7 @@ k_obs_prepare(LgGrid g, LgParams prm, const double *__restrict__ xb, const doubl
                     atomicOr(status, LG_ST_BAD_OBS);
                 }
             } else {
-                // find_obs_grid (letkf_obs.F90:199-241); the spacing is a float difference
-                const int tx = first_ge(g.glat, g.nlat + 1, lat);
-                const int ty = first_ge(g.glon, g.nlon + 1, lon);
-                double ax = 0.0, ay = 0.0;
-                if (tx > 1) {
-                    const double dlat = (double)(g.glat[tx - 1] - g.glat[tx - 2]);
-                    ax = (dlat - lat + (double)g.glat[tx - 2]) / dlat;
-                }
-                if (ty > 1) {
-                    const double dlon = (double)(g.glon[ty - 1] - g.glon[ty - 2]);
-                    ay = (dlon - lon + (double)g.glon[ty - 2]) / dlon;
-                }
-                // rows beyond the poles clamp, columns wrap around the circle
-                const int la0 = min(max(tx - 2, 0), g.nlat - 1), la1 = min(max(tx - 1, 0), g.nlat - 1);
-                const int lo0 = ((ty - 2) % g.nlon + g.nlon) % g.nlon, lo1 = (ty - 1) % g.nlon;
-                q.c11 = la0 + (int64_t)g.nlat * lo0;
-                q.c21 = la1 + (int64_t)g.nlat * lo0;
-                q.c12 = la0 + (int64_t)g.nlat * lo1;
-                q.c22 = la1 + (int64_t)g.nlat * lo1;
-                q.t1 = ax;
-                q.t2 = ay;
-                const int start = is3d ? g.nvar2d + (v - g.nvar2d) * g.nz : v;
-                psearch = is3d && prm.h_mode == 0;
-                row = (is3d && prm.h_mode == 1) ? start + lev - 1 : start;
+                obs_stencil(g, prm, lat, lon, v, lev, q, row, psearch);
                 if (psearch) p_obs = oph[o];
                 const float rf = (float)orinv[o];
                 // scaled perturbations for the tensor-core products: y sqrt(rdiaginv)
@@ -319,6 +394,28 @@ cudaError_t lg_launch_obs_prepare(letkf_ctx *ctx, const LgGrid &g, const double 
         lg_is_mixed(ctx->params.precision) ? ctx->d_ys32.p : nullptr,
         lg_is_mixed(ctx->params.precision) ? ctx->d_oef.p : nullptr,
         ctx->nblat, ctx->nblon, ctx->cell_lat, ctx->cell_lon, ctx->d_status.p, mode);
+    return cudaGetLastError();
+}
+
+cudaError_t lg_launch_gather_rows(letkf_ctx *ctx, cudaStream_t stream, const LgGrid &g, int64_t nobs,
+                                  const double *olat, const double *olon, const double *oph,
+                                  const int32_t *olev, const int32_t *ovar, const double *hxb,
+                                  const double *haxb, double *dxb, double *daxb)
+{
+    if (nobs == 0) return cudaSuccess;
+    const size_t words = ((size_t)ctx->ncol * ctx->n + 31) / 32;
+    cudaError_t e = ctx->d_rowmark.reserve(words);
+    if (e == cudaSuccess) e = cudaMemsetAsync(ctx->d_rowmark.p, 0, words * sizeof(unsigned), stream);
+    if (e != cudaSuccess) return e;
+    const LgParams prm = lg_params(ctx);
+    lg_count_launch();
+    // two blocks per SM keep ~1 MB of reads in flight (enough for the host
+    // link) and leave the SMs to the geometry and search running beside it
+    int nsm = 0;
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device);
+    k_gather_rows<<<grid_for(nobs * 32, 256, 2 * (nsm > 0 ? nsm : 152)), 256, 0, stream>>>(
+        g, prm, nobs, olat, olon, oph, olev, ovar, hxb, haxb, ctx->host_ld, ctx->host_off, dxb, daxb,
+        ctx->d_rowmark.p, (g.k % 2 == 0 && (uintptr_t)hxb % 16 == 0 && (uintptr_t)dxb % 16 == 0) ? 1 : 0);
     return cudaGetLastError();
 }
 

@@ -40,7 +40,7 @@ ERROR_NAMES = {
 
 EXPORTED = [
     "letkf_gpu_create", "letkf_gpu_set_stream", "letkf_gpu_set_keep_trans", "letkf_gpu_run",
-    "letkf_gpu_run_halo", "letkf_gpu_set_schedule",
+    "letkf_gpu_run_halo", "letkf_gpu_set_schedule", "letkf_gpu_set_host_read",
     "letkf_gpu_synchronize", "letkf_gpu_obs_operator", "letkf_gpu_local_obs",
     "letkf_gpu_last_trans", "letkf_gpu_core_batch", "letkf_gpu_get_stats",
     "letkf_gpu_last_error", "letkf_gpu_destroy", "letkf_gpu_launch_count",
@@ -127,6 +127,7 @@ def load_library(path: str = LIB_PATH):
     L.letkf_gpu_run.argtypes = [vp, vp, vp, C.POINTER(Obs), vp, vp, i32]
     L.letkf_gpu_run_halo.argtypes = [vp, i32, vp, vp, C.POINTER(Obs), vp, vp]
     L.letkf_gpu_set_schedule.argtypes = [vp, i32]
+    L.letkf_gpu_set_host_read.argtypes = [vp, i32]
     L.letkf_gpu_synchronize.argtypes = [vp]
     L.letkf_gpu_obs_operator.argtypes = [vp, vp, vp, C.POINTER(Obs), vp, vp]
     L.letkf_gpu_local_obs.argtypes = [vp, vp, vp, vp]
@@ -360,6 +361,11 @@ class LetkfGPU:
         """Most polls of each bounded tensor-core wait (< 0: the default; 0:
         every wait gives up at once, which exercises the timeout path)."""
         self._check(self.L.letkf_gpu_set_wait_limit(self.h, int(polls)), "set_wait_limit")
+
+    def set_host_read(self, on: bool = True):
+        """Let H read its state rows from the host arrays while the state is
+        copied in (same results; off: H waits for the whole state)."""
+        self._check(self.L.letkf_gpu_set_host_read(self.h, int(on)), "set_host_read")
 
     def set_schedule(self, chunk: int = 0):
         """Work-queue chunk of the mixed form (0: the default); speed only."""

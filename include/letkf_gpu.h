@@ -178,6 +178,16 @@ int letkf_gpu_set_stream(letkf_ctx *ctx, void *stream);
 int letkf_gpu_run(letkf_ctx *ctx, const double *xb, const double *axb, const letkf_obs *obs,
                   double *xa, double *axa, int flags);
 
+/* With host buffers (letkf_gpu_run, letkf_gpu_run_halo), let the kernels
+ * read the state rows of the observation operator straight from the caller's
+ * arrays when the device can address them (page-locked memory, or pageable
+ * memory on a device that uses the host's page tables, such as a Grace
+ * host): H and the local analyses then run while the bulk copy of the state
+ * is still under way, and each block of the analysis waits only for its own
+ * columns.  on = 0: H waits for the whole state.  The default is 1; the
+ * results are the same either way.  No counterpart in the reference.        */
+int letkf_gpu_set_host_read(letkf_ctx *ctx, int on);
+
 /* letkf_gpu_run on host arrays in letkf_run's own layout with a halo
  * (letkf.F90:157-257; xb(ens, n, 1-halo:nlat+halo, 1-halo:nlon+halo), axb,
  * xa, axa alike): the copies read and write the interior columns in place

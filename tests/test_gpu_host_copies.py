@@ -67,14 +67,20 @@ def halo_untouched(a, w, h, fill):
 
 
 # 91 x 182 columns: the staged core's three copy-out blocks end at cubes 12288
-# and 16384, both in the middle of a longitude line (91 columns each)
-@pytest.mark.parametrize("precision", ["mixed", "fp64"])
-def test_host_paths_equal_device_run(letkf, synthetic, precision):
+# and 16384, both in the middle of a longitude line (91 columns each).
+# host_read: H reads its rows from the host arrays while the state is copied
+# in (each block's update waits for its own columns), or waits for the copy.
+@pytest.mark.parametrize("precision,h_mode,host_read", [("mixed", 1, True), ("mixed", 1, False),
+                                                        ("fp64", 1, True), ("fp64", 0, True),
+                                                        ("fp64", 0, False)])
+def test_host_paths_equal_device_run(letkf, synthetic, precision, h_mode, host_read):
     nlat = 91 if precision == "mixed" else 15
     k = 64 if precision == "mixed" else 16
-    w = synthetic.small_case(nlat=nlat, nlon=2 * nlat, nz=2, k=k, nobs=2500, loc_dist_km=900.0, seed=71)
+    w = synthetic.small_case(nlat=nlat, nlon=2 * nlat, nz=2, k=k, nobs=2500, loc_dist_km=900.0, seed=71,
+                             h_mode=h_mode)
     prec = letkf.LETKF_PREC_MIXED if precision == "mixed" else letkf.LETKF_PREC_FP64
     ctx = letkf.LetkfGPU.from_workload(w, precision=prec)
+    ctx.set_host_read(host_read)
     xa_d, axa_d = device_run(letkf, ctx, w)
     # pageable numpy buffers (the copy thread)
     xa_p, axa_p = ctx.run(np.array(w.xb), np.array(w.axb), w.obs)
