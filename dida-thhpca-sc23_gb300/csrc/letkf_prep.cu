@@ -98,10 +98,12 @@ __device__ __forceinline__ bool obs_valid(const LgGrid &g, const LgParams &prm, 
 // host arrays (a device-accessible view: mapped page-locked memory, or
 // pageable memory where the device shares the host's page tables) into the
 // device state, so that H can run while the bulk copy of the state is still
-// under way.  One warp per observation: the rows of its four stencil columns
-// (the level's row; with the pressure search the surface-pressure row and
-// every level of the variable), each (column, row) once per run (a bit in
-// `mark` decides which warp copies it), k doubles of xb and one of axb.  The
+// under way: the level's row of each observation's four stencil columns (with
+// the pressure search, the surface-pressure row and every level of the
+// variable), each (column, row) once per run (a bit in `mark` decides which
+// lane claims it), k doubles of xb and one of axb.  A lane owns one
+// (observation, corner) pair; the warp then copies the rows its lanes claimed,
+// four at a time, so that many reads over the host link are in flight.  The
 // host arrays hold column c at host column off + c % nlat + ld * (c / nlat).
 __global__ void __launch_bounds__(256)
 k_gather_rows(LgGrid g, LgParams prm, int64_t nobs, const double *__restrict__ olat,
@@ -114,38 +116,84 @@ k_gather_rows(LgGrid g, LgParams prm, int64_t nobs, const double *__restrict__ o
     const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const int k = g.k, n = g.n;
-    for (int64_t o = warp; o < nobs; o += nwarps) {
-        const double lat = olat[o], lon = olon[o];
-        const int v = ovar[o];
-        int lev = 1;
-        if (!obs_valid(g, prm, lat, lon, v, olev, oph, o, lev)) continue;
-        Corners q;
-        int row = 0;
-        bool psearch = false;
-        obs_stencil(g, prm, lat, lon, v, lev, q, row, psearch);
-        const int nrows = psearch ? g.nz + 1 : 1;
-        const int64_t cols[4] = {q.c11, q.c21, q.c12, q.c22};
-        for (int ci = 0; ci < 4; ci++) {
-            const int64_t c = cols[ci];
-            const int64_t hc = off + c % g.nlat + ld * (c / g.nlat);
-            for (int ri = 0; ri < nrows; ri++) {
-                const int r = ri == g.nz ? g.ps_row : row + ri;
-                const int64_t bit = c * n + r;
-                unsigned fresh = 0;
-                if (lane == 0) {
-                    const unsigned m = 1u << (bit & 31);
-                    fresh = (atomicOr(mark + (bit >> 5), m) & m) == 0;
+    const int64_t npairs = 4 * nobs;
+    for (int64_t base = warp * 32; base < npairs; base += nwarps * 32) {
+        // this lane's (observation, corner): its column, first row and rows
+        const int64_t pr = base + lane;
+        int64_t col = 0, hcol = 0;
+        int row0 = 0, nrows = 0;
+        if (pr < npairs) {
+            const int64_t o = pr >> 2;
+            const double lat = olat[o], lon = olon[o];
+            const int v = ovar[o];
+            int lev = 1;
+            if (obs_valid(g, prm, lat, lon, v, olev, oph, o, lev)) {
+                Corners q;
+                bool psearch = false;
+                obs_stencil(g, prm, lat, lon, v, lev, q, row0, psearch);
+                const int corner = (int)(pr & 3);
+                col = corner == 0 ? q.c11 : corner == 1 ? q.c21 : corner == 2 ? q.c12 : q.c22;
+                hcol = off + col % g.nlat + ld * (col / g.nlat);
+                nrows = psearch ? g.nz + 1 : 1;
+            }
+        }
+        int maxr = nrows;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) maxr = max(maxr, __shfl_xor_sync(0xffffffffu, maxr, o));
+        for (int ri = 0; ri < maxr; ri++) {
+            const int r = ri == g.nz ? g.ps_row : row0 + ri;
+            bool fresh = false;
+            if (ri < nrows) {
+                const int64_t bit = col * n + r;
+                const unsigned m = 1u << (bit & 31);
+                fresh = (atomicOr(mark + (bit >> 5), m) & m) == 0;
+                if (fresh) daxb[bit] = haxb[hcol * n + r];
+            }
+            unsigned todo = __ballot_sync(0xffffffffu, fresh);
+            while (todo) {
+                // up to four claimed rows, copied by the whole warp
+                int src[4];
+                int cnt = 0;
+#pragma unroll
+                for (int t = 0; t < 4; t++) {
+                    src[t] = todo ? __ffs(todo) - 1 : -1;
+                    if (todo) {
+                        todo &= todo - 1;
+                        cnt++;
+                    }
                 }
-                if (!__shfl_sync(0xffffffffu, fresh, 0)) continue;
-                const double *src = hxb + (hc * n + r) * k;
-                double *dst = dxb + bit * k;
+                const double *sp[4];
+                double *dp[4];
+#pragma unroll
+                for (int t = 0; t < 4; t++) {
+                    const int sl = src[t] < 0 ? 0 : src[t];
+                    const long long c = __shfl_sync(0xffffffffu, (long long)col, sl);
+                    const long long hc = __shfl_sync(0xffffffffu, (long long)hcol, sl);
+                    const int rr = __shfl_sync(0xffffffffu, r, sl);
+                    sp[t] = hxb + ((int64_t)hc * n + rr) * k;
+                    dp[t] = dxb + ((int64_t)c * n + rr) * k;
+                }
                 if (vec2) {
-                    for (int e = lane; e < k / 2; e += 32)
-                        reinterpret_cast<double2 *>(dst)[e] = reinterpret_cast<const double2 *>(src)[e];
+                    for (int e = lane; e < k / 2; e += 32) {
+                        double2 x[4];
+#pragma unroll
+                        for (int t = 0; t < 4; t++)
+                            if (t < cnt) x[t] = reinterpret_cast<const double2 *>(sp[t])[e];
+#pragma unroll
+                        for (int t = 0; t < 4; t++)
+                            if (t < cnt) reinterpret_cast<double2 *>(dp[t])[e] = x[t];
+                    }
                 } else {
-                    for (int e = lane; e < k; e += 32) dst[e] = src[e];
+                    for (int e = lane; e < k; e += 32) {
+                        double x[4];
+#pragma unroll
+                        for (int t = 0; t < 4; t++)
+                            if (t < cnt) x[t] = sp[t][e];
+#pragma unroll
+                        for (int t = 0; t < 4; t++)
+                            if (t < cnt) dp[t][e] = x[t];
+                    }
                 }
-                if (lane == 0) daxb[bit] = haxb[hc * n + r];
             }
         }
     }
