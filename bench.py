@@ -297,9 +297,14 @@ def run_reference(args, rank, world):
 
 
 # ---------------------------------------------------------------------------
-def _time_form(torch, letkf, ctx, bufs, stream, steps, warmup):
-    """Warm up, then time `steps` device-resident analyses with CUDA events."""
+def _time_form(torch, letkf, ctx, bufs, stream, steps, warmup, autotune=False):
+    """Warm up, then time `steps` device-resident analyses with CUDA events.
+    autotune: first let the library pick the work-queue schedule
+    (letkf_gpu_autotune, untimed, as a caller does once per context; the
+    schedule changes the speed only, not the analysis)."""
     xb_d, axb_d, obs_dev, xa_d, axa_d = bufs
+    if autotune:
+        ctx.autotune_device(xb_d, axb_d, obs_dev, xa_d, axa_d)
     for _ in range(warmup):
         ctx.run_device(xb_d, axb_d, obs_dev, xa_d, axa_d)
     torch.cuda.synchronize()
@@ -490,7 +495,8 @@ def run_ours(args, rank, world, local_rank):
             clocks.start()
             time.sleep(0.3)
         bufs = (xb_d, axb_d, obs_dev, outs[nm][0], outs[nm][1])
-        res[nm] = _time_form(torch, letkf, forms[nm], bufs, stream, args.steps, args.warmup)
+        res[nm] = _time_form(torch, letkf, forms[nm], bufs, stream, args.steps, args.warmup,
+                             autotune=nm != "fp64")
         if nm == head:
             clk = clocks.stop()
     if dist:
@@ -625,6 +631,7 @@ def run_ours(args, rank, world, local_rank):
                    "columns": w.ncol, "ensemble": w.k, "obs": int(w.obs["lat"].size),
                    "sum_p": st["sum_p"], "max_p": st["max_p"],
                    "jacobi_max_sweeps": st["max_sweeps"], "jacobi_sweep_cap_hits": st["n_not_converged"],
+                   "sched_chunk": st["sched_chunk"],
                    "l2": f"inputs larger than L2 (xb {w.xb.nbytes / 1e9:.1f} GB)",
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": whole_job_columns_per_s(world, w.ncol, ms_e2e), "unit": "columns/s",
