@@ -334,6 +334,10 @@ struct letkf_ctx {
     // polls of each bounded tensor-core wait (letkf_gpu_set_wait_limit; < 0: the default)
     int64_t wait_limit = -1;
     DevBuf<int> d_queue;
+    // the staged k = 64 core's eigensolve runs (8 cubes, by cube / 8): the
+    // sweeps each took in the last call, and a block's runs ordered longest
+    // first by them (the next call's warps take the long runs first)
+    DevBuf<int> d_runcost, d_rorder;
     // per-cube results
     DevBuf<double> d_trans, d_w;
     // core_batch staging

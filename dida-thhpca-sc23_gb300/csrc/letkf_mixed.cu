@@ -982,6 +982,42 @@ k_chunk_queue(const int32_t *__restrict__ lcnt, int64_t win0, int64_t win1, int 
     for (int i = threadIdx.x; i < nchunks; i += blockDim.x) queue[i] = (int)(qkeys[i] & 0xffffffffull);
 }
 
+// The eigensolve runs run0 .. run0 + nruns - 1 ordered by their cost in the
+// last call (sweeps summed over the run), longest first, ties in run order
+// (bitonic, one CTA; nruns <= kQueueMax).
+__global__ void __launch_bounds__(1024)
+k_run_order(const int *__restrict__ runcost, int64_t run0, int nruns, int *__restrict__ order)
+{
+    extern __shared__ unsigned long long rkeys[];
+    int np2 = 1;
+    while (np2 < nruns) np2 <<= 1;
+    for (int i = threadIdx.x; i < np2; i += blockDim.x) {
+        unsigned long long key = 0ull;
+        if (i < nruns) {
+            const unsigned long long w = (unsigned long long)(unsigned)max(runcost[run0 + i], 0);
+            key = (w << 32) | (0xffffffffu - (unsigned)i);
+        }
+        rkeys[i] = key;
+    }
+    __syncthreads();
+    for (int k2 = 2; k2 <= np2; k2 <<= 1)
+        for (int j = k2 >> 1; j > 0; j >>= 1) {
+            for (int i = threadIdx.x; i < np2; i += blockDim.x) {
+                const int ixj = i ^ j;
+                if (ixj > i) {
+                    const unsigned long long a = rkeys[i], b = rkeys[ixj];
+                    const bool desc = (i & k2) == 0;
+                    if ((a < b) == desc) {
+                        rkeys[i] = b;
+                        rkeys[ixj] = a;
+                    }
+                }
+            }
+            __syncthreads();
+        }
+    for (int i = threadIdx.x; i < nruns; i += blockDim.x) order[i] = (int)(0xffffffffu - (unsigned)(rkeys[i] & 0xffffffffull));
+}
+
 }  // namespace
 
 // Cubes per work-queue chunk for the run's cube range: the context's
@@ -1039,7 +1075,7 @@ template <int K>
 __global__ void __launch_bounds__(kTE, 1)
 k_eig_warp(int64_t cube0, int64_t cube_end, int R, double cdiag, float tol, const float *__restrict__ mA,
            float *__restrict__ mX, float *__restrict__ mlam, double *__restrict__ mgv, int emit_tw,
-           unsigned long long *__restrict__ counters)
+           unsigned long long *__restrict__ counters, const int *__restrict__ order, int *__restrict__ runcost)
 {
     constexpr int LDW = K + 4, NS = K / 2;
     static_assert(NS == 32, "one lane per column pair");
@@ -1073,6 +1109,10 @@ k_eig_warp(int64_t cube0, int64_t cube_end, int R, double cdiag, float tol, cons
         if (lane == 0) run = (int64_t)atomicAdd(&counters[LG_CNT_QUEUE], 1ull);
         run = __shfl_sync(0xffffffffu, run, 0);
         if (run >= nruns) break;
+        // longest runs of the last call first (the order only decides which
+        // warp takes a run; each run is solved the same way)
+        if (order) run = order[run];
+        int run_sweeps = 0;
         const int64_t c0 = max(cube0, base + run * R), c1 = min(cube_end, base + (run + 1) * R);
         for (int64_t c = c0; c < c1; c++) {
             const float *Ac = mA + (c - cube0) * K * K;
@@ -1146,6 +1186,7 @@ k_eig_warp(int64_t cube0, int64_t cube_end, int R, double cdiag, float tol, cons
             __syncwarp();
             LG_EPHASE(0);
             const int sw = lg_jacobi32w<K, LDW>(Wp, tol, 24);
+            run_sweeps += sw;
             LG_EPHASE(1);
             // lambda_j = |w_j|, x_j = w_j / lambda_j (kept in Wp for the next cube)
             float lo = 3.0e38f, hi = 0.0f;
@@ -1288,6 +1329,8 @@ k_eig_warp(int64_t cube0, int64_t cube_end, int R, double cdiag, float tol, cons
             }
             LG_EPHASE(2);
         }
+        // this run's cost for the next call's order
+        if (runcost && lane == 0) runcost[base / R + run] = run_sweeps;
     }
 #ifdef LG_PHASE_CLOCKS
     if (blockIdx.x == 0 && threadIdx.x == 0)
@@ -1681,6 +1724,29 @@ cudaError_t launch_mixed(letkf_ctx *ctx, const LgGrid &g, const double *xb, cons
             if ((e = cudaMemsetAsync(ctx->d_counters.p + LG_CNT_QUEUE, 0, sizeof(unsigned long long),
                                      ctx->stream)) != cudaSuccess)
                 break;
+            // the block's runs longest first by their sweeps in the last call
+            // (all equal before the first: cube order), so that the warps end
+            // together instead of waiting on a few long runs
+            const int64_t nrun_all = (ctx->ncubes + R - 1) / R;
+            if (ctx->d_runcost.n < (size_t)nrun_all) {
+                if ((e = ctx->d_runcost.reserve((size_t)nrun_all)) != cudaSuccess) break;
+                if ((e = cudaMemsetAsync(ctx->d_runcost.p, 0, sizeof(int) * nrun_all, ctx->stream)) != cudaSuccess)
+                    break;
+            }
+            int *rorder = nullptr;
+            if (runs <= kQueueMax) {
+                if ((e = ctx->d_rorder.reserve((size_t)runs)) != cudaSuccess) break;
+                int np2 = 1;
+                while (np2 < runs) np2 <<= 1;
+                const size_t rsm = sizeof(unsigned long long) * np2;
+                if ((e = cudaFuncSetAttribute(k_run_order, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsm)) !=
+                    cudaSuccess)
+                    break;
+                lg_count_launch();
+                k_run_order<<<1, 1024, rsm, ctx->stream>>>(ctx->d_runcost.p, b0 / R, (int)runs, ctx->d_rorder.p);
+                if ((e = cudaGetLastError()) != cudaSuccess) break;
+                rorder = ctx->d_rorder.p;
+            }
             lg_count_launch();
             lg_stage_mark(ctx, 1, false);
             // LETKF_PREC_MIXED: the warps also form wbar and T (for the update
@@ -1690,7 +1756,7 @@ cudaError_t launch_mixed(letkf_ctx *ctx, const LgGrid &g, const double *xb, cons
             k_eig_warp<K><<<eblocks, kTE, ew, ctx->stream>>>(b0, b1, R, (double)(K - 1) / ctx->params.inflation,
                                                           LG_MIXED_JACOBI_TOL, ctx->d_mA.p, ctx->d_mX.p,
                                                           ctx->d_mlam.p, ctx->d_mg.p, f64eig ? 0 : 1,
-                                                          ctx->d_counters.p);
+                                                          ctx->d_counters.p, rorder, ctx->d_runcost.p);
             lg_stage_mark(ctx, 1, true);
             if ((e = cudaGetLastError()) != cudaSuccess) break;
             if (f64eig) {
