@@ -873,7 +873,57 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
                         break;
                     }
                     lg_tc_fence_after();
-                    if (warp < 4) {
+                    if constexpr (ST == 3 && !MEM) {
+                        // all 8 warps: warp w reads row quadrant w % 4 (the
+                        // tensor-memory lanes it may access) and members
+                        // (w / 4) K/2 .. +K/2 - 1.  The member mean keeps the
+                        // summation order of the one-warp form: the first
+                        // half's eight partial sums go to the second half
+                        // through shared memory, which continues them and
+                        // hands the mean back.
+                        const int q4 = warp & 3, hh = warp >> 2;
+                        const int r = q4 * 32 + lane;
+                        float *xch = reinterpret_cast<float *>(area + 49152);   // [row][8 partials, mean]
+                        float v[K / 2];
+#pragma unroll
+                        for (int c0 = 0; c0 < K / 2; c0 += 16)
+                            lg_tmem_ld16(tmem + ((uint32_t)(q4 * 32) << 16) + (uint32_t)(hh * (K / 2) + c0), v + c0);
+                        float part[8];
+#pragma unroll
+                        for (int q = 0; q < 8; q++) part[q] = 0.0f;
+                        if (hh == 0) {
+#pragma unroll
+                            for (int e = 0; e < K / 2; e++) part[e & 7] += v[e];
+#pragma unroll
+                            for (int q = 0; q < 8; q++) xch[r * 9 + q] = part[q];
+                        }
+                        __syncthreads();
+                        if (hh == 1) {
+#pragma unroll
+                            for (int q = 0; q < 8; q++) part[q] = xch[r * 9 + q];
+#pragma unroll
+                            for (int e = 0; e < K / 2; e++) part[(K / 2 + e) & 7] += v[e];
+                            xch[r * 9 + 8] = (((part[0] + part[1]) + (part[2] + part[3])) +
+                                              ((part[4] + part[5]) + (part[6] + part[7]))) /
+                                             (float)K;
+                        }
+                        __syncthreads();
+                        if (r < R) {
+                            const float meanf = xch[r * 9 + 8];
+                            const int64_t row = col * n + r0 + r;
+                            double *dst = xac + (int64_t)(r0 + r) * K + hh * (K / 2);
+                            if (hh == 0) {
+                                double incr = incp[r];
+#pragma unroll
+                                for (int c = 1; c < K / 8; c++) incr += incp[c * 128 + r];
+                                axa[row] = axb[row] + incr + lg_f2d_bits(meanf);
+                            }
+#pragma unroll
+                            for (int e = 0; e < K / 2; e += 2)
+                                *reinterpret_cast<double2 *>(dst + e) =
+                                    make_double2(lg_f2d_bits(v[e] - meanf), lg_f2d_bits(v[e + 1] - meanf));
+                        }
+                    } else if (warp < 4) {
                         const int r = warp * 32 + lane;
                         float v[K];
 #pragma unroll
