@@ -97,6 +97,13 @@ struct MCfg {
     // the two gather stages: three CTAs per SM
     static constexpr size_t AREA1 = 2 * (size_t)TILE;
     static constexpr size_t SMEM1 = 1024 + AREA1 + B1 + VEC;
+    // the update launch without the members (ST 3): the xb and T tiles (48 KB),
+    // the epilogue's exchange rows, and the mean-increment partials in place of
+    // B1 (T is read from its slot in global memory): three CTAs per SM
+    static constexpr size_t AREA3 = 53 * 1024;
+    static constexpr size_t B13 = sizeof(double) * 128 * (K / 8);
+    static constexpr size_t SMEM3 = 1024 + AREA3 + B13 + VEC;
+    static_assert(49152 + 128 * 9 * sizeof(float) <= AREA3, "update tiles and exchange rows");
     static_assert(2 * (size_t)K * (K + 1) * sizeof(float) <= AREA1, "Dhh and Dlh must fit over the tiles");
     static_assert(AREA1 % 1024 == 0, "1024-byte aligned tiles");
     // gathered FP32 observation rows of one chunk; two stages: the first in B1
@@ -169,7 +176,7 @@ __device__ __forceinline__ void members_epilogue(const LgParams &prm, const LgGr
 // MEM: the fused members run (LgParams::members; stages 0 and 3), a separate
 // instantiation so the plain update keeps its registers.
 template <int K, int ST, bool MEM = false>
-__global__ void __launch_bounds__(kT, ST == 1 ? 3 : 2)
+__global__ void __launch_bounds__(kT, (ST == 1 || (ST == 3 && !MEM)) ? 3 : 2)
 k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32_t *__restrict__ lidx,
              const float2 *__restrict__ lmeta, const int *__restrict__ queue, int nchunks, int chunk,
              const int64_t *__restrict__ loff, const int32_t *__restrict__ lcnt, int64_t ncubes,
@@ -182,8 +189,9 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
     constexpr int CH = C::CH;
     extern __shared__ unsigned char smem_raw[];
     unsigned char *area = (unsigned char *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    double *B1 = reinterpret_cast<double *>(area + (ST == 1 ? C::AREA1 : C::AREA));
-    double *gv = B1 + K * K;
+    constexpr bool U3 = ST == 3 && !MEM;      // the compact update layout (MCfg::SMEM3)
+    double *B1 = reinterpret_cast<double *>(area + (ST == 1 ? C::AREA1 : U3 ? C::AREA3 : C::AREA));
+    double *gv = B1 + (U3 ? 128 * (K / 8) : K * K);
     double *wbar = gv + K;
     double *misc = wbar + K;       // 2K
     double *inc = misc + 2 * K;    // 128
@@ -541,9 +549,11 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
                     asm volatile("prefetch.global.L2 [%0];" ::"l"(a));
                 }
             }
-            float *T32s = reinterpret_cast<float *>(B1);
-            for (int idx = tid; idx < K * K / 4; idx += kT)
-                reinterpret_cast<float4 *>(T32s)[idx] = reinterpret_cast<const float4 *>(mX + ci * K * K)[idx];
+            if constexpr (!U3) {
+                float *T32s = reinterpret_cast<float *>(B1);
+                for (int idx = tid; idx < K * K / 4; idx += kT)
+                    reinterpret_cast<float4 *>(T32s)[idx] = reinterpret_cast<const float4 *>(mX + ci * K * K)[idx];
+            }
             if (tid < K) wbar[tid] = mgv[ci * K + tid];
             __syncthreads();
         }
@@ -744,7 +754,8 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
         if (trans_out) {
             for (int idx = tid; idx < K * K; idx += kT) {
                 const int i = idx % K, j = idx / K;
-                trans_out[(int64_t)cube * K * K + idx] = (double)T32[i * K + j] + wbar[i];
+                const float tij = U3 ? mX[ci * K * K + i * K + j] : T32[i * K + j];
+                trans_out[(int64_t)cube * K * K + idx] = (double)tij + wbar[i];
             }
             if (tid < K) w_out[(int64_t)cube * K + tid] = wbar[tid];
         }
@@ -757,8 +768,15 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
         for (int t = tid; t < K * (K / 8); t += kT) {
             const int e = t / (K / 8), c = t % (K / 8);
             float v[8];
+            if constexpr (U3) {
+                const float4 *tg = reinterpret_cast<const float4 *>(mX + ci * K * K + e * K + 8 * c);
+                const float4 a = tg[0], bq = tg[1];
+                v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+                v[4] = bq.x; v[5] = bq.y; v[6] = bq.z; v[7] = bq.w;
+            } else {
 #pragma unroll
-            for (int j = 0; j < 8; j++) v[j] = T32[e * K + 8 * c + j];
+                for (int j = 0; j < 8; j++) v[j] = T32[e * K + 8 * c + j];
+            }
             uint4 hi, lo;
             split8(v, hi, lo);
             *reinterpret_cast<uint4 *>(tb_hi + lg_sw128_offset(e, c)) = hi;
@@ -767,7 +785,7 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
         const int n = g.n;
         // FP64 mean increment xb^T wbar: partial sums over 8 members, [c][row],
         // after T in the space of A' (free in this phase)
-        double *incp = reinterpret_cast<double *>(T32 + K * K);
+        double *incp = U3 ? B1 : reinterpret_cast<double *>(T32 + K * K);
         // fused members run: squared perturbations summed over 8 members,
         // [c][row], beside the mean-increment partials (k >= 48) or after the
         // warm-start vectors (k = 32)
@@ -1685,7 +1703,9 @@ template <int K, int ST>
 cudaError_t launch_stage(letkf_ctx *ctx, const LgGrid &g, const double *xb, const double *axb, double *xa,
                          double *axa, double *trans_out, double *w_out, int chunk, int nchunks, int nsm)
 {
-    const size_t smem = ST == 1 ? MCfg<K>::SMEM1 : MCfg<K>::SMEM;
+    // the update without the members takes the compact layout
+    const bool u3 = ST == 3 && !ctx->members_on;
+    const size_t smem = ST == 1 ? MCfg<K>::SMEM1 : u3 ? MCfg<K>::SMEM3 : MCfg<K>::SMEM;
     auto kern = (ST != 1 && ctx->members_on) ? k_core_mixed<K, ST, ST != 1> : k_core_mixed<K, ST, false>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -1695,9 +1715,9 @@ cudaError_t launch_stage(letkf_ctx *ctx, const LgGrid &g, const double *xb, cons
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&smem_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, dev);
     // CTAs per SM: as many as the launch bounds give registers for (2; 3 for
-    // the A build) when their shared memory (plus the 1 KB the system keeps per
+    // the A build and the plain update) when their shared memory (plus the 1 KB the system keeps per
     // CTA and the static barriers) fits
-    int per_sm = ST == 1 ? 3 : 2;
+    int per_sm = (ST == 1 || u3) ? 3 : 2;
     while (per_sm > 1 && (size_t)per_sm * (smem + 1024 + 64) > (size_t)smem_sm) per_sm--;
     // persistent grid: each CTA allocates its tensor memory once
     const int64_t want = (int64_t)nsm * per_sm;
