@@ -828,6 +828,8 @@ int letkf_gpu_create(letkf_ctx **out, const letkf_grid *grid, const letkf_params
         LG_CUDA(ctx->d_lneed.reserve((size_t)ctx->ncubes));
         LG_CUDA(ctx->d_status.reserve(1));
         LG_CUDA(ctx->d_counters.reserve(LG_CNT_N));
+        LG_CUDA(ctx->d_ymax.reserve(1));
+        LG_CUDA(cudaMemsetAsync(ctx->d_ymax.p, 0, sizeof(unsigned), ctx->stream));
         LG_CUDA(cudaStreamSynchronize(ctx->stream));
         return LETKF_OK;
     };
@@ -1375,6 +1377,7 @@ int letkf_gpu_destroy(letkf_ctx *ctx)
     ctx->d_bidx.release();
     ctx->d_status.release();
     ctx->d_counters.release();
+    ctx->d_ymax.release();
     for (int i = 0; i < 8; i++)
         if (ctx->ev[i]) cudaEventDestroy(ctx->ev[i]);
     for (int s = 0; s < letkf_ctx::kStages; s++)

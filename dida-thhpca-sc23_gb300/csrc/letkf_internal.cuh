@@ -302,6 +302,7 @@ struct letkf_ctx {
     DevBuf<float> d_ys32;         // yb * sqrt(rinv) in FP32 (mixed precision)
     DevBuf<float> d_rinvf;
     DevBuf<float> d_oef;          // mixed form: sqrt(rdiaginv) dep per obs
+    DevBuf<unsigned> d_ymax;      // mixed form: bits of the largest |ys32| or |oef| (H)
     DevBuf<double> d_row_s, d_row_c, d_col_yr, d_col_cos, d_col_sin;   // search geometry tables
     DevBuf<double> d_os, d_oc, d_oyr;
     DevBuf<float4> d_oxyz;

@@ -5,15 +5,17 @@
 // dense products on the Blackwell tensor cores and the conditioning-sensitive
 // steps in FP64:
 //
-//   1. A = Yhat Yhat^T on tcgen05 (BF16 operands, FP32 accumulation in TMEM).
-//      Yhat = Y sqrt(rdiaginv rloc) is split per element into hi + lo BF16
-//      parts; one MMA stream multiplies the stacked [Yhat_hi; Yhat_lo]
-//      (M = 128 rows) by Yhat_hi (N = k), so A = HH + LH + LH^T recovers the
-//      hi*lo cross terms.  The observation rows are gathered, scaled and split
-//      into 128-byte-swizzled K-major tiles by all threads while the previous
-//      tile's MMAs run (two tiles, mbarrier-tracked).
-//      g = Yhat e with e = sqrt(rdiaginv rloc) dep comes out of the same MMAs:
-//      e's hi and lo parts are two more rows of the B operand (N = k + 16).
+//   1. A = Yhat Yhat^T on tcgen05 (FP16 operands, FP32 accumulation in TMEM).
+//      Yhat = Y sqrt(rdiaginv rloc), times a power of two that fits FP16's
+//      range, is split per element into hi + lo FP16 parts; one MMA stream
+//      multiplies the stacked [Yhat_lo; Yhat_hi] (M = 128 rows) by Yhat_hi
+//      (N = k), so A = HH + LH + LH^T recovers the hi*lo cross terms.  The
+//      observation rows are gathered, scaled and split into 128-byte-swizzled
+//      K-major tiles by all threads while the previous tile's MMAs run (two
+//      tiles, mbarrier-tracked).  g = Yhat e with e = sqrt(rdiaginv rloc) dep
+//      and the diagonal of A are summed on the FP32 pipe by the same threads
+//      (round to nearest: the tensor-core sums drift with the number of
+//      observations, which those terms would pass to the analysis).
 //   2. A' = A + (k-1)/rho I in FP64.
 //   3. FP32 one-sided Jacobi of A' (warm-started from the neighbouring
 //      cube's eigenvectors inside aligned runs of cubes, so that results do
@@ -44,6 +46,14 @@
 #include "letkf_jacobi.cuh"
 #include "letkf_mixed_util.cuh"
 #include "letkf_umma.cuh"
+
+// Chunks of observations (64 each) whose products the tensor cores sum in a
+// scratch accumulator before its sums are added to the running ones in FP32
+// round-to-nearest (the tensor cores' own sums drift by about 1e-8 of the sum
+// per observation).
+#ifndef LG_ACC_FLUSH
+#define LG_ACC_FLUSH 16
+#endif
 
 // Column-cosine tolerance of the FP32 Jacobi.  It bounds the eigenvectors'
 // orthogonality error, which reaches T (BF16 hi/lo in the update, ~1e-5
@@ -81,10 +91,11 @@ struct MCfg {
     static constexpr int MF = (NFULL + kT - 1) / kT;
     static constexpr int G = (K / 2 * 16 <= kT) ? 16 : (K / 2 * 8 <= kT) ? 8 : 4;
     static constexpr int CH = 64;                      // observations per MMA tile (K of the MMA)
-    static constexpr uint32_t TMEM_COLS = 128;         // A build: N = K + 16 columns
-    // A-build tile rows: Yhat_lo (K), Yhat_hi (K), e_hi, e_lo, zeros (to K + 16
-    // B rows), and at least the M = 128 rows of the A operand
-    static constexpr int TROWS = (2 * K + 16 > 128) ? 2 * K + 16 : 128;
+    static constexpr uint32_t TMEM_COLS = 128;         // A build: N = K columns, twice
+    static constexpr uint32_t ACC1 = 64;               // the A build's scratch accumulator
+    // A-build tile rows: Yhat_lo (K), Yhat_hi (K), zeros to the M = 128 rows
+    // of the A operand
+    static constexpr int TROWS = (2 * K > 128) ? 2 * K : 128;
     static constexpr int TILE = TROWS * 128;
     static constexpr int LDW = K + 4;                  // padded column stride of the FP32 Jacobi
     static constexpr size_t AREA = 64 * 1024;          // tiles / FP32 scratch / P, R, Xhat
@@ -95,7 +106,9 @@ struct MCfg {
     static constexpr size_t SMEM = 1024 + AREA + B1 + VEC + 256;
     // the A-build launch (ST 1) holds only the two tiles (then Dhh, Dlh) and
     // the two gather stages: three CTAs per SM
-    static constexpr size_t AREA1 = 2 * (size_t)TILE;
+    static constexpr size_t AREA1 = ((2 * (size_t)TILE > 2 * (size_t)K * (K + 1) * sizeof(float)
+                                          ? 2 * (size_t)TILE
+                                          : 2 * (size_t)K * (K + 1) * sizeof(float)) + 1023) & ~(size_t)1023;
     static constexpr size_t SMEM1 = 1024 + AREA1 + B1 + VEC;
     // the update launch without the members (ST 3): the xb and T tiles (48 KB),
     // the epilogue's exchange rows, and the mean-increment partials in place of
@@ -113,14 +126,18 @@ struct MCfg {
     static_assert(2 * K <= 128, "stacked hi/lo rows must fit M = 128");
     static_assert(K % 16 == 0, "N must be a multiple of 16");
     static_assert(2 * TILE <= 49152, "A-build tiles must not reach the warm-start vectors");
-    static_assert(K + 16 <= (int)TMEM_COLS, "A-build accumulator must fit the TMEM allocation");
+    static_assert(K <= (int)ACC1 && ACC1 + K <= TMEM_COLS, "A-build accumulators must fit the TMEM allocation");
+    // the conversion threads' partial sums of g and diag(A), [2][8][K] floats,
+    // pass through the first gather stage after the last chunk
+    static_assert(16 * K * sizeof(float) <= STAGE, "g and diagonal partials");
     static_assert(STAGE <= B1 && (STAGE1_IN_B1 || 2 * TILE + STAGE <= 49152), "gather stages must fit");
 };
 
 // The end of a fused members run for one state row (letkf2dnn,
 // module_da_parallel.F90:214-258), from the update's FP32 products v (member
-// mean meanf), the row's background mean mb and the FP64 mean increment:
-// axa = mb + incr + meanf; where |grid_lat| <= polar the members are
+// mean meanf), the row's background mean mb and the FP64 mean increment
+// (with the member mean of xb^T T, sqrt(rho) xbar, in it):
+// axa = mb + incr; where |grid_lat| <= polar the members are
 // gamma1 (axb + xb) + gamma2 (axa + xa), taken as the FP64 row constant
 // gamma1 mb + gamma2 axa plus the FP32 perturbation part gamma1 xb + gamma2
 // xa (xb from the row's BF16 hi/lo tile, 2^-17 of xb), else the background
@@ -136,7 +153,7 @@ __device__ __forceinline__ void members_epilogue(const LgParams &prm, const LgGr
     float sb = 0.0f;
 #pragma unroll
     for (int c = 0; c < K / 8; c++) sb += sqp[c * 128 + r];
-    const double ma = mb + incr + lg_f2d_bits(meanf);
+    const double ma = mb + incr;
     const bool blend = fabs((double)g.glat[col % g.nlat]) <= prm.polar;
     if (!blend) {
         for (int e = 0; e < K; e += 2)
@@ -183,7 +200,8 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
              const double *__restrict__ xb, const double *__restrict__ axb, double *__restrict__ xa,
              double *__restrict__ axa, double *__restrict__ trans_out, double *__restrict__ w_out,
              unsigned long long *__restrict__ counters, unsigned *__restrict__ status,
-             float *__restrict__ mA, double *__restrict__ mgv, const float *__restrict__ mX)
+             float *__restrict__ mA, double *__restrict__ mgv, const float *__restrict__ mX,
+             const unsigned *__restrict__ ymax)
 {
     using C = MCfg<K>;
     constexpr int CH = C::CH;
@@ -219,7 +237,14 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
     lg_tc_fence_after();
     const uint32_t tmem = s_tmem;
     const uint32_t idesc = lg_idesc_bf16(128, K);           // update: xb (hi/lo) x T
-    const uint32_t idesc_a = lg_idesc_bf16(128, K + 16);    // A build: [Yhat; e] products
+    const uint32_t idesc_a = lg_idesc_f16(128, K);          // A build: Yhat products
+    // the A build's operands times 2^E (FP16 range), its products times 2^-2E
+    float ysc = 1.0f, yunsc = 1.0f;
+    if (ST == 0 || ST == 1) {
+        const int ye = lg_f16_scale_exp(*ymax);
+        ysc = lg_pow2f(ye);
+        yunsc = lg_pow2f(-2 * ye);
+    }
     uint32_t ncommit[3] = {0u, 0u, 0u};
     bool pending[3] = {false, false, false};
     bool failed = false;
@@ -250,12 +275,11 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
     }
     // A-build conversion task of this thread: columns tm, tm + 1 of the
     // observations 8 tc .. 8 tc + 7 of a chunk (tile offsets fixed for the
-    // whole launch); thread te_base + c converts e of the observations 8 c ..
+    // whole launch)
     const bool has_task = tid < 4 * K;
     const int tm = 2 * (tid % (K / 2)), tc = tid / (K / 2);
     const uint32_t o_h0 = lg_sw128_offset(K + tm, tc), o_l0 = lg_sw128_offset(tm, tc);
     const uint32_t o_h1 = lg_sw128_offset(K + tm + 1, tc), o_l1 = lg_sw128_offset(tm + 1, tc);
-    const int te = (4 * K + 8 <= kT) ? tid - 4 * K : tid;
     int fbi[C::MF], fbj[C::MF];
     bool fok[C::MF];
 #pragma unroll
@@ -322,14 +346,20 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
         (void)ci;
 
         if (ST == 0 || ST == 1) {
-        // ---------------- phase 1: A and g on the tensor cores ----------------------
-        // Tile rows: Yhat_lo (0..K-1), Yhat_hi (K..2K-1), e_hi (2K), e_lo (2K+1),
-        // zeros to TROWS.  The A operand is rows 0..127, the B operand rows
-        // K..2K+15 (N = K + 16), so D[lo/hi m][n < K] = Yhat_lo/hi(m) . Yhat_hi(n)
-        // and D[.][K], D[.][K+1] = Yhat(m) . e_hi/e_lo with
-        // e_o = sqrt(rdiaginv rloc) dep: g = sum_o y r rloc dep = Yhat e.
+        // ---------------- phase 1: A on the tensor cores, g and diag(A) -------------
+        // Tile rows: Yhat_lo (0..K-1), Yhat_hi (K..2K-1), zeros to TROWS.  The
+        // A operand is rows 0..127, the B operand rows K..2K-1 (N = K), so
+        // D[lo/hi m][n] = Yhat_lo/hi(m) . Yhat_hi(n).  The tensor cores'
+        // accumulation drifts with the number of products summed (about 1e-8
+        // of the sum per observation, one sign for sums of positive terms),
+        // so the terms whose relative error reaches the analysis whole, g =
+        // Yhat e (e_o = sqrt(rdiaginv rloc) dep: g = sum_o y r rloc dep) and
+        // the diagonal of A, are summed on the FP32 pipe in round-to-nearest
+        // by the conversion threads, which hold Yhat and e in registers; the
+        // off-diagonal sums of A, whose terms cancel, stay on the tensor cores.
+        unsigned long long acc_g = 0ull, acc_d = 0ull;     // packed (column tm, tm + 1)
         {
-            constexpr int Z0 = 2 * K + 2, NZ = C::TROWS - Z0;   // rows that stay zero
+            constexpr int Z0 = 2 * K, NZ = C::TROWS - Z0;   // rows that stay zero
             for (int t = tid; t < 2 * NZ * 8; t += kT) {
                 const int b = t / (NZ * 8), rest = t % (NZ * 8);
                 const int r = Z0 + rest / 8, c = rest % 8;
@@ -355,8 +385,8 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
         auto put_meta = [&](int x, int gi, float2 mf) {
             const int r = (x % 3) * CH + tid;
             mg[r] = gi;
-            msq[r] = mf.x;
-            me[r] = mf.y;
+            msq[r] = mf.x * ysc;
+            me[r] = mf.y * ysc;
         };
         auto issue_rows = [&](int x) {       // all threads; ring slot x % 3 is visible
             float *st = (x & 1) ? stage1 : stage0;
@@ -432,31 +462,57 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
                     }
                 }
                 uint4 h0, l0, h1, l1;
-                split8x2(x, h0, l0, h1, l1);
+                split8x2_f16(x, h0, l0, h1, l1);
                 *reinterpret_cast<uint4 *>(tile + o_h0) = h0;
                 *reinterpret_cast<uint4 *>(tile + o_l0) = l0;
                 *reinterpret_cast<uint4 *>(tile + o_h1) = h1;
                 *reinterpret_cast<uint4 *>(tile + o_l1) = l1;
-            }
-            if (te >= 0 && te < 8) {
-                float v[8];
-                uint4 hi, lo;
+                // g and the diagonal, observation by observation (e is zero
+                // past the list's end, as the rows are)
 #pragma unroll
-                for (int j = 0; j < 8; j++) v[j] = ev[8 * te + j];
-                split8(v, hi, lo);
-                *reinterpret_cast<uint4 *>(tile + lg_sw128_offset(2 * K, te)) = hi;
-                *reinterpret_cast<uint4 *>(tile + lg_sw128_offset(2 * K + 1, te)) = lo;
+                for (int j = 0; j < 8; j++) {
+                    const float e = ev[8 * tc + j];
+                    acc_g = lg_ffma2(x[j], lg_pk2(e, e), acc_g);
+                    acc_d = lg_ffma2(x[j], x[j], acc_d);
+                }
             }
             lg_fence_async_smem();
             __syncthreads();
             LG_PHASE(9);
+            if (ch > 0 && ch % LG_ACC_FLUSH == 0) {
+                // the last group's sums (chunks ch - F .. ch - 1) into the
+                // running ones in FP32 round to nearest (the first group's are
+                // copied) before this chunk's products restart the scratch
+                // accumulator; chunk ch - 2's products were waited for above
+                if (!wait_bar(b ^ 1, prm.spin_limit)) {
+                    failed = true;
+                    break;
+                }
+                lg_tc_fence_after();
+                if (warp < 4) {
+                    const uint32_t tl = tmem + ((uint32_t)(warp * 32) << 16);
+#pragma unroll
+                    for (int c0 = 0; c0 < K; c0 += 16) {
+                        float v[16], u[16];
+                        lg_tmem_ld16x2(tl + C::ACC1 + (uint32_t)c0, tl + (uint32_t)c0, v, u);
+                        if (ch > LG_ACC_FLUSH) {
+#pragma unroll
+                            for (int j = 0; j < 16; j++) v[j] = u[j] + v[j];
+                        }
+                        lg_tmem_st16(tl + (uint32_t)c0, v);
+                    }
+                }
+                lg_tc_fence_before();
+                __syncthreads();
+            }
             if (tid == 0) {
                 lg_tc_fence_after();
                 const uint64_t da = lg_desc_sw128(lg_smem_u32(tile));
                 const uint64_t db = lg_desc_sw128(lg_smem_u32(tile + K * 128));
 #pragma unroll
                 for (int kk = 0; kk < 4; kk++)
-                    lg_umma_bf16(tmem, da + 2 * kk, db + 2 * kk, idesc_a, (ch > 0 || kk > 0) ? 1u : 0u);
+                    lg_umma_bf16(tmem + C::ACC1, da + 2 * kk, db + 2 * kk, idesc_a,
+                                 (ch % LG_ACC_FLUSH != 0 || kk > 0) ? 1u : 0u);
                 lg_umma_commit(&mbar[b]);
             }
             ncommit[b]++;
@@ -467,6 +523,14 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
         }
         cp_async_wait<0>();
         if (failed) break;
+        // the partial sums of g and the diagonal through the first gather
+        // stage (no copy is in flight and every chunk's rows were read before
+        // the last chunk's barrier): [g | diag][tc][column]
+        if (has_task) {
+            float *pg = stage0 + tc * K + tm, *pd = stage0 + 8 * K + tc * K + tm;
+            lg_upk2(acc_g, pg[0], pg[1]);
+            lg_upk2(acc_d, pd[0], pd[1]);
+        }
         // the first list entries of the next cube into L2 (its first three chunks)
         if (warp == 0 && cube + 1 < cube_end) {
             const int64_t o2 = loff[cube + 1];
@@ -485,6 +549,19 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
             break;
         }
         lg_tc_fence_after();
+        __syncthreads();
+        // g and diag(A) over the 8 observation groups in a fixed order (FP64
+        // sums of the FP32 partials), times 2^-2E, in misc
+        if (tid < K) {
+            double sg = 0.0, sd = 0.0;
+#pragma unroll
+            for (int q = 0; q < 8; q++) {
+                sg += (double)stage0[q * K + tid];
+                sd += (double)stage0[8 * K + q * K + tid];
+            }
+            misc[tid] = sg * (double)yunsc;
+            misc[K + tid] = sd * (double)yunsc;
+        }
 
         LG_PHASE(0);
         // ---------------- phase 2: A' = HH + LH + LH^T + (k-1)/rho I -------------------
@@ -495,7 +572,14 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
             for (int c0 = 0; c0 < K; c0 += 16) {
                 float v[16];
                 if (p > 0) {
-                    lg_tmem_ld16(tl + (uint32_t)c0, v);
+                    // the last group's sums, plus the running ones of the
+                    // groups before it
+                    float u[16];
+                    lg_tmem_ld16x2(tl + C::ACC1 + (uint32_t)c0, tl + (uint32_t)c0, v, u);
+                    if (nch > LG_ACC_FLUSH) {
+#pragma unroll
+                        for (int j = 0; j < 16; j++) v[j] = u[j] + v[j];
+                    }
                 } else {
 #pragma unroll
                     for (int j = 0; j < 16; j++) v[j] = 0.0f;
@@ -508,27 +592,21 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
                     for (int j = 0; j < 16; j++) Dhh[(row - K) * LDD + c0 + j] = v[j];
                 }
             }
-            // g parts: Yhat_lo/hi(m) . (e_hi + e_lo)
-            float v[16];
-            if (p > 0) {
-                lg_tmem_ld16(tl + (uint32_t)K, v);
-            } else {
-#pragma unroll
-                for (int j = 0; j < 16; j++) v[j] = 0.0f;
-            }
-            if (row < 2 * K) misc[row] = (double)v[0] + (double)v[1];
         }
         lg_tc_fence_before();
         __syncthreads();
-        // A = HH + LH + LH^T is formed in FP32 (the accumulators are FP32), then
+        // A = HH + LH + LH^T is formed in FP32 (the accumulators are FP32) off
+        // the diagonal, the diagonal and g from the FP32-pipe sums, then
         // A' = A + (k-1)/rho I in FP64 and in FP32 for the Jacobi
         if (tid < K) {
-            gv[tid] = misc[K + tid] + misc[tid];
+            gv[tid] = misc[tid];
             if (ST == 1) mgv[ci * K + tid] = gv[tid];
         }
         for (int idx = tid; idx < K * K; idx += kT) {
             const int i = idx / K, j = idx % K;
-            const float a32 = 0.5f * (Dhh[i * LDD + j] + Dhh[j * LDD + i]) + (Dlh[i * LDD + j] + Dlh[j * LDD + i]);
+            const float a32 = i == j ? (float)misc[K + i]
+                                     : (0.5f * (Dhh[i * LDD + j] + Dhh[j * LDD + i]) +
+                                        (Dlh[i * LDD + j] + Dlh[j * LDD + i])) * yunsc;
             if (ST == 1) mA[ci * K * K + idx] = a32;
             else B1[idx] = (double)a32 + (i == j ? cdiag : 0.0);
         }
@@ -758,7 +836,16 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
                 trans_out[(int64_t)cube * K * K + idx] = (double)tij + wbar[i];
             }
             if (tid < K) w_out[(int64_t)cube * K + tid] = wbar[tid];
+            __syncthreads();
         }
+        // The analysis mean is the member mean of axb + xb^T (T + wbar 1^T)
+        // (xb_2_xa, letkf_compute.F90:283-295), and the member mean of xb^T T
+        // is sqrt(rho) xbar exactly: Yhat 1 = 0 (H centres the members), so
+        // A' 1 = (k-1)/rho 1 and T 1 = sqrt(rho) 1.  It is taken in the FP64
+        // increment, xb^T (wbar + sqrt(rho)/k 1), rather than from the tensor
+        // products, whose BF16 hi/lo error (~2^-16 of xb) would reach the mean.
+        if (tid < K) wbar[tid] += sqrt(prm.inflation) / (double)K;
+        __syncthreads();
 
         LG_PHASE(4);
         // ---------------- phase 6: xa = xb^T (T + wbar 1^T) -------------------------------
@@ -934,7 +1021,7 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
                                 double incr = incp[r];
 #pragma unroll
                                 for (int c = 1; c < K / 8; c++) incr += incp[c * 128 + r];
-                                axa[row] = axb[row] + incr + lg_f2d_bits(meanf);
+                                axa[row] = axb[row] + incr;
                             }
 #pragma unroll
                             for (int e = 0; e < K / 2; e += 2)
@@ -965,7 +1052,7 @@ k_core_mixed(LgGrid g, LgParams prm, const float *__restrict__ ys32, const int32
                             const int64_t row = col * n + r0 + r;
                             double *dst = xac + (int64_t)(r0 + r) * K;
                             if constexpr (!MEM) {
-                                axa[row] = axb[row] + incr + lg_f2d_bits(meanf);
+                                axa[row] = axb[row] + incr;
 #pragma unroll
                                 for (int e = 0; e < K; e += 2)
                                     *reinterpret_cast<double2 *>(dst + e) =
@@ -1729,7 +1816,7 @@ cudaError_t launch_stage(letkf_ctx *ctx, const LgGrid &g, const double *xb, cons
     kern<<<blocks, kT, smem, ctx->stream>>>(
         g, lg_params(ctx), ctx->d_ys32.p, ctx->d_lidx.p, ctx->d_lmeta.p, ctx->d_queue.p, nchunks, chunk,
         ctx->d_loff.p, ctx->d_lcnt.p, ctx->win1, xb, axb, xa, axa, trans_out, w_out, ctx->d_counters.p,
-        ctx->d_status.p, ctx->d_mA.p, ctx->d_mg.p, ctx->d_mX.p);
+        ctx->d_status.p, ctx->d_mA.p, ctx->d_mg.p, ctx->d_mX.p, ctx->d_ymax.p);
     return cudaGetLastError();
 }
 

@@ -4,10 +4,11 @@
 // letkf_core, code/x86/TradDA/DA/LETKF/src/letkf_core.F90:14-233, and
 // xb_2_xa, letkf_compute.F90:231-301) for ensembles whose stacked hi/lo rows
 // (2k) do not fit one MMA's 128 rows.  Differences of layout:
-//   * A and g: the tile holds Yhat_lo in rows 0..k-1 (zero to 127) and
-//     Yhat_hi, e_hi, e_lo from row 128; two MMAs per K step, lo x [hi; e] and
-//     hi x [hi; e] (N = k + 16), accumulate into two TMEM ranges (columns 0
-//     and 256 of a 512-column allocation: one CTA per SM);
+//   * A: the tile holds Yhat_lo in rows 0..k-1 (zero to 127) and Yhat_hi
+//     from row 128; two MMAs per K step, lo x hi and hi x hi (N = k),
+//     accumulate into two TMEM ranges (columns 0 and 256 of a 512-column
+//     allocation: one CTA per SM); g and the diagonal of A are summed on the
+//     FP32 pipe by the conversion threads, as in the narrow core;
 //   * A = 0.5 (S + S^T) with S = HH + 2 LH staged once (no FP64 copy of A':
 //     the w-bar residual adds (k-1)/rho in FP64 to the FP32 A);
 //   * the update's operands (xb rows and T, k members deep) are two
@@ -22,6 +23,11 @@
 
 #ifndef LG_MIXED_JACOBI_TOL
 #define LG_MIXED_JACOBI_TOL 2e-6f
+#endif
+// chunks summed by the tensor cores in the scratch accumulators before the
+// FP32 round-to-nearest addition to the running sums (as in letkf_mixed.cu)
+#ifndef LG_ACC_FLUSH
+#define LG_ACC_FLUSH 16
 #endif
 
 namespace {
@@ -58,7 +64,8 @@ struct WCfg {
     static constexpr int CH = 64;                        // observations per MMA tile
     static constexpr uint32_t TMEM_COLS = 512;
     static constexpr uint32_t HI_COL = 256;              // first TMEM column of the hi accumulator
-    static constexpr int NB = K + 16;                    // A-build N: Yhat_hi, e_hi, e_lo, zeros
+    static constexpr uint32_t ACC1 = 128;                // scratch accumulators after the running ones
+    static constexpr int NB = K;                         // A-build N: Yhat_hi
     static constexpr int TROWS = (128 + NB > 256) ? 128 + NB : 256;
     static constexpr int TILE = TROWS * 128;
     // Jacobi column stride and moving-buffer stride: K + 16 puts the two slots
@@ -78,6 +85,8 @@ struct WCfg {
     static_assert(K > 64 && K <= 128 && K % 32 == 0, "wide form: k = 96 or 128");
     static_assert(TILE % 1024 == 0 && STAGE % 1024 == 0 && TBSUB % 1024 == 0, "1024-byte aligned tiles");
     static_assert(SMEM <= 227 * 1024, "shared memory");
+    static_assert(16 * K * sizeof(float) <= STAGE, "g and diagonal task sums pass through a gather stage");
+    static_assert(K <= (int)ACC1 && HI_COL + ACC1 + K <= TMEM_COLS, "A-build accumulators must fit the TMEM allocation");
 };
 
 template <int K>
@@ -87,7 +96,8 @@ k_core_mixed_wide(LgGrid g, LgParams prm, const float *__restrict__ ys32, const 
                   const int64_t *__restrict__ loff, const int32_t *__restrict__ lcnt, int64_t ncubes,
                   const double *__restrict__ xb, const double *__restrict__ axb, double *__restrict__ xa,
                   double *__restrict__ axa, double *__restrict__ trans_out, double *__restrict__ w_out,
-                  unsigned long long *__restrict__ counters, unsigned *__restrict__ status)
+                  unsigned long long *__restrict__ counters, unsigned *__restrict__ status,
+                  const unsigned *__restrict__ ymax)
 {
     using C = WCfg<K>;
     constexpr int CH = C::CH;
@@ -118,7 +128,10 @@ k_core_mixed_wide(LgGrid g, LgParams prm, const float *__restrict__ ys32, const 
     lg_tc_fence_after();
     const uint32_t tmem = s_tmem;
     const uint32_t idesc_u = lg_idesc_bf16(128, K);         // update: xb (hi/lo) x T
-    const uint32_t idesc_a = lg_idesc_bf16(128, C::NB);     // A build
+    const uint32_t idesc_a = lg_idesc_f16(128, C::NB);      // A build
+    // the A build's operands times 2^E (FP16 range), its products times 2^-2E
+    const int ye = lg_f16_scale_exp(*ymax);
+    const float ysc = lg_pow2f(ye), yunsc = lg_pow2f(-2 * ye);
     uint32_t ncommit[3] = {0u, 0u, 0u};
     bool pending[3] = {false, false, false};
     bool failed = false;
@@ -161,15 +174,21 @@ k_core_mixed_wide(LgGrid g, LgParams prm, const float *__restrict__ ys32, const 
         const int p = lcnt[cube];
         LGW_PHASE(6);
 
-        // ---------------- phase 1: A and g on the tensor cores ----------------------
-        // rows K..127 and 130+K..TROWS-1 of both tiles stay zero
+        // ---------------- phase 1: A on the tensor cores, g and diag(A) -------------
+        // rows K..127 and 128+K..TROWS-1 of both tiles stay zero
         for (int t = tid; t < 2 * C::TROWS * 8; t += kTW) {
             const int b = t / (C::TROWS * 8), rest = t % (C::TROWS * 8);
             const int r = rest / 8, c = rest % 8;
-            if ((r >= K && r < 128) || r >= 130 + K)
+            if ((r >= K && r < 128) || r >= 128 + K)
                 *reinterpret_cast<uint4 *>(RA + b * C::TILE + lg_sw128_offset(r, c)) = make_uint4(0, 0, 0, 0);
         }
         const int nch = (p + CH - 1) / CH;
+        // the FP32-pipe sums of this thread's conversion tasks (t = tid + i kTW:
+        // column t % K, observations 8 (t / K) .. + 7 of every chunk)
+        constexpr int NTASK = (K * 8 + kTW - 1) / kTW;
+        float acc_g[NTASK], acc_d[NTASK];
+#pragma unroll
+        for (int i = 0; i < NTASK; i++) acc_g[i] = acc_d[i] = 0.0f;
         auto load_meta = [&](int x, int &gi, float2 &mf) {      // tid < CH
             const int o = x * CH + tid;
             if (x < nch && o < p) {
@@ -183,8 +202,8 @@ k_core_mixed_wide(LgGrid g, LgParams prm, const float *__restrict__ ys32, const 
         auto put_meta = [&](int x, int gi, float2 mf) {
             const int r = (x % 3) * CH + tid;
             mg[r] = gi;
-            msq[r] = mf.x;
-            me[r] = mf.y;
+            msq[r] = mf.x * ysc;
+            me[r] = mf.y * ysc;
         };
         auto issue_rows = [&](int x) {
             float *st = (x & 1) ? stage1 : stage0;
@@ -225,39 +244,70 @@ k_core_mixed_wide(LgGrid g, LgParams prm, const float *__restrict__ ys32, const 
                 break;
             }
             const int cnt = min(CH, p - ch * CH);
-            for (int t = tid; t < K * 8 + 8; t += kTW) {
-                float v[8];
-                uint4 hi, lo;
+#pragma unroll
+            for (int i = 0; i < NTASK; i++) {
+                const int t = tid + i * kTW;
                 if (t < K * 8) {
                     const int m = t % K, c = t / K;
+                    float v[8];
+                    uint4 hi, lo;
 #pragma unroll
                     for (int j = 0; j < 8; j++) {
                         const int o = 8 * c + j;
                         v[j] = (o < cnt) ? st[o * K + m] * sq[o] : 0.0f;
                     }
-                    split8(v, hi, lo);
+                    split8_f16(v, hi, lo);
                     *reinterpret_cast<uint4 *>(tile + lg_sw128_offset(128 + m, c)) = hi;
                     *reinterpret_cast<uint4 *>(tile + lg_sw128_offset(m, c)) = lo;
-                } else {
-                    const int c = t - K * 8;
+                    // g and the diagonal (e is zero past the list's end)
 #pragma unroll
-                    for (int j = 0; j < 8; j++) v[j] = ev[8 * c + j];
-                    split8(v, hi, lo);
-                    *reinterpret_cast<uint4 *>(tile + lg_sw128_offset(128 + K, c)) = hi;
-                    *reinterpret_cast<uint4 *>(tile + lg_sw128_offset(129 + K, c)) = lo;
+                    for (int j = 0; j < 8; j++) {
+                        acc_g[i] = fmaf(v[j], ev[8 * c + j], acc_g[i]);
+                        acc_d[i] = fmaf(v[j], v[j], acc_d[i]);
+                    }
                 }
             }
             lg_fence_async_smem();
             __syncthreads();
+            if (ch > 0 && ch % LG_ACC_FLUSH == 0) {
+                // the last group's sums into the running ones in FP32 round to
+                // nearest (the first group's copied) before this chunk's
+                // products restart the scratch accumulators; chunk ch - 2's
+                // products were waited for above
+                if (!wait_bar(b ^ 1, prm.spin_limit)) {
+                    failed = true;
+                    break;
+                }
+                lg_tc_fence_after();
+                if (warp < 4) {
+                    const uint32_t tl = tmem + ((uint32_t)(warp * 32) << 16);
+#pragma unroll 1
+                    for (int h = 0; h < 2; h++) {
+                        const uint32_t base = tl + (h ? C::HI_COL : 0u);
+#pragma unroll 1
+                        for (int c0 = 0; c0 < K; c0 += 16) {
+                            float v[16], u[16];
+                            lg_tmem_ld16x2(base + C::ACC1 + (uint32_t)c0, base + (uint32_t)c0, v, u);
+                            if (ch > LG_ACC_FLUSH) {
+#pragma unroll
+                                for (int j = 0; j < 16; j++) v[j] = u[j] + v[j];
+                            }
+                            lg_tmem_st16(base + (uint32_t)c0, v);
+                        }
+                    }
+                }
+                lg_tc_fence_before();
+                __syncthreads();
+            }
             if (tid == 0) {
                 lg_tc_fence_after();
                 const uint64_t dlo = lg_desc_sw128(lg_smem_u32(tile));
                 const uint64_t dhi = lg_desc_sw128(lg_smem_u32(tile + 128 * 128));   // Yhat_hi, e: A_hi and B
 #pragma unroll
                 for (int kk = 0; kk < 4; kk++) {
-                    const uint32_t acc = (ch > 0 || kk > 0) ? 1u : 0u;
-                    lg_umma_bf16(tmem, dlo + 2 * kk, dhi + 2 * kk, idesc_a, acc);
-                    lg_umma_bf16(tmem + C::HI_COL, dhi + 2 * kk, dhi + 2 * kk, idesc_a, acc);
+                    const uint32_t acc = (ch % LG_ACC_FLUSH != 0 || kk > 0) ? 1u : 0u;
+                    lg_umma_bf16(tmem + C::ACC1, dlo + 2 * kk, dhi + 2 * kk, idesc_a, acc);
+                    lg_umma_bf16(tmem + C::HI_COL + C::ACC1, dhi + 2 * kk, dhi + 2 * kk, idesc_a, acc);
                 }
                 lg_umma_commit(&mbar[b]);
             }
@@ -272,11 +322,35 @@ k_core_mixed_wide(LgGrid g, LgParams prm, const float *__restrict__ ys32, const 
         }
         cp_async_wait<0>();
         if (failed) break;
+        // the task sums through the first gather stage (no copy in flight, its
+        // rows read before the last chunk's barrier): [g | diag][task]
+#pragma unroll
+        for (int i = 0; i < NTASK; i++) {
+            const int t = tid + i * kTW;
+            if (t < K * 8) {
+                stage0[t] = acc_g[i];
+                stage0[K * 8 + t] = acc_d[i];
+            }
+        }
         if (!wait_bar(0, prm.spin_limit) || !wait_bar(1, prm.spin_limit)) {
             failed = true;
             break;
         }
         lg_tc_fence_after();
+        __syncthreads();
+        // g and diag(A) over the 8 observation groups in a fixed order, times
+        // 2^-2E, in misc (before S, which overlaps the stage, is written)
+        if (tid < K) {
+            double sg = 0.0, sd = 0.0;
+#pragma unroll
+            for (int c = 0; c < 8; c++) {
+                sg += (double)stage0[c * K + tid];
+                sd += (double)stage0[K * 8 + c * K + tid];
+            }
+            misc[tid] = sg * (double)yunsc;
+            misc[K + tid] = sd * (double)yunsc;
+        }
+        __syncthreads();
         LGW_PHASE(0);
 
         // ---------------- phase 2: A = 0.5 (S + S^T), S = HH + 2 LH; g -------------------
@@ -289,8 +363,18 @@ k_core_mixed_wide(LgGrid g, LgParams prm, const float *__restrict__ ys32, const 
             for (int c0 = 0; c0 < K; c0 += 16) {
                 float lo[16], hi[16];
                 if (p > 0) {
-                    lg_tmem_ld16(tl + (uint32_t)c0, lo);
-                    lg_tmem_ld16(tl + C::HI_COL + (uint32_t)c0, hi);
+                    // the last group's sums, plus the running ones before it
+                    float u[16];
+                    lg_tmem_ld16x2(tl + C::ACC1 + (uint32_t)c0, tl + (uint32_t)c0, lo, u);
+                    if (nch > LG_ACC_FLUSH) {
+#pragma unroll
+                        for (int j = 0; j < 16; j++) lo[j] = u[j] + lo[j];
+                    }
+                    lg_tmem_ld16x2(tl + C::HI_COL + C::ACC1 + (uint32_t)c0, tl + C::HI_COL + (uint32_t)c0, hi, u);
+                    if (nch > LG_ACC_FLUSH) {
+#pragma unroll
+                        for (int j = 0; j < 16; j++) hi[j] = u[j] + hi[j];
+                    }
                 } else {
 #pragma unroll
                     for (int j = 0; j < 16; j++) lo[j] = hi[j] = 0.0f;
@@ -300,21 +384,13 @@ k_core_mixed_wide(LgGrid g, LgParams prm, const float *__restrict__ ys32, const 
                     for (int j = 0; j < 16; j++) S[row * C::LDS + c0 + j] = fmaf(2.0f, lo[j], hi[j]);
                 }
             }
-            float lo[16], hi[16];
-            if (p > 0) {
-                lg_tmem_ld16(tl + (uint32_t)K, lo);
-                lg_tmem_ld16(tl + C::HI_COL + (uint32_t)K, hi);
-            } else {
-#pragma unroll
-                for (int j = 0; j < 16; j++) lo[j] = hi[j] = 0.0f;
-            }
-            if (row < K) gv[row] = ((double)hi[0] + (double)hi[1]) + ((double)lo[0] + (double)lo[1]);
+            if (row < K) gv[row] = misc[row];
         }
         lg_tc_fence_before();
         __syncthreads();
         for (int idx = tid; idx < K * K; idx += kTW) {
             const int i = idx / K, j = idx % K;
-            A32[idx] = 0.5f * (S[i * C::LDS + j] + S[j * C::LDS + i]);
+            A32[idx] = i == j ? (float)misc[K + i] : 0.5f * (S[i * C::LDS + j] + S[j * C::LDS + i]) * yunsc;
         }
         __syncthreads();                                          // S is dead
         const double cdiag = (double)(K - 1) / prm.inflation;
@@ -514,7 +590,13 @@ k_core_mixed_wide(LgGrid g, LgParams prm, const float *__restrict__ ys32, const 
                 trans_out[(int64_t)cube * K * K + idx] = (double)T32[i * K + j] + wbar[i];
             }
             if (tid < K) w_out[(int64_t)cube * K + tid] = wbar[tid];
+            __syncthreads();
         }
+        // the member mean of xb^T T is sqrt(rho) xbar (T 1 = sqrt(rho) 1): the
+        // FP64 increment takes it, xb^T (wbar + sqrt(rho)/k 1), not the tensor
+        // products (as in the narrow core)
+        if (tid < K) wbar[tid] += sqrt(prm.inflation) / (double)K;
+        __syncthreads();
 
         LGW_PHASE(4);
 
@@ -617,7 +699,7 @@ k_core_mixed_wide(LgGrid g, LgParams prm, const float *__restrict__ ys32, const 
                             (float)K;
                         if (r < R) {
                             const int64_t row = col * n + r0 + r;
-                            axa[row] = axb[row] + inc[r] + lg_f2d_bits(meanf);
+                            axa[row] = axb[row] + inc[r];
                         }
                         double *dst = xac + (int64_t)(r0 + r) * K;
                         for (int c0 = 0; c0 < K; c0 += 16) {
@@ -681,7 +763,7 @@ cudaError_t launch_wide(letkf_ctx *ctx, const LgGrid &g, const double *xb, const
     k_core_mixed_wide<K><<<blocks, kTW, smem, ctx->stream>>>(
         g, lg_params(ctx), ctx->d_ys32.p, ctx->d_lidx.p, ctx->d_lmeta.p, ctx->d_queue.p, nchunks, chunk,
         ctx->d_loff.p, ctx->d_lcnt.p, ctx->win1, xb, axb, xa, axa, trans_out, w_out, ctx->d_counters.p,
-        ctx->d_status.p);
+        ctx->d_status.p, ctx->d_ymax.p);
     return cudaGetLastError();
 }
 

@@ -223,7 +223,7 @@ k_obs_prepare(LgGrid g, LgParams prm, const double *__restrict__ xb, const doubl
               const double *__restrict__ orinv, double *__restrict__ yb, double *__restrict__ dep,
               float *__restrict__ rinvf, double *__restrict__ os, double *__restrict__ oc,
               double *__restrict__ oyr, float4 *__restrict__ oxyz, int *__restrict__ obucket,
-              float *__restrict__ ys32, float *__restrict__ oef,
+              float *__restrict__ ys32, float *__restrict__ oef, unsigned *__restrict__ ymax,
               int nblat, int nblon, double cell_lat, double cell_lon, unsigned *status, int mode)
 {
     const int lane = threadIdx.x & 31;
@@ -233,6 +233,7 @@ k_obs_prepare(LgGrid g, LgParams prm, const double *__restrict__ xb, const doubl
     // the mean as sum * 2^-m when k is a power of two (exact, equal to sum / k)
     const bool kpow2 = (k & (k - 1)) == 0;
     const double invk = 1.0 / (double)k;
+    float amax = 0.0f;       // the largest |ys32| and |oef| this lane wrote (mixed form)
 
     for (int64_t base = warp * 32; base < nobs; base += nwarps * 32) {
         // ---- per-observation terms, observation base + lane on this lane
@@ -354,7 +355,11 @@ k_obs_prepare(LgGrid g, LgParams prm, const double *__restrict__ xb, const doubl
 #pragma unroll
                 for (int i = 0; i < LG_MAX_ENS / 32; i++) {
                     const int e = lane + 32 * i;
-                    if (e < k) ys32[oj * k + e] = (float)((yv[i] - mean) * srj);
+                    if (e < k) {
+                        const float v = (float)((yv[i] - mean) * srj);
+                        ys32[oj * k + e] = v;
+                        amax = fmaxf(amax, fabsf(v));
+                    }
                 }
             }
         }
@@ -364,8 +369,19 @@ k_obs_prepare(LgGrid g, LgParams prm, const double *__restrict__ xb, const doubl
             const double d = oyo[o] - mymean;
             dep[o] = d;
             // the mixed form's departure factor: e = sqrt(rloc) sqrt(rdiaginv) dep
-            if (oef) oef[o] = sqrtf(rinvf[o]) * (float)d;
+            if (oef) {
+                const float ef = sqrtf(rinvf[o]) * (float)d;
+                oef[o] = ef;
+                amax = fmaxf(amax, fabsf(ef));
+            }
         }
+    }
+    // the run's largest magnitude of the A build's operands (float bits of a
+    // non-negative value order as unsigned integers)
+    if (ymax && mode != 1) {
+#pragma unroll
+        for (int s = 16; s > 0; s >>= 1) amax = fmaxf(amax, __shfl_xor_sync(0xffffffffu, amax, s));
+        if (lane == 0 && amax > 0.0f) atomicMax(ymax, __float_as_uint(amax));
     }
 }
 
@@ -432,6 +448,11 @@ cudaError_t lg_launch_obs_prepare(letkf_ctx *ctx, const LgGrid &g, const double 
                                   const double *olon, const double *oph, const int32_t *olev,
                                   const int32_t *ovar, const double *oyo, const double *orinv, int mode)
 {
+    const bool mixed = lg_is_mixed(ctx->params.precision);
+    if (mixed && mode != 1) {
+        const cudaError_t e = cudaMemsetAsync(ctx->d_ymax.p, 0, sizeof(unsigned), ctx->stream);
+        if (e != cudaSuccess) return e;
+    }
     if (nobs == 0) return cudaSuccess;
     const LgParams prm = lg_params(ctx);
     const int blocks = grid_for(nobs, 256, 152 * 64);
@@ -439,8 +460,7 @@ cudaError_t lg_launch_obs_prepare(letkf_ctx *ctx, const LgGrid &g, const double 
     k_obs_prepare<<<blocks, 256, 0, ctx->stream>>>(
         g, prm, xb, axb, nobs, olat, olon, oph, olev, ovar, oyo, orinv, ctx->d_yb.p, ctx->d_dep.p,
         ctx->d_rinvf.p, ctx->d_os.p, ctx->d_oc.p, ctx->d_oyr.p, ctx->d_oxyz.p, ctx->d_obucket.p,
-        lg_is_mixed(ctx->params.precision) ? ctx->d_ys32.p : nullptr,
-        lg_is_mixed(ctx->params.precision) ? ctx->d_oef.p : nullptr,
+        mixed ? ctx->d_ys32.p : nullptr, mixed ? ctx->d_oef.p : nullptr, mixed ? ctx->d_ymax.p : nullptr,
         ctx->nblat, ctx->nblon, ctx->cell_lat, ctx->cell_lon, ctx->d_status.p, mode);
     return cudaGetLastError();
 }

@@ -1,7 +1,7 @@
 // letkf_umma.cuh -- Blackwell tensor-core building blocks (tcgen05 + TMEM) in
 // inline PTX: TMEM allocation, shared-memory matrix descriptors for K-major
-// 128-byte-swizzled BF16 tiles, the MMA issue, commit to an mbarrier, bounded
-// mbarrier waits and TMEM loads.
+// 128-byte-swizzled 16-bit (BF16 or FP16) tiles, the MMA issue, commit to an
+// mbarrier, bounded mbarrier waits, TMEM loads and stores.
 //
 // Tile convention (K-major, SWIZZLE_128B, 16-bit elements): a tile holds R rows
 // (R a multiple of 8) of 64 elements (128 bytes) along K.  Row r, 16-byte chunk
@@ -50,6 +50,12 @@ __host__ __device__ constexpr uint32_t lg_idesc_bf16(int M, int N)
            ((uint32_t)(M >> 4) << 24);
 }
 
+// The same with FP16 A and B (type fields 0).
+__host__ __device__ constexpr uint32_t lg_idesc_f16(int M, int N)
+{
+    return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
 __device__ __forceinline__ void lg_tmem_alloc(uint32_t dst_smem, uint32_t ncols)
 {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(dst_smem),
@@ -93,7 +99,8 @@ __device__ __forceinline__ bool lg_mbar_wait(uint64_t *mbar, uint32_t parity, ui
     return false;
 }
 
-// D[tmem] (+)= A * B^T for one K step of 16 BF16 elements.
+// D[tmem] (+)= A * B^T for one K step of 16 BF16 or FP16 elements (the
+// instruction descriptor gives the type of both operands).
 __device__ __forceinline__ void lg_umma_bf16(uint32_t tmem_d, uint64_t adesc, uint64_t bdesc,
                                              uint32_t idesc, uint32_t accumulate)
 {
@@ -124,4 +131,43 @@ __device__ __forceinline__ void lg_tmem_ld16(uint32_t taddr, float *v)
     asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 #pragma unroll
     for (int i = 0; i < 16; i++) v[i] = __uint_as_float(r[i]);
+}
+
+// Load 16 consecutive 32-bit columns at each of two TMEM addresses of this
+// thread's lane, with one wait (in the same statement, so nothing reads the
+// registers before the loads are done).
+__device__ __forceinline__ void lg_tmem_ld16x2(uint32_t ta, uint32_t tb, float *va, float *vb)
+{
+    uint32_t a[16], b[16];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%32];\n"
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%33];\n"
+        "tcgen05.wait::ld.sync.aligned;"
+        : "=r"(a[0]), "=r"(a[1]), "=r"(a[2]), "=r"(a[3]), "=r"(a[4]), "=r"(a[5]), "=r"(a[6]), "=r"(a[7]),
+          "=r"(a[8]), "=r"(a[9]), "=r"(a[10]), "=r"(a[11]), "=r"(a[12]), "=r"(a[13]), "=r"(a[14]), "=r"(a[15]),
+          "=r"(b[0]), "=r"(b[1]), "=r"(b[2]), "=r"(b[3]), "=r"(b[4]), "=r"(b[5]), "=r"(b[6]), "=r"(b[7]),
+          "=r"(b[8]), "=r"(b[9]), "=r"(b[10]), "=r"(b[11]), "=r"(b[12]), "=r"(b[13]), "=r"(b[14]), "=r"(b[15])
+        : "r"(ta), "r"(tb)
+        : "memory");
+#pragma unroll
+    for (int i = 0; i < 16; i++) {
+        va[i] = __uint_as_float(a[i]);
+        vb[i] = __uint_as_float(b[i]);
+    }
+}
+
+// Store 16 consecutive 32-bit columns of this thread's TMEM lane and wait
+// until the stores are done.
+__device__ __forceinline__ void lg_tmem_st16(uint32_t taddr, const float *v)
+{
+    asm volatile(
+        "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16};"
+        ::"r"(taddr), "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])),
+        "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])),
+        "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7])), "r"(__float_as_uint(v[8])),
+        "r"(__float_as_uint(v[9])), "r"(__float_as_uint(v[10])), "r"(__float_as_uint(v[11])),
+        "r"(__float_as_uint(v[12])), "r"(__float_as_uint(v[13])), "r"(__float_as_uint(v[14])),
+        "r"(__float_as_uint(v[15]))
+        : "memory");
+    asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
 }

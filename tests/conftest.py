@@ -63,6 +63,30 @@ def spread(xa):
     return np.sqrt(np.mean(xa * xa, axis=-1))
 
 
+def var_rows(w):
+    """Row slice of each state variable: ps, then u, v, T on w.nz levels."""
+    rows = {"ps": slice(0, w.nvar2d)}
+    for i, nm in enumerate(["u", "v", "T"][: w.nvar3d]):
+        rows[nm] = slice(w.nvar2d + i * w.nz, w.nvar2d + (i + 1) * w.nz)
+    return rows
+
+
+def increment_errors(xa, axa, xa_ref, axa_ref, xb, axb, w):
+    """Per-variable errors of the analysis mean and spread on the scale of
+    what the analysis adds: max|a - ref| over a variable's rows divided by
+    max|ref - background| there (the mean's change axa - axb, the spread's
+    change spread_a - spread_b)."""
+    out = {}
+    for kind, a, r, bg in (("mean", axa, axa_ref, axb),
+                           ("spread", spread(xa), spread(xa_ref), spread(xb))):
+        out[kind] = {}
+        for nm, sl in var_rows(w).items():
+            d = np.abs(a[:, sl] - r[:, sl]).max()
+            inc = np.abs(r[:, sl] - bg[:, sl]).max()
+            out[kind][nm] = float(d / inc) if inc > 0 else float(d)
+    return out
+
+
 def mean_spread_errors(xa, axa, xa_ref, axa_ref, w):
     """Per-variable relative errors of the analysis mean and spread (max abs
     difference over the variable's rows and columns / max abs reference)."""
