@@ -31,6 +31,9 @@ REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, REPO)
 PKG = "dida-thhpca-sc23_gb300"
 METRIC = "LETKF columns/s: mixed-prec vs FP64 on one GB300 at ≤1e-4 err vs FP64"
+# the arithmetic of the mixed forms' products
+MIXED_DTYPE = ("fp16 hi/lo tensor products for A off the diagonal (f32 accumulation, added in f32 every "
+               "16 chunks) + f32-pipe g and diag(A) + bf16 hi/lo tensor products for the update")
 
 
 def pkg(name):
@@ -612,10 +615,9 @@ def run_ours(args, rank, world, local_rank):
                 "algorithmic_flops_per_launch": flops, "kernel_ms": core,
                 "peak_source": "cuBLAS DGEMM 4096^3 measured here (MEASURED_PEAKS.json has no FP64 figure)"}
     stages = res[head][2]
-    dtype_of = {"mixed": "bf16 hi/lo tensor products (f32 accum) + f32 eigensolve/T + f64 wbar residual "
-                         "and mean increment",
-                "mixed_f64eig": "bf16 hi/lo tensor products (f32 accum) + f64-refined eigenpairs, "
-                                "1/sqrt(lambda), T, wbar + f64 mean increment",
+    dtype_of = {"mixed": MIXED_DTYPE + " + f32 eigensolve/T + f64 wbar residual and mean increment",
+                "mixed_f64eig": MIXED_DTYPE + " + f64-refined eigenpairs, 1/sqrt(lambda), T, wbar + f64 "
+                                "mean increment",
                 "fp64": "f64"}
     form_of = {"mixed": "mixed precision (LETKF_PREC_MIXED)",
                "mixed_f64eig": "mixed precision, FP64 eigenpairs (LETKF_PREC_MIXED_F64EIG)",
@@ -788,8 +790,8 @@ def run_ours_c4(args, rank, world, local_rank):
         "metric": METRIC, "value": value, "unit": "columns/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "bf16 hi/lo tensor products (f32 accum) + f32 eigensolve/T + f64 wbar residual and mean "
-                 "increment (not the FP8 E4M3 per-tile-scaled products this configuration names)",
+        "dtype": MIXED_DTYPE + " + f32 eigensolve/T + f64 wbar residual and mean increment (not the FP8 "
+                 "E4M3 per-tile-scaled products this configuration names)",
         "data": "synthetic (seeded; members built on the device)",
         "config": {"workload": f"config4: {w.nlon}x{w.nlat}x{w.nz}, k={w.k}, {o['lat'].size} obs "
                                "(uniform + 3 clusters at 10x), GC c=250 km (cut-off 500 km), rho=1.05",
@@ -964,8 +966,7 @@ def run_ours_batch(args, rank, world, local_rank):
         "metric": METRIC, "value": value, "unit": "columns/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "bf16 hi/lo tensor products (f32 accum) + f32 eigensolve/T + f64 wbar residual and mean "
-                 "increment",
+        "dtype": MIXED_DTYPE + " + f32 eigensolve/T + f64 wbar residual and mean increment",
         "data": "synthetic (seeded; no public dataset for this path)",
         "config": {"workload": "config3: 8 instances 90x180..240x480 x32, k in {32,48,64,96}, "
                                "20k-400k obs, one CUDA graph",

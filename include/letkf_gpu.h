@@ -51,11 +51,14 @@ extern "C" {
 /* letkf_params.precision (the reference's computing_precision knob,
  * da_namelist_mod.F90:49, selects the core's arithmetic the same way)       */
 #define LETKF_PREC_FP64    0   /* FP64 throughout                                  */
-#define LETKF_PREC_MIXED   1   /* BF16 hi/lo tensor-core products for A, g and the
-                                  update (FP32 accumulation); FP32 Jacobi
-                                  eigenpairs and FP32 T; wbar in FP32 with one
-                                  FP64-residual refinement step; FP64 mean
-                                  increment                                        */
+#define LETKF_PREC_MIXED   1   /* FP16 hi/lo tensor-core products for A off the
+                                  diagonal (FP32 accumulation, added in FP32
+                                  every 16 chunks of 64 observations); g and
+                                  diag(A) on the FP32 pipe; BF16 hi/lo
+                                  tensor-core products for the update; FP32
+                                  Jacobi eigenpairs and FP32 T; wbar in FP32
+                                  with one FP64-residual refinement step; FP64
+                                  mean increment                                   */
 #define LETKF_PREC_MIXED_F64EIG 2 /* the same tensor-core products, with the FP32
                                   Jacobi eigenpairs refined to FP64 (one
                                   Ogita-Aishima step on FP64 residuals), FP64
