@@ -1191,10 +1191,23 @@ int lg_run_chunk(const letkf_ctx *ctx)
 // Build the mixed core's work queue for the cubes of the last search (the
 // window win0 .. win1 - 1): the chunks of lg_run_chunk cubes that meet the
 // window (aligned to multiples of the chunk size in cube numbering), heaviest
-// first, into ctx->d_queue.
+// first, into ctx->d_queue.  The staged k = 64 core's launches (the A build
+// and the update: no warm start) halve the chunk, down to 8 cubes, while the
+// window has fewer than 8 chunks per A-build CTA: the blocks of a run that
+// goes back to host memory are small, and with two chunks per CTA the
+// heaviest ones leave a tail (1.6 ms of A build over the three blocks at the
+// 1-degree configuration).  The chunk only decides which CTA takes which
+// cubes, so the analysis is the same.
 cudaError_t lg_build_chunk_queue(letkf_ctx *ctx, int &chunk, int &nchunks)
 {
     chunk = lg_run_chunk(ctx);
+    if (ctx->k == 64) {
+        int nsm = 0;
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, ctx->device);
+        const int64_t want = 8LL * 3 * (nsm > 0 ? nsm : 152), n = ctx->win1 - ctx->win0;
+        while (chunk > 8 && (n + chunk - 1) / chunk < want && 2 * ((n + chunk - 1) / chunk) + 2 <= kQueueMax)
+            chunk /= 2;
+    }
     const int64_t base = ctx->win0 / chunk * chunk;
     nchunks = (int)((ctx->win1 - base + chunk - 1) / chunk);
     cudaError_t e = ctx->d_queue.reserve((size_t)nchunks);
