@@ -632,6 +632,189 @@ __device__ int lg_jacobi32b2(float *W, float *extra, int *s_rot, float tol, int 
 }
 
 
+// FP32 one-sided Jacobi with the hierarchical ordering over blocks of three
+// columns, for K = 96 (32 blocks, a power of two): K/6 slots of 256/(K/6)
+// lanes each keep a fixed block in registers and rotate it against a moving
+// block, nine rotations per step taken three at a time on disjoint pairs
+// (F_a with M_(a+s) mod 3 for s = 0, 1, 2) with their inner products reduced
+// together; at the last level each block's own three pairs are rotated too.
+// A sweep takes K/3 - 1 steps, with a block barrier only where the moving
+// blocks pass to another warp (every second step), against K - 1 barriered
+// steps of the round-robin lg_jacobi32.  Buffers, norms, the early exit and
+// the hand-overs are those of lg_jacobi32b2 with three columns per block.
+template <int K, int LD, int BS>
+__device__ int lg_jacobi32b3(float *W, float *extra, int *s_rot, float tol, int max_sweeps)
+{
+    constexpr int BW = 3, NB = K / BW, NSL = NB / 2, G = 256 / NSL, RPL = K / G, SPW = 32 / G;
+    constexpr int VW = (RPL % 4 == 0) ? 4 : 2, NC = RPL / VW;
+    static_assert(K == 96, "block-3 ordering for K = 96");
+    static_assert((NB & (NB - 1)) == 0 && 32 % G == 0 && RPL % 2 == 0, "power-of-two blocks, packed rows");
+    static_assert(2 * NSL * BW * BS <= K * LD && LD % VW == 0 && BS % VW == 0, "moving-block buffers fit in W");
+    const int tid = threadIdx.x;
+    const int slot = tid / G, lane = tid % G;
+    const int lw = tid & 31, ws = lw / G, wl = lw % G;
+    const float tol2 = tol * tol;
+    float *buf = W;                                    // [2][NSL][BW columns][BS]
+    float *bn = extra;                                 // [2][NSL][BW] squared norms
+    int *bid = reinterpret_cast<int *>(bn + 2 * NSL * BW);   // [2][NSL] block ids
+    float F[BW][RPL], M[BW][RPL], fn[BW], mn[BW];
+    auto ld = [&](const float *src, float *r) {
+#pragma unroll
+        for (int c = 0; c < NC; c++) {
+            const int o = (c * G + lane) * VW, i = c * VW;
+            if constexpr (VW == 4) {
+                const float4 x = *reinterpret_cast<const float4 *>(src + o);
+                r[i] = x.x; r[i + 1] = x.y; r[i + 2] = x.z; r[i + 3] = x.w;
+            } else {
+                const float2 x = *reinterpret_cast<const float2 *>(src + o);
+                r[i] = x.x; r[i + 1] = x.y;
+            }
+        }
+    };
+    auto st = [&](float *dst, const float *r) {
+#pragma unroll
+        for (int c = 0; c < NC; c++) {
+            const int o = (c * G + lane) * VW, i = c * VW;
+            if constexpr (VW == 4) *reinterpret_cast<float4 *>(dst + o) = make_float4(r[i], r[i + 1], r[i + 2], r[i + 3]);
+            else *reinterpret_cast<float2 *>(dst + o) = make_float2(r[i], r[i + 1]);
+        }
+    };
+    auto pdot = [&](const float *x, const float *y) {
+        unsigned long long a = 0ull;
+#pragma unroll
+        for (int i = 0; i < RPL; i += 2) a = lg_ffma2(lg_pk2(x[i], x[i + 1]), lg_pk2(y[i], y[i + 1]), a);
+        float p0, p1;
+        lg_upk2(a, p0, p1);
+        return p0 + p1;
+    };
+    auto red3 = [&](float &a, float &b, float &c) {
+#pragma unroll
+        for (int o = G / 2; o > 0; o >>= 1) {
+            a += __shfl_xor_sync(0xffffffffu, a, o);
+            b += __shfl_xor_sync(0xffffffffu, b, o);
+            c += __shfl_xor_sync(0xffffffffu, c, o);
+        }
+    };
+    bool rotated_any = false, big_any = false;
+    auto apply = [&](float *X, float *Y, float &nx, float &ny, float gam) {
+        if (LG_JACOBI32W_QSTOP > 0.0f && gam * gam > LG_JACOBI32W_QSTOP * LG_JACOBI32W_QSTOP * (nx * ny))
+            big_any = true;
+        if (gam * gam > tol2 * (nx * ny)) {
+            float c, s, tt;
+            lg_rotation(nx, ny, gam, c, s, tt);
+            const unsigned long long c2 = lg_pk2(c, c), s2 = lg_pk2(s, s), ns2 = lg_pk2(-s, -s);
+#pragma unroll
+            for (int r = 0; r < RPL; r += 2) {
+                const unsigned long long x = lg_pk2(X[r], X[r + 1]), y = lg_pk2(Y[r], Y[r + 1]);
+                lg_upk2(lg_ffma2(c2, x, lg_fmul2(ns2, y)), X[r], X[r + 1]);
+                lg_upk2(lg_ffma2(s2, x, lg_fmul2(c2, y)), Y[r], Y[r + 1]);
+            }
+            nx = nx - tt * gam;
+            ny = ny + tt * gam;
+            rotated_any = true;
+        }
+    };
+    int sweep, moves = 0;
+    for (sweep = 1; sweep <= max_sweeps; sweep++) {
+        if (tid == 0) *s_rot = 0;
+        rotated_any = false;
+        big_any = false;
+        for (int B = NB; B >= 2; B >>= 1) {            // B blocks per group
+            const int half = B / 2, u = slot / half, i = slot % half;
+            const int fb = u * B + i;
+            int mbk = u * B + half + i;
+            __syncthreads();                           // W holds every column
+#pragma unroll
+            for (int a = 0; a < BW; a++) {
+                ld(W + (BW * fb + a) * LD, F[a]);
+                ld(W + (BW * mbk + a) * LD, M[a]);
+            }
+#pragma unroll
+            for (int a = 0; a < BW; a++) {
+                fn[a] = pdot(F[a], F[a]);
+                mn[a] = pdot(M[a], M[a]);
+            }
+            red3(fn[0], fn[1], fn[2]);
+            red3(mn[0], mn[1], mn[2]);
+            __syncthreads();                           // W becomes the hand-over buffers
+            for (int t = 0; t < half; t++) {
+                // the nine pairs of the fixed and the moving block
+#pragma unroll
+                for (int s = 0; s < BW; s++) {
+                    float g0 = pdot(F[0], M[s]), g1 = pdot(F[1], M[(s + 1) % BW]), g2 = pdot(F[2], M[(s + 2) % BW]);
+                    red3(g0, g1, g2);
+                    apply(F[0], M[s], fn[0], mn[s], g0);
+                    apply(F[1], M[(s + 1) % BW], fn[1], mn[(s + 1) % BW], g1);
+                    apply(F[2], M[(s + 2) % BW], fn[2], mn[(s + 2) % BW], g2);
+                }
+                if (B == 2) {
+                    // each block's own pairs, the fixed and the moving block's together
+#pragma unroll
+                    for (int q = 0; q < BW; q++) {
+                        const int a = q == 2 ? 1 : 0, b = q == 0 ? 1 : 2;
+                        float g0 = pdot(F[a], F[b]), g1 = pdot(M[a], M[b]), g2 = 0.0f;
+                        red3(g0, g1, g2);
+                        apply(F[a], F[b], fn[a], fn[b], g0);
+                        apply(M[a], M[b], mn[a], mn[b], g1);
+                    }
+                }
+                if (t == half - 1) break;
+                const bool handover = half > SPW && (t + 1) % SPW == 0;
+                if (!handover) {
+                    // the next slot of the group inside the warp (cyclic)
+                    const int gs = half < SPW ? half : SPW;
+                    const int gbase = (ws / gs) * gs;
+                    const int src = (gbase + (ws - gbase + 1) % gs) * G + wl;
+#pragma unroll
+                    for (int a = 0; a < BW; a++) {
+#pragma unroll
+                        for (int r = 0; r < RPL; r++) M[a][r] = __shfl_sync(0xffffffffu, M[a][r], src);
+                        mn[a] = __shfl_sync(0xffffffffu, mn[a], src);
+                    }
+                    mbk = __shfl_sync(0xffffffffu, mbk, src);
+                } else {
+                    // the same slot of the next warp of the group
+                    const int par = moves & 1;
+                    moves++;
+                    const int gw = i / SPW, nw = half / SPW;
+                    const int ss = u * half + ((gw + 1) % nw) * SPW + ws;
+                    float *mine = buf + (size_t)(par * NSL + slot) * BW * BS;
+#pragma unroll
+                    for (int a = 0; a < BW; a++) st(mine + a * BS, M[a]);
+                    if (lane == 0) {
+#pragma unroll
+                        for (int a = 0; a < BW; a++) bn[(par * NSL + slot) * BW + a] = mn[a];
+                        bid[par * NSL + slot] = mbk;
+                    }
+                    __syncthreads();
+                    const float *theirs = buf + (size_t)(par * NSL + ss) * BW * BS;
+#pragma unroll
+                    for (int a = 0; a < BW; a++) {
+                        ld(theirs + a * BS, M[a]);
+                        mn[a] = bn[(par * NSL + ss) * BW + a];
+                    }
+                    mbk = bid[par * NSL + ss];
+                }
+            }
+            __syncthreads();                           // every read of the buffers is done
+#pragma unroll
+            for (int a = 0; a < BW; a++) {
+                st(W + (BW * fb + a) * LD, F[a]);
+                st(W + (BW * mbk + a) * LD, M[a]);
+            }
+        }
+        if (lane == 0 && (rotated_any || big_any)) atomicOr(s_rot, (rotated_any ? 1 : 0) | (big_any ? 2 : 0));
+        __syncthreads();
+        const int rotated = *s_rot;
+        __syncthreads();
+        if (!(rotated & 1)) break;
+        // the early exit of lg_jacobi32w: a sweep of rotations all below the
+        // stop level ends the solve
+        if (LG_JACOBI32W_QSTOP > 0.0f && !(rotated & 2)) break;
+    }
+    return sweep;
+}
+
 // FP32 one-sided Jacobi of one K x K problem by one warp (K = 64): lane l
 // owns a column pair in registers, so the inner products need no reduction
 // and a step needs no barrier; the hierarchical ordering passes the moving

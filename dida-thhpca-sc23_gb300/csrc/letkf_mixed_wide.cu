@@ -13,6 +13,8 @@
 //     the w-bar residual adds (k-1)/rho in FP64 to the FP32 A);
 //   * the update's operands (xb rows and T, k members deep) are two
 //     128-byte-swizzled tiles along the member axis.
+// The FP32 Jacobi takes the hierarchical ordering over blocks of two columns
+// (k = 128, lg_jacobi32b2) or three (k = 96, lg_jacobi32b3).
 // Shared memory (k = 128): the previous cube's eigenvectors and X (64 KB),
 // the Jacobi columns / S / T tiles (67 KB), A / T / xb tiles (65 KB); the
 // A-build tiles and gather stages overlay the last two.
@@ -435,8 +437,8 @@ k_core_mixed_wide(LgGrid g, LgParams prm, const float *__restrict__ ys32, const 
         int sw;
         if constexpr (K == 128)
             sw = lg_jacobi32b2<K, C::LDW, C::LDW>(W32, W32 + K * C::LDW, &s_rot, LG_MIXED_JACOBI_TOL, 24);
-        else sw = lg_jacobi32<K, C::G, C::LDW>(W32, nrm32, &s_rot, LG_MIXED_JACOBI_TOL,
-                                          LG_JACOBI32W_QSTOP > 0.0f ? LG_JACOBI32W_QSTOP : LG_MIXED_JACOBI_TOL, 24);
+        else
+            sw = lg_jacobi32b3<K, C::LDW, C::LDW>(W32, W32 + K * C::LDW, &s_rot, LG_MIXED_JACOBI_TOL, 24);
         if (tid == 0) {
             atomicMax(&counters[LG_CNT_MAXSWEEP], (unsigned long long)sw);
             atomicAdd(&counters[LG_CNT_SUMSWEEP], (unsigned long long)sw);
